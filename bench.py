@@ -1,0 +1,355 @@
+"""Benchmark: split-step grid-point-steps/s of GPEtask.solve_split on one GB300.
+
+Workload (BASELINE configs[1]): grid3d 256^3, box +-12, V = 0.5 (x^2 + y^2 +
+(4 z)^2), g = 0.5, Ntotal = 1e5, ground state by imaginary-time propagation
+(FP32 + FP64 polish, untimed), then real-time steps of dt = 0.002 with damping
+gamma = 0.01.  One bench step = one outer step of solve_split = 100 split
+steps (10 blocks of n_recalc = 10, mu feedback every block).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is complex-FP32 throughput with the state
+resident in HBM; `fp64` is the same kernels in FP64 on the same start state;
+`error` states the FP32 result against the FP64 one after 100 steps; `e2e`
+runs each step through the public host API with pinned host buffers (state
+upload, 100 steps, state download).  `--impl reference` times the FP64 CPU
+restatement of the reference's solve_split (the reference is MATLAB, which
+this machine does not have) on the same workload, all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (str(ROOT), str(ROOT / "gpe-matlab_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "split-step grid-pt-steps/s (complex FP32, vs FP64 same kernels)"
+UNIT = "grid-pt-steps/s"
+INNER = 100  # split steps per bench step (outer step of solve_split)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """Barrier + max/sum over ranks (gloo on host tensors); no data-path collective."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX if op == "max" else self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ground_state(gpe, W, precision="single", device=0):
+    """Untimed setup: FP32 ITP with FP64 polish from the seeded Gaussian."""
+    grid, task = W.make_task(precision, device=device)
+    psi0 = W.initial_state(grid)
+    phi = task.groundstate_itp(W.itp_dt, W.itp_eps, psi0)
+    return grid, task, phi
+
+
+def cpu_reference_steps(W, phi, steps: int, cores: int):
+    """Times `steps` inner split steps of the FP64 oracle (reference restatement)."""
+    from oracle import gpe_oracle as O
+
+    O.set_workers(cores)
+    og = O.Grid(W.box[0], W.n[0], W.box[1], W.n[1], W.box[2], W.n[2])
+    ot = O.GPEtask(og, W.potential())
+    ot.Ntotal, ot.g, ot.gamma = W.Ntotal, W.g, W.gamma
+    ot.init_state = np.asarray(phi, dtype=np.complex128)
+    stamps = []
+
+    class Done(Exception):
+        pass
+
+    def on_inner(i):
+        stamps.append(time.perf_counter())
+        if len(stamps) > steps:
+            raise Done
+
+    t0 = time.perf_counter()
+    try:
+        ot.solve_split(W.dt, 10, 10 ** 6, inner_callback=on_inner)
+    except Done:
+        pass
+    t_steps = stamps[-1] - t0 if stamps else float("nan")
+    n = len(stamps)
+    return W.npoints * n / t_steps, n, t_steps
+
+
+def run_reference(args, dist):
+    from gpe_gb300.workloads import DAMPED3D as W
+
+    if dist.rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    # Start state: the seeded Gaussian (the timed work does not depend on it).
+    grid = W.make_grid("double")
+    phi = W.initial_state(grid) * 10.0
+    val, n, t = cpu_reference_steps(W, phi, args.warmup + args.steps, cores)
+    line = {
+        "metric": METRIC, "value": val, "unit": UNIT, "impl": "reference", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / max(n, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": W.name, "grid": list(W.n), "dt": W.dt, "gamma": W.gamma, "step": "1 split step"},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{n} split steps of the 256^3 FP64 oracle (numpy + scipy.fft, {cores} workers)"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, dist):
+    import gpe_gb300 as gpe
+    from gpe_gb300.workloads import DAMPED3D as W
+
+    dev = dist.local
+    P = W.npoints
+    grid, task, phi = ground_state(gpe, W, "single", device=dev)
+    itp = task.last_itp
+    phi = np.asarray(phi)
+    # ---- FP32 timed region ------------------------------------------------
+    task.init_state = phi
+    task.current_iter = 0
+    task.solve_split(W.dt, INNER, 1)                  # first warm-up step
+    psi32_1 = task.current_state.astype(np.complex128)
+    mu32 = task.history["mu"][0]
+    task.solve_split(W.dt, INNER, max(1, args.warmup))
+    k0 = task.kernel_launches()
+    task.profile(True)
+    dist.barrier()
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        from gpe_gb300 import _lib as L
+        import ctypes as C
+
+        L.check(task._ctx, L.lib.gpe_timer_start(task._ctx))
+        task.solve_split(W.dt, INNER, int(task.current_iter) + args.steps)
+        ms = C.c_double()
+        L.check(task._ctx, L.lib.gpe_timer_stop(task._ctx, C.byref(ms)))
+        wall = time.perf_counter() - t0
+    stats = task.profile_read()
+    task.profile(False)
+    launches = task.kernel_launches() - k0
+    t_s = dist.reduce(ms.value / 1e3, "max")
+    work = dist.reduce(float(P) * INNER * args.steps, "sum")
+    value = work / t_s
+    # ---- roofline of the dominant kernel ------------------------------------
+    hbm, peak_kind = peaks()
+    top = max(stats, key=lambda s: s["total_ms"])
+    avg_ms = top["total_ms"] / top["launches"]
+    achieved = top["bytes_per_launch"] / (avg_ms / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        d = json.loads(tf.read_text())
+        traffic = d.get(top["name"], {}).get("bytes_per_launch_256cube")
+    # ---- FP64 arm (same kernels, same start) ----------------------------------
+    g64, t64 = W.make_task("double", device=dev)
+    t64.init_state = phi.astype(np.complex128)
+    t64.solve_split(W.dt, INNER, 1)
+    psi64_1 = t64.current_state
+    mu64 = t64.history["mu"][0]
+    k64 = max(1, min(args.steps, 3))
+    L.check(t64._ctx, L.lib.gpe_timer_start(t64._ctx))
+    t64.solve_split(W.dt, INNER, 1 + k64)
+    ms64 = C.c_double()
+    L.check(t64._ctx, L.lib.gpe_timer_stop(t64._ctx, C.byref(ms64)))
+    value64 = float(P) * INNER * k64 / (ms64.value / 1e3)
+    err_l2 = float(np.linalg.norm(psi32_1 - psi64_1) / np.linalg.norm(psi64_1))
+    t64.close()
+    # ---- e2e through the public API with pinned host buffers --------------------
+    host_in = np.ascontiguousarray(phi.astype(np.complex64))
+    host_out = np.empty_like(host_in)
+    e2e_steps = max(1, min(args.steps, 5))
+    with gpe.pinned(host_in), gpe.pinned(host_out):
+        task.init_state = host_in
+        task.current_iter = 0
+        task.solve_split(W.dt, INNER, 1)
+        task._download(host_out)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            task.init_state = host_in
+            task.current_iter = 0
+            task.solve_split(W.dt, INNER, 1)
+            task._download(host_out)
+        e2e_t = time.perf_counter() - t0
+    e2e_t = dist.reduce(e2e_t, "max")
+    e2e_val = dist.reduce(float(P) * INNER * e2e_steps, "sum") / e2e_t
+    # ---- CPU baseline (rank 0, N = 1 only): bounded sample ---------------------
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
+        cores = os.cpu_count() or 1
+        cval, n, t = cpu_reference_steps(W, phi, args.cpu_steps, cores)
+        cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{n} split steps of the same 256^3 workload in the FP64 oracle "
+                         f"(numpy + scipy.fft with {cores} workers), {t:.1f} s"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms.value / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 (FP64 reductions)", "data": "synthetic (seeded Gaussian -> ITP ground state)",
+        "config": {"workload": W.name, "grid": list(W.n), "box": W.box[0], "trap_lambda": W.trap[2], "g": W.g,
+                   "Ntotal": W.Ntotal, "dt": W.dt, "gamma": W.gamma, "step": f"{INNER} split steps (1 outer step)",
+                   "n_recalc": 10, "l2": "inputs larger than L2 (state 134 MB + V 67 MB per GPU)",
+                   "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU"},
+        "fp64": {"value": value64, "unit": UNIT, "steps": INNER * k64, "ratio_fp32_over_fp64": value / dist.world / value64},
+        "error": {"fp32_vs_fp64_rel_l2_after_100_steps": err_l2,
+                  "mu_rel_after_100_steps": abs(mu32 - mu64) / abs(mu64),
+                  "itp_iters": itp.iters, "itp_fp32_iters": itp.fp32_iters, "itp_converged": bool(itp.converged)},
+        "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": top["bytes_per_launch"], "avg_launch_ms": avg_ms},
+        "kernels": stats,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(host_in.nbytes),
+                "d2h_bytes_per_step": int(host_out.nbytes), "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "wall_s_timed": wall,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    task.close()
+
+
+def run_profile_case(precision: str, blocks: int):
+    """Small fixed case for ncu captures: the bench workload's grid and
+    parameters from the seeded Gaussian (no ITP), `blocks` blocks of 10 steps."""
+    from gpe_gb300.workloads import DAMPED3D as W
+
+    grid, task = W.make_task(precision)
+    task.init_state = W.initial_state(grid) * 30.0
+    task.solve_split(W.dt, 10, blocks)
+    print(json.dumps({"profile_case": precision, "blocks": blocks, "launches": task.kernel_launches(),
+                      "mu": task.current_mu, "n": task.current_n}))
+    task.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--profile-case", choices=["single", "double"], default=None,
+                    help="run the small fixed case used for ncu captures and exit")
+    ap.add_argument("--profile-blocks", type=int, default=2)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args.profile_case, args.profile_blocks)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_gpu(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

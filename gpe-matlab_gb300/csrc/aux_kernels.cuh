@@ -1,0 +1,86 @@
+// aux_kernels.cuh - declarations of the elementwise, reduction and
+// finalizer kernels (aux_kernels.cu) used by the host drivers.
+#pragma once
+#include "common.cuh"
+
+namespace gpe {
+
+// Grid of the elementwise kernels: a multiple of the SM count.
+int elem_grid(long long n, int threads);
+
+// Per-block finalizer of solve_split (solve_split.m:65-78).
+struct BlockFinalArgs {
+  const double* partials;
+  int cap;
+  int nblk_epi;          // CTAs of the block-end pass (slots n, Vn, n2)
+  int nblk_kin[3];       // CTAs of the kinetic-energy passes (x, y, z), 0 = skipped
+  double weight, g;
+  int feedback;          // gamma > 0 && mu_init == 0
+  double tau, time2;
+  double* hist_mu;       // nullptr or &history[j]
+  double* hist_n;
+  int* hist_ok;
+};
+
+struct ItpFinalArgs {
+  const double* partials;
+  int cap, nblk;
+  double weight, dt, Ntotal, mu_init;
+  int iter;              // 1-based iteration index
+  double* MU;
+};
+
+struct CheckFinalArgs {
+  const double* partials;
+  int cap;
+  int nblk_check;        // CTAs of itp_check (slots maxd, maxa)
+  int nblk_pot;          // CTAs of the energy y pass with potential sums (0 = none)
+  int nblk_kin[3];
+  double weight, g, dt, eps, nnn;
+  int iter;
+  int want_mu2;
+  int adjust;
+  int fp32_phase;        // 1: end the phase on delta < switch_delta or a stall
+  double switch_delta;
+  const double* MU;
+  double* MU2;
+  double* EE;
+};
+
+struct ObsFinalArgs {
+  const double* partials;
+  int cap, nblk_pot;
+  int nblk_kin[3];
+  double weight, g;
+  double div;            // muc = mu_integral / div (0: not stored)
+  int set_mu;            // also set sc->mu (solve_split.m:42-46)
+  double mu_init;
+};
+
+void launch_finalize_block(const BlockFinalArgs& a, DevScalars* sc, cudaStream_t s);
+void launch_finalize_itp(const ItpFinalArgs& a, DevScalars* sc, cudaStream_t s);
+void launch_finalize_check(const CheckFinalArgs& a, DevScalars* sc, cudaStream_t s);
+void launch_finalize_obs(const ObsFinalArgs& a, DevScalars* sc, cudaStream_t s);
+// scale = Ntotal > 0 ? sqrt(Ntotal / (sum_n*w)) : 1 (GPEtask.m:159-160); returns CTAs read.
+void launch_finalize_norm0(const double* partials, int cap, int nblk, double weight, double Ntotal,
+                           DevScalars* sc, cudaStream_t s);
+void launch_reset_scalars(DevScalars* sc, cudaStream_t s);
+void launch_set_scale_one(DevScalars* sc, cudaStream_t s);
+
+template <typename R>
+int launch_norm(const cx<R>* psi, long long n, DevScalars* sc, double* partials, int cap, cudaStream_t s);
+template <typename R>
+int launch_itp_check(const cx<R>* psi, R* absprev, long long n, DevScalars* sc, double* partials, int cap,
+                     cudaStream_t s);
+template <typename R>
+void launch_abs_init(const cx<R>* psi, R* absprev, long long n, DevScalars* sc, cudaStream_t s);
+// psi *= sc->scale (in place); the caller resets the scale afterwards.
+template <typename R>
+void launch_apply_scale(cx<R>* psi, long long n, DevScalars* sc, cudaStream_t s);
+// out = in (element type conversion), optionally times sc->scale.
+template <typename RI, typename RO>
+void launch_convert_cx(const cx<RI>* in, cx<RO>* out, long long n, const DevScalars* sc, cudaStream_t s);
+template <typename RI, typename RO>
+void launch_convert_re(const RI* in, RO* out, long long n, cudaStream_t s);
+
+}  // namespace gpe

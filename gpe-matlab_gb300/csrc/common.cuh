@@ -1,0 +1,151 @@
+// common.cuh - shared types of libgpe's device code.
+//
+// State arrays hold interleaved complex values in MATLAB column-major order
+// (iy + ny*(ix + nx*iz), lib/@grid3d/init.m:75-79 of GPE-MATLAB).  The FFT
+// axis passes read and write that layout directly; nothing is transposed in
+// HBM.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gpe {
+
+template <typename R>
+struct __align__(2 * sizeof(R)) cx {
+  R x, y;
+};
+
+template <typename R>
+__host__ __device__ __forceinline__ cx<R> mk(R a, R b) {
+  cx<R> r;
+  r.x = a;
+  r.y = b;
+  return r;
+}
+template <typename R>
+__device__ __forceinline__ cx<R> operator+(cx<R> a, cx<R> b) { return mk<R>(a.x + b.x, a.y + b.y); }
+template <typename R>
+__device__ __forceinline__ cx<R> operator-(cx<R> a, cx<R> b) { return mk<R>(a.x - b.x, a.y - b.y); }
+template <typename R>
+__device__ __forceinline__ cx<R> cmul(cx<R> a, cx<R> b) {
+  return mk<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename R>
+__device__ __forceinline__ cx<R> cmulc(cx<R> a, cx<R> b) {
+  return mk<R>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename R>
+__device__ __forceinline__ cx<R> rmul(cx<R> a, R s) { return mk<R>(a.x * s, a.y * s); }
+template <typename R>
+__device__ __forceinline__ R norm2(cx<R> a) { return a.x * a.x + a.y * a.y; }
+
+// Read-only (non-coherent cache) loads of table entries.
+__device__ __forceinline__ cx<float> ldg(const cx<float>* p) {
+  float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return mk<float>(v.x, v.y);
+}
+__device__ __forceinline__ cx<double> ldg(const cx<double>* p) {
+  double2 v = __ldg(reinterpret_cast<const double2*>(p));
+  return mk<double>(v.x, v.y);
+}
+
+// exp(a * (dre + i dim)) for real a: the nonlinear / potential phase factor
+// of the split step, with complex time step dt = i*ddt/(1 + i*gamma).
+__device__ __forceinline__ cx<float> cexp_real_times(float a, float dre, float dim) {
+  float s, c;
+  sincosf(a * dim, &s, &c);
+  float m = (dre == 0.0f) ? 1.0f : expf(a * dre);
+  return mk<float>(m * c, m * s);
+}
+__device__ __forceinline__ cx<double> cexp_real_times(double a, double dre, double dim) {
+  double s, c;
+  sincos(a * dim, &s, &c);
+  double m = (dre == 0.0) ? 1.0 : exp(a * dre);
+  return mk<double>(m * c, m * s);
+}
+__device__ __forceinline__ float rexp(float a) { return expf(a); }
+__device__ __forceinline__ double rexp(double a) { return exp(a); }
+
+// Device-resident scalars of one solver context.  Everything that the
+// reference keeps in MATLAB scalars between array operations (mu, the renorm
+// factor, ncur, the ITP residual) lives here so that whole blocks of steps
+// run without a host round trip.
+struct DevScalars {
+  double scale;       // pending multiplicative factor of the stored state
+  double mu;          // chemical potential subtracted from V (VV = V - mu)
+  double ncur;        // integrate(|psi|^2) at the last block end / iteration
+  double muc;         // mu reported at the last block end
+  double NNN;         // target norm (NN0 or NN0*exp(-t/tau))
+  double NN0;
+  double delta;       // last ITP residual
+  double best_delta;  // smallest residual seen in the current ITP phase
+  double mu_itp;      // last MU(i)
+  double mu2, ee;     // last MU2(i), EE(i) before division by Ntotal
+  double maxabs;      // max |psi| at the last ITP check
+  double dtmin;       // groundstate_itp.m:35,63-65
+  double sums[8];     // last finalized sums (see Slot), weighted by the cell volume
+  int stop;           // nonzero: pass kernels and finalizers do nothing
+  int iter;           // ITP iterations completed
+  int stall;          // ITP checks in a row without a 10% residual drop
+  int status;         // StopReason
+  int nonfinite;      // a reduction produced NaN/Inf
+  int pad_[3];
+};
+
+enum StopReason { RUNNING = 0, CONVERGED = 1, SWITCH_FP64 = 2, HALVE_DT = 3, NONFINITE = 4 };
+
+// Reduction slots of the per-CTA partial-sum buffer.
+enum Slot {
+  S_N = 0,     // sum |psi|^2
+  S_VN = 1,    // sum V |psi|^2
+  S_N2 = 2,    // sum |psi|^4
+  S_KX = 3,    // sum over x pencils of (1/nx) sum_k kx^2/2 |psi_hat|^2
+  S_KY = 4,
+  S_KZ = 5,
+  S_MAXD = 6,  // max | |psi| - |psi_prev| |
+  S_MAXA = 7,  // max |psi|
+  NSLOTS = 8
+};
+
+// Prologue applied right after a pencil is loaded (first axis pass).
+enum Prologue {
+  PRO_NONE = 0,
+  PRO_SCALE = 1,    // psi *= scale
+  PRO_RT_HALF = 2,  // psi = exp((-VV - g|s psi|^2) dt/2) s psi   (solve_split.m:55-56)
+  PRO_RT_FULL = 3,  // psi = exp((-VV - g|psi|^2) dt) psi         (solve_split.m:60-61)
+  PRO_ITP = 4       // nl = exp(-dt/2 (g|s psi|^2 + V)); aux = nl; psi = nl s psi
+                    // (groundstate_itp.m:36/76 then :40)
+};
+// Epilogue applied before a pencil is stored (last axis pass).
+enum Epilogue {
+  EPI_NONE = 0,
+  EPI_RT_END = 1,  // full NL, inverse half NL, sums n, Vn, n^2 (solve_split.m:60-67)
+  EPI_ITP = 2      // psi *= aux, sum n (groundstate_itp.m:42-44)
+};
+
+enum PassKind { KIND_STEP = 0, KIND_ENERGY = 1 };
+
+template <typename R>
+struct PassArgs {
+  cx<R>* psi;              // state, updated in place
+  const R* V;              // total potential V(t)
+  R* aux;                  // ITP: nonlinear factor written by pass 1, read by the last
+  const cx<R>* phase;      // kinetic factor exp(-k^2/2 dt)/N of this axis (length N)
+  const cx<R>* tw;         // twiddles exp(-2 pi i q/N), q < N
+  const R* k2h;            // k^2/2 of this axis divided by N (energy pass)
+  double* partials;        // [NSLOTS][cap] per-CTA partial sums
+  DevScalars* sc;
+  long long n_batch;       // number of pencils
+  long long stride;        // element stride along the axis
+  long long inner, outer;  // pencil b starts at (b % inner) + (b / inner) * outer
+  int cap;                 // partials capacity per slot
+  int kind;                // PassKind
+  int pro, epi;            // Prologue / Epilogue
+  int kin_slot;            // energy pass: slot of the kinetic sum
+  int energy_pot;          // energy pass: also accumulate n, Vn, n^2
+  double g;                // coupling
+  double dre, dim;         // time step (real, imag) of the phase factors
+};
+
+}  // namespace gpe

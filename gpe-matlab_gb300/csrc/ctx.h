@@ -1,0 +1,77 @@
+// ctx.h - the solver context behind the gpe_ctx handle of include/gpe.h.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gpe.h"
+#include "aux_kernels.cuh"
+#include "pass.cuh"
+
+namespace gpe {
+
+// Device arrays of one precision (the context's own, or the FP64 polish
+// copy of an FP32 context).
+struct Field {
+  int prec = 0;             // GPE_FP32 / GPE_FP64
+  void* psi = nullptr;      // P complex
+  void* V = nullptr;        // P real
+  void* aux = nullptr;      // P real: ITP nonlinear factor
+  void* absprev = nullptr;  // P real: |psi| at the previous ITP check
+  void* tw[3] = {nullptr, nullptr, nullptr};     // per axis, N complex
+  void* phase[3] = {nullptr, nullptr, nullptr};  // per axis, N complex
+  void* k2h[3] = {nullptr, nullptr, nullptr};    // per axis, N real
+  double phase_dt[2] = {0.0, 0.0};               // dt the phase tables hold
+  bool phase_valid = false;
+  bool V_valid = false;
+};
+
+struct ProfRec {
+  int cls;
+  cudaEvent_t a, b;
+};
+
+struct ProfClass {
+  std::string name;
+  long long launches = 0;
+  double total_ms = 0.0;
+  double bytes = 0.0;
+};
+
+}  // namespace gpe
+
+struct gpe_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int ndims = 2;
+  int n[3] = {1, 1, 1};  // nx, ny, nz
+  double dx[3] = {1, 1, 1}, span[3] = {1, 1, 1};
+  long long P = 0;
+  double weight = 1.0;
+  int prec = GPE_FP64;
+  gpe_params prm{};
+  gpe_current cur{};
+  std::vector<double> hist_mu, hist_n;
+
+  gpe::Field main, polish;  // polish: FP64 field of an FP32 context
+  double* V64 = nullptr;    // FP64 copy of V (upload staging; polish potential)
+  bool have_V = false, have_state = false;
+  double* partials = nullptr;
+  int cap = 0;
+  gpe::DevScalars* sc = nullptr;      // device
+  gpe::DevScalars* sc_host = nullptr; // pinned, 2 slots
+  double* d_hist = nullptr;           // device history scratch
+  size_t d_hist_len = 0;
+  double* pinned_V[2] = {nullptr, nullptr};
+  cudaEvent_t ev_V[2] = {nullptr, nullptr};
+  cudaEvent_t ev_sc[2] = {nullptr, nullptr};
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  std::string err;
+
+  bool prof = false;
+  std::vector<gpe::ProfRec> prof_pending;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<gpe::ProfClass> prof_classes;
+  long long launches = 0;
+};

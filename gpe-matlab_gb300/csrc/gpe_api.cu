@@ -1,0 +1,1212 @@
+// gpe_api.cu - C ABI of libgpe (include/gpe.h): context, data movement and
+// the host drivers of GPEtask.groundstate_itp / GPEtask.solve_split.
+//
+// The drivers enqueue every kernel of a run on the context stream and keep
+// the reference's scalar bookkeeping (norms, mu, the ITP residual) in device
+// memory, so the host only synchronises where the reference's semantics need
+// a host decision: at ITP convergence checks (one check interval behind the
+// device, the kernels of speculatively enqueued iterations return at once
+// once a finalizer has stopped the run), at outer-step callbacks, and when a
+// time-dependent potential is evaluated on the host.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "ctx.h"
+
+using namespace gpe;
+
+namespace {
+
+thread_local std::string g_create_err;
+
+gpe_status fail(gpe_ctx* c, gpe_status st, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_create_err = msg;
+  return st;
+}
+
+#define CU(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(c, GPE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define CHECK(st)                  \
+  do {                             \
+    gpe_status s_ = (st);          \
+    if (s_ != GPE_OK) return s_;   \
+  } while (0)
+
+bool supported_n(int n) {
+  switch (n) {
+#define X(v) case v:
+    GPE_FOR_EACH_N(X)
+#undef X
+    return true;
+    default:
+      return false;
+  }
+}
+
+template <typename R>
+cudaError_t dispatch_pass(int N, const PassArgs<R>& a, bool strided, cudaStream_t s) {
+  switch (N) {
+#define X(v) \
+  case v:    \
+    return launch_pass<R, v>(a, strided, s);
+    GPE_FOR_EACH_N(X)
+#undef X
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename R>
+PassGeom dispatch_geom(int N, bool strided) {
+  switch (N) {
+#define X(v) \
+  case v:    \
+    return pass_geom<R, v>(strided);
+    GPE_FOR_EACH_N(X)
+#undef X
+  }
+  return PassGeom{0, 1, 0};
+}
+
+struct AxisPass {
+  int axis;  // 0 = x, 1 = y, 2 = z
+  int N;
+  bool strided;
+  long long n_batch, stride, inner, outer;
+};
+
+// Pass order: y (contiguous, carries the prologue), x, then z (3D).  The
+// last pass carries the epilogue.
+std::vector<AxisPass> axis_passes(const gpe_ctx* c) {
+  const long long nx = c->n[0], ny = c->n[1], nz = c->ndims == 3 ? c->n[2] : 1;
+  std::vector<AxisPass> v;
+  v.push_back({1, (int)ny, false, nx * nz, 1, 1, 0});
+  v.push_back({0, (int)nx, true, ny * nz, ny, ny, nx * ny});
+  if (c->ndims == 3) v.push_back({2, (int)nz, true, nx * ny, nx * ny, nx * ny, 0});
+  return v;
+}
+
+template <typename R>
+long long pass_blocks(const AxisPass& p) {
+  PassGeom g = dispatch_geom<R>(p.N, p.strided);
+  return (p.n_batch + g.ffts - 1) / g.ffts;
+}
+
+template <typename R>
+size_t rsize() {
+  return sizeof(R);
+}
+
+// ---- profiling --------------------------------------------------------------
+enum ProfCls {
+  PC_PASS_Y, PC_PASS_X, PC_PASS_Z, PC_ENERGY_Y, PC_ENERGY_X, PC_ENERGY_Z, PC_FINALIZE, PC_ITP_CHECK,
+  PC_NORM, PC_ELEMENTWISE, PC_COUNT
+};
+const char* kProfNames[PC_COUNT] = {"pass_y",   "pass_x",    "pass_z",    "energy_y",
+                                    "energy_x", "energy_z",  "finalize",  "itp_check",
+                                    "norm",     "elementwise"};
+
+cudaEvent_t pool_event(gpe_ctx* c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+struct Launch {
+  gpe_ctx* c;
+  int cls;
+  double bytes;
+  cudaEvent_t a = nullptr;
+  Launch(gpe_ctx* c_, int cls_, double bytes_) : c(c_), cls(cls_), bytes(bytes_) {
+    c->launches++;
+    if (c->prof) {
+      a = pool_event(c);
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~Launch() {
+    if (c->prof) {
+      cudaEvent_t b = pool_event(c);
+      cudaEventRecord(b, c->stream);
+      c->prof_pending.push_back({cls, a, b});
+      c->prof_classes[cls].bytes += bytes;
+    }
+  }
+};
+
+// ---- tables -------------------------------------------------------------------
+double kval(const gpe_ctx* c, int axis, int p) {
+  const int N = c->n[axis];
+  const int q = (p <= N / 2) ? p : p - N;  // [0:n/2, -(n/2-1):-1], init.m:27
+  return q * 2.0 * M_PI / (c->span[axis] + c->dx[axis]);
+}
+
+// FP32 rounding of a table entry z that keeps |z| as exact as the format
+// allows: among the float pairs within 2 ulps of (Re z, Im z) whose angle is
+// within about an ulp of arg z, take the one whose squared modulus is
+// closest to |z|^2.  Independent rounding of both parts leaves |z| off by up
+// to ~1e-7 with a fixed sign per entry, which a kinetic factor applied every
+// step turns into a norm drift.
+void round_pair_f32(std::complex<double> z, float* a, float* b) {
+  const float a0 = (float)z.real(), b0 = (float)z.imag();
+  const double m2 = std::norm(z), ang = std::arg(z);
+  const double amax = 1.5e-7;
+  double best = INFINITY;
+  *a = a0;
+  *b = b0;
+  float ca = a0;
+  for (int i = 0; i < 2; ++i) ca = std::nextafter(ca, -INFINITY);
+  for (int i = -2; i <= 2; ++i, ca = std::nextafter(ca, INFINITY)) {
+    float cb = b0;
+    for (int j = 0; j < 2; ++j) cb = std::nextafter(cb, -INFINITY);
+    for (int j = -2; j <= 2; ++j, cb = std::nextafter(cb, INFINITY)) {
+      const double da = (double)ca, db = (double)cb;
+      if (m2 > 0 && std::fabs(std::remainder(std::atan2(db, da) - ang, 2 * M_PI)) > amax) continue;
+      const double err = std::fabs(da * da + db * db - m2);
+      if (err < best) {
+        best = err;
+        *a = ca;
+        *b = cb;
+      }
+    }
+  }
+}
+
+template <typename R>
+gpe_status upload_cx(gpe_ctx* c, void* dst, const std::vector<std::complex<double>>& v) {
+  std::vector<R> h(2 * v.size());
+  for (size_t i = 0; i < v.size(); ++i) {
+    if constexpr (sizeof(R) == 4) {
+      float a, b;
+      round_pair_f32(v[i], &a, &b);
+      h[2 * i] = a;
+      h[2 * i + 1] = b;
+    } else {
+      h[2 * i] = (R)v[i].real();
+      h[2 * i + 1] = (R)v[i].imag();
+    }
+  }
+  CU(cudaMemcpy(dst, h.data(), h.size() * sizeof(R), cudaMemcpyHostToDevice));
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status build_static_tables(gpe_ctx* c, Field& f) {
+  const int na = c->ndims;
+  for (int ax = 0; ax < na; ++ax) {
+    const int N = c->n[ax];
+    CU(cudaMalloc(&f.tw[ax], N * 2 * sizeof(R)));
+    CU(cudaMalloc(&f.phase[ax], N * 2 * sizeof(R)));
+    CU(cudaMalloc(&f.k2h[ax], N * sizeof(R)));
+    std::vector<std::complex<double>> tw(N);
+    for (int q = 0; q < N; ++q) {
+      const double ang = 2.0 * M_PI * (double)q / (double)N;
+      tw[q] = std::complex<double>(std::cos(ang), -std::sin(ang));
+    }
+    CHECK(upload_cx<R>(c, f.tw[ax], tw));
+    std::vector<R> k2(N);
+    for (int p = 0; p < N; ++p) {
+      const double k = kval(c, ax, p);
+      k2[p] = (R)(k * k / 2.0 / N);
+    }
+    CU(cudaMemcpy(f.k2h[ax], k2.data(), N * sizeof(R), cudaMemcpyHostToDevice));
+  }
+  f.phase_valid = false;
+  return GPE_OK;
+}
+
+// kinop = exp(-kk*dt) (set_kinop.m:9), as one factor per axis with the 1/N of
+// ifft folded in: exp(-k^2/2*dt)/N, dt = dre + i*dim, evaluated in FP64.
+template <typename R>
+gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
+  if (f.phase_valid && f.phase_dt[0] == dre && f.phase_dt[1] == dim) return GPE_OK;
+  for (int ax = 0; ax < c->ndims; ++ax) {
+    const int N = c->n[ax];
+    std::vector<std::complex<double>> ph(N);
+    for (int p = 0; p < N; ++p) {
+      const double k = kval(c, ax, p);
+      const double kk = k * k / 2.0;
+      const double mag = std::exp(-kk * dre) / N;
+      ph[p] = std::complex<double>(mag * std::cos(kk * dim), -mag * std::sin(kk * dim));
+    }
+    CHECK(upload_cx<R>(c, f.phase[ax], ph));
+  }
+  f.phase_dt[0] = dre;
+  f.phase_dt[1] = dim;
+  f.phase_valid = true;
+  return GPE_OK;
+}
+
+// ---- field allocation -----------------------------------------------------------
+template <typename R>
+gpe_status alloc_field(gpe_ctx* c, Field& f, int prec, bool share_V64) {
+  f.prec = prec;
+  CU(cudaMalloc(&f.psi, (size_t)c->P * 2 * sizeof(R)));
+  if (share_V64) {
+    f.V = c->V64;
+  } else {
+    CU(cudaMalloc(&f.V, (size_t)c->P * sizeof(R)));
+  }
+  return build_static_tables<R>(c, f);
+}
+
+template <typename R>
+gpe_status ensure_itp_buffers(gpe_ctx* c, Field& f) {
+  if (!f.aux) CU(cudaMalloc(&f.aux, (size_t)c->P * sizeof(R)));
+  if (!f.absprev) CU(cudaMalloc(&f.absprev, (size_t)c->P * sizeof(R)));
+  return GPE_OK;
+}
+
+void free_field(Field& f, const double* V64) {
+  cudaFree(f.psi);
+  if (f.V != (void*)V64) cudaFree(f.V);
+  cudaFree(f.aux);
+  cudaFree(f.absprev);
+  for (int i = 0; i < 3; ++i) {
+    cudaFree(f.tw[i]);
+    cudaFree(f.phase[i]);
+    cudaFree(f.k2h[i]);
+  }
+  f = Field();
+}
+
+// FP64 polish field of an FP32 context (shares V64 as its potential).
+gpe_status ensure_polish(gpe_ctx* c) {
+  if (c->polish.psi) return GPE_OK;
+  CHECK(alloc_field<double>(c, c->polish, GPE_FP64, true));
+  c->polish.V_valid = true;
+  return ensure_itp_buffers<double>(c, c->polish);
+}
+
+// ---- scalar helpers ---------------------------------------------------------------
+gpe_status read_scalars(gpe_ctx* c, DevScalars* out) {
+  CU(cudaMemcpyAsync(&c->sc_host[0], c->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  *out = c->sc_host[0];
+  return GPE_OK;
+}
+
+gpe_status write_scalars(gpe_ctx* c, const DevScalars& v) {
+  c->sc_host[1] = v;
+  CU(cudaMemcpyAsync(c->sc, &c->sc_host[1], sizeof(DevScalars), cudaMemcpyHostToDevice, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  return GPE_OK;
+}
+
+// ---- passes ---------------------------------------------------------------------
+template <typename R>
+gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro, int epi, int energy_pot,
+                    double dre, double dim, int* nblk) {
+  PassArgs<R> a;
+  a.psi = (cx<R>*)f.psi;
+  a.V = (const R*)f.V;
+  a.aux = (R*)f.aux;
+  a.phase = (const cx<R>*)f.phase[ap.axis];
+  a.tw = (const cx<R>*)f.tw[ap.axis];
+  a.k2h = (const R*)f.k2h[ap.axis];
+  a.partials = c->partials;
+  a.sc = c->sc;
+  a.n_batch = ap.n_batch;
+  a.stride = ap.stride;
+  a.inner = ap.inner;
+  a.outer = ap.outer;
+  a.cap = c->cap;
+  a.kind = kind;
+  a.pro = pro;
+  a.epi = epi;
+  a.kin_slot = S_KX + ap.axis;
+  a.energy_pot = energy_pot;
+  a.g = c->prm.g;
+  a.dre = dre;
+  a.dim = dim;
+  const double P = (double)c->P;
+  double bytes = (kind == KIND_ENERGY ? 1.0 : 2.0) * P * 2 * sizeof(R);
+  const bool useV = pro == PRO_RT_HALF || pro == PRO_RT_FULL || pro == PRO_ITP || epi == EPI_RT_END ||
+                    (kind == KIND_ENERGY && energy_pot);
+  if (useV) bytes += P * sizeof(R);
+  if (pro == PRO_ITP || epi == EPI_ITP) bytes += P * sizeof(R);
+  int cls = (kind == KIND_ENERGY ? PC_ENERGY_Y : PC_PASS_Y);
+  cls += (ap.axis == 1 ? 0 : ap.axis == 0 ? 1 : 2);
+  if (nblk) *nblk = (int)pass_blocks<R>(ap);
+  {
+    Launch L(c, cls, bytes);
+    CU(dispatch_pass<R>(ap.N, a, ap.strided, c->stream));
+  }
+  return GPE_OK;
+}
+
+// Kinetic-energy passes (one forward FFT per axis); with `pot`, the y pass
+// also sums n, Vn, n^2 and every pass applies the pending scale.
+template <typename R>
+gpe_status energy_passes(gpe_ctx* c, Field& f, bool pot, int nblk_kin[3], int* nblk_pot) {
+  auto passes = axis_passes(c);
+  nblk_kin[0] = nblk_kin[1] = nblk_kin[2] = 0;
+  for (auto& ap : passes) {
+    int nb = 0;
+    const bool ep = pot && ap.axis == 1;
+    CHECK(run_pass<R>(c, f, ap, KIND_ENERGY, pot ? PRO_SCALE : PRO_NONE, EPI_NONE, ep ? 1 : 0, 0.0, 0.0, &nb));
+    nblk_kin[ap.axis] = nb;
+    if (ep && nblk_pot) *nblk_pot = nb;
+  }
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status observables_impl(gpe_ctx* c, Field& f, double div, int set_mu, DevScalars* out) {
+  int nk[3], np = 0;
+  CHECK(energy_passes<R>(c, f, true, nk, &np));
+  ObsFinalArgs a{c->partials, c->cap, np, {nk[0], nk[1], nk[2]}, c->weight, c->prm.g, div, set_mu,
+                 c->prm.mu_init};
+  {
+    Launch L(c, PC_FINALIZE, 0);
+    launch_finalize_obs(a, c->sc, c->stream);
+    CU(cudaGetLastError());
+  }
+  if (out) CHECK(read_scalars(c, out));
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status norm_impl(gpe_ctx* c, Field& f, double Ntotal) {
+  int nb;
+  {
+    Launch L(c, PC_NORM, (double)c->P * 2 * sizeof(R));
+    nb = launch_norm<R>((const cx<R>*)f.psi, c->P, c->sc, c->partials, c->cap, c->stream);
+    CU(cudaGetLastError());
+  }
+  {
+    Launch L(c, PC_FINALIZE, 0);
+    launch_finalize_norm0(c->partials, c->cap, nb, c->weight, Ntotal, c->sc, c->stream);
+    CU(cudaGetLastError());
+  }
+  return GPE_OK;
+}
+
+// ---- groundstate_itp ------------------------------------------------------------
+struct ItpState {
+  double dt;
+  int i;  // iterations completed
+};
+
+template <typename R>
+gpe_status itp_iteration(gpe_ctx* c, Field& f, double dt, int i) {
+  auto passes = axis_passes(c);
+  int nb = 0;
+  for (size_t k = 0; k < passes.size(); ++k) {
+    const bool first = k == 0, last = k + 1 == passes.size();
+    CHECK(run_pass<R>(c, f, passes[k], KIND_STEP, first ? PRO_ITP : PRO_NONE, last ? EPI_ITP : EPI_NONE, 0,
+                      dt, 0.0, last ? &nb : nullptr));
+  }
+  ItpFinalArgs a{c->partials, c->cap, nb, c->weight, dt, c->prm.Ntotal, c->prm.mu_init, i, c->d_hist};
+  Launch L(c, PC_FINALIZE, 0);
+  launch_finalize_itp(a, c->sc, c->stream);
+  CU(cudaGetLastError());
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status itp_check(gpe_ctx* c, Field& f, const gpe_itp_params* prm, double dt, int i, bool fp32_phase) {
+  const bool want = prm->want_mu2 || prm->want_energy;
+  int nk[3] = {0, 0, 0}, np = 0;
+  if (want) CHECK(energy_passes<R>(c, f, true, nk, &np));
+  int nbc;
+  {
+    Launch L(c, PC_ITP_CHECK, (double)c->P * (2 * sizeof(R) + 2 * sizeof(R)));
+    nbc = launch_itp_check<R>((const cx<R>*)f.psi, (R*)f.absprev, c->P, c->sc, c->partials, c->cap,
+                              c->stream);
+    CU(cudaGetLastError());
+  }
+  const int maxit = c->prm.itp_max_iter;
+  CheckFinalArgs a;
+  a.partials = c->partials;
+  a.cap = c->cap;
+  a.nblk_check = nbc;
+  a.nblk_pot = want ? np : 0;
+  a.nblk_kin[0] = nk[0];
+  a.nblk_kin[1] = nk[1];
+  a.nblk_kin[2] = nk[2];
+  a.weight = c->weight;
+  a.g = c->prm.g;
+  a.dt = dt;
+  a.eps = prm->eps;
+  a.nnn = c->prm.Ntotal > 0 ? c->prm.Ntotal : 1.0;
+  a.iter = i;
+  a.want_mu2 = prm->want_mu2;
+  a.adjust = c->prm.itp_adjust_stepsize;
+  a.fp32_phase = fp32_phase ? 1 : 0;
+  a.switch_delta = prm->switch_delta > 0 ? prm->switch_delta : 2e-4;
+  a.MU = c->d_hist;
+  a.MU2 = c->d_hist + maxit;
+  a.EE = c->d_hist + 2 * (size_t)maxit;
+  Launch L(c, PC_FINALIZE, 0);
+  launch_finalize_check(a, c->sc, c->stream);
+  CU(cudaGetLastError());
+  return GPE_OK;
+}
+
+// Runs iterations in one precision until a finalizer stops the run or
+// itp_max_iter is reached.  Returns the stop reason in *reason.
+template <typename R>
+gpe_status itp_phase(gpe_ctx* c, Field& f, const gpe_itp_params* prm, ItpState& st, bool fp32_phase,
+                     int* reason) {
+  CHECK(set_kinop<R>(c, f, st.dt, 0.0));
+  const int maxit = c->prm.itp_max_iter, minit = c->prm.itp_min_iter;
+  const bool adjust = c->prm.itp_adjust_stepsize != 0;
+  int slot = 0, prev = -1;
+  int i = st.i;
+  *reason = RUNNING;
+  bool stopped = false;
+  while (i < maxit && !stopped) {
+    ++i;
+    CHECK(itp_iteration<R>(c, f, st.dt, i));
+    if (i > minit && i % 10 == 0) {
+      CHECK(itp_check<R>(c, f, prm, st.dt, i, fp32_phase));
+      CU(cudaMemcpyAsync(&c->sc_host[slot], c->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, c->stream));
+      CU(cudaEventRecord(c->ev_sc[slot], c->stream));
+      if (adjust) {
+        CU(cudaEventSynchronize(c->ev_sc[slot]));
+        const DevScalars& h = c->sc_host[slot];
+        if (h.stop) {
+          if (h.status == HALVE_DT) {  // groundstate_itp.m:68-71
+            st.dt /= 2;
+            CHECK(set_kinop<R>(c, f, st.dt, 0.0));
+            DevScalars v = h;
+            v.stop = 0;
+            v.status = RUNNING;
+            CHECK(write_scalars(c, v));
+          } else {
+            stopped = true;
+          }
+        }
+      } else {
+        // Look one check interval behind: the GPU keeps running meanwhile.
+        if (prev >= 0) {
+          CU(cudaEventSynchronize(c->ev_sc[prev]));
+          if (c->sc_host[prev].stop) stopped = true;
+        }
+        prev = slot;
+        slot ^= 1;
+      }
+    }
+  }
+  DevScalars h;
+  CHECK(read_scalars(c, &h));
+  st.i = h.iter;
+  *reason = h.stop ? h.status : RUNNING;
+  if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "groundstate_itp: non-finite norm or residual");
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* MU2, double* EE, int cap,
+                    gpe_itp_result* res) {
+  Field& f = c->main;
+  const int maxit = c->prm.itp_max_iter;
+  CHECK(ensure_itp_buffers<R>(c, f));
+  if (c->d_hist_len < 3 * (size_t)maxit) {
+    cudaFree(c->d_hist);
+    c->d_hist = nullptr;
+    CU(cudaMalloc(&c->d_hist, 3 * (size_t)maxit * sizeof(double)));
+    c->d_hist_len = 3 * (size_t)maxit;
+  }
+  CU(cudaMemsetAsync(c->d_hist, 0, 3 * (size_t)maxit * sizeof(double), c->stream));
+  // Reset the run scalars; dtmin = sqrt(eps) (groundstate_itp.m:35).
+  DevScalars s0;
+  CHECK(read_scalars(c, &s0));
+  s0.stop = 0;
+  s0.status = RUNNING;
+  s0.nonfinite = 0;
+  s0.iter = 0;
+  s0.stall = 0;
+  s0.best_delta = INFINITY;
+  s0.dtmin = std::sqrt(prm->eps);
+  CHECK(write_scalars(c, s0));
+  // process_init_state (GPEtask.m:159-160) and current_state = phi (:28).
+  CHECK(norm_impl<R>(c, f, c->prm.Ntotal));
+  {
+    Launch L(c, PC_ELEMENTWISE, (double)c->P * 3 * sizeof(R));
+    launch_abs_init<R>((const cx<R>*)f.psi, (R*)f.absprev, c->P, c->sc, c->stream);
+    CU(cudaGetLastError());
+  }
+  ItpState st{prm->dt, 0};
+  int reason = RUNNING;
+  int fp32_iters = 0;
+  const bool polish = (c->prec == GPE_FP32) && prm->fp64_polish;
+  CHECK(itp_phase<R>(c, f, prm, st, polish, &reason));
+  if (polish && reason == SWITCH_FP64 && st.i < maxit) {
+    fp32_iters = st.i;
+    CHECK(ensure_polish(c));
+    Field& p = c->polish;
+    {
+      Launch L(c, PC_ELEMENTWISE, (double)c->P * 24);
+      launch_convert_cx<R, double>((const cx<R>*)f.psi, (cx<double>*)p.psi, c->P, c->sc, c->stream);
+      launch_convert_re<R, double>((const R*)f.absprev, (double*)p.absprev, c->P, c->stream);
+      launch_set_scale_one(c->sc, c->stream);
+      launch_reset_scalars(c->sc, c->stream);
+      CU(cudaGetLastError());
+    }
+    CHECK(itp_phase<double>(c, p, prm, st, false, &reason));
+    {
+      Launch L(c, PC_ELEMENTWISE, (double)c->P * 24);
+      launch_convert_cx<double, R>((const cx<double>*)p.psi, (cx<R>*)f.psi, c->P, c->sc, c->stream);
+      launch_set_scale_one(c->sc, c->stream);
+      CU(cudaGetLastError());
+    }
+  } else if (polish) {
+    fp32_iters = st.i;
+  }
+  DevScalars h;
+  CHECK(read_scalars(c, &h));
+  launch_reset_scalars(c->sc, c->stream);
+  CU(cudaGetLastError());
+  const int iters = st.i;
+  std::vector<double> hist(3 * (size_t)maxit);
+  CU(cudaMemcpy(hist.data(), c->d_hist, hist.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  const double* hMU = hist.data();
+  const double* hMU2 = hist.data() + maxit;
+  const double* hEE = hist.data() + 2 * (size_t)maxit;
+  const int ncopy = std::min(iters, cap);
+  const bool pos = c->prm.Ntotal > 0;
+  for (int k = 0; k < ncopy; ++k) {
+    if (MU) MU[k] = hMU[k];
+    if (MU2) MU2[k] = pos ? hMU2[k] / c->prm.Ntotal : hMU2[k] / hMU[k];
+    if (EE) EE[k] = pos ? hEE[k] / c->prm.Ntotal : hEE[k] / hMU[k];
+  }
+  if (iters > 0) {  // groundstate_itp.m:84-109
+    if (pos) {
+      c->cur.current_mu = hMU[iters - 1];
+      c->cur.current_n = c->prm.Ntotal;
+    } else if (prm->want_mu2) {
+      c->cur.current_mu = hMU2[iters - 1] / hMU[iters - 1];
+      c->cur.current_n = hMU[iters - 1];
+    }
+  }
+  if (res) {
+    res->iters = iters;
+    res->converged = reason == CONVERGED;
+    res->fp32_iters = fp32_iters;
+    res->final_dt = st.dt;
+    res->last_delta = h.delta;
+  }
+  if (reason == RUNNING && iters >= maxit)
+    c->err = "groundstate_itp: Convergence not reached";  // groundstate_itp.m:79 (a warning)
+  return GPE_OK;
+}
+
+// ---- solve_split -----------------------------------------------------------------
+template <typename R>
+gpe_status upload_V_double(gpe_ctx* c, const double* hostV, bool async_pinned) {
+  const size_t bytes = (size_t)c->P * sizeof(double);
+  CU(cudaMemcpyAsync(c->V64, hostV, bytes, cudaMemcpyHostToDevice, c->stream));
+  if (c->prec == GPE_FP32) {
+    Launch L(c, PC_ELEMENTWISE, (double)c->P * 12);
+    launch_convert_re<double, float>(c->V64, (float*)c->main.V, c->P, c->stream);
+    CU(cudaGetLastError());
+  }
+  if (!async_pinned) CU(cudaStreamSynchronize(c->stream));
+  c->main.V_valid = true;
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status vtd_upload(gpe_ctx* c, const gpe_split_params* prm, double time, int& k) {
+  const size_t bytes = (size_t)c->P * sizeof(double);
+  if (!c->pinned_V[k]) CU(cudaMallocHost(&c->pinned_V[k], bytes));
+  CU(cudaEventSynchronize(c->ev_V[k]));  // the previous copy out of this buffer is done
+  if (prm->vtd(prm->vtd_user, time, c->pinned_V[k]) != 0)
+    return fail(c, GPE_ERR_CALLBACK, "solve_split: potential callback failed");
+  CHECK(upload_V_double<R>(c, c->pinned_V[k], true));
+  CU(cudaEventRecord(c->ev_V[k], c->stream));
+  k ^= 1;
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
+  Field& f = c->main;
+  const double ddt = prm->ddt;
+  const double gam = c->prm.gamma;
+  int n_rec = c->prm.n_recalc;
+  if (n_rec < 1) return fail(c, GPE_ERR_INVALID, "n_recalc must be >= 1");
+  if (prm->niter_inner < 1) return fail(c, GPE_ERR_INVALID, "niter_inner must be >= 1");
+  if (prm->niter_inner % n_rec != 0) n_rec = 1;  // solve_split.m:25-27
+  const int start = c->cur.current_iter;
+  const int nout = prm->niter_outer;
+  // dt = ddt*1i/(1+1i*gam) (solve_split.m:31)
+  const std::complex<double> dtc = ddt * std::complex<double>(0.0, 1.0) / std::complex<double>(1.0, gam);
+  const double dre = dtc.real(), dim = dtc.imag();
+  CHECK(set_kinop<R>(c, f, dre, dim));
+  int vk = 0;
+  DevScalars s0;
+  CHECK(read_scalars(c, &s0));
+  // NN0 (solve_split.m:17-21)
+  double NN0 = c->prm.Ntotal;
+  if (!(NN0 > 0)) {
+    CHECK(norm_impl<R>(c, f, 0.0));
+    DevScalars h;
+    CHECK(read_scalars(c, &h));
+    NN0 = h.ncur;
+    s0 = h;
+  }
+  s0.stop = 0;
+  s0.status = RUNNING;
+  s0.nonfinite = 0;
+  s0.NN0 = NN0;
+  s0.NNN = NN0;
+  CHECK(write_scalars(c, s0));
+  // muc/mu at the start (solve_split.m:40-46): applyham at current_time.
+  if (prm->vtd) CHECK(vtd_upload<R>(c, prm, c->cur.current_time, vk));
+  CHECK(observables_impl<R>(c, f, NN0, 1, nullptr));
+  const bool feedback = gam > 0 && c->prm.mu_init == 0;
+  const double dt_outer = ddt * prm->niter_inner;
+  const int nb = prm->niter_inner / n_rec;
+  auto passes = axis_passes(c);
+  const int nsteps_out = std::max(0, nout - start);
+  std::vector<double> dh(3 * (size_t)std::max(1, nsteps_out), 0.0);
+  if (c->d_hist_len < dh.size()) {
+    cudaFree(c->d_hist);
+    c->d_hist = nullptr;
+    CU(cudaMalloc(&c->d_hist, dh.size() * sizeof(double)));
+    c->d_hist_len = dh.size();
+  }
+  CU(cudaMemsetAsync(c->d_hist, 0, dh.size() * sizeof(double), c->stream));
+  int last_j = start;
+  double last_time2 = c->cur.current_time;
+  bool stop_req = false;
+  for (int j = start + 1; j <= nout && !stop_req; ++j) {
+    const double time = (j - 1) * dt_outer;
+    double time2 = time;
+    for (int jj = 1; jj <= nb; ++jj) {
+      time2 = time + (jj - 1) * ddt * n_rec;  // solve_split.m:53
+      if (prm->vtd) CHECK(vtd_upload<R>(c, prm, time2, vk));
+      int nb_epi = 0;
+      for (int i = 1; i <= n_rec; ++i) {
+        for (size_t k = 0; k < passes.size(); ++k) {
+          const bool first = k == 0, last = k + 1 == passes.size();
+          const int pro = first ? (i == 1 ? PRO_RT_HALF : PRO_RT_FULL) : PRO_NONE;
+          const int epi = (last && i == n_rec) ? EPI_RT_END : EPI_NONE;
+          CHECK(run_pass<R>(c, f, passes[k], KIND_STEP, pro, epi, 0, dre, dim,
+                            (last && i == n_rec) ? &nb_epi : nullptr));
+        }
+      }
+      const bool need_mu = feedback || jj == nb;
+      int nk[3] = {0, 0, 0};
+      if (need_mu) CHECK(energy_passes<R>(c, f, false, nk, nullptr));
+      BlockFinalArgs a;
+      a.partials = c->partials;
+      a.cap = c->cap;
+      a.nblk_epi = nb_epi;
+      a.nblk_kin[0] = nk[0];
+      a.nblk_kin[1] = nk[1];
+      a.nblk_kin[2] = nk[2];
+      a.weight = c->weight;
+      a.g = c->prm.g;
+      a.feedback = feedback;
+      a.tau = c->prm.decay_rate;
+      a.time2 = time2;
+      const size_t hj = (size_t)(j - start - 1);
+      a.hist_mu = (jj == nb) ? c->d_hist + 3 * hj : nullptr;
+      a.hist_n = (jj == nb) ? c->d_hist + 3 * hj + 1 : nullptr;
+      a.hist_ok = nullptr;
+      Launch L(c, PC_FINALIZE, 0);
+      launch_finalize_block(a, c->sc, c->stream);
+      CU(cudaGetLastError());
+    }
+    last_j = j;
+    last_time2 = time2;
+    if (prm->on_step) {  // ext_callback (solve_split.m:80)
+      DevScalars h;
+      CHECK(read_scalars(c, &h));
+      if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
+      c->cur.current_iter = j;
+      c->cur.current_time = time2;
+      c->cur.current_mu = h.muc;
+      c->cur.current_n = h.ncur;
+      if ((int)c->hist_mu.size() < j) {
+        c->hist_mu.resize(j, 0.0);
+        c->hist_n.resize(j, 0.0);
+      }
+      c->hist_mu[j - 1] = h.muc;
+      c->hist_n[j - 1] = h.ncur;
+      if (prm->on_step(prm->step_user, j, time2, h.muc, h.ncur) != 0) stop_req = true;
+    }
+  }
+  DevScalars h;
+  CHECK(read_scalars(c, &h));
+  if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
+  if (last_j > start) {
+    CU(cudaMemcpy(dh.data(), c->d_hist, dh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if ((int)c->hist_mu.size() < last_j) {
+      c->hist_mu.resize(last_j, 0.0);
+      c->hist_n.resize(last_j, 0.0);
+    }
+    for (int j = start + 1; j <= last_j; ++j) {
+      c->hist_mu[j - 1] = dh[3 * (size_t)(j - start - 1)];
+      c->hist_n[j - 1] = dh[3 * (size_t)(j - start - 1) + 1];
+    }
+    c->cur.current_iter = last_j;
+    c->cur.current_time = last_time2;
+    c->cur.current_mu = h.muc;
+    c->cur.current_n = h.ncur;
+  }
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status materialize(gpe_ctx* c) {
+  Launch L(c, PC_ELEMENTWISE, (double)c->P * 4 * sizeof(R));
+  launch_apply_scale<R>((cx<R>*)c->main.psi, c->P, c->sc, c->stream);
+  launch_set_scale_one(c->sc, c->stream);
+  CU(cudaGetLastError());
+  return GPE_OK;
+}
+
+gpe_status check_ctx(gpe_ctx* c) {
+  if (!c) return fail(nullptr, GPE_ERR_INVALID, "null context");
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return fail(c, GPE_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  return GPE_OK;
+}
+
+gpe_status need_state(gpe_ctx* c) {
+  if (!c->have_state) return fail(c, GPE_ERR_STATE, "no state: call gpe_set_state first");
+  return GPE_OK;
+}
+gpe_status need_V(gpe_ctx* c) {
+  if (!c->have_V) return fail(c, GPE_ERR_STATE, "no potential: call gpe_set_potential first");
+  return GPE_OK;
+}
+
+// io staging (P complex doubles) for precision conversions of state copies.
+// The FP64 polish field's psi is idle outside groundstate_itp and is reused;
+// otherwise a temporary buffer is allocated (the caller frees it).
+gpe_status io_buffer(gpe_ctx* c, void** out) {
+  if (c->prec == GPE_FP32 && c->polish.psi) {
+    *out = c->polish.psi;
+    return GPE_OK;
+  }
+  void* p = nullptr;
+  CU(cudaMalloc(&p, (size_t)c->P * 16));
+  *out = p;
+  return GPE_OK;
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+int gpe_abi_version(void) { return GPE_ABI_VERSION; }
+
+int gpe_device_available(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return 0;
+  for (int d = 0; d < n; ++d) {
+    int maj = 0, min = 0;
+    cudaDeviceGetAttribute(&maj, cudaDevAttrComputeCapabilityMajor, d);
+    cudaDeviceGetAttribute(&min, cudaDevAttrComputeCapabilityMinor, d);
+    if (maj == 10 && min == 3) return 1;
+  }
+  return 0;
+}
+
+const char* gpe_last_error(const gpe_ctx* ctx) {
+  if (!ctx) return g_create_err.c_str();
+  return ctx->err.c_str();
+}
+
+void gpe_default_params(gpe_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->n_recalc = 10;
+  p->itp_max_iter = 5000;
+  p->itp_min_iter = 50;
+}
+
+gpe_status gpe_create(const gpe_grid_desc* d, gpe_ctx** out) {
+  gpe_ctx* c = nullptr;
+  if (!d || !out) return fail(nullptr, GPE_ERR_INVALID, "gpe_create: null argument");
+  *out = nullptr;
+  if (d->ndims != 2 && d->ndims != 3) return fail(nullptr, GPE_ERR_INVALID, "ndims must be 2 or 3");
+  if (d->precision != GPE_FP32 && d->precision != GPE_FP64)
+    return fail(nullptr, GPE_ERR_INVALID, "precision must be GPE_FP32 or GPE_FP64");
+  for (int a = 0; a < d->ndims; ++a) {
+    if (!supported_n(d->n[a]))
+      return fail(nullptr, GPE_ERR_UNSUPPORTED,
+                  "axis length " + std::to_string(d->n[a]) +
+                      " has no FFT plan (supported: even 2^a*3^b in 8..1024: 8 12 16 24 32 48 64 96 128 192 "
+                      "256 384 512 768 1024)");
+    if (!(d->dx[a] > 0) || !std::isfinite(d->dx[a]) || !std::isfinite(d->span[a]))
+      return fail(nullptr, GPE_ERR_INVALID, "dx must be positive and finite");
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+    return fail(nullptr, GPE_ERR_NO_DEVICE, "no CUDA device");
+  if (d->device < 0 || d->device >= ndev) return fail(nullptr, GPE_ERR_INVALID, "device ordinal out of range");
+  int maj = 0, min = 0;
+  cudaDeviceGetAttribute(&maj, cudaDevAttrComputeCapabilityMajor, d->device);
+  cudaDeviceGetAttribute(&min, cudaDevAttrComputeCapabilityMinor, d->device);
+  if (!(maj == 10 && min == 3))
+    return fail(nullptr, GPE_ERR_NO_DEVICE,
+                "libgpe is built for sm_103a (GB300); device is sm_" + std::to_string(maj * 10 + min));
+  c = new gpe_ctx();
+  c->device = d->device;
+  c->ndims = d->ndims;
+  for (int a = 0; a < 3; ++a) {
+    c->n[a] = (a < d->ndims) ? d->n[a] : 1;
+    c->dx[a] = (a < d->ndims) ? d->dx[a] : 1.0;
+    c->span[a] = (a < d->ndims) ? d->span[a] : 0.0;
+  }
+  c->P = (long long)c->n[0] * c->n[1] * c->n[2];
+  c->weight = c->dx[0] * c->dx[1] * (d->ndims == 3 ? c->dx[2] : 1.0);  // init.m:36, grid3d/init.m:83
+  c->prec = d->precision;
+  gpe_default_params(&c->prm);
+  c->main.prec = c->prec;
+  auto cleanup = [&](gpe_status st) {
+    std::string m = c->err;
+    gpe_destroy(c);
+    return fail(nullptr, st, m);
+  };
+  if (cudaSetDevice(c->device) != cudaSuccess) return cleanup(GPE_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    c->err = "cudaStreamCreate failed";
+    return cleanup(GPE_ERR_CUDA);
+  }
+  // partial-sum capacity: the largest grid of any pass in either precision
+  long long cap = 8LL * 1024;
+  for (auto& ap : axis_passes(c)) {
+    cap = std::max(cap, pass_blocks<float>(ap));
+    cap = std::max(cap, pass_blocks<double>(ap));
+  }
+  c->cap = (int)cap;
+  gpe_status st = GPE_OK;
+  if (cudaMalloc(&c->partials, (size_t)NSLOTS * c->cap * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->sc, sizeof(DevScalars)) != cudaSuccess ||
+      cudaMallocHost(&c->sc_host, 2 * sizeof(DevScalars)) != cudaSuccess ||
+      cudaMalloc(&c->V64, (size_t)c->P * sizeof(double)) != cudaSuccess) {
+    c->err = "device allocation failed";
+    return cleanup(GPE_ERR_ALLOC);
+  }
+  DevScalars z;
+  memset(&z, 0, sizeof(z));
+  z.scale = 1.0;
+  z.best_delta = INFINITY;
+  cudaMemcpy(c->sc, &z, sizeof(z), cudaMemcpyHostToDevice);
+  if (c->prec == GPE_FP32) st = alloc_field<float>(c, c->main, GPE_FP32, false);
+  else st = alloc_field<double>(c, c->main, GPE_FP64, true);
+  if (st != GPE_OK) return cleanup(st);
+  for (int k = 0; k < 2; ++k) {
+    cudaEventCreateWithFlags(&c->ev_V[k], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_sc[k], cudaEventDisableTiming);
+    cudaEventRecord(c->ev_V[k], c->stream);
+  }
+  cudaEventCreate(&c->t0);
+  cudaEventCreate(&c->t1);
+  c->prof_classes.resize(PC_COUNT);
+  for (int k = 0; k < PC_COUNT; ++k) c->prof_classes[k].name = kProfNames[k];
+  if (cudaGetLastError() != cudaSuccess) {
+    c->err = "CUDA error during context creation";
+    return cleanup(GPE_ERR_CUDA);
+  }
+  *out = c;
+  return GPE_OK;
+}
+
+void gpe_destroy(gpe_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_field(c->main, c->V64);
+  free_field(c->polish, c->V64);
+  cudaFree(c->V64);
+  cudaFree(c->partials);
+  cudaFree(c->sc);
+  cudaFree(c->d_hist);
+  if (c->sc_host) cudaFreeHost(c->sc_host);
+  for (int k = 0; k < 2; ++k) {
+    if (c->pinned_V[k]) cudaFreeHost(c->pinned_V[k]);
+    if (c->ev_V[k]) cudaEventDestroy(c->ev_V[k]);
+    if (c->ev_sc[k]) cudaEventDestroy(c->ev_sc[k]);
+  }
+  for (auto& r : c->prof_pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+gpe_status gpe_set_params(gpe_ctx* c, const gpe_params* p) {
+  CHECK(check_ctx(c));
+  if (!p) return fail(c, GPE_ERR_INVALID, "null params");
+  if (p->n_recalc < 1) return fail(c, GPE_ERR_INVALID, "n_recalc must be >= 1");
+  if (p->itp_max_iter < 1) return fail(c, GPE_ERR_INVALID, "itp_max_iter must be >= 1");
+  if (p->itp_min_iter < 0) return fail(c, GPE_ERR_INVALID, "itp_min_iter must be >= 0");
+  if (!std::isfinite(p->g) || !std::isfinite(p->gamma) || !std::isfinite(p->Ntotal) ||
+      !std::isfinite(p->mu_init) || !std::isfinite(p->decay_rate) || p->gamma < 0)
+    return fail(c, GPE_ERR_INVALID, "parameters must be finite, gamma >= 0");
+  c->prm = *p;
+  return GPE_OK;
+}
+
+gpe_status gpe_get_params(const gpe_ctx* c, gpe_params* p) {
+  if (!c || !p) return GPE_ERR_INVALID;
+  *p = c->prm;
+  return GPE_OK;
+}
+
+gpe_status gpe_get_current(const gpe_ctx* c, gpe_current* cur) {
+  if (!c || !cur) return GPE_ERR_INVALID;
+  *cur = c->cur;
+  return GPE_OK;
+}
+
+gpe_status gpe_set_current(gpe_ctx* c, const gpe_current* cur) {
+  CHECK(check_ctx(c));
+  if (!cur || cur->current_iter < 0) return fail(c, GPE_ERR_INVALID, "invalid current");
+  c->cur = *cur;
+  return GPE_OK;
+}
+
+gpe_status gpe_get_history(const gpe_ctx* c, double* mu, double* n, int cap, int* len) {
+  if (!c) return GPE_ERR_INVALID;
+  const int L = (int)c->hist_mu.size();
+  if (len) *len = L;
+  for (int k = 0; k < std::min(L, cap); ++k) {
+    if (mu) mu[k] = c->hist_mu[k];
+    if (n) n[k] = c->hist_n[k];
+  }
+  return GPE_OK;
+}
+
+gpe_status gpe_clear_history(gpe_ctx* c) {
+  CHECK(check_ctx(c));
+  c->hist_mu.clear();
+  c->hist_n.clear();
+  return GPE_OK;
+}
+
+gpe_status gpe_set_potential(gpe_ctx* c, const double* V) {
+  CHECK(check_ctx(c));
+  if (!V) return fail(c, GPE_ERR_INVALID, "null potential");
+  if (c->prec == GPE_FP32) CHECK(upload_V_double<float>(c, V, false));
+  else CHECK(upload_V_double<double>(c, V, false));
+  c->have_V = true;
+  return GPE_OK;
+}
+
+gpe_status gpe_set_potential_f32(gpe_ctx* c, const float* V) {
+  CHECK(check_ctx(c));
+  if (!V) return fail(c, GPE_ERR_INVALID, "null potential");
+  std::vector<double> tmp(V, V + c->P);
+  return gpe_set_potential(c, tmp.data());
+}
+
+static gpe_status set_state_any(gpe_ctx* c, const void* src, int src_prec, cudaMemcpyKind kind) {
+  CHECK(check_ctx(c));
+  if (!src) return fail(c, GPE_ERR_INVALID, "null state");
+  const size_t n = (size_t)c->P;
+  if (src_prec == c->prec) {
+    CU(cudaMemcpyAsync(c->main.psi, src, n * 2 * (src_prec == GPE_FP32 ? 4 : 8), kind, c->stream));
+  } else {
+    void* io = nullptr;
+    CHECK(io_buffer(c, &io));
+    CU(cudaMemcpyAsync(io, src, n * 2 * (src_prec == GPE_FP32 ? 4 : 8), kind, c->stream));
+    if (src_prec == GPE_FP64)
+      launch_convert_cx<double, float>((const cx<double>*)io, (cx<float>*)c->main.psi, c->P, nullptr, c->stream);
+    else
+      launch_convert_cx<float, double>((const cx<float>*)io, (cx<double>*)c->main.psi, c->P, nullptr, c->stream);
+    c->launches++;
+    CU(cudaStreamSynchronize(c->stream));
+    if (io != c->polish.psi) cudaFree(io);
+  }
+  launch_set_scale_one(c->sc, c->stream);
+  c->launches++;
+  CU(cudaStreamSynchronize(c->stream));
+  c->have_state = true;
+  return GPE_OK;
+}
+
+static gpe_status get_state_any(gpe_ctx* c, void* dst, int dst_prec, cudaMemcpyKind kind) {
+  CHECK(check_ctx(c));
+  CHECK(need_state(c));
+  if (!dst) return fail(c, GPE_ERR_INVALID, "null output");
+  const size_t n = (size_t)c->P;
+  if (c->prec == GPE_FP32) CHECK(materialize<float>(c));
+  else CHECK(materialize<double>(c));
+  if (dst_prec == c->prec) {
+    CU(cudaMemcpyAsync(dst, c->main.psi, n * 2 * (dst_prec == GPE_FP32 ? 4 : 8), kind, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+  } else {
+    void* io = nullptr;
+    CHECK(io_buffer(c, &io));
+    if (dst_prec == GPE_FP64)
+      launch_convert_cx<float, double>((const cx<float>*)c->main.psi, (cx<double>*)io, c->P, nullptr, c->stream);
+    else
+      launch_convert_cx<double, float>((const cx<double>*)c->main.psi, (cx<float>*)io, c->P, nullptr, c->stream);
+    c->launches++;
+    CU(cudaMemcpyAsync(dst, io, n * 2 * (dst_prec == GPE_FP32 ? 4 : 8), kind, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    if (io != c->polish.psi) cudaFree(io);
+  }
+  return GPE_OK;
+}
+
+gpe_status gpe_set_state(gpe_ctx* c, const double* psi) {
+  return set_state_any(c, psi, GPE_FP64, cudaMemcpyHostToDevice);
+}
+gpe_status gpe_set_state_f32(gpe_ctx* c, const float* psi) {
+  return set_state_any(c, psi, GPE_FP32, cudaMemcpyHostToDevice);
+}
+gpe_status gpe_get_state(gpe_ctx* c, double* psi) {
+  return get_state_any(c, psi, GPE_FP64, cudaMemcpyDeviceToHost);
+}
+gpe_status gpe_get_state_f32(gpe_ctx* c, float* psi) {
+  return get_state_any(c, psi, GPE_FP32, cudaMemcpyDeviceToHost);
+}
+gpe_status gpe_set_state_device(gpe_ctx* c, const void* d, int precision) {
+  if (precision != GPE_FP32 && precision != GPE_FP64) return fail(c, GPE_ERR_INVALID, "bad precision");
+  return set_state_any(c, d, precision, cudaMemcpyDeviceToDevice);
+}
+gpe_status gpe_get_state_device(gpe_ctx* c, void* d, int precision) {
+  if (precision != GPE_FP32 && precision != GPE_FP64) return fail(c, GPE_ERR_INVALID, "bad precision");
+  return get_state_any(c, d, precision, cudaMemcpyDeviceToDevice);
+}
+
+gpe_status gpe_groundstate_itp(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* MU2, double* EE,
+                               int cap, gpe_itp_result* res) {
+  CHECK(check_ctx(c));
+  CHECK(need_state(c));
+  CHECK(need_V(c));
+  if (!prm || !(prm->dt > 0) || !std::isfinite(prm->dt) || !(prm->eps > 0))
+    return fail(c, GPE_ERR_INVALID, "groundstate_itp: dt and eps must be positive");
+  if (cap < 0) return fail(c, GPE_ERR_INVALID, "negative cap");
+  c->err.clear();
+  if (c->prec == GPE_FP32) return itp_impl<float>(c, prm, MU, MU2, EE, cap, res);
+  return itp_impl<double>(c, prm, MU, MU2, EE, cap, res);
+}
+
+gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
+  CHECK(check_ctx(c));
+  CHECK(need_state(c));
+  if (!prm || !(prm->ddt > 0) || !std::isfinite(prm->ddt))
+    return fail(c, GPE_ERR_INVALID, "solve_split: ddt must be positive");
+  if (!prm->vtd) CHECK(need_V(c));
+  c->err.clear();
+  if (c->prec == GPE_FP32) return split_impl<float>(c, prm);
+  return split_impl<double>(c, prm);
+}
+
+gpe_status gpe_observables(gpe_ctx* c, gpe_obs* o) {
+  CHECK(check_ctx(c));
+  CHECK(need_state(c));
+  CHECK(need_V(c));
+  if (!o) return fail(c, GPE_ERR_INVALID, "null output");
+  DevScalars h;
+  if (c->prec == GPE_FP32) CHECK(observables_impl<float>(c, c->main, 0.0, 0, &h));
+  else CHECK(observables_impl<double>(c, c->main, 0.0, 0, &h));
+  o->norm = h.sums[S_N];
+  o->ekin = h.sums[S_KX] + h.sums[S_KY] + h.sums[S_KZ];
+  o->epot = h.sums[S_VN];
+  o->eint = c->prm.g * h.sums[S_N2];
+  o->mu_integral = o->ekin + o->epot + o->eint;
+  o->energy = o->ekin + o->epot + 0.5 * o->eint;
+  return GPE_OK;
+}
+
+gpe_status gpe_synchronize(gpe_ctx* c) {
+  CHECK(check_ctx(c));
+  CU(cudaStreamSynchronize(c->stream));
+  return GPE_OK;
+}
+
+gpe_status gpe_timer_start(gpe_ctx* c) {
+  CHECK(check_ctx(c));
+  CU(cudaStreamSynchronize(c->stream));
+  CU(cudaEventRecord(c->t0, c->stream));
+  return GPE_OK;
+}
+
+gpe_status gpe_timer_stop(gpe_ctx* c, double* ms) {
+  CHECK(check_ctx(c));
+  CU(cudaEventRecord(c->t1, c->stream));
+  CU(cudaEventSynchronize(c->t1));
+  float f = 0;
+  CU(cudaEventElapsedTime(&f, c->t0, c->t1));
+  if (ms) *ms = f;
+  return GPE_OK;
+}
+
+gpe_status gpe_profile_enable(gpe_ctx* c, int on) {
+  CHECK(check_ctx(c));
+  c->prof = on != 0;
+  return GPE_OK;
+}
+
+gpe_status gpe_profile_read(gpe_ctx* c, gpe_kernel_stat* out, int cap, int* n) {
+  CHECK(check_ctx(c));
+  CU(cudaStreamSynchronize(c->stream));
+  for (auto& r : c->prof_pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    c->prof_classes[r.cls].launches++;
+    c->prof_classes[r.cls].total_ms += ms;
+    c->ev_pool.push_back(r.a);
+    c->ev_pool.push_back(r.b);
+  }
+  c->prof_pending.clear();
+  int k = 0;
+  for (auto& pc : c->prof_classes) {
+    if (pc.launches == 0) continue;
+    if (out && k < cap) {
+      memset(&out[k], 0, sizeof(gpe_kernel_stat));
+      snprintf(out[k].name, sizeof(out[k].name), "%s", pc.name.c_str());
+      out[k].launches = pc.launches;
+      out[k].total_ms = pc.total_ms;
+      out[k].bytes_per_launch = pc.bytes / (double)pc.launches;
+    }
+    ++k;
+  }
+  if (n) *n = k;
+  return GPE_OK;
+}
+
+long long gpe_kernel_launches(const gpe_ctx* c) { return c ? c->launches : 0; }
+
+gpe_status gpe_host_register(void* ptr, size_t bytes) {
+  gpe_ctx* c = nullptr;
+  if (!ptr || bytes == 0) return fail(c, GPE_ERR_INVALID, "gpe_host_register: null or empty buffer");
+  CU(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return GPE_OK;
+}
+
+gpe_status gpe_host_unregister(void* ptr) {
+  gpe_ctx* c = nullptr;
+  if (!ptr) return fail(c, GPE_ERR_INVALID, "gpe_host_unregister: null buffer");
+  CU(cudaHostUnregister(ptr));
+  return GPE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,6 @@
+// Axis-pass kernels, float, N in {384}.
+#include "pass_launch.cuh"
+
+namespace gpe {
+GPE_INST_PASS(float, 384)
+}  // namespace gpe

@@ -1,0 +1,49 @@
+// plans.cuh - FFT plans per axis length.
+//
+// A plan fixes the threads per pencil T, the points per thread E = N/T, the
+// radix of every Stockham stage (each radix divides E) and the padding of the
+// shared-memory exchange buffer of the contiguous-axis pass (PADSH: position p
+// lives at p + (p >> PADSH); -1 = no padding).  The padding was chosen by
+// counting shared-memory wavefronts of each exchange pattern.
+#pragma once
+#include "fft.cuh"
+
+namespace gpe {
+
+template <int N_, int T_, int PADSH_, int... RADS>
+struct PlanT {
+  static constexpr int N = N_;
+  static constexpr int T = T_;
+  static constexpr int E = N_ / T_;
+  static constexpr int PADSH = PADSH_;
+  template <typename R>
+  using St = Stages<R, N_, T_, 1, RADS...>;
+  static constexpr int prod() { return (RADS * ...); }
+  static_assert(prod() == N_, "radices must multiply to N");
+  static_assert((((N_ / T_) % RADS == 0) && ...), "every radix must divide E");
+};
+
+template <int N>
+struct Plan;  // only the lengths below are supported
+
+template <> struct Plan<8>    : PlanT<8, 1, -1, 8> {};
+template <> struct Plan<12>   : PlanT<12, 1, -1, 4, 3> {};
+template <> struct Plan<16>   : PlanT<16, 1, -1, 16> {};
+template <> struct Plan<24>   : PlanT<24, 2, 4, 4, 6> {};
+template <> struct Plan<32>   : PlanT<32, 2, 4, 16, 2> {};
+template <> struct Plan<48>   : PlanT<48, 4, 4, 4, 4, 3> {};
+template <> struct Plan<64>   : PlanT<64, 4, 4, 16, 4> {};
+template <> struct Plan<96>   : PlanT<96, 4, 4, 8, 4, 3> {};
+template <> struct Plan<128>  : PlanT<128, 8, 4, 16, 8> {};
+template <> struct Plan<192>  : PlanT<192, 8, 4, 8, 8, 3> {};
+template <> struct Plan<256>  : PlanT<256, 16, 4, 16, 16> {};
+template <> struct Plan<384>  : PlanT<384, 16, 4, 8, 8, 6> {};
+template <> struct Plan<512>  : PlanT<512, 32, 4, 16, 16, 2> {};
+template <> struct Plan<768>  : PlanT<768, 32, 4, 8, 8, 6, 2> {};
+template <> struct Plan<1024> : PlanT<1024, 64, 4, 16, 16, 4> {};
+
+// The axis lengths with a plan (host-side check before any launch).
+#define GPE_FOR_EACH_N(X) \
+  X(8) X(12) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768) X(1024)
+
+}  // namespace gpe

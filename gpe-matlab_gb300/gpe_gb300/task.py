@@ -1,0 +1,340 @@
+"""GPEtask: the reference's solver class API over libgpe.
+
+Mirrors the public surface of lib/@GPEtask/GPEtask.m (constructor, properties,
+getVtotal, groundstate_itp, solve_split, get_energy, the ext_callback
+bookkeeping) so scripts written against GPE-MATLAB port line by line.  The
+loops themselves (groundstate_itp.m, solve_split.m) run inside libgpe on the
+GPU; this class only packs properties, uploads arrays, evaluates host-side
+callbacks (time-dependent potential, user callback) and exposes the results.
+
+Differences from the reference, all deliberate:
+* ``omega`` (rotating frame) is not part of this hot path; nonzero values raise.
+* ``'rand'`` initial states use a seeded numpy generator (the reference calls
+  an unseeded ``rand``, GPEtask.m:49-52).
+* ``show_image`` and the console status line are not implemented (UI).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import warnings
+
+import numpy as np
+
+from . import _lib as L
+from .grid import _GridBase
+
+
+class GPEtask:
+    """GPEtask(grid, V) (GPEtask.m:41-60); V is an array or V(X, Y, Z)."""
+
+    def __init__(self, grid: _GridBase, trappot, device: int = 0):
+        self.grid = grid
+        self._ctx = C.c_void_p()
+        L.check(None, L.lib.gpe_create(C.byref(grid.desc(device)), C.byref(self._ctx)))
+        # public properties with the reference defaults (GPEtask.m:4-34)
+        self.g = 0.0
+        self.omega = 0.0
+        self.n_recalc = 10
+        self.gamma = 0.0
+        self.decay_rate = 0.0
+        self.Ntotal = 0.0
+        self.mu_init = 0.0
+        self.Vtd = None
+        self.V0 = 0
+        self.user_callback = None
+        self.itp_max_iter = 5000
+        self.itp_min_iter = 50
+        self.itp_adjust_stepsize = False
+        self.fp64_polish = True      # FP32 grids: finish ITP in FP64 once FP32 stalls
+        self.history = {"mu": np.zeros(0), "n": np.zeros(0)}
+        self.current_time = 0.0
+        self.current_iter = 0
+        self.current_mu = 0.0
+        self.current_n = 0.0
+        self.init_state = np.zeros(grid.shape, dtype=np.complex128)
+        self._current_state = None
+        self._state_on_device = None     # 'current' when the device holds current_state
+        self._V_key = None
+        if callable(trappot):
+            V = trappot(grid.mesh["x"], grid.mesh["y"], grid.mesh["z"])
+        else:
+            V = trappot
+        self.Vtrap = np.broadcast_to(np.asarray(V, dtype=np.float64), grid.shape).copy()
+        self.last_itp = None
+
+    # ---- lifetime ----------------------------------------------------------
+    def close(self):
+        if self._ctx:
+            L.lib.gpe_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- properties ---------------------------------------------------------
+    @property
+    def Vtrap(self):
+        return self._Vtrap
+
+    @Vtrap.setter
+    def Vtrap(self, v):
+        self._Vtrap = np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), self.grid.shape))
+        self._V_key = None
+
+    @property
+    def current_state(self):
+        if self._state_on_device == "current" and self._current_state is None:
+            self._current_state = self._download()
+        return self._current_state
+
+    @current_state.setter
+    def current_state(self, v):
+        self._current_state = None if v is None else np.asarray(v, dtype=np.complex128)
+        self._state_on_device = None
+
+    def _push_params(self):
+        if self.omega != 0:
+            raise NotImplementedError("omega != 0 (rotating frame) is not supported by this build")
+        p = L.gpe_params()
+        p.g = float(self.g)
+        p.gamma = float(self.gamma)
+        p.decay_rate = float(self.decay_rate)
+        p.Ntotal = float(self.Ntotal)
+        p.mu_init = float(self.mu_init)
+        p.n_recalc = int(self.n_recalc)
+        p.itp_max_iter = int(self.itp_max_iter)
+        p.itp_min_iter = int(self.itp_min_iter)
+        p.itp_adjust_stepsize = int(bool(self.itp_adjust_stepsize))
+        L.check(self._ctx, L.lib.gpe_set_params(self._ctx, C.byref(p)))
+        cur = L.gpe_current()
+        cur.current_iter = int(self.current_iter)
+        cur.current_time = float(self.current_time)
+        cur.current_mu = float(self.current_mu)
+        cur.current_n = float(self.current_n)
+        L.check(self._ctx, L.lib.gpe_set_current(self._ctx, C.byref(cur)))
+
+    def _upload_V(self, V):
+        key = (id(V), V.ctypes.data)
+        if key == self._V_key:
+            return
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        L.check(self._ctx, L.lib.gpe_set_potential(self._ctx, L.dptr(V)))
+        self._V_key = (id(V), V.ctypes.data)
+        self._V_keep = V
+
+    def _upload_state(self, phi):
+        phi = np.broadcast_to(phi, self.grid.shape)
+        if phi.dtype == np.complex64:  # single-precision host arrays go as they are
+            phi = np.ascontiguousarray(phi)
+            L.check(self._ctx, L.lib.gpe_set_state_f32(self._ctx, L.fptr(phi.view(np.float32))))
+            return
+        phi = np.ascontiguousarray(phi, dtype=np.complex128)
+        L.check(self._ctx, L.lib.gpe_set_state(self._ctx, L.dptr(phi.view(np.float64))))
+
+    def _download(self, out=None):
+        """The device state as a host array: complex64 on single-precision
+        grids, complex128 otherwise (or into `out`, e.g. a pinned buffer)."""
+        if out is None:
+            dt = np.complex64 if self.grid.precision == "single" else np.complex128
+            out = np.empty(self.grid.shape, dtype=dt)
+        if out.dtype == np.complex64:
+            L.check(self._ctx, L.lib.gpe_get_state_f32(self._ctx, L.fptr(out.view(np.float32))))
+        else:
+            L.check(self._ctx, L.lib.gpe_get_state(self._ctx, L.dptr(out.view(np.float64))))
+        return out
+
+    # ---- GPEtask.m methods ---------------------------------------------------
+    def getVtotal(self, time):
+        """GPEtask.m:62-71."""
+        if time == 0 and np.size(self.V0) > 1:
+            return np.broadcast_to(np.asarray(self.V0, dtype=np.float64), self.grid.shape)
+        if callable(self.Vtd):
+            return self.Vtrap + self.Vtd(self, time)
+        return self.Vtrap
+
+    def _time_dependent(self):
+        return callable(self.Vtd) or np.size(self.V0) > 1
+
+    def process_init_state(self, phi0, rng=None):
+        """GPEtask.m:144-164 for string arguments; arrays are normalised on the
+        device by groundstate_itp."""
+        if isinstance(phi0, str):
+            if self.Ntotal > 0:
+                if phi0 == "tf":
+                    return self.groundstate_tf(np.finfo(float).eps)[0].astype(np.complex128)
+                rng = rng or np.random.default_rng()
+                r = rng.random(self.grid.shape) + 1j * rng.random(self.grid.shape)
+                return math.sqrt(self.Ntotal) * self.grid.normalize(r)
+            V = self.getVtotal(0)
+            return np.real(np.sqrt((self.mu_init - V).astype(np.complex128) / self.g)).astype(np.complex128)
+        return np.asarray(phi0, dtype=np.complex128)
+
+    def groundstate_tf(self, eps, N=None, V=None, mul=None, mur=None):
+        """Thomas-Fermi bisection, lib/@GPEtask/groundstate_tf.m:1-37 (host)."""
+        N = self.Ntotal if N is None else N
+        V = self.getVtotal(0) if V is None else V
+        if mul is None:
+            mul, mur = float(np.min(V)), float(np.max(V))
+        NC = N * self.g
+        mu = (mul + mur) / 2
+        vvv = (mu - V) * (V < mu)
+        while (mur - mul) / mu > eps:
+            vvv = (mu - V) * (V < mu)
+            NN = self.grid.integrate(vvv)
+            if NN > NC:
+                mur = mu
+            else:
+                mul = mu
+            mu = (mul + mur) / 2
+        return np.sqrt(vvv / self.g), mu
+
+    def groundstate_itp(self, dt, eps, phi0="rand", nargout=1, rng=None):
+        """groundstate_itp.m:1-112.  Returns phi, or (phi, MU, MU2, EE)[:nargout]."""
+        self._push_params()
+        self._upload_V(np.ascontiguousarray(self.getVtotal(0)))
+        phi = self.process_init_state(phi0, rng=rng)
+        self._upload_state(phi)
+        prm = L.gpe_itp_params()
+        prm.dt = float(dt)
+        prm.eps = float(eps)
+        prm.want_mu2 = int(nargout >= 3)
+        prm.want_energy = int(nargout >= 4)
+        prm.fp64_polish = int(bool(self.fp64_polish))
+        prm.switch_delta = 0.0
+        cap = int(self.itp_max_iter)
+        MU = np.zeros(cap)
+        MU2 = np.zeros(cap)
+        EE = np.zeros(cap)
+        res = L.gpe_itp_result()
+        L.check(self._ctx, L.lib.gpe_groundstate_itp(self._ctx, C.byref(prm), L.dptr(MU), L.dptr(MU2),
+                                                     L.dptr(EE), cap, C.byref(res)))
+        n = res.iters
+        self.last_itp = res
+        if not res.converged:
+            warnings.warn("Convergence not reached")  # groundstate_itp.m:79
+        cur = L.gpe_current()
+        L.check(self._ctx, L.lib.gpe_get_current(self._ctx, C.byref(cur)))
+        if nargout >= 2 or self.Ntotal <= 0:
+            self.current_mu, self.current_n = cur.current_mu, cur.current_n
+        phi = self._download()
+        self.init_state = phi                      # groundstate_itp.m:111
+        self._current_state = phi
+        self._state_on_device = "current"
+        outs = (phi, MU[:n].copy(), MU2[:n].copy(), EE[:n].copy())
+        return phi if nargout <= 1 else outs[:nargout]
+
+    def solve_split(self, ddt, niter_inner, niter_outer):
+        """solve_split.m:1-84: run outer steps current_iter+1 .. niter_outer."""
+        self._push_params()
+        start = int(self.current_iter)
+        if start > 0:
+            if self._state_on_device != "current":
+                if self._current_state is None:
+                    raise RuntimeError("current_iter > 0 but no current_state")
+                self._upload_state(self._current_state)
+        else:
+            self._upload_state(self.init_state)
+        errors = []
+        vtd_cb = L.VTD_FN()
+        if self._time_dependent():
+            P = self.grid.npoints
+
+            def _vtd(user, time, out):
+                try:
+                    v = np.asarray(self.getVtotal(time), dtype=np.float64)
+                    np.ctypeslib.as_array(out, shape=(P,))[:] = np.broadcast_to(v, self.grid.shape).ravel()
+                    return 0
+                except BaseException as e:  # surfaced after the call returns
+                    errors.append(e)
+                    return 1
+
+            vtd_cb = L.VTD_FN(_vtd)
+            self._V_key = None
+        else:
+            self._upload_V(self.Vtrap)
+
+        def _step(user, step, time, mu, n):
+            try:
+                self._ext_callback(step, time, mu, n)
+                return 0
+            except BaseException as e:
+                errors.append(e)
+                return 1
+
+        step_cb = L.STEP_FN(_step) if self.user_callback is not None else L.STEP_FN()
+        prm = L.gpe_split_params()
+        prm.ddt = float(ddt)
+        prm.niter_inner = int(niter_inner)
+        prm.niter_outer = int(niter_outer)
+        prm.vtd = vtd_cb
+        prm.on_step = step_cb
+        st = L.lib.gpe_solve_split(self._ctx, C.byref(prm))
+        if errors:
+            raise errors[0]
+        L.check(self._ctx, st)
+        cur = L.gpe_current()
+        L.check(self._ctx, L.lib.gpe_get_current(self._ctx, C.byref(cur)))
+        self.current_iter, self.current_time = cur.current_iter, cur.current_time
+        self.current_mu, self.current_n = cur.current_mu, cur.current_n
+        self._sync_history()
+        self._current_state = None
+        self._state_on_device = "current"
+        return self.current_state
+
+    def _sync_history(self):
+        n = C.c_int()
+        L.check(self._ctx, L.lib.gpe_get_history(self._ctx, None, None, 0, C.byref(n)))
+        mu = np.zeros(n.value)
+        nn = np.zeros(n.value)
+        L.check(self._ctx, L.lib.gpe_get_history(self._ctx, L.dptr(mu), L.dptr(nn), n.value, C.byref(n)))
+        self.history["mu"], self.history["n"] = mu, nn
+
+    def _ext_callback(self, step, time, mu, n):
+        """GPEtask.m:115-142 (plot and console line omitted)."""
+        self.current_time = time
+        self.current_iter = step
+        self.current_mu = mu
+        self.current_n = n
+        self._current_state = None
+        self._state_on_device = "current"
+        self._sync_history()
+        if callable(self.user_callback):
+            self.user_callback(self)
+
+    def observables(self, phi=None):
+        """<psi|H psi> pieces of psi (default: the current device state)."""
+        self._push_params()
+        self._upload_V(np.ascontiguousarray(self.getVtotal(self.current_time)))
+        if phi is not None:
+            self._upload_state(phi)
+            self._state_on_device = None
+        o = L.gpe_obs()
+        L.check(self._ctx, L.lib.gpe_observables(self._ctx, C.byref(o)))
+        return {k: getattr(o, k) for k, _ in L.gpe_obs._fields_}
+
+    def get_energy(self, phi=None):
+        """GPEtask.m:97-107."""
+        return self.observables(phi if phi is not None else self.current_state)["energy"]
+
+    def chemical_potential_integral(self, phi=None):
+        """real(inner(phi, applyham(phi))) (GPEtask.m:73-78 with grid.inner)."""
+        return self.observables(phi if phi is not None else self.current_state)["mu_integral"]
+
+    # ---- profiling -----------------------------------------------------------
+    def profile(self, on: bool = True):
+        L.check(self._ctx, L.lib.gpe_profile_enable(self._ctx, int(on)))
+
+    def profile_read(self):
+        cap = 32
+        arr = (L.gpe_kernel_stat * cap)()
+        n = C.c_int()
+        L.check(self._ctx, L.lib.gpe_profile_read(self._ctx, arr, cap, C.byref(n)))
+        return [{"name": arr[i].name.decode(), "launches": arr[i].launches, "total_ms": arr[i].total_ms,
+                 "bytes_per_launch": arr[i].bytes_per_launch} for i in range(n.value)]
+
+    def kernel_launches(self) -> int:
+        return int(L.lib.gpe_kernel_launches(self._ctx))

@@ -1,0 +1,108 @@
+"""Seeded synthetic workloads (the reference publishes no datasets).
+
+Each workload fixes a grid, trap, coupling, particle number, initial state and
+time steps.  Where the workload description leaves a value open it is fixed
+here and marked ``assumed``:
+
+* "Gaussian width 4" means psi0 = exp(-r^2/(2*4^2)) plus complex noise
+  1e-3*(N(0,1) + i N(0,1))/sqrt(2) from numpy's default_rng(seed).
+* 3D ITP time steps: the reference's ITP applies the nonlinear factor
+  explicitly and oscillates once mu*dt exceeds ~1 (the 256^3 workload at
+  dt = 0.02 has mu*dt ~ 1.4 and never meets eps; the FP64 oracle shows the
+  same), so 0.01 (256^3, mu ~ 71) and 0.004 (512^3, mu ~ 180) are used,
+  with eps = 1e-6.
+
+``scale`` shrinks the grid for fast parity tests while keeping the box, so
+the same physics runs at 32^2 / 64^2 / 32^3.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .grid import grid2d, grid3d
+
+
+@dataclass
+class Workload:
+    name: str
+    ndims: int
+    n: tuple
+    box: tuple                      # xmax, ymax[, zmax]
+    trap: tuple                     # anisotropy (1, 1[, lambda])
+    g: float
+    Ntotal: float
+    itp_dt: float
+    itp_eps: float
+    dt: float
+    niter_inner: int
+    niter_outer: int
+    gamma: float = 0.0
+    vortex_x0: float | None = None
+    ring_frac: float | None = None  # vortex ring radius / R_TF
+    sigma: float = 4.0
+    noise: float = 1e-3
+    seed: int = 1
+    notes: list = field(default_factory=list)
+
+    @property
+    def npoints(self) -> int:
+        return int(np.prod(self.n))
+
+    def make_grid(self, precision: str = "double", n=None):
+        n = tuple(n or self.n)
+        if self.ndims == 2:
+            return grid2d(self.box[0], n[0], self.box[1], n[1], precision=precision)
+        return grid3d(self.box[0], n[0], self.box[1], n[1], self.box[2], n[2], precision=precision)
+
+    def potential(self):
+        lam = self.trap
+
+        def V(X, Y, Z):
+            if self.ndims == 2:
+                return 0.5 * ((lam[0] * X) ** 2 + (lam[1] * Y) ** 2)
+            return 0.5 * ((lam[0] * X) ** 2 + (lam[1] * Y) ** 2 + (lam[2] * Z) ** 2)
+
+        return V
+
+    def initial_state(self, grid):
+        rng = np.random.default_rng(self.seed)
+        X, Y, Z = grid.mesh["x"], grid.mesh["y"], grid.mesh["z"]
+        r2 = X ** 2 + Y ** 2 + (Z ** 2 if self.ndims == 3 else 0.0)
+        phi = np.exp(-r2 / (2 * self.sigma ** 2)).astype(np.complex128)
+        noise = (rng.standard_normal(grid.shape) + 1j * rng.standard_normal(grid.shape)) / np.sqrt(2)
+        return phi + self.noise * noise
+
+    def make_task(self, precision: str = "double", n=None, device: int = 0):
+        from .task import GPEtask
+
+        grid = self.make_grid(precision, n)
+        task = GPEtask(grid, self.potential(), device=device)
+        task.Ntotal = self.Ntotal
+        task.g = self.g
+        task.gamma = self.gamma
+        return grid, task
+
+
+# Plain-method 2D example: 256^2, box [-17, 17]^2, V = 0.5 r^2, N = 1e5, g = 0.06,
+# ITP 0.02 / 1e-6 from a Gaussian, vortex at x0 = 5, then 20 x 50 steps of 0.004.
+VORTEX2D = Workload(
+    name="vortex2d_256", ndims=2, n=(256, 256), box=(17.0, 17.0), trap=(1.0, 1.0), g=0.06, Ntotal=1e5,
+    itp_dt=0.02, itp_eps=1e-6, dt=0.004, niter_inner=50, niter_outer=20, vortex_x0=5.0)
+
+# 3D 256^3, box +-12, V = 0.5 (x^2 + y^2 + (4 z)^2), g = 0.5, N = 1e5; ITP
+# then 2000 steps of 0.002 with gamma = 0.01 (20 outer x 100 inner).
+DAMPED3D = Workload(
+    name="damped3d_256", ndims=3, n=(256, 256, 256), box=(12.0, 12.0, 12.0), trap=(1.0, 1.0, 4.0), g=0.5,
+    Ntotal=1e5, itp_dt=0.01, itp_eps=1e-6, dt=0.002, niter_inner=100, niter_outer=20, gamma=0.01,
+    notes=["ITP dt 0.01 and eps 1e-6 assumed (dt 0.02 oscillates)"])
+
+# 3D 512^3, lambda = (1, 1, 2), g = 1, N = 1e6, vortex ring at 0.5 R_TF,
+# 10000 steps of 0.001.  Box +-24 assumed (TF radius ~18.9 in x, y).
+RING3D = Workload(
+    name="ring3d_512", ndims=3, n=(512, 512, 512), box=(24.0, 24.0, 24.0), trap=(1.0, 1.0, 2.0), g=1.0,
+    Ntotal=1e6, itp_dt=0.004, itp_eps=1e-6, dt=0.001, niter_inner=100, niter_outer=100, ring_frac=0.5,
+    notes=["box +-24 assumed", "ITP dt 0.004 and eps 1e-6 assumed"])
+
+WORKLOADS = {w.name: w for w in (VORTEX2D, DAMPED3D, RING3D)}

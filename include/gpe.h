@@ -1,0 +1,217 @@
+/*
+ * gpe.h - C ABI of libgpe, a GB300-native (sm_103a) split-step Fourier solver
+ * for the Gross-Pitaevskii equation.  It is a drop-in for the hot path of
+ * GPE-MATLAB's GPEtask.groundstate_itp / GPEtask.solve_split on grid2d/grid3d.
+ *
+ * Plain C types only: host buffers are caller-owned and copied in or out
+ * before the call returns; device buffers, kernels, tables and the CUDA
+ * stream are owned by the context.  Every call returns a gpe_status; the
+ * message of the last failure is available from gpe_last_error().  No call
+ * exits or aborts the process.
+ *
+ * Array layout is MATLAB's: ny x nx (x nz) column-major meshgrid arrays, so
+ * element (iy, ix, iz) sits at linear index iy + ny*(ix + nx*iz)
+ * (lib/@grid2d/init.m:30-34, lib/@grid3d/init.m:75-79 of GPE-MATLAB).
+ * Complex arrays are interleaved (re, im) pairs, as MATLAB R2018a+ and
+ * gpuArray store them.
+ *
+ * Threading: one context is used by one host thread at a time; separate
+ * contexts may be used concurrently from different threads.
+ */
+#ifndef GPE_H
+#define GPE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPE_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define GPE_API __attribute__((visibility("default")))
+#else
+#define GPE_API
+#endif
+
+typedef struct gpe_ctx gpe_ctx;
+
+typedef enum {
+    GPE_OK = 0,
+    GPE_ERR_INVALID = 1,     /* bad argument: null pointer, size, parameter   */
+    GPE_ERR_UNSUPPORTED = 2, /* e.g. an axis length without an FFT plan       */
+    GPE_ERR_CUDA = 3,        /* CUDA runtime error (see gpe_last_error)       */
+    GPE_ERR_ALLOC = 4,       /* device or pinned allocation failed            */
+    GPE_ERR_STATE = 5,       /* call out of order (no potential, no state)    */
+    GPE_ERR_TIMEOUT = 6,     /* a bounded device-side wait expired            */
+    GPE_ERR_NONFINITE = 7,   /* NaN/Inf met in a reduction (norm, mu, delta)  */
+    GPE_ERR_NO_DEVICE = 8,   /* no CUDA device, or not an sm_103 device       */
+    GPE_ERR_CALLBACK = 9     /* a host callback returned nonzero              */
+} gpe_status;
+
+enum { GPE_FP32 = 1, GPE_FP64 = 2 };
+
+/* Grid: replaces grid2d(xmax,nx,ymax,ny) / grid3d(...) construction,
+ * lib/@grid2d/init.m:1-38 and lib/@grid3d/init.m:1-47.  Per axis the caller
+ * passes dx = x(2)-x(1) and span = x(end)-x(1) exactly as the MATLAB grid
+ * computes them; the wave numbers are [0:n/2, -(n/2-1):-1]*2*pi/(span+dx)
+ * (init.m:27-28) and the integration weight is prod(dx) (init.m:36). */
+typedef struct {
+    int ndims;        /* 2 (grid2d) or 3 (grid3d)                               */
+    int n[3];         /* nx, ny, nz (nz ignored in 2D); even, 2^a*3^b, 8..1024  */
+    double dx[3];     /* grid spacing per axis (x, y, z)                        */
+    double span[3];   /* x(end)-x(1) per axis                                   */
+    int precision;    /* GPE_FP32 or GPE_FP64: arithmetic type of the step      */
+    int device;       /* CUDA device ordinal                                    */
+} gpe_grid_desc;
+
+/* Public properties of GPEtask that the hot path reads,
+ * lib/@GPEtask/GPEtask.m:4-34 (defaults in brackets). */
+typedef struct {
+    double g;               /* coupling coefficient                      [0]    */
+    double gamma;           /* phenomenological damping                  [0]    */
+    double decay_rate;      /* 1/e decay time of N, 0 = none             [0]    */
+    double Ntotal;          /* particle number, <= 0: keep the state norm [0]   */
+    double mu_init;         /* fixed chemical potential, 0 = from state  [0]    */
+    int n_recalc;           /* steps per potential / mu refresh          [10]   */
+    int itp_max_iter;       /* ITP iteration cap                         [5000] */
+    int itp_min_iter;       /* ITP iterations before the first check     [50]   */
+    int itp_adjust_stepsize;/* halve dt on convergence until dt < dtmin  [0]    */
+} gpe_params;
+
+/* Imaginary-time propagation, lib/@GPEtask/groundstate_itp.m:1-112. */
+typedef struct {
+    double dt;              /* imaginary time step                               */
+    double eps;             /* convergence threshold on the residual delta       */
+    int want_mu2;           /* compute MU2 = <psi|H psi> at checks (nargout>=3)  */
+    int want_energy;        /* compute EE = energy at checks (nargout>=4)        */
+    int fp64_polish;        /* FP32 contexts: once FP32 rounding stalls delta,
+                               finish the iteration in FP64 (default 1)         */
+    double switch_delta;    /* FP32 phase ends once delta < switch_delta
+                               (0 = 2e-4), or when delta stalls                  */
+} gpe_itp_params;
+
+typedef struct {
+    int iters;              /* number of iterations run (length of MU)           */
+    int converged;          /* 1 if delta < eps was reached                      */
+    int fp32_iters;         /* iterations run in FP32 before the FP64 polish     */
+    double final_dt;        /* dt at exit (differs if itp_adjust_stepsize)       */
+    double last_delta;      /* last residual delta                               */
+} gpe_itp_result;
+
+/* Host callbacks of solve_split.  Both run on the calling thread. */
+/* Fill V_out (nx*ny*nz doubles, MATLAB order) with getVtotal(time),
+ * GPEtask.m:62-71; called once per block of n_recalc steps
+ * (solve_split.m:53-54).  Return 0 on success. */
+typedef int (*gpe_vtd_fn)(void *user, double time, double *V_out);
+/* ext_callback (GPEtask.m:115-142): called after each outer step j with the
+ * block time, mu and norm; the state may be read with gpe_get_state().
+ * Return 0 to continue; nonzero stops the run after this outer step. */
+typedef int (*gpe_step_fn)(void *user, int step, double time, double mu, double n);
+
+/* Real-time split step, lib/@GPEtask/solve_split.m:1-84. */
+typedef struct {
+    double ddt;             /* real time step                                    */
+    int niter_inner;        /* steps per outer step                              */
+    int niter_outer;        /* run outer steps current_iter+1 .. niter_outer      */
+    gpe_vtd_fn vtd;         /* NULL: the potential set by gpe_set_potential      */
+    void *vtd_user;
+    gpe_step_fn on_step;    /* NULL: no per-outer-step host synchronisation       */
+    void *step_user;
+} gpe_split_params;
+
+/* Dynamics bookkeeping properties, GPEtask.m:18-24. */
+typedef struct {
+    int current_iter;
+    double current_time;
+    double current_mu;
+    double current_n;
+} gpe_current;
+
+/* <psi|H psi> pieces, GPEtask.m:73-107 (omega = 0). */
+typedef struct {
+    double norm;            /* integrate(|psi|^2)                                */
+    double ekin;            /* real(inner(psi, lap(psi)))                        */
+    double epot;            /* integrate(V |psi|^2)                              */
+    double eint;            /* g * integrate(|psi|^4)                            */
+    double mu_integral;     /* real(inner(psi, applyham(psi))) = ekin+epot+eint  */
+    double energy;          /* get_energy(psi) = ekin + epot + eint/2            */
+} gpe_obs;
+
+/* Per-kernel-class timings collected while profiling is enabled. */
+typedef struct {
+    char name[48];
+    long long launches;
+    double total_ms;
+    double bytes_per_launch;   /* algorithmic HBM bytes of one launch          */
+} gpe_kernel_stat;
+
+/* ---- context ---------------------------------------------------------- */
+/* grid2d/grid3d init + GPEtask constructor (GPEtask.m:41-60). */
+GPE_API gpe_status gpe_create(const gpe_grid_desc *desc, gpe_ctx **out);
+GPE_API void gpe_destroy(gpe_ctx *ctx);
+/* Message of the last failed call on ctx (ctx may be NULL: last failure of
+ * gpe_create on this thread). Never NULL. */
+GPE_API const char *gpe_last_error(const gpe_ctx *ctx);
+GPE_API int gpe_abi_version(void);
+/* 1 if a usable sm_103 CUDA device is present, else 0. */
+GPE_API int gpe_device_available(void);
+
+/* ---- properties (GPEtask.m:4-34) -------------------------------------- */
+GPE_API void gpe_default_params(gpe_params *p);
+GPE_API gpe_status gpe_set_params(gpe_ctx *ctx, const gpe_params *p);
+GPE_API gpe_status gpe_get_params(const gpe_ctx *ctx, gpe_params *p);
+GPE_API gpe_status gpe_get_current(const gpe_ctx *ctx, gpe_current *cur);
+GPE_API gpe_status gpe_set_current(gpe_ctx *ctx, const gpe_current *cur);
+/* history.mu / history.n (GPEtask.m:123-126): up to cap entries, *len = count */
+GPE_API gpe_status gpe_get_history(const gpe_ctx *ctx, double *mu, double *n, int cap, int *len);
+GPE_API gpe_status gpe_clear_history(gpe_ctx *ctx);
+
+/* ---- data ------------------------------------------------------------- */
+/* Vtrap / getVtotal (GPEtask.m:44-46, 62-71): nx*ny*nz real values. */
+GPE_API gpe_status gpe_set_potential(gpe_ctx *ctx, const double *V);
+GPE_API gpe_status gpe_set_potential_f32(gpe_ctx *ctx, const float *V);
+/* init_state / current_state: nx*ny*nz interleaved complex values. */
+GPE_API gpe_status gpe_set_state(gpe_ctx *ctx, const double *psi);
+GPE_API gpe_status gpe_set_state_f32(gpe_ctx *ctx, const float *psi);
+GPE_API gpe_status gpe_get_state(gpe_ctx *ctx, double *psi);
+GPE_API gpe_status gpe_get_state_f32(gpe_ctx *ctx, float *psi);
+/* Device-resident variants (gpuArray inputs): d_psi is a device pointer on
+ * the context's device holding interleaved complex values of `precision`. */
+GPE_API gpe_status gpe_set_state_device(gpe_ctx *ctx, const void *d_psi, int precision);
+GPE_API gpe_status gpe_get_state_device(gpe_ctx *ctx, void *d_psi, int precision);
+
+/* Page-lock (pin) a caller-owned host buffer so state copies run at full
+ * link bandwidth and asynchronously; unregister before freeing it. */
+GPE_API gpe_status gpe_host_register(void *ptr, size_t bytes);
+GPE_API gpe_status gpe_host_unregister(void *ptr);
+
+/* ---- hot path --------------------------------------------------------- */
+/* groundstate_itp.m:1-112 from the current state (process_init_state for an
+ * array phi0 is applied: psi <- sqrt(Ntotal)*normalize(psi) when Ntotal > 0).
+ * MU, MU2, EE (each may be NULL) receive up to cap entries, already divided
+ * by Ntotal as the reference returns them.  On return the state holds the
+ * ground state (init_state = phi, groundstate_itp.m:111). */
+GPE_API gpe_status gpe_groundstate_itp(gpe_ctx *ctx, const gpe_itp_params *prm,
+                               double *MU, double *MU2, double *EE, int cap,
+                               gpe_itp_result *res);
+/* solve_split.m:1-84 from the current state; resumes at current_iter. */
+GPE_API gpe_status gpe_solve_split(gpe_ctx *ctx, const gpe_split_params *prm);
+/* applyham / get_energy pieces for the current state at the current V. */
+GPE_API gpe_status gpe_observables(gpe_ctx *ctx, gpe_obs *obs);
+
+/* ---- profiling and timing (CUDA events on the context stream) ---------- */
+GPE_API gpe_status gpe_synchronize(gpe_ctx *ctx);
+GPE_API gpe_status gpe_timer_start(gpe_ctx *ctx);
+GPE_API gpe_status gpe_timer_stop(gpe_ctx *ctx, double *ms);
+GPE_API gpe_status gpe_profile_enable(gpe_ctx *ctx, int on);
+GPE_API gpe_status gpe_profile_read(gpe_ctx *ctx, gpe_kernel_stat *out, int cap, int *n);
+/* Launch counters of this library's kernels since the context was created. */
+GPE_API long long gpe_kernel_launches(const gpe_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPE_H */

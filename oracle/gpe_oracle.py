@@ -1,0 +1,403 @@
+"""FP64 CPU oracle for the GPE-MATLAB split-step hot path.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker: only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may import
+it.  The product (``libgpe.so`` and its host mirror) never calls it.
+
+It restates, line by line and in FP64 numpy/scipy, the reference's
+``GPEtask.groundstate_itp`` / ``GPEtask.solve_split`` on ``grid2d`` /
+``grid3d``, with every operation in the reference's order.  Each function
+cites the reference file:line it follows (paths relative to the GPE-MATLAB
+project root).
+
+PARITY UNPINNED: the reference is MATLAB-only, ships no tests, no golden
+vectors and no known-answer fixtures, and neither MATLAB nor Octave exists on
+this machine, so the restatement cannot be checked against the reference's own
+outputs.  It is instead pinned to analytic known answers (harmonic-oscillator
+ground states, exact free propagation of a plane wave, unit-modulus phases at
+gamma = 0); see ``tests/test_oracle.py``.
+
+Array layout: MATLAB ``meshgrid`` arrays are ny x nx (x nz), column major, so
+the linear index is ``iy + ny*(ix + nx*iz)`` (lib/@grid2d/init.m:30-34,
+lib/@grid3d/init.m:75-79).  Here the same memory order is held as C-order numpy
+arrays of shape (nx, ny) in 2D and (nz, nx, ny) in 3D: ``a.ravel()`` is the
+MATLAB linear order.  FFTs run over every axis, which is what ``fft2`` /
+``fftn`` do on the MATLAB array (lib/@grid2d/fft.m:11, lib/@grid3d/fft.m:11).
+The third-party FFT arithmetic of the reference is MATLAB's bundled FFTW
+(version not pinned by the reference); here it is pocketfft through
+``scipy.fft`` with the same conventions (unnormalised forward, 1/N inverse).
+"""
+from __future__ import annotations
+
+import math
+import os
+import warnings
+
+import numpy as np
+import scipy.fft as sfft
+
+_WORKERS = int(os.environ.get("GPE_ORACLE_WORKERS", os.cpu_count() or 1))
+
+
+def set_workers(n: int) -> None:
+    """Number of threads scipy.fft may use (the CPU baseline uses all cores)."""
+    global _WORKERS
+    _WORKERS = max(1, int(n))
+
+
+# ---------------------------------------------------------------------------
+# Grids: lib/@grid1d, lib/@grid2d, lib/@grid3d
+# ---------------------------------------------------------------------------
+def _kvec(x: np.ndarray) -> np.ndarray:
+    """FFT-ordered wave numbers, lib/@grid2d/init.m:27 (same rule for y, z)."""
+    n = x.size
+    dx = x[1] - x[0]
+    idx = np.concatenate([np.arange(0, n // 2 + 1), -np.arange(n // 2 - 1, 0, -1)])
+    return idx * 2.0 * np.pi / (x[-1] - x[0] + dx)
+
+
+class Grid:
+    """grid2d / grid3d (lib/@grid2d/init.m:1-38, lib/@grid3d/init.m:1-47).
+
+    ``Grid(xmax, nx, ymax, ny)`` or ``Grid(xmax, nx, ymax, ny, zmax, nz)``
+    builds ``linspace(-xmax, xmax, n)`` axes (init.m:12-13); explicit axes
+    can be given with ``Grid.from_axes(x, y[, z])`` (init.m:5-9).
+    """
+
+    def __init__(self, *args):
+        if len(args) == 4:
+            axes = [np.linspace(-args[0], args[0], int(args[1])),
+                    np.linspace(-args[2], args[2], int(args[3]))]
+        elif len(args) == 6:
+            axes = [np.linspace(-args[0], args[0], int(args[1])),
+                    np.linspace(-args[2], args[2], int(args[3])),
+                    np.linspace(-args[4], args[4], int(args[5]))]
+        else:
+            raise ValueError("Grid(xmax,nx,ymax,ny[,zmax,nz])")
+        self._init(axes)
+
+    @classmethod
+    def from_axes(cls, *axes):
+        obj = cls.__new__(cls)
+        obj._init([np.asarray(a, dtype=np.float64) for a in axes])
+        return obj
+
+    def _init(self, axes):
+        self.ndims = len(axes)
+        self.x, self.y = axes[0], axes[1]
+        self.z = axes[2] if self.ndims == 3 else np.zeros(1)
+        self.nx, self.ny = self.x.size, self.y.size
+        self.nz = self.z.size if self.ndims == 3 else 1
+        # init.m:20-21 / 63-65
+        self.dx = self.x[1] - self.x[0]
+        self.dy = self.y[1] - self.y[0]
+        self.dz = (self.z[1] - self.z[0]) if self.ndims == 3 else 1.0
+        kx, ky = _kvec(self.x), _kvec(self.y)
+        kz = _kvec(self.z) if self.ndims == 3 else np.zeros(1)
+        self.kx1, self.ky1, self.kz1 = kx, ky, kz
+        if self.ndims == 2:
+            # meshgrid(x, y) -> arrays indexed [ix, iy] here (column-major ny x nx)
+            KX, KY = np.meshgrid(kx, ky, indexing="ij")
+            self.kk = (KX ** 2 + KY ** 2) / 2                  # init.m:31
+            X, Y = np.meshgrid(self.x, self.y, indexing="ij")  # init.m:34
+            self.mesh = {"x": X, "y": Y, "z": 0.0}
+            self.weight = self.dx * self.dy                    # init.m:36
+            self.shape = (self.nx, self.ny)
+        else:
+            KZ, KX, KY = np.meshgrid(kz, kx, ky, indexing="ij")
+            self.kk = (KX ** 2 + KY ** 2 + KZ ** 2) / 2        # grid3d/init.m:76
+            Z, X, Y = np.meshgrid(self.z, self.x, self.y, indexing="ij")
+            self.mesh = {"x": X, "y": Y, "z": Z}               # grid3d/init.m:79-82
+            self.weight = self.dx * self.dy * self.dz          # grid3d/init.m:83
+            self.shape = (self.nz, self.nx, self.ny)
+
+    # lib/@grid2d/fft.m:11, lib/@grid3d/fft.m:11
+    def fft(self, f):
+        return sfft.fftn(f, workers=_WORKERS)
+
+    # lib/@grid2d/ifft.m:11, lib/@grid3d/ifft.m:11
+    def ifft(self, f):
+        return sfft.ifftn(f, workers=_WORKERS)
+
+    # lib/@grid1d/integrate.m:11
+    def integrate(self, f):
+        return np.sum(f) * self.weight
+
+    # lib/@grid1d/inner.m:12
+    def inner(self, lhs, rhs):
+        return self.integrate(np.conj(lhs) * rhs)
+
+    # lib/@grid1d/norm.m:11
+    def norm(self, psi):
+        return math.sqrt(self.integrate(np.abs(psi) ** 2))
+
+    # lib/@grid1d/normalize.m:13-15
+    def normalize(self, psi):
+        return psi * (1.0 / self.norm(psi))
+
+    # lib/@grid2d/lap.m:5-6, lib/@grid3d/lap.m:5-6 (omega == 0 branch)
+    def lap(self, phi):
+        return self.ifft(self.kk * self.fft(phi))
+
+
+# ---------------------------------------------------------------------------
+# Solver: lib/@GPEtask
+# ---------------------------------------------------------------------------
+class GPEtask:
+    """lib/@GPEtask/GPEtask.m:1-167, omega == 0 branch only."""
+
+    def __init__(self, grid: Grid, trappot):
+        # GPEtask.m:41-60 (rng('shuffle') and the FFTW planner are not numerics)
+        self.grid = grid
+        self.g = 0.0
+        self.omega = 0.0
+        self.n_recalc = 10
+        self.gamma = 0.0
+        self.decay_rate = 0.0
+        self.Ntotal = 0.0
+        self.mu_init = 0.0
+        self.Vtd = None
+        self.V0 = 0
+        self.init_state = np.zeros(grid.shape, dtype=np.complex128)
+        self.current_state = None
+        self.current_time = 0.0
+        self.current_iter = 0
+        self.current_mu = 0.0
+        self.current_n = 0.0
+        self.history = {"mu": [], "n": []}
+        self.user_callback = None
+        self.itp_max_iter = 5000
+        self.itp_min_iter = 50
+        self.itp_adjust_stepsize = False
+        self.kinop = None
+        self.nlinop = None
+        if callable(trappot):
+            self.Vtrap = trappot(grid.mesh["x"], grid.mesh["y"], grid.mesh["z"])  # :44
+        else:
+            self.Vtrap = np.asarray(trappot, dtype=np.float64)                  # :46
+        self.Vtrap = np.broadcast_to(self.Vtrap, grid.shape).astype(np.float64)
+
+    # GPEtask.m:62-71
+    def getVtotal(self, time):
+        if time == 0 and np.size(self.V0) > 1:
+            return self.V0
+        if callable(self.Vtd):
+            return self.Vtrap + self.Vtd(self, time)
+        return self.Vtrap
+
+    # GPEtask.m:73-78
+    def applyham(self, phi, time=None):
+        if time is None:
+            time = self.current_time
+        return self.applyh0(phi, time) + self.g * np.abs(phi) ** 2 * phi
+
+    # GPEtask.m:80-95 (omega == 0)
+    def applyh0(self, phi, time=None):
+        if time is None:
+            time = self.current_time
+        return self.getVtotal(time) * phi + self.grid.lap(phi)
+
+    # GPEtask.m:97-107
+    def get_energy(self, phi=None, time=None):
+        if phi is None:
+            phi = self.current_state
+        tmp = self.g
+        self.g = 0.5 * self.g
+        try:
+            res = np.real(self.grid.inner(phi, self.applyham(phi, time)))
+        finally:
+            self.g = tmp
+        return res
+
+    # GPEtask.m:115-142 (plot and console line omitted)
+    def ext_callback(self, phi, step, time, mu, n):
+        self.current_state = phi
+        self.current_time = time
+        self.current_iter = step
+        self.current_mu = mu
+        _set_hist(self.history["mu"], step, mu)
+        self.current_n = n
+        _set_hist(self.history["n"], step, n)
+        if callable(self.user_callback):
+            self.user_callback(self)
+
+    # GPEtask.m:144-164
+    def process_init_state(self, phi0, rng=None):
+        if isinstance(phi0, str):
+            if self.Ntotal > 0:
+                if phi0 == "tf":
+                    res, _ = self.groundstate_tf(np.finfo(float).eps)
+                    return res.astype(np.complex128)
+                rng = rng or np.random.default_rng()
+                r = rng.random(self.grid.shape) + 1j * rng.random(self.grid.shape)
+                return math.sqrt(self.Ntotal) * self.grid.normalize(r)
+            V = self.getVtotal(0)  # the reference leaves V undefined here (:157)
+            return np.real(np.sqrt((self.mu_init - V).astype(np.complex128) / self.g))
+        if self.Ntotal > 0:
+            return math.sqrt(self.Ntotal) * self.grid.normalize(np.asarray(phi0, np.complex128))
+        return np.asarray(phi0, np.complex128)
+
+    # lib/@GPEtask/groundstate_tf.m:1-37
+    def groundstate_tf(self, eps, N=None, V=None, mul=None, mur=None):
+        if N is None:
+            N = self.Ntotal
+        if V is None:
+            V = self.getVtotal(0)
+        if mul is None:
+            mul, mur = float(np.min(V)), float(np.max(V))
+        NC = N * self.g
+        mu = (mul + mur) / 2
+        vvv = (mu - V) * (V < mu)
+        while (mur - mul) / mu > eps:
+            vvv = (mu - V) * (V < mu)
+            NN = self.grid.integrate(vvv)
+            if NN > NC:
+                mur = mu
+            else:
+                mul = mu
+            mu = (mul + mur) / 2
+        return np.sqrt(vvv / self.g), mu
+
+    # lib/@GPEtask/set_kinop.m:1-11 (omega == 0 branch, :9)
+    def set_kinop(self, dt):
+        self.kinop = np.exp(-self.grid.kk * dt)
+
+    # lib/@GPEtask/ssft_kin_step.m:17
+    def ssft_kin_step(self, phi, dt):
+        return self.grid.ifft(self.kinop * self.grid.fft(phi))
+
+    # lib/@GPEtask/groundstate_itp.m:1-112
+    def groundstate_itp(self, dt, eps, phi0="rand", nargout=4, rng=None):
+        """Returns (phi, MU, MU2, EE) with MU2/EE computed iff nargout >= 3/4."""
+        grid = self.grid
+        V = self.getVtotal(0)                                           # :20
+        nnn = self.Ntotal if self.Ntotal > 0 else 1                     # :21-25
+        phi = self.process_init_state(phi0, rng=rng)                    # :27
+        self.current_state = phi                                        # :28
+        self.set_kinop(dt)                                              # :30
+        MU = np.zeros(self.itp_max_iter)
+        MU2 = np.zeros(self.itp_max_iter)
+        EE = np.zeros(self.itp_max_iter)
+        i = 0
+        self.itp_deltas = []
+        dtmin = math.sqrt(eps)                                          # :35
+        self.nlinop = np.exp(-dt * 0.5 * (np.abs(phi) ** 2 * self.g + V))  # :36
+        while True:
+            i += 1
+            phi = self.nlinop * phi                                     # :40
+            phi = self.ssft_kin_step(phi, dt)                           # :41
+            phi = self.nlinop * phi                                     # :42
+            self.nlinop = np.abs(phi) ** 2                              # :44
+            if self.Ntotal > 0:
+                mu = math.sqrt(self.Ntotal / grid.integrate(self.nlinop))  # :46
+                MU[i - 1] = math.log(mu) / dt
+            else:
+                mu = math.exp(self.mu_init * dt)
+                MU[i - 1] = grid.integrate(self.nlinop) * mu ** 2
+            phi = phi * mu                                              # :52
+            if i > self.itp_min_iter and i % 10 == 0:                   # :54
+                if nargout >= 3:
+                    MU2[i - 1] = np.real(grid.inner(phi, self.applyham(phi)))
+                if nargout >= 4:
+                    EE[i - 1] = self.get_energy(phi)
+                delta = np.max(np.abs(np.abs(phi.ravel()) - np.abs(self.current_state.ravel()))) / (dt * 10)
+                self.itp_deltas.append((i, delta))  # diagnostics only
+                self.current_state = phi
+                if delta < eps:
+                    if nargout >= 3:
+                        dtmin = dt * math.sqrt(eps / abs(MU[i - 1] - MU2[i - 1] / nnn))
+                    if (not self.itp_adjust_stepsize) or dt < dtmin:
+                        break
+                    dt = dt / 2
+                    self.set_kinop(dt)
+            self.nlinop = np.exp(-dt * 0.5 * (self.nlinop * self.g * mu ** 2 + V))  # :76
+            if i >= self.itp_max_iter:
+                warnings.warn("Convergence not reached")
+                break
+        MU = MU[:i].copy()
+        if self.Ntotal > 0:
+            self.current_mu = MU[-1]
+            self.current_n = self.Ntotal
+            MU2 = MU2[:i] / self.Ntotal
+            EE = EE[:i] / self.Ntotal
+        else:
+            MU2 = MU2[:i] / MU
+            self.current_mu = MU2[-1]
+            self.current_n = MU[-1]
+            EE = EE[:i] / MU
+        self.init_state = phi                                           # :111
+        return phi, MU, MU2, EE
+
+    # lib/@GPEtask/solve_split.m:1-84
+    def solve_split(self, ddt, niter_inner, niter_outer, inner_callback=None):
+        """``inner_callback(i)`` (timing hook, not in the reference) runs after
+        every inner step; it may raise to stop the run."""
+        grid = self.grid
+        g = self.g
+        NN0 = self.Ntotal if self.Ntotal > 0 else grid.integrate(np.abs(self.init_state) ** 2)  # :17-21
+        NNN = NN0
+        gam = self.gamma
+        n_rec = self.n_recalc
+        if niter_inner % n_rec != 0:                                    # :25-27
+            n_rec = 1
+        tau = self.decay_rate
+        start = self.current_iter
+        dt = ddt * 1j / (1 + 1j * gam)                                  # :31
+        self.set_kinop(dt)
+        phi = self.current_state if start > 0 else self.init_state      # :34-38
+        self.nlinop = np.real(phi * np.conj(phi))                       # :40
+        muc = np.real(grid.inner(phi, self.applyham(phi))) / NN0        # :41
+        mu = self.mu_init if self.mu_init > 0 else muc                  # :42-46
+        dt_outer = ddt * niter_inner
+        ncur = None
+        time2 = None
+        for j in range(start + 1, niter_outer + 1):                     # :49
+            time = (j - 1) * dt_outer
+            for jj in range(1, niter_inner // n_rec + 1):               # :51
+                time2 = time + (jj - 1) * ddt * n_rec
+                VV = self.getVtotal(time2) - mu                         # :54
+                self.nlinop = np.exp((-VV - g * self.nlinop) * dt * 0.5)
+                phi = self.nlinop * phi
+                for _ in range(n_rec):                                  # :58-62
+                    phi = self.ssft_kin_step(phi, dt)
+                    self.nlinop = np.exp((-VV - g * phi * np.conj(phi)) * dt)
+                    phi = self.nlinop * phi
+                    if inner_callback is not None:
+                        inner_callback(j)
+                self.nlinop = np.exp((VV + g * phi * np.conj(phi)) * dt * 0.5)  # :63-64
+                phi = self.nlinop * phi
+                self.nlinop = np.real(phi * np.conj(phi))               # :65
+                ncur = grid.integrate(self.nlinop)                      # :67
+                if gam > 0 and self.mu_init == 0:                       # :68-75
+                    if tau > 0:
+                        NNN = NN0 * math.exp(-time2 / tau)
+                    phi = phi * math.sqrt(NNN / ncur)
+                    self.nlinop = self.nlinop * (NNN / ncur)
+                    muc = np.real(grid.inner(phi, self.applyham(phi, time2))) / NNN
+                    mu = muc
+                else:                                                   # :76-78
+                    muc = np.real(grid.inner(phi, self.applyham(phi, time2))) / ncur
+            self.ext_callback(phi, j, time2, muc, ncur)                 # :80
+        return phi
+
+
+def _set_hist(lst, step, val):
+    """MATLAB ``history.mu(step) = mu`` grows the row vector with zeros."""
+    while len(lst) < step:
+        lst.append(0.0)
+    lst[step - 1] = val
+
+
+# ---------------------------------------------------------------------------
+# Vortex imprint: examples/example1_vortex.m:26-30 (also README.md:93-97)
+# ---------------------------------------------------------------------------
+def imprint_vortex(grid: Grid, phi, g, x0, y0=0.0):
+    """psi * tanh(r/xi) * exp(i*atan2(X - x0, Y - y0)), xi = 1/sqrt(2 g max|psi|^2).
+
+    The argument order of atan2 follows example1_vortex.m:29 exactly.
+    """
+    xi = 1.0 / math.sqrt(2 * g * np.max(np.abs(phi)) ** 2)
+    X, Y = grid.mesh["x"], grid.mesh["y"]
+    rr = np.sqrt((X - x0) ** 2 + (Y - y0) ** 2)
+    angs = np.arctan2(X - x0, Y - y0)
+    return phi * np.tanh(rr / xi) * np.exp(1j * angs)

@@ -1,0 +1,151 @@
+"""CPU checks of the FP64 oracle (oracle/gpe_oracle.py).
+
+The reference ships no tests or golden vectors and MATLAB is absent, so the
+oracle is pinned to analytic known answers of the Gross-Pitaevskii equation
+and of the reference's split-step scheme, plus the committed golden fixtures
+(regression pins of the oracle itself, tests/golden/make_golden.py).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import gpe_oracle as O
+
+
+def harmonic(lam=(1.0, 1.0, 1.0)):
+    def V(X, Y, Z):
+        return 0.5 * ((lam[0] * X) ** 2 + (lam[1] * Y) ** 2 + (lam[2] * Z) ** 2)
+    return V
+
+
+def test_grid_matches_matlab_definitions():
+    g = O.Grid(17, 8, 5, 12)
+    assert g.shape == (8, 12)
+    x = np.linspace(-17, 17, 8)
+    dx = x[1] - x[0]
+    L = x[-1] - x[0] + dx
+    np.testing.assert_allclose(g.kx1, np.array([0, 1, 2, 3, 4, -3, -2, -1]) * 2 * np.pi / L, rtol=0, atol=1e-15)
+    assert g.weight == pytest.approx(dx * (10 / 11))
+    # meshgrid layout: X varies along axis 0 (MATLAB columns), Y along axis 1 (rows, contiguous)
+    assert np.all(g.mesh["x"][:, 0] == g.x) and np.all(g.mesh["y"][0, :] == g.y)
+    g3 = O.Grid(1, 8, 2, 8, 3, 12)
+    assert g3.shape == (12, 8, 8)
+    assert g3.kk.shape == g3.shape
+    assert g3.kk[0, 0, 1] == pytest.approx(g3.ky1[1] ** 2 / 2)
+
+
+def test_fft_convention_unnormalised_forward():
+    g = O.Grid(4, 16, 4, 16)
+    a = np.ones(g.shape, dtype=complex)
+    assert g.fft(a)[0, 0] == pytest.approx(256)
+    np.testing.assert_allclose(g.ifft(g.fft(a)), a, atol=1e-14)
+
+
+@pytest.mark.parametrize("dt", [0.01])
+def test_itp_harmonic_2d_ground_state_energy(dt):
+    # g = 0, omega = 1: mu = E/N = 1 (two 1/2 zero-point energies).
+    g = O.Grid(8, 64, 8, 64)
+    t = O.GPEtask(g, harmonic())
+    t.Ntotal = 1.0
+    t.g = 0.0
+    phi0 = np.exp(-((g.mesh["x"] - 0.3) ** 2 + g.mesh["y"] ** 2) / 3.0).astype(complex)
+    phi, MU, MU2, EE = t.groundstate_itp(dt, 1e-9, phi0)
+    assert MU[-1] == pytest.approx(1.0, abs=5e-5)        # Strang error O(dt^2)
+    assert EE[-1] == pytest.approx(1.0, abs=1e-7)        # variational: O(dt^4)
+    assert MU2[-1] == pytest.approx(1.0, abs=1e-7)
+    assert g.integrate(np.abs(phi) ** 2) == pytest.approx(1.0, rel=1e-12)
+
+
+def test_itp_anisotropic_3d_ground_state_energy():
+    # g = 0, lambda = 4: mu = (1 + 1 + 4)/2 = 3.
+    g = O.Grid(6, 32, 6, 32, 6, 32)
+    t = O.GPEtask(g, harmonic((1, 1, 4)))
+    t.Ntotal = 1.0
+    t.g = 0.0
+    X, Y, Z = g.mesh["x"], g.mesh["y"], g.mesh["z"]
+    phi0 = np.exp(-(X ** 2 + Y ** 2 + 4 * Z ** 2) / 1.5).astype(complex)
+    phi, MU, MU2, EE = t.groundstate_itp(0.005, 1e-8, phi0)
+    assert EE[-1] == pytest.approx(3.0, abs=1e-5)        # grid + convergence error
+    assert MU[-1] == pytest.approx(3.0, abs=1e-4)
+
+
+def test_itp_thomas_fermi_limit_2d():
+    # Large gN: mu -> sqrt(g N / pi) for V = r^2/2 (loose, kinetic energy neglected).
+    g = O.Grid(17, 128, 17, 128)
+    t = O.GPEtask(g, harmonic())
+    t.Ntotal = 1e5
+    t.g = 0.06
+    phi0 = np.exp(-(g.mesh["x"] ** 2 + g.mesh["y"] ** 2) / 32).astype(complex)
+    phi, MU = t.groundstate_itp(0.02, 1e-6, phi0, nargout=2)[:2]
+    assert MU[-1] == pytest.approx(math.sqrt(0.06 * 1e5 / math.pi), rel=2e-3)
+
+
+def test_split_plane_wave_is_exact():
+    # V = 0, g = 0: a grid plane wave only acquires exp(-i (k^2/2 - mu) t).
+    g = O.Grid(5, 32, 5, 32)
+    t = O.GPEtask(g, lambda X, Y, Z: 0 * X)
+    kx, ky = g.kx1[3], g.ky1[-2]
+    psi0 = np.exp(1j * (kx * g.mesh["x"] + ky * g.mesh["y"]))
+    t.init_state = psi0
+    t.mu_init = 0.3
+    t.solve_split(0.01, 20, 3)
+    T = 0.01 * 20 * 3
+    expect = psi0 * np.exp(-1j * ((kx ** 2 + ky ** 2) / 2 - 0.3) * T)
+    np.testing.assert_allclose(t.current_state, expect, rtol=0, atol=1e-12)
+
+
+def test_split_gamma0_conserves_norm_and_is_time_reversible():
+    g = O.Grid(6, 32, 6, 32)
+    t = O.GPEtask(g, harmonic((1.0, 1.3, 1.0)))
+    t.g = 2.0
+    t.mu_init = 1.5  # a fixed mu: the state-derived mu is not time-symmetric
+    rng = np.random.default_rng(5)
+    psi0 = np.exp(-(g.mesh["x"] ** 2 + g.mesh["y"] ** 2) / 4) * (1 + 0.1 * rng.standard_normal(g.shape))
+    psi0 = psi0 * np.exp(0.4j * g.mesh["x"])
+    t.init_state = psi0
+    t.solve_split(0.005, 10, 4)
+    n0 = g.integrate(np.abs(psi0) ** 2)
+    np.testing.assert_allclose(t.history["n"], n0, rtol=1e-12)
+    # conj -> propagate -> conj returns the start (symmetric Strang, gamma = 0)
+    back = O.GPEtask(g, harmonic((1.0, 1.3, 1.0)))
+    back.g = 2.0
+    back.mu_init = 1.5
+    back.init_state = np.conj(t.current_state)
+    back.solve_split(0.005, 10, 4)
+    np.testing.assert_allclose(np.conj(back.current_state), psi0, rtol=0, atol=1e-11)
+
+
+def test_split_damping_renormalises_and_decays():
+    g = O.Grid(6, 32, 6, 32)
+    t = O.GPEtask(g, harmonic())
+    t.g = 1.0
+    t.Ntotal = 50.0
+    t.gamma = 0.05
+    t.decay_rate = 2.0
+    phi0 = np.exp(-(g.mesh["x"] ** 2 + g.mesh["y"] ** 2) / 4).astype(complex)
+    t.init_state = math.sqrt(50) * g.normalize(phi0)
+    t.solve_split(0.01, 10, 3)
+    # after renormalisation the norm is NNN = N0 exp(-time2/tau) of the last block
+    assert g.integrate(np.abs(t.current_state) ** 2) == pytest.approx(50 * math.exp(-t.current_time / 2.0),
+                                                                     rel=1e-12)
+
+
+def test_vortex_imprint_matches_example():
+    g = O.Grid(8, 32, 8, 32)
+    phi = np.ones(g.shape, complex) * 2.0
+    out = O.imprint_vortex(g, phi, 0.5, 1.0)
+    xi = 1 / math.sqrt(2 * 0.5 * 4.0)
+    X, Y = g.mesh["x"], g.mesh["y"]
+    np.testing.assert_allclose(np.abs(out), 2 * np.tanh(np.sqrt((X - 1) ** 2 + Y ** 2) / xi))
+    np.testing.assert_allclose(np.angle(out[5, 20]), np.arctan2(X[5, 20] - 1, Y[5, 20]))
+
+
+def test_golden_fixtures_reproduce():
+    from tests.golden import make_golden as MG
+
+    for name, fn in MG.CASES.items():
+        ref = np.load(MG.path(name))
+        out = fn()
+        for k in ref.files:
+            np.testing.assert_allclose(out[k], ref[k], rtol=1e-12, atol=1e-12, err_msg=f"{name}:{k}")
