@@ -204,6 +204,7 @@ def run_gpu(args, dist):
     dev = dist.local
     P = W.npoints
     grid, task, phi = ground_state(gpe, W, "single", device=dev)
+    task.set_pass_variant(args.pass_variant)
     itp = task.last_itp
     phi = np.asarray(phi)
     # ---- FP32 timed region ------------------------------------------------
@@ -242,6 +243,11 @@ def run_gpu(args, dist):
     if tf.exists():
         d = json.loads(tf.read_text())
         traffic = d.get(top["name"], {}).get("bytes_per_launch_256cube")
+    if args.quick:
+        print(json.dumps({"value": value, "roofline_kernel": top["name"], "frac": achieved / hbm,
+                          "kernels": [(k["name"], round(1e3 * k["total_ms"] / k["launches"], 1)) for k in stats]}))
+        task.close()
+        return
     # ---- FP64 arm (same kernels, same start) ----------------------------------
     g64, t64 = W.make_task("double", device=dev)
     t64.init_state = phi.astype(np.complex128)
@@ -311,12 +317,13 @@ def run_gpu(args, dist):
     task.close()
 
 
-def run_profile_case(precision: str, blocks: int):
+def run_profile_case(precision: str, blocks: int, variant: int = 0):
     """Small fixed case for ncu captures: the bench workload's grid and
     parameters from the seeded Gaussian (no ITP), `blocks` blocks of 10 steps."""
     from gpe_gb300.workloads import DAMPED3D as W
 
     grid, task = W.make_task(precision)
+    task.set_pass_variant(variant)
     task.init_state = W.initial_state(grid) * 30.0
     task.solve_split(W.dt, 10, blocks)
     print(json.dumps({"profile_case": precision, "blocks": blocks, "launches": task.kernel_launches(),
@@ -335,9 +342,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="FP32 timed region only (no FP64, e2e, CPU legs)")
+    ap.add_argument("--pass-variant", type=int, default=0, help="0: TMA-staged passes (default), 1: direct")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args.profile_case, args.profile_blocks)
+        run_profile_case(args.profile_case, args.profile_blocks, args.pass_variant)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -41,11 +41,14 @@ def _headers_mtime() -> float:
     return max((h.stat().st_mtime for h in hs), default=0.0)
 
 
+EXTRA: list = []
+
+
 def _compile(src: Path, force: bool, verbose: bool) -> Path:
     obj = BUILD / (src.stem + ".o")
     if not force and obj.exists() and obj.stat().st_mtime >= max(src.stat().st_mtime, _headers_mtime()):
         return obj
-    cmd = [nvcc(), *ARCH, *NVFLAGS, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *NVFLAGS, *EXTRA, "-c", str(src), "-o", str(obj)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -56,8 +59,16 @@ def _compile(src: Path, force: bool, verbose: bool) -> Path:
     return obj
 
 
-def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -> Path:
-    BUILD.mkdir(exist_ok=True)
+def build(force: bool = False, jobs: int | None = None, verbose: bool = False, out: Path | None = None,
+          build_dir: Path | None = None, defines: list | None = None) -> Path:
+    """Compile and link; `out`/`build_dir`/`defines` (-D macros) select a variant build."""
+    global BUILD, LIB, EXTRA
+    if out is not None:
+        LIB = Path(out)
+    if build_dir is not None:
+        BUILD = Path(build_dir)
+    EXTRA = [f"-D{d}" for d in (defines or [])]
+    BUILD.mkdir(parents=True, exist_ok=True)
     srcs = sorted(CSRC.glob("*.cu"))
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
@@ -75,7 +86,10 @@ if __name__ == "__main__":
     ap.add_argument("--force", action="store_true")
     ap.add_argument("--jobs", type=int, default=None)
     ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--out", default=None, help="output library path (default: gpe-matlab_gb300/libgpe.so)")
+    ap.add_argument("--build-dir", default=None)
+    ap.add_argument("-D", dest="defines", action="append", default=[], help="preprocessor define NAME=VALUE")
     a = ap.parse_args()
-    p = build(a.force, a.jobs, a.verbose)
+    p = build(a.force, a.jobs, a.verbose, a.out, a.build_dir, a.defines)
     print(p)
     sys.exit(0)

@@ -3,6 +3,9 @@
 // trip), grid reductions and elementwise conversions.
 #include <math.h>
 
+#include <mutex>
+#include <vector>
+
 #include "aux_kernels.cuh"
 
 namespace gpe {
@@ -415,4 +418,39 @@ INST_CONV(float, double)
 INST_CONV(double, float)
 INST_CONV(double, double)
 
+}  // namespace gpe
+
+namespace gpe {
+// Occupancy cache for the TMA passes (host side).
+int resident_ctas(const void* kern, int threads, size_t smem) {
+  struct Key {
+    const void* k;
+    size_t smem;
+    int dev;
+    int val;
+  };
+  static std::mutex mu;
+  static std::vector<Key> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  for (auto& e : cache)
+    if (e.k == kern && e.smem == smem && e.dev == dev) return e.val;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem) != cudaSuccess) n = 1;
+  cache.push_back({kern, smem, dev, n});
+  return n;
+}
+}  // namespace gpe
+
+namespace gpe {
+// Self-test of the FP32 device trigonometry used by the phase factors.
+__global__ void k_selftest_trig(const float* x, float* s, float* c, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    sincos_bounded(x[i], &s[i], &c[i]);
+}
+cudaError_t launch_selftest_trig(const float* x, float* s, float* c, long long n, cudaStream_t st) {
+  k_selftest_trig<<<elem_grid(n, 256), 256, 0, st>>>(x, s, c, n);
+  return cudaGetLastError();
+}
 }  // namespace gpe

@@ -66,6 +66,7 @@ void launch_finalize_norm0(const double* partials, int cap, int nblk, double wei
                            DevScalars* sc, cudaStream_t s);
 void launch_reset_scalars(DevScalars* sc, cudaStream_t s);
 void launch_set_scale_one(DevScalars* sc, cudaStream_t s);
+cudaError_t launch_selftest_trig(const float* x, float* s, float* c, long long n, cudaStream_t st);
 
 template <typename R>
 int launch_norm(const cx<R>* psi, long long n, DevScalars* sc, double* partials, int cap, cudaStream_t s);

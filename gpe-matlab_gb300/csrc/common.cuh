@@ -50,11 +50,43 @@ __device__ __forceinline__ cx<double> ldg(const cx<double>* p) {
   return mk<double>(v.x, v.y);
 }
 
+// sin and cos of x in FP32.  For |x| <= 65536 (any physically meaningful
+// phase per step): Cody-Waite reduction x = q*pi/2 + r with pi/2 split into
+// two floats (q*hi is exact inside the FMA), then the Taylor series of sin
+// to r^9 and of cos to r^10 on |r| <= pi/4 (truncation < 2e-9), and the
+// quadrant rotation.  Larger arguments take sincosf.
+__device__ __forceinline__ void sincos_bounded(float x, float* sp, float* cp) {
+  if (!(fabsf(x) <= 65536.0f)) {
+    sincosf(x, sp, cp);
+    return;
+  }
+  const float q = rintf(x * 0.636619772f);  // 2/pi
+  float r = fmaf(q, -1.57079637e+00f, x);   // pi/2 rounded to float
+  r = fmaf(q, 4.37113900e-08f, r);          // minus (pi/2 - float(pi/2))
+  const float r2 = r * r;
+  float s = fmaf(r2, 2.75573192e-06f, -1.98412698e-04f);  // 1/9!, -1/7!
+  s = fmaf(r2, s, 8.33333333e-03f);                       // 1/5!
+  s = fmaf(r2, s, -1.66666667e-01f);                      // -1/3!
+  s = fmaf(r2 * r, s, r);
+  float c = fmaf(r2, -2.75573192e-07f, 2.48015873e-05f);  // -1/10!, 1/8!
+  c = fmaf(r2, c, -1.38888889e-03f);                      // -1/6!
+  c = fmaf(r2, c, 4.16666667e-02f);                       // 1/4!
+  c = fmaf(r2, c, -0.5f);
+  c = fmaf(r2, c, 1.0f);
+  const int qi = (int)q;
+  float ss = (qi & 1) ? c : s;
+  float cc = (qi & 1) ? s : c;
+  if (qi & 2) ss = -ss;
+  if ((qi + 1) & 2) cc = -cc;
+  *sp = ss;
+  *cp = cc;
+}
+
 // exp(a * (dre + i dim)) for real a: the nonlinear / potential phase factor
 // of the split step, with complex time step dt = i*ddt/(1 + i*gamma).
 __device__ __forceinline__ cx<float> cexp_real_times(float a, float dre, float dim) {
   float s, c;
-  sincosf(a * dim, &s, &c);
+  sincos_bounded(a * dim, &s, &c);
   float m = (dre == 0.0f) ? 1.0f : expf(a * dre);
   return mk<float>(m * c, m * s);
 }
@@ -90,7 +122,8 @@ struct DevScalars {
   int stall;          // ITP checks in a row without a 10% residual drop
   int status;         // StopReason
   int nonfinite;      // a reduction produced NaN/Inf
-  int pad_[3];
+  int timeout;        // a bounded device-side wait gave up
+  int pad_[2];
 };
 
 enum StopReason { RUNNING = 0, CONVERGED = 1, SWITCH_FP64 = 2, HALVE_DT = 3, NONFINITE = 4 };
@@ -131,9 +164,10 @@ struct PassArgs {
   cx<R>* psi;              // state, updated in place
   const R* V;              // total potential V(t)
   R* aux;                  // ITP: nonlinear factor written by pass 1, read by the last
-  const cx<R>* phase;      // kinetic factor exp(-k^2/2 dt)/N of this axis (length N)
-  const cx<R>* tw;         // twiddles exp(-2 pi i q/N), q < N
-  const R* k2h;            // k^2/2 of this axis divided by N (energy pass)
+  const cx<R>* php;        // kinetic factor exp(-k^2/2 dt)/N of this axis, in the
+                           // spectrum-slot order of the threads (pass.cuh apply_phase)
+  const cx<R>* tws;        // stage twiddle rows of the plan (plans.cuh)
+  const R* k2p;            // k^2/2/N in the same permuted order (energy pass)
   double* partials;        // [NSLOTS][cap] per-CTA partial sums
   DevScalars* sc;
   long long n_batch;       // number of pencils
@@ -142,6 +176,7 @@ struct PassArgs {
   int cap;                 // partials capacity per slot
   int kind;                // PassKind
   int pro, epi;            // Prologue / Epilogue
+  int side;                // TMA pass: 0 none, 1 stage V, 2 stage aux with the tile
   int kin_slot;            // energy pass: slot of the kinetic sum
   int energy_pot;          // energy pass: also accumulate n, Vn, n^2
   double g;                // coupling

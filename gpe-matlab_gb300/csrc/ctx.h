@@ -19,9 +19,9 @@ struct Field {
   void* V = nullptr;        // P real
   void* aux = nullptr;      // P real: ITP nonlinear factor
   void* absprev = nullptr;  // P real: |psi| at the previous ITP check
-  void* tw[3] = {nullptr, nullptr, nullptr};     // per axis, N complex
-  void* phase[3] = {nullptr, nullptr, nullptr};  // per axis, N complex
-  void* k2h[3] = {nullptr, nullptr, nullptr};    // per axis, N real
+  void* tws[3] = {nullptr, nullptr, nullptr};    // per axis: stage twiddle rows
+  void* php[3] = {nullptr, nullptr, nullptr};    // per axis: permuted kinetic factor, N complex
+  void* k2p[3] = {nullptr, nullptr, nullptr};    // per axis: permuted k^2/2/N, N real
   double phase_dt[2] = {0.0, 0.0};               // dt the phase tables hold
   bool phase_valid = false;
   bool V_valid = false;
@@ -69,6 +69,8 @@ struct gpe_ctx {
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   std::string err;
 
+  int sms = 152;          // SM count of the device
+  int pass_variant = 0;   // 0: TMA-staged passes where they apply, 1: direct passes only
   bool prof = false;
   std::vector<gpe::ProfRec> prof_pending;
   std::vector<cudaEvent_t> ev_pool;

@@ -45,31 +45,38 @@ __device__ __forceinline__ void dft4(cx<R>& a0, cx<R>& a1, cx<R>& a2, cx<R>& a3)
   a3 = t1 - t3;
 }
 
-// Multiplication by the irrational butterfly constants.  FP32-rounded
-// constants all lie inside the unit circle (|c + i s|^2 - 1 = -3e-8 .. -6e-8),
-// which made every FP32 pass shrink the norm by a fixed ~1e-7; splitting each
-// constant into hi + lo floats and multiplying with an FMA (x*hi + x*lo) makes
-// the product correctly rounded to the exact constant, so the remaining error
-// is unbiased rounding.  FP64 uses the plain constant.
-struct KC {
-  double v;
-  float hi, lo;
+// Irrational butterfly constants.  FP64 uses the correctly rounded values.
+// FP32 cannot hold these unit complex numbers with |z| = 1 exactly: the
+// nearest floats of (cos pi/8, sin pi/8), (1, 1)/sqrt(2) and (-1/2, sqrt(3)/2)
+// all lie inside the unit circle (|z|^2 - 1 = -3e-8 .. -6e-8), which shrank
+// the norm of every FP32 pass by a fixed ~1e-7.  Each FP32 constant is
+// instead a neighbour within one ulp (angle error < 2e-8 rad) picked so that
+// the modulus errors of the constant multiplications inside one butterfly
+// (and one forward + inverse pair) cancel to first order.
+template <typename R>
+struct BK;
+template <>
+struct BK<double> {
+  static constexpr double c16 = 0.92387953251128675613, s16 = 0.38268343236508977173;
+  static constexpr double c2 = 0.70710678118654752440, c2b = 0.70710678118654752440;
+  static constexpr double h3 = 0.86602540378443864676, h3b = 0.86602540378443864676;
 };
-constexpr KC K_C16 = {0.92387953251128675613, 0.9238795042037964f, 2.830748968563057e-08f};  // cos(pi/8)
-constexpr KC K_S16 = {0.38268343236508977173, 0.3826834261417389f, 6.2233507236442165e-09f};  // sin(pi/8)
-constexpr KC K_C2 = {0.70710678118654752440, 0.7071067690849304f, 1.2101617485882343e-08f};   // 1/sqrt(2)
-constexpr KC K_H3 = {0.86602540378443864676, 0.8660253882408142f, 1.5543625053737742e-08f};   // sin(2 pi/3)
+template <>
+struct BK<float> {
+  // |(c16, s16)|^2 - 1 = +5.3e-8 offsets the four 1/sqrt(2) products of a
+  // radix-16 butterfly (2 c2^2 - 1 = -3.4e-8 each).
+  static constexpr float c16 = 0.9238795638084412f, s16 = 0.3826834261417389f;
+  static constexpr float c2 = 0.7071067690849304f;   // 2 c^2 - 1 = -3.4e-8
+  static constexpr float c2b = 0.7071068286895752f;  // 2 c^2 - 1 = +1.3e-7, one use in four
+  static constexpr float h3 = 0.8660253882408142f;   // 1/4 + h^2 - 1 = -2.7e-8
+  static constexpr float h3b = 0.866025447845459f;   // 1/4 + h^2 - 1 = +7.6e-8, one use in four
+};
 
-__device__ __forceinline__ float kmul(float x, KC k) { return fmaf(x, k.hi, x * k.lo); }
-__device__ __forceinline__ double kmul(double x, KC k) { return x * k.v; }
-
-// a * (sc*C + i*ss*S) for constants C, S and signs sc, ss in {+1, -1}.
+// a * (SC*C + i*SS*S) for constants C, S and signs SC, SS in {+1, -1}.
 template <typename R, int SC, int SS>
-__device__ __forceinline__ cx<R> rotk(cx<R> a, KC C, KC S) {
-  const R xc = kmul(a.x, C), yc = kmul(a.y, C), xs = kmul(a.x, S), ys = kmul(a.y, S);
-  const R c_x = SC > 0 ? xc : -xc, c_y = SC > 0 ? yc : -yc;
-  const R s_x = SS > 0 ? xs : -xs, s_y = SS > 0 ? ys : -ys;
-  return mk<R>(c_x - s_y, s_x + c_y);
+__device__ __forceinline__ cx<R> rotk(cx<R> a, R C, R S) {
+  const R cc = SC > 0 ? C : -C, ss = SS > 0 ? S : -S;
+  return mk<R>(a.x * cc - a.y * ss, a.x * ss + a.y * cc);
 }
 
 template <typename R, int DIR>
@@ -77,7 +84,7 @@ __device__ __forceinline__ void dft3(cx<R>& a0, cx<R>& a1, cx<R>& a2) {
   cx<R> t = a1 + a2;
   cx<R> d = a1 - a2;
   cx<R> m = mk<R>(a0.x - R(0.5) * t.x, a0.y - R(0.5) * t.y);
-  const R hx = kmul(d.x, K_H3), hy = kmul(d.y, K_H3);  // sin(2 pi/3) * d
+  const R hx = d.x * BK<R>::h3, hy = d.y * BK<R>::h3;  // sin(2 pi/3) * d
   // forward: X1 = m - i h d, X2 = m + i h d
   cx<R> s = DIR < 0 ? mk<R>(hy, -hx) : mk<R>(-hy, hx);
   a0 = a0 + t;
@@ -85,17 +92,17 @@ __device__ __forceinline__ void dft3(cx<R>& a0, cx<R>& a1, cx<R>& a2) {
   a2 = m - s;
 }
 
-template <typename R, int DIR>
-__device__ __forceinline__ cx<R> w8(cx<R> a, int q) {  // a * exp(DIR*2 pi i q/8), q in 0..3
+// a * exp(DIR*2 pi i q/8), q in 0..3; ALT selects the second 1/sqrt(2).
+template <typename R, int DIR, bool ALT = false>
+__device__ __forceinline__ cx<R> w8(cx<R> a, int q) {
+  const R c = ALT ? BK<R>::c2b : BK<R>::c2;
   if (q == 0) return a;
   if (q == 2) return mul_mi<R, DIR>(a);
   if (q == 1) {  // (c, DIR*c)
-    return DIR < 0 ? mk<R>(kmul(a.x + a.y, K_C2), kmul(a.y - a.x, K_C2))
-                   : mk<R>(kmul(a.x - a.y, K_C2), kmul(a.x + a.y, K_C2));
+    return DIR < 0 ? mk<R>((a.x + a.y) * c, (a.y - a.x) * c) : mk<R>((a.x - a.y) * c, (a.x + a.y) * c);
   }
   // q == 3: (-c, DIR*c)
-  return DIR < 0 ? mk<R>(kmul(a.y - a.x, K_C2), -kmul(a.x + a.y, K_C2))
-                 : mk<R>(-kmul(a.x + a.y, K_C2), kmul(a.x - a.y, K_C2));
+  return DIR < 0 ? mk<R>((a.y - a.x) * c, -((a.x + a.y) * c)) : mk<R>(-((a.x + a.y) * c), (a.x - a.y) * c);
 }
 
 template <typename R, int DIR>
@@ -106,7 +113,7 @@ __device__ __forceinline__ void dft8(cx<R>* u) {
   dft4<R, DIR>(o0, o1, o2, o3);
   o1 = w8<R, DIR>(o1, 1);
   o2 = w8<R, DIR>(o2, 2);
-  o3 = w8<R, DIR>(o3, 3);
+  o3 = w8<R, DIR, (DIR > 0)>(o3, 3);  // forward + inverse: three c2, one c2b
   u[0] = e0 + o0; u[4] = e0 - o0;
   u[1] = e1 + o1; u[5] = e1 - o1;
   u[2] = e2 + o2; u[6] = e2 - o2;
@@ -118,12 +125,12 @@ __device__ __forceinline__ cx<R> w16(cx<R> a, int q) {  // a * exp(DIR*2 pi i q/
   constexpr int D = DIR < 0 ? -1 : 1;
   switch (q) {
     case 0: return a;
-    case 1: return rotk<R, 1, D>(a, K_C16, K_S16);     // ( cos pi/8,  D sin pi/8)
-    case 2: return w8<R, DIR>(a, 1);                   // ( c2,  D c2)
-    case 3: return rotk<R, 1, D>(a, K_S16, K_C16);     // ( sin pi/8,  D cos pi/8)
+    case 1: return rotk<R, 1, D>(a, BK<R>::c16, BK<R>::s16);    // ( cos pi/8,  D sin pi/8)
+    case 2: return w8<R, DIR>(a, 1);                            // ( c2,  D c2)
+    case 3: return rotk<R, 1, D>(a, BK<R>::s16, BK<R>::c16);    // ( sin pi/8,  D cos pi/8)
     case 4: return mul_mi<R, DIR>(a);
-    case 6: return w8<R, DIR>(a, 3);                   // (-c2,  D c2)
-    case 9: return rotk<R, -1, -D>(a, K_C16, K_S16);   // (-cos pi/8, -D sin pi/8)
+    case 6: return w8<R, DIR>(a, 3);                            // (-c2,  D c2)
+    case 9: return rotk<R, -1, -D>(a, BK<R>::c16, BK<R>::s16);  // (-cos pi/8, -D sin pi/8)
     default: return a;  // q = 5, 7, 8 never occur (q = n2*k1, n2,k1 < 4)
   }
 }
@@ -159,9 +166,10 @@ __device__ __forceinline__ void dft6(cx<R>* u) {
   cx<R> o0 = u[1], o1 = u[3], o2 = u[5];
   dft3<R, DIR>(e0, e1, e2);
   dft3<R, DIR>(o0, o1, o2);
-  // W6^1 = (1/2, DIR*h), W6^2 = (-1/2, DIR*h), h = sin(2 pi/3)
-  const R h1x = kmul(o1.x, K_H3), h1y = kmul(o1.y, K_H3);
-  const R h2x = kmul(o2.x, K_H3), h2y = kmul(o2.y, K_H3);
+  // W6^1 = (1/2, DIR*h), W6^2 = (-1/2, DIR*h), h = sin(2 pi/3); with the two
+  // DFT3s: three uses of h3, one of h3b.
+  const R h1x = o1.x * BK<R>::h3b, h1y = o1.y * BK<R>::h3b;
+  const R h2x = o2.x * BK<R>::h3, h2y = o2.y * BK<R>::h3;
   o1 = DIR < 0 ? mk<R>(R(0.5) * o1.x + h1y, R(0.5) * o1.y - h1x) : mk<R>(R(0.5) * o1.x - h1y, R(0.5) * o1.y + h1x);
   o2 = DIR < 0 ? mk<R>(-R(0.5) * o2.x + h2y, -R(0.5) * o2.y - h2x)
                : mk<R>(-R(0.5) * o2.x - h2y, -R(0.5) * o2.y + h2x);
@@ -189,8 +197,40 @@ __device__ __forceinline__ int scatter_pos(int j, int r) {
   return (j / Ns) * Ns * RAD + (j % Ns) + r * Ns;
 }
 
+// u[r] *= w_r (DIR < 0) or u[r] *= conj(w_r) (DIR > 0), r = 1..RAD-1, where
+// w_r = exp(-2 pi i r k/(Ns RAD)) comes from the stage's twiddle rows.  The
+// rows are stored k-fastest so that adjacent lanes (adjacent k) read adjacent
+// addresses: FP32 stages of even radix as [r/2][k] pairs of entries (one
+// 16-byte vector load gives w_{2i}, w_{2i+1}), otherwise as [r][k] entries.
+template <int Ns, int RAD, int DIR>
+__device__ __forceinline__ void apply_row(cx<float>* u, const cx<float>* __restrict__ rows, int k) {
+  if constexpr (RAD % 2 == 0) {
+    const float4* r4 = reinterpret_cast<const float4*>(rows) + k;
+#pragma unroll
+    for (int i = 0; i < RAD / 2; ++i) {
+      const float4 q = __ldg(r4 + i * Ns);
+      if (i > 0) u[2 * i] = DIR < 0 ? cmul(u[2 * i], mk<float>(q.x, q.y)) : cmulc(u[2 * i], mk<float>(q.x, q.y));
+      u[2 * i + 1] = DIR < 0 ? cmul(u[2 * i + 1], mk<float>(q.z, q.w)) : cmulc(u[2 * i + 1], mk<float>(q.z, q.w));
+    }
+  } else {
+#pragma unroll
+    for (int r = 1; r < RAD; ++r) {
+      const cx<float> w = ldg(rows + r * Ns + k);
+      u[r] = DIR < 0 ? cmul(u[r], w) : cmulc(u[r], w);
+    }
+  }
+}
+template <int Ns, int RAD, int DIR>
+__device__ __forceinline__ void apply_row(cx<double>* u, const cx<double>* __restrict__ rows, int k) {
+#pragma unroll
+  for (int r = 1; r < RAD; ++r) {
+    const cx<double> w = ldg(rows + r * Ns + k);
+    u[r] = DIR < 0 ? cmul(u[r], w) : cmulc(u[r], w);
+  }
+}
+
 template <typename R, int N, int T, int Ns, int RAD>
-__device__ __forceinline__ void fwd_stage(cx<R>* v, int t, const cx<R>* __restrict__ tw) {
+__device__ __forceinline__ void fwd_stage(cx<R>* v, int t, const cx<R>* __restrict__ rows) {
   constexpr int E = N / T;
   constexpr int NB = E / RAD;
 #pragma unroll
@@ -198,11 +238,7 @@ __device__ __forceinline__ void fwd_stage(cx<R>* v, int t, const cx<R>* __restri
     cx<R> u[RAD];
 #pragma unroll
     for (int r = 0; r < RAD; ++r) u[r] = v[b + r * NB];
-    if constexpr (Ns > 1) {
-      const int k = (t + T * b) % Ns;
-#pragma unroll
-      for (int r = 1; r < RAD; ++r) u[r] = cmul(u[r], ldg(&tw[r * k * (N / (Ns * RAD))]));
-    }
+    if constexpr (Ns > 1) apply_row<Ns, RAD, -1>(u, rows, (t + T * b) % Ns);
     dft<R, RAD, -1>(u);
 #pragma unroll
     for (int r = 0; r < RAD; ++r) v[b + r * NB] = u[r];
@@ -210,7 +246,7 @@ __device__ __forceinline__ void fwd_stage(cx<R>* v, int t, const cx<R>* __restri
 }
 
 template <typename R, int N, int T, int Ns, int RAD>
-__device__ __forceinline__ void inv_stage(cx<R>* v, int t, const cx<R>* __restrict__ tw) {
+__device__ __forceinline__ void inv_stage(cx<R>* v, int t, const cx<R>* __restrict__ rows) {
   constexpr int E = N / T;
   constexpr int NB = E / RAD;
 #pragma unroll
@@ -219,11 +255,7 @@ __device__ __forceinline__ void inv_stage(cx<R>* v, int t, const cx<R>* __restri
 #pragma unroll
     for (int r = 0; r < RAD; ++r) u[r] = v[b + r * NB];
     dft<R, RAD, +1>(u);
-    if constexpr (Ns > 1) {
-      const int k = (t + T * b) % Ns;
-#pragma unroll
-      for (int r = 1; r < RAD; ++r) u[r] = cmulc(u[r], ldg(&tw[r * k * (N / (Ns * RAD))]));
-    }
+    if constexpr (Ns > 1) apply_row<Ns, RAD, +1>(u, rows, (t + T * b) % Ns);
 #pragma unroll
     for (int r = 0; r < RAD; ++r) v[b + r * NB] = u[r];
   }
@@ -259,35 +291,27 @@ __device__ __forceinline__ void xchg_own_to_scatter(cx<R>* v, cx<R>* sm, const S
   pol.sync();
 }
 
-template <typename R, int N, int T, int Ns, int RAD, int... REST>
+// OFF: offset of this stage's twiddle rows (used when Ns > 1).
+template <typename R, int N, int T, int Ns, int OFF, int RAD, int... REST>
 struct Stages {
+  static constexpr int NEXT_OFF = (Ns > 1) ? OFF + ((Ns * RAD + 1) & ~1) : OFF;
   template <class SM>
   static __device__ __forceinline__ void forward(cx<R>* v, cx<R>* sm, const SM& pol, int t,
-                                                 const cx<R>* __restrict__ tw) {
-    fwd_stage<R, N, T, Ns, RAD>(v, t, tw);
+                                                 const cx<R>* __restrict__ tws) {
+    fwd_stage<R, N, T, Ns, RAD>(v, t, tws + OFF);
     if constexpr (sizeof...(REST) > 0) {
       xchg_scatter_to_own<R, N, T, Ns, RAD>(v, sm, pol, t);
-      Stages<R, N, T, Ns * RAD, REST...>::forward(v, sm, pol, t, tw);
+      Stages<R, N, T, Ns * RAD, NEXT_OFF, REST...>::forward(v, sm, pol, t, tws);
     }
   }
   template <class SM>
   static __device__ __forceinline__ void inverse(cx<R>* v, cx<R>* sm, const SM& pol, int t,
-                                                 const cx<R>* __restrict__ tw) {
+                                                 const cx<R>* __restrict__ tws) {
     if constexpr (sizeof...(REST) > 0) {
-      Stages<R, N, T, Ns * RAD, REST...>::inverse(v, sm, pol, t, tw);
+      Stages<R, N, T, Ns * RAD, NEXT_OFF, REST...>::inverse(v, sm, pol, t, tws);
       xchg_own_to_scatter<R, N, T, Ns, RAD>(v, sm, pol, t);
     }
-    inv_stage<R, N, T, Ns, RAD>(v, t, tw);
-  }
-  // Natural-order spectrum position held in register slot m after forward().
-  static __device__ __forceinline__ int spec_pos(int t, int m) {
-    if constexpr (sizeof...(REST) > 0) {
-      return Stages<R, N, T, Ns * RAD, REST...>::spec_pos(t, m);
-    } else {
-      constexpr int NB = (N / T) / RAD;
-      const int b = m % NB, r = m / NB;
-      return scatter_pos<Ns, RAD>(t + T * b, r);
-    }
+    inv_stage<R, N, T, Ns, RAD>(v, t, tws + OFF);
   }
 };
 

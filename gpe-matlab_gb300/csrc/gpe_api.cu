@@ -99,6 +99,81 @@ std::vector<AxisPass> axis_passes(const gpe_ctx* c) {
 }
 
 template <typename R>
+cudaError_t dispatch_tma(int N, const PassArgs<R>& a, bool strided, cudaStream_t s, int sms) {
+  switch (N) {
+#define X(v) \
+  case v:    \
+    return launch_pass_tma<R, v>(a, strided, s, sms, nullptr);
+    GPE_FOR_EACH_N(X)
+#undef X
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <typename R>
+int dispatch_tma_grid(int N, const PassArgs<R>& a, bool strided, int sms) {
+  switch (N) {
+#define X(v) \
+  case v:    \
+    return pass_tma_grid<R, v>(a, strided, sms);
+    GPE_FOR_EACH_N(X)
+#undef X
+  }
+  return 0;
+}
+
+template <typename R>
+int dispatch_tma_ffts(int N, bool strided) {
+  switch (N) {
+#define X(v) \
+  case v:    \
+    return pass_tma_ffts<R, v>(strided);
+    GPE_FOR_EACH_N(X)
+#undef X
+  }
+  return 0;
+}
+
+PlanInfo dispatch_plan(int N);
+
+// The TMA pass applies when every tile is one contiguous range (contiguous
+// axis) or N rows of FFTS contiguous, 16-byte aligned elements (strided
+// axes), and a CTA is at least two warps.  pass_variant: 0 = TMA where it
+// applies, 1 = always the direct pass.
+template <typename R>
+size_t dispatch_tma_smem(int N, bool strided) {
+  switch (N) {
+#define X(v) \
+  case v:    \
+    return pass_tma_smem<R, v>(strided);
+    GPE_FOR_EACH_N(X)
+#undef X
+  }
+  return ~(size_t)0;
+}
+
+template <typename R>
+bool use_tma(const gpe_ctx* c, const AxisPass& ap) {
+  if (c->pass_variant == 1) return false;
+  if (dispatch_tma_smem<R>(ap.N, ap.strided) > 200 * 1024) return false;
+  const int ffts = dispatch_tma_ffts<R>(ap.N, ap.strided);
+  if (!ap.strided) return true;
+  const PlanInfo pi = dispatch_plan(ap.N);
+  return ap.inner % ffts == 0 && ap.stride % ffts == 0 && ffts * pi.T >= 64 && (ffts * pi.T) % 32 == 0;
+}
+
+PlanInfo dispatch_plan(int N) {
+  switch (N) {
+#define X(v) \
+  case v:    \
+    return plan_info<v>();
+    GPE_FOR_EACH_N(X)
+#undef X
+  }
+  return PlanInfo{};
+}
+
+template <typename R>
 long long pass_blocks(const AxisPass& p) {
   PassGeom g = dispatch_geom<R>(p.N, p.strided);
   return (p.n_batch + g.ffts - 1) / g.ffts;
@@ -207,46 +282,76 @@ gpe_status upload_cx(gpe_ctx* c, void* dst, const std::vector<std::complex<doubl
   return GPE_OK;
 }
 
+// Table layouts read by the pass kernels (fft.cuh apply_row, pass.cuh
+// apply_phase): k- or thread-fastest, FP32 entries paired for 16-byte loads.
+template <typename R>
+int tw_index(int off, int Ns, int RAD, int k, int r) {
+  if (sizeof(R) == 4 && RAD % 2 == 0) return off + 2 * ((r / 2) * Ns + k) + (r % 2);
+  return off + r * Ns + k;
+}
+template <typename R>
+int slot_index(int T, int t, int m) {
+  if (sizeof(R) == 4) return 2 * ((m / 2) * T + t) + (m % 2);
+  return m * T + t;
+}
+
+// Tables of one axis: stage twiddle rows and k^2/2/N in spectrum-slot order.
 template <typename R>
 gpe_status build_static_tables(gpe_ctx* c, Field& f) {
-  const int na = c->ndims;
-  for (int ax = 0; ax < na; ++ax) {
+  for (int ax = 0; ax < c->ndims; ++ax) {
     const int N = c->n[ax];
-    CU(cudaMalloc(&f.tw[ax], N * 2 * sizeof(R)));
-    CU(cudaMalloc(&f.phase[ax], N * 2 * sizeof(R)));
-    CU(cudaMalloc(&f.k2h[ax], N * sizeof(R)));
-    std::vector<std::complex<double>> tw(N);
-    for (int q = 0; q < N; ++q) {
-      const double ang = 2.0 * M_PI * (double)q / (double)N;
-      tw[q] = std::complex<double>(std::cos(ang), -std::sin(ang));
+    const PlanInfo pi = dispatch_plan(N);
+    int total = 0, Ns = pi.radix[0];
+    for (int s = 1; s < pi.nstages; ++s) {
+      total += (Ns * pi.radix[s] + 1) & ~1;
+      Ns *= pi.radix[s];
     }
-    CHECK(upload_cx<R>(c, f.tw[ax], tw));
+    std::vector<std::complex<double>> rows(std::max(total, 2), std::complex<double>(0.0, 0.0));
+    Ns = pi.radix[0];
+    for (int s = 1; s < pi.nstages; ++s) {
+      const int RAD = pi.radix[s];
+      const int off = stage_rows_offset(pi, s);
+      for (int k = 0; k < Ns; ++k)
+        for (int r = 0; r < RAD; ++r) {
+          const double ang = -2.0 * M_PI * (double)(r * k) / (double)(Ns * RAD);
+          rows[tw_index<R>(off, Ns, RAD, k, r)] = std::complex<double>(std::cos(ang), std::sin(ang));
+        }
+      Ns *= RAD;
+    }
+    CU(cudaMalloc(&f.tws[ax], rows.size() * 2 * sizeof(R)));
+    CHECK(upload_cx<R>(c, f.tws[ax], rows));
+    CU(cudaMalloc(&f.php[ax], N * 2 * sizeof(R)));
+    CU(cudaMalloc(&f.k2p[ax], N * sizeof(R)));
     std::vector<R> k2(N);
-    for (int p = 0; p < N; ++p) {
-      const double k = kval(c, ax, p);
-      k2[p] = (R)(k * k / 2.0 / N);
-    }
-    CU(cudaMemcpy(f.k2h[ax], k2.data(), N * sizeof(R), cudaMemcpyHostToDevice));
+    for (int t = 0; t < pi.T; ++t)
+      for (int m = 0; m < pi.E; ++m) {
+        const double k = kval(c, ax, plan_spec_pos(pi, t, m));
+        k2[m * pi.T + t] = (R)(k * k / 2.0 / N);
+      }
+    CU(cudaMemcpy(f.k2p[ax], k2.data(), N * sizeof(R), cudaMemcpyHostToDevice));
   }
   f.phase_valid = false;
   return GPE_OK;
 }
 
 // kinop = exp(-kk*dt) (set_kinop.m:9), as one factor per axis with the 1/N of
-// ifft folded in: exp(-k^2/2*dt)/N, dt = dre + i*dim, evaluated in FP64.
+// ifft folded in: exp(-k^2/2*dt)/N, dt = dre + i*dim, evaluated in FP64 and
+// stored in the threads' spectrum-slot order.
 template <typename R>
 gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
   if (f.phase_valid && f.phase_dt[0] == dre && f.phase_dt[1] == dim) return GPE_OK;
   for (int ax = 0; ax < c->ndims; ++ax) {
     const int N = c->n[ax];
+    const PlanInfo pi = dispatch_plan(N);
     std::vector<std::complex<double>> ph(N);
-    for (int p = 0; p < N; ++p) {
-      const double k = kval(c, ax, p);
-      const double kk = k * k / 2.0;
-      const double mag = std::exp(-kk * dre) / N;
-      ph[p] = std::complex<double>(mag * std::cos(kk * dim), -mag * std::sin(kk * dim));
-    }
-    CHECK(upload_cx<R>(c, f.phase[ax], ph));
+    for (int t = 0; t < pi.T; ++t)
+      for (int m = 0; m < pi.E; ++m) {
+        const double k = kval(c, ax, plan_spec_pos(pi, t, m));
+        const double kk = k * k / 2.0;
+        const double mag = std::exp(-kk * dre) / N;
+        ph[slot_index<R>(pi.T, t, m)] = std::complex<double>(mag * std::cos(kk * dim), -mag * std::sin(kk * dim));
+      }
+    CHECK(upload_cx<R>(c, f.php[ax], ph));
   }
   f.phase_dt[0] = dre;
   f.phase_dt[1] = dim;
@@ -280,9 +385,9 @@ void free_field(Field& f, const double* V64) {
   cudaFree(f.aux);
   cudaFree(f.absprev);
   for (int i = 0; i < 3; ++i) {
-    cudaFree(f.tw[i]);
-    cudaFree(f.phase[i]);
-    cudaFree(f.k2h[i]);
+    cudaFree(f.tws[i]);
+    cudaFree(f.php[i]);
+    cudaFree(f.k2p[i]);
   }
   f = Field();
 }
@@ -318,9 +423,9 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.psi = (cx<R>*)f.psi;
   a.V = (const R*)f.V;
   a.aux = (R*)f.aux;
-  a.phase = (const cx<R>*)f.phase[ap.axis];
-  a.tw = (const cx<R>*)f.tw[ap.axis];
-  a.k2h = (const R*)f.k2h[ap.axis];
+  a.php = (const cx<R>*)f.php[ap.axis];
+  a.tws = (const cx<R>*)f.tws[ap.axis];
+  a.k2p = (const R*)f.k2p[ap.axis];
   a.partials = c->partials;
   a.sc = c->sc;
   a.n_batch = ap.n_batch;
@@ -344,8 +449,18 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   if (pro == PRO_ITP || epi == EPI_ITP) bytes += P * sizeof(R);
   int cls = (kind == KIND_ENERGY ? PC_ENERGY_Y : PC_PASS_Y);
   cls += (ap.axis == 1 ? 0 : ap.axis == 0 ? 1 : 2);
-  if (nblk) *nblk = (int)pass_blocks<R>(ap);
-  {
+  // The array staged with each tile by the TMA pass.
+  a.side = (pro == PRO_RT_HALF || pro == PRO_RT_FULL || pro == PRO_ITP || epi == EPI_RT_END ||
+            (kind == KIND_ENERGY && energy_pot))
+               ? 1
+               : (epi == EPI_ITP ? 2 : 0);
+  if (use_tma<R>(c, ap)) {
+    const int grid = dispatch_tma_grid<R>(ap.N, a, ap.strided, c->sms);
+    if (nblk) *nblk = grid;
+    Launch L(c, cls, bytes);
+    CU(dispatch_tma<R>(ap.N, a, ap.strided, c->stream, c->sms));
+  } else {
+    if (nblk) *nblk = (int)pass_blocks<R>(ap);
     Launch L(c, cls, bytes);
     CU(dispatch_pass<R>(ap.N, a, ap.strided, c->stream));
   }
@@ -510,6 +625,7 @@ gpe_status itp_phase(gpe_ctx* c, Field& f, const gpe_itp_params* prm, ItpState& 
   CHECK(read_scalars(c, &h));
   st.i = h.iter;
   *reason = h.stop ? h.status : RUNNING;
+  if (h.timeout) return fail(c, GPE_ERR_TIMEOUT, "groundstate_itp: a device-side wait for staged data expired");
   if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "groundstate_itp: non-finite norm or residual");
   return GPE_OK;
 }
@@ -750,6 +866,7 @@ gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
   }
   DevScalars h;
   CHECK(read_scalars(c, &h));
+  if (h.timeout) return fail(c, GPE_ERR_TIMEOUT, "solve_split: a device-side wait for staged data expired");
   if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
   if (last_j > start) {
     CU(cudaMemcpy(dh.data(), c->d_hist, dh.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -891,6 +1008,8 @@ gpe_status gpe_create(const gpe_grid_desc* d, gpe_ctx** out) {
     c->err = "cudaStreamCreate failed";
     return cleanup(GPE_ERR_CUDA);
   }
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (c->sms <= 0) c->sms = 152;
   // partial-sum capacity: the largest grid of any pass in either precision
   long long cap = 8LL * 1024;
   for (auto& ap : axis_passes(c)) {
@@ -1194,6 +1313,27 @@ gpe_status gpe_profile_read(gpe_ctx* c, gpe_kernel_stat* out, int cap, int* n) {
 }
 
 long long gpe_kernel_launches(const gpe_ctx* c) { return c ? c->launches : 0; }
+
+gpe_status gpe_selftest_trig(const float* x, float* s, float* co, long long n) {
+  gpe_ctx* c = nullptr;
+  if (!x || !s || !co || n <= 0) return fail(c, GPE_ERR_INVALID, "gpe_selftest_trig: bad arguments");
+  float* d = nullptr;
+  CU(cudaMalloc(&d, 3 * (size_t)n * sizeof(float)));
+  cudaError_t e = cudaMemcpy(d, x, n * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_selftest_trig(d, d + n, d + 2 * n, n, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(s, d + n, n * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(co, d + 2 * n, n * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(c, GPE_ERR_CUDA, std::string("gpe_selftest_trig: ") + cudaGetErrorString(e));
+  return GPE_OK;
+}
+
+gpe_status gpe_set_pass_variant(gpe_ctx* c, int variant) {
+  CHECK(check_ctx(c));
+  if (variant < 0 || variant > 1) return fail(c, GPE_ERR_INVALID, "pass variant must be 0 (auto) or 1 (direct)");
+  c->pass_variant = variant;
+  return GPE_OK;
+}
 
 gpe_status gpe_host_register(void* ptr, size_t bytes) {
   gpe_ctx* c = nullptr;

@@ -115,11 +115,119 @@ __device__ __forceinline__ void cta_reduce_store(double* vals, const int* slots,
   }
 }
 
-template <typename R, class P, class L>
-__global__ void __launch_bounds__(L::THREADS) pass_kernel(const PassArgs<R> a) {
+// Multiply v[0..E) by the thread's kinetic factors.  The permuted table is
+// stored slot-major so adjacent lanes read adjacent addresses: FP32 as
+// [m/2][t] pairs of entries (16-byte vectors), FP64 as [m][t] entries.
+template <int T, int E>
+__device__ __forceinline__ void apply_phase(cx<float>* v, const cx<float>* __restrict__ php, int t) {
+  const float4* r4 = reinterpret_cast<const float4*>(php) + t;
+#pragma unroll
+  for (int i = 0; i < E / 2; ++i) {
+    const float4 q = __ldg(r4 + i * T);
+    v[2 * i] = cmul(v[2 * i], mk<float>(q.x, q.y));
+    v[2 * i + 1] = cmul(v[2 * i + 1], mk<float>(q.z, q.w));
+  }
+}
+template <int T, int E>
+__device__ __forceinline__ void apply_phase(cx<double>* v, const cx<double>* __restrict__ php, int t) {
+#pragma unroll
+  for (int m = 0; m < E; ++m) v[m] = cmul(v[m], ldg(php + m * T + t));
+}
+
+// Occupancy hint: FP32 passes aim at GPE_FP32_THREADS_PER_SM resident
+// threads per SM (the register budget per thread follows from it).
+#ifndef GPE_FP32_THREADS_PER_SM
+#define GPE_FP32_THREADS_PER_SM 768  // 80 registers: no spills; 1024 (64) spilled heavily
+#endif
+template <typename R, class L>
+struct MinBlocks {
+  static constexpr int value =
+      (sizeof(R) == 4 && L::THREADS <= 256) ? GPE_FP32_THREADS_PER_SM / L::THREADS : 1;
+};
+
+// Prologue of the first pass on one pencil's E values (sv: V for the phase
+// modes, unused otherwise).  The mode switch sits outside the unrolled loops
+// so only the selected variant executes (branches inside an unrolled loop
+// are if-converted, which ran every variant).
+template <typename R, int E>
+__device__ __forceinline__ void prologue(cx<R>* v, const R* sv, const PassArgs<R>& a, bool valid,
+                                         long long first, long long dm) {
+  const R s = (R)a.sc->scale;
+  const R mu = (R)a.sc->mu;
+  const R g = (R)a.g, dre = (R)a.dre, dim = (R)a.dim;
+  switch (a.pro) {
+    case PRO_SCALE:
+#pragma unroll
+      for (int m = 0; m < E; ++m) v[m] = rmul(v[m], s);
+      break;
+    case PRO_RT_HALF:  // solve_split.m:55-56
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        const cx<R> p = rmul(v[m], s);
+        const R ex = (-(sv[m] - mu) - g * norm2(p)) * R(0.5);
+        v[m] = cmul(cexp_real_times(ex, dre, dim), p);
+      }
+      break;
+    case PRO_RT_FULL:  // solve_split.m:60-61
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        const R ex = -(sv[m] - mu) - g * norm2(v[m]);
+        v[m] = cmul(cexp_real_times(ex, dre, dim), v[m]);
+      }
+      break;
+    case PRO_ITP:  // groundstate_itp.m:36/76, :40
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        const cx<R> p = rmul(v[m], s);
+        const R nl = rexp(-dre * R(0.5) * (norm2(p) * g + sv[m]));
+        if (valid) a.aux[first + m * dm] = nl;
+        v[m] = rmul(p, nl);
+      }
+      break;
+    default:
+      break;
+  }
+}
+
+// Epilogue of the last pass; sums of valid pencils go to acc.
+template <typename R, int E>
+__device__ __forceinline__ void epilogue(cx<R>* v, const R* sv, const PassArgs<R>& a, Kahan<R>* acc,
+                                         bool valid) {
+  if (a.epi == EPI_RT_END) {
+    const R mu = (R)a.sc->mu;
+    const R g = (R)a.g, dre = (R)a.dre, dim = (R)a.dim;
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      cx<R> p = v[m];
+      const R VV = sv[m] - mu;
+      p = cmul(cexp_real_times(-VV - g * norm2(p), dre, dim), p);            // solve_split.m:60-61
+      p = cmul(cexp_real_times((VV + g * norm2(p)) * R(0.5), dre, dim), p);  // solve_split.m:63-64
+      const R n = norm2(p);                                                  // solve_split.m:65
+      if (valid) {
+        acc[0].add(n);
+        acc[1].add(sv[m] * n);
+        acc[2].add(n * n);
+      }
+      v[m] = p;
+    }
+  } else if (a.epi == EPI_ITP) {
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      v[m] = rmul(v[m], sv[m]);  // groundstate_itp.m:42
+      if (valid) acc[0].add(norm2(v[m]));
+    }
+  }
+}
+
+// KIND is a template parameter so the step and energy variants are separate
+// kernels, each with only its own live ranges and code.
+template <typename R, class P, class L, int KIND>
+__global__ void __launch_bounds__(L::THREADS, MinBlocks<R, L>::value) pass_kernel(const PassArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);
-  if (a.sc->stop) return;  // grid-uniform: an earlier finalizer ended the run
+  // An earlier finalizer (or a timed-out pass) ended the run; the block-wide
+  // vote keeps the decision uniform within the CTA.
+  if (__syncthreads_or(a.sc->stop != 0)) return;
 
   constexpr int T = P::T, E = P::E;
   using St = typename P::template St<R>;
@@ -127,125 +235,90 @@ __global__ void __launch_bounds__(L::THREADS) pass_kernel(const PassArgs<R> a) {
   L::map(threadIdx.x, f, t);
   const long long b = (long long)blockIdx.x * L::FFTS + f;
   const bool valid = b < a.n_batch;
-  const long long base = valid ? L::base(a, b) : 0;
   const long long st = L::step(a);
+  // element m of this thread sits at offset m*dm from its first element
+  const long long first = (valid ? L::base(a, b) : 0) + (long long)t * st;
+  const long long dm = (long long)T * st;
   const auto pol = L::pol(f);
 
   cx<R> v[E];
+  {
+    const cx<R>* __restrict__ src = a.psi + first;
 #pragma unroll
-  for (int m = 0; m < E; ++m)
-    v[m] = valid ? a.psi[base + (long long)(t + T * m) * st] : mk<R>(R(0), R(0));
-
-  Kahan<R> acc[4];
-  int slots[4];
-  int nred = 0;
-
-  // ---- prologue ---------------------------------------------------------
-  if (a.pro != PRO_NONE) {
-    const R s = (R)a.sc->scale;
-    const R mu = (R)a.sc->mu;
-    const R g = (R)a.g, dre = (R)a.dre, dim = (R)a.dim;
-    const bool needV = a.pro == PRO_RT_HALF || a.pro == PRO_RT_FULL || a.pro == PRO_ITP ||
-                       (a.kind == KIND_ENERGY && a.energy_pot);
-    R Vv[E];
-#pragma unroll
-    for (int m = 0; m < E; ++m)
-      Vv[m] = (valid && needV) ? a.V[base + (long long)(t + T * m) * st] : R(0);
-    if (a.kind == KIND_ENERGY && a.energy_pot) nred = 3;
-#pragma unroll
-    for (int m = 0; m < E; ++m) {
-      cx<R> p = v[m];
-      if (a.pro == PRO_SCALE) {
-        p = rmul(p, s);
-        if (a.kind == KIND_ENERGY && a.energy_pot) {
-          R n = norm2(p);
-          acc[0].add(n);
-          acc[1].add(Vv[m] * n);
-          acc[2].add(n * n);
-        }
-      } else if (a.pro == PRO_RT_HALF) {
-        p = rmul(p, s);
-        R ex = (-(Vv[m] - mu) - g * norm2(p)) * R(0.5);
-        p = cmul(cexp_real_times(ex, dre, dim), p);
-      } else if (a.pro == PRO_RT_FULL) {
-        R ex = -(Vv[m] - mu) - g * norm2(p);
-        p = cmul(cexp_real_times(ex, dre, dim), p);
-      } else if (a.pro == PRO_ITP) {
-        p = rmul(p, s);
-        R nl = rexp(-dre * R(0.5) * (norm2(p) * g + Vv[m]));
-        if (valid) a.aux[base + (long long)(t + T * m) * st] = nl;
-        p = rmul(p, nl);
-      }
-      v[m] = p;
-    }
+    for (int m = 0; m < E; ++m) v[m] = valid ? src[m * dm] : mk<R>(R(0), R(0));
   }
 
-  // ---- FFT along the axis -----------------------------------------------
-  St::forward(v, sm, pol, t, a.tw);
-
-  if (a.kind == KIND_ENERGY) {
+  if constexpr (KIND == KIND_ENERGY) {
+    // <psi|L_axis psi> (+ the n, Vn, n^2 sums on request) of the state times
+    // the pending scale (PRO_SCALE) or as stored (PRO_NONE).
+    const R s = a.pro == PRO_SCALE ? (R)a.sc->scale : R(1);
+    Kahan<R> acc[3];
+    const bool pot = a.energy_pot != 0;
+    const R* __restrict__ vs = a.V + first;
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      v[m] = rmul(v[m], s);
+      if (pot) {
+        const R n = norm2(v[m]);
+        const R Vm = valid ? vs[m * dm] : R(0);
+        acc[0].add(n);
+        acc[1].add(Vm * n);
+        acc[2].add(n * n);
+      }
+    }
+    St::forward(v, sm, pol, t, a.tws);
     Kahan<R> kin;
 #pragma unroll
-    for (int m = 0; m < E; ++m) kin.add(__ldg(&a.k2h[St::spec_pos(t, m)]) * norm2(v[m]));
+    for (int m = 0; m < E; ++m) kin.add(__ldg(a.k2p + m * T + t) * norm2(v[m]));
     double vals[4];
-    if (nred == 3) {
+    int slots[4];
+    int nred;
+    if (pot) {
       vals[0] = valid ? acc[0].value() : 0.0;
       vals[1] = valid ? acc[1].value() : 0.0;
       vals[2] = valid ? acc[2].value() : 0.0;
-      slots[0] = S_N; slots[1] = S_VN; slots[2] = S_N2;
+      vals[3] = valid ? kin.value() : 0.0;
+      slots[0] = S_N; slots[1] = S_VN; slots[2] = S_N2; slots[3] = a.kin_slot;
+      nred = 4;
+    } else {
+      vals[0] = valid ? kin.value() : 0.0;
+      slots[0] = a.kin_slot;
+      nred = 1;
     }
-    vals[nred] = valid ? kin.value() : 0.0;
-    slots[nred] = a.kin_slot;
-    cta_reduce_store<L::THREADS>(vals, slots, nred + 1, a.partials, a.cap);
-    return;
-  }
-
-#pragma unroll
-  for (int m = 0; m < E; ++m) v[m] = cmul(v[m], ldg(&a.phase[St::spec_pos(t, m)]));
-
-  St::inverse(v, sm, pol, t, a.tw);
-
-  // ---- epilogue ---------------------------------------------------------
-  if (a.epi == EPI_RT_END) {
-    const R mu = (R)a.sc->mu;
-    const R g = (R)a.g, dre = (R)a.dre, dim = (R)a.dim;
-    R Vv[E];
-#pragma unroll
-    for (int m = 0; m < E; ++m) Vv[m] = valid ? a.V[base + (long long)(t + T * m) * st] : R(0);
-    nred = 3;
-#pragma unroll
-    for (int m = 0; m < E; ++m) {
-      cx<R> p = v[m];
-      const R VV = Vv[m] - mu;
-      p = cmul(cexp_real_times(-VV - g * norm2(p), dre, dim), p);            // solve_split.m:60-61
-      p = cmul(cexp_real_times((VV + g * norm2(p)) * R(0.5), dre, dim), p);  // solve_split.m:63-64
-      const R n = norm2(p);                                                  // solve_split.m:65
-      acc[0].add(n);
-      acc[1].add(Vv[m] * n);
-      acc[2].add(n * n);
-      v[m] = p;
-    }
-    slots[0] = S_N; slots[1] = S_VN; slots[2] = S_N2;
-  } else if (a.epi == EPI_ITP) {
-    nred = 1;
-#pragma unroll
-    for (int m = 0; m < E; ++m) {
-      const R nl = valid ? a.aux[base + (long long)(t + T * m) * st] : R(0);
-      v[m] = rmul(v[m], nl);  // groundstate_itp.m:42
-      acc[0].add(norm2(v[m]));
-    }
-    slots[0] = S_N;
-  }
-
-  if (valid) {
-#pragma unroll
-    for (int m = 0; m < E; ++m) a.psi[base + (long long)(t + T * m) * st] = v[m];
-  }
-  if (nred > 0) {
-    double vals[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) vals[i] = (i < nred && valid) ? acc[i].value() : 0.0;
     cta_reduce_store<L::THREADS>(vals, slots, nred, a.partials, a.cap);
+  } else {
+    // The side array (V for the phase factors, or the ITP factors) is read
+    // right before the phase that uses it: a pass has a prologue or an
+    // epilogue, never both, so it is never held across the FFTs.
+    R sv[E];
+    auto load_side = [&]() {
+      const R* __restrict__ ss = (a.side == 2 ? a.aux : a.V) + first;
+#pragma unroll
+      for (int m = 0; m < E; ++m) sv[m] = valid ? ss[m * dm] : R(0);
+    };
+    if (a.pro != PRO_NONE) {
+      if (a.side != 0) load_side();
+      prologue<R, E>(v, sv, a, valid, first, dm);
+    }
+    St::forward(v, sm, pol, t, a.tws);
+    apply_phase<T, E>(v, a.php, t);
+    St::inverse(v, sm, pol, t, a.tws);
+    Kahan<R> acc[3];
+    if (a.epi != EPI_NONE) {
+      load_side();
+      epilogue<R, E>(v, sv, a, acc, valid);
+    }
+    if (valid) {
+      cx<R>* __restrict__ dst = a.psi + first;
+#pragma unroll
+      for (int m = 0; m < E; ++m) dst[m * dm] = v[m];
+    }
+    const int nred = a.epi == EPI_RT_END ? 3 : a.epi == EPI_ITP ? 1 : 0;
+    if (nred > 0) {
+      double vals[4] = {acc[0].value(), acc[1].value(), acc[2].value(), 0.0};
+      const int slots[4] = {S_N, S_VN, S_N2, 0};
+      cta_reduce_store<L::THREADS>(vals, slots, nred, a.partials, a.cap);
+    }
   }
 }
 
@@ -258,6 +331,18 @@ struct PassGeom {
 
 template <typename R, int N>
 PassGeom pass_geom(bool strided);
+
+template <int N>
+PlanInfo plan_info();
+
+template <typename R, int N>
+cudaError_t launch_pass_tma(const PassArgs<R>& a, bool strided, cudaStream_t s, int sms, int* grid_out);
+template <typename R, int N>
+int pass_tma_grid(const PassArgs<R>& a, bool strided, int sms);
+template <typename R, int N>
+int pass_tma_ffts(bool strided);
+template <typename R, int N>
+size_t pass_tma_smem(bool strided);
 
 template <typename R, int N>
 cudaError_t launch_pass(const PassArgs<R>& a, bool strided, cudaStream_t s);

@@ -3,4 +3,5 @@
 
 namespace gpe {
 GPE_INST_PASS(float, 256)
+GPE_INST_PLAN(256)
 }  // namespace gpe

@@ -3,4 +3,5 @@
 
 namespace gpe {
 GPE_INST_PASS(float, 384)
+GPE_INST_PLAN(384)
 }  // namespace gpe

@@ -3,4 +3,5 @@
 
 namespace gpe {
 GPE_INST_PASS(float, 512)
+GPE_INST_PLAN(512)
 }  // namespace gpe

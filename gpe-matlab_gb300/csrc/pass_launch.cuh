@@ -2,7 +2,7 @@
 // instantiated per (precision, axis length) in the pass_*.cu files so that
 // the FFT kernels compile in parallel translation units.
 #pragma once
-#include "pass.cuh"
+#include "pass_tma.cuh"
 
 namespace gpe {
 
@@ -17,9 +17,21 @@ PassGeom pass_geom(bool strided) {
   return PassGeom{L::THREADS, L::FFTS, L::smem_bytes()};
 }
 
+template <int N>
+PlanInfo plan_info() {
+  using P = Plan<N>;
+  PlanInfo pi{};
+  pi.N = P::N;
+  pi.T = P::T;
+  pi.E = P::E;
+  pi.nstages = P::NSTAGES;
+  for (int s = 0; s < P::NSTAGES; ++s) pi.radix[s] = P::radix[s];
+  return pi;
+}
+
 template <typename R, class P, class L>
 static cudaError_t launch_layout(const PassArgs<R>& a, cudaStream_t s) {
-  auto kern = pass_kernel<R, P, L>;
+  auto kern = a.kind == KIND_ENERGY ? pass_kernel<R, P, L, KIND_ENERGY> : pass_kernel<R, P, L, KIND_STEP>;
   const size_t smem = L::smem_bytes();
   // Above 32 KB of dynamic shared memory opt in explicitly: the static
   // reduction scratch counts toward the 48 KB default limit too.
@@ -40,8 +52,87 @@ cudaError_t launch_pass(const PassArgs<R>& a, bool strided, cudaStream_t s) {
   return launch_layout<R, P, ContigLayout<P, R>>(a, s);
 }
 
-#define GPE_INST_PASS(R, N)                                                      \
-  template PassGeom pass_geom<R, N>(bool);                                       \
-  template cudaError_t launch_pass<R, N>(const PassArgs<R>&, bool, cudaStream_t);
+// ---- TMA-staged persistent variant --------------------------------------
+// Resident CTAs per SM of a kernel at a given dynamic shared-memory size,
+// cached (the occupancy query costs a few microseconds of host time).
+int resident_ctas(const void* kern, int threads, size_t smem);
+
+template <typename R, class P, class L>
+static cudaError_t launch_tma_layout(const PassArgs<R>& a, cudaStream_t s, int sms) {
+  using SMB = TmaSmem<L, R>;
+  auto kern = a.kind == KIND_ENERGY ? pass_tma_kernel<R, P, L, KIND_ENERGY> : pass_tma_kernel<R, P, L, KIND_STEP>;
+  const size_t smem = SMB::bytes(a.side != 0);
+  if (smem > 32 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const long long ntiles = (a.n_batch + L::FFTS - 1) / L::FFTS;
+  const int per_sm = resident_ctas((const void*)kern, L::THREADS, smem);
+  long long grid = (long long)sms * (per_sm > 0 ? per_sm : 1);
+  if (grid > ntiles) grid = ntiles;
+  if (grid > a.cap) grid = a.cap;
+  kern<<<(unsigned)grid, L::THREADS, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename R, int N>
+cudaError_t launch_pass_tma(const PassArgs<R>& a, bool strided, cudaStream_t s, int sms, int* grid_out) {
+  using P = Plan<N>;
+  cudaError_t e;
+  if (strided) {
+    using L = TStrided<P, R>;
+    e = launch_tma_layout<R, P, L>(a, s, sms);
+  } else {
+    using L = TContig<P, R>;
+    e = launch_tma_layout<R, P, L>(a, s, sms);
+  }
+  return e;
+}
+
+// CTAs a TMA pass launches (partial sums land in that many slots).
+template <typename R, int N>
+int pass_tma_grid(const PassArgs<R>& a, bool strided, int sms) {
+  using P = Plan<N>;
+  auto g = [&](auto L_) {
+    using L = decltype(L_);
+    using SMB = TmaSmem<L, R>;
+    auto kern = a.kind == KIND_ENERGY ? pass_tma_kernel<R, P, L, KIND_ENERGY> : pass_tma_kernel<R, P, L, KIND_STEP>;
+    const size_t smem = SMB::bytes(a.side != 0);
+    if (smem > 32 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const long long ntiles = (a.n_batch + L::FFTS - 1) / L::FFTS;
+    const int per_sm = resident_ctas((const void*)kern, L::THREADS, smem);
+    long long grid = (long long)sms * (per_sm > 0 ? per_sm : 1);
+    if (grid > ntiles) grid = ntiles;
+    if (grid > a.cap) grid = a.cap;
+    return (int)grid;
+  };
+  if (strided) return g(TStrided<P, R>{});
+  return g(TContig<P, R>{});
+}
+
+// Pencils per tile of the TMA pass (strided tiles must not straddle rows).
+template <typename R, int N>
+int pass_tma_ffts(bool strided) {
+  using P = Plan<N>;
+  return strided ? TStrided<P, R>::FFTS : TContig<P, R>::FFTS;
+}
+
+// Dynamic shared memory of a TMA pass with side staging (the larger case).
+template <typename R, int N>
+size_t pass_tma_smem(bool strided) {
+  using P = Plan<N>;
+  return strided ? TmaSmem<TStrided<P, R>, R>::bytes(true) : TmaSmem<TContig<P, R>, R>::bytes(true);
+}
+
+#define GPE_INST_PASS(R, N)                                                                  \
+  template PassGeom pass_geom<R, N>(bool);                                                   \
+  template cudaError_t launch_pass<R, N>(const PassArgs<R>&, bool, cudaStream_t);            \
+  template cudaError_t launch_pass_tma<R, N>(const PassArgs<R>&, bool, cudaStream_t, int, int*); \
+  template int pass_tma_grid<R, N>(const PassArgs<R>&, bool, int);                          \
+  template int pass_tma_ffts<R, N>(bool);                                                   \
+  template size_t pass_tma_smem<R, N>(bool);
+
+// Plan descriptions are precision independent: instantiated once (FP32 files).
+#define GPE_INST_PLAN(N) template PlanInfo plan_info<N>();
 
 }  // namespace gpe

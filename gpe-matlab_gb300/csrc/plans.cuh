@@ -16,8 +16,10 @@ struct PlanT {
   static constexpr int T = T_;
   static constexpr int E = N_ / T_;
   static constexpr int PADSH = PADSH_;
+  static constexpr int NSTAGES = sizeof...(RADS);
+  static constexpr int radix[sizeof...(RADS)] = {RADS...};
   template <typename R>
-  using St = Stages<R, N_, T_, 1, RADS...>;
+  using St = Stages<R, N_, T_, 1, 0, RADS...>;
   static constexpr int prod() { return (RADS * ...); }
   static_assert(prod() == N_, "radices must multiply to N");
   static_assert((((N_ / T_) % RADS == 0) && ...), "every radix must divide E");
@@ -41,6 +43,36 @@ template <> struct Plan<384>  : PlanT<384, 16, 4, 8, 8, 6> {};
 template <> struct Plan<512>  : PlanT<512, 32, 4, 16, 16, 2> {};
 template <> struct Plan<768>  : PlanT<768, 32, 4, 8, 8, 6, 2> {};
 template <> struct Plan<1024> : PlanT<1024, 64, 4, 16, 16, 4> {};
+
+// Host-side description of a plan: the tables the pass kernels read are
+// built from it (stage twiddle rows, per-thread permuted kinetic factors).
+struct PlanInfo {
+  int N, T, E, nstages;
+  int radix[8];
+};
+
+// Twiddle rows of stage s (s >= 1, Ns = R_0*...*R_{s-1}) start at
+// sum over earlier stages s' >= 1 of even(Ns' * R_s'); row k holds
+// exp(-2 pi i r k/(Ns R_s)) for r = 0..R_s-1.
+inline int stage_rows_offset(const PlanInfo& p, int s) {
+  int off = 0, Ns = p.radix[0];
+  for (int q = 1; q < s; ++q) {
+    off += (Ns * p.radix[q] + 1) & ~1;
+    Ns *= p.radix[q];
+  }
+  return off;
+}
+
+// Natural-order spectrum position that register slot m of thread t holds
+// after the forward transform (the last stage's scatter position).
+inline int plan_spec_pos(const PlanInfo& p, int t, int m) {
+  const int Rl = p.radix[p.nstages - 1];
+  const int Ns = p.N / Rl;
+  const int NB = p.E / Rl;
+  const int b = m % NB, r = m / NB;
+  const int j = t + p.T * b;
+  return (j / Ns) * Ns * Rl + (j % Ns) + r * Ns;
+}
 
 // The axis lengths with a plan (host-side check before any launch).
 #define GPE_FOR_EACH_N(X) \

@@ -338,3 +338,7 @@ class GPEtask:
 
     def kernel_launches(self) -> int:
         return int(L.lib.gpe_kernel_launches(self._ctx))
+
+    def set_pass_variant(self, variant: int):
+        """0: TMA-staged passes where they apply (default), 1: direct passes."""
+        L.check(self._ctx, L.lib.gpe_set_pass_variant(self._ctx, int(variant)))

@@ -208,6 +208,13 @@ GPE_API gpe_status gpe_timer_start(gpe_ctx *ctx);
 GPE_API gpe_status gpe_timer_stop(gpe_ctx *ctx, double *ms);
 GPE_API gpe_status gpe_profile_enable(gpe_ctx *ctx, int on);
 GPE_API gpe_status gpe_profile_read(gpe_ctx *ctx, gpe_kernel_stat *out, int cap, int *n);
+/* Axis-pass implementation: 0 (default) = TMA-staged persistent passes
+ * where the tile geometry allows, 1 = direct-load passes everywhere.  Both
+ * compute the same result; the knob exists for measurement. */
+GPE_API gpe_status gpe_set_pass_variant(gpe_ctx *ctx, int variant);
+/* Diagnostic: the FP32 device sin/cos used by the phase factors, on n host
+ * values (device 0).  Lets tests bound its error against FP64 references. */
+GPE_API gpe_status gpe_selftest_trig(const float *x, float *s, float *c, long long n);
 /* Launch counters of this library's kernels since the context was created. */
 GPE_API long long gpe_kernel_launches(const gpe_ctx *ctx);
 

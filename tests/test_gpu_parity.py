@@ -215,7 +215,29 @@ def test_gamma0_conserves_norm_fp32(gpe):
     task.init_state = psi0
     task.solve_split(0.002, 50, 4)
     n0 = grid.integrate(np.abs(psi0) ** 2)
-    np.testing.assert_allclose(task.history["n"], n0, rtol=2e-6)
+    # FP32 rounding of unit-modulus factors leaves a drift of a few 1e-8 per
+    # step (the FP64 path conserves to ~1e-17 per step): bound 1e-7 per step.
+    np.testing.assert_allclose(task.history["n"], n0, rtol=200 * 1e-7)
+
+
+def test_device_sincos_error_bound(gpe):
+    """The FP32 phase factors' sin/cos: absolute error <= 2 ulp(1) = 2.4e-7
+    against FP64 over the bounded range and beyond it (library fallback)."""
+    from gpe_gb300 import _lib as L
+
+    rng = np.random.default_rng(7)
+    x = np.concatenate([np.linspace(-7e4, 7e4, 20001), np.linspace(-10, 10, 200001),
+                        rng.uniform(-3.5, 3.5, 100000), np.array([0.0, 1e-30, -1e-8, 65536.0, -65536.0])])
+    x = x.astype(np.float32)
+    s = np.empty_like(x)
+    c = np.empty_like(x)
+    L.check(None, L.lib.gpe_selftest_trig(L.fptr(x), L.fptr(s), L.fptr(c), x.size))
+    xd = x.astype(np.float64)
+    assert np.max(np.abs(s - np.sin(xd))) <= 2.4e-7
+    assert np.max(np.abs(c - np.cos(xd))) <= 2.4e-7
+    # no systematic modulus bias over phases of one step's typical range
+    m = s.astype(np.float64) ** 2 + c.astype(np.float64) ** 2 - 1
+    assert abs(np.mean(m[20001:220002])) < 2e-8
 
 
 def test_errors_are_reported_not_crashing(gpe):
