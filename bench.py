@@ -1,6 +1,6 @@
 """Benchmark: split-step grid-point-steps/s of GPEtask.solve_split on one GB300.
 
-Workload (BASELINE configs[1]): grid3d 256^3, box +-12, V = 0.5 (x^2 + y^2 +
+Workload (the damped 3D configuration): grid3d 256^3, box +-12, V = 0.5 (x^2 + y^2 +
 (4 z)^2), g = 0.5, Ntotal = 1e5, ground state by imaginary-time propagation
 (FP32 + FP64 polish, untimed), then real-time steps of dt = 0.002 with damping
 gamma = 0.01.  One bench step = one outer step of solve_split = 100 split
@@ -239,7 +239,7 @@ def run_gpu(args, dist):
     avg_ms = top["total_ms"] / top["launches"]
     achieved = top["bytes_per_launch"] / (avg_ms / 1e3) / 1e9
     traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
+    tf = ROOT / "profiles" / "pass_traffic_damped3d_256.json"
     if tf.exists():
         d = json.loads(tf.read_text())
         traffic = d.get(top["name"], {}).get("bytes_per_launch_256cube")
@@ -343,7 +343,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="FP32 timed region only (no FP64, e2e, CPU legs)")
-    ap.add_argument("--pass-variant", type=int, default=0, help="0: TMA-staged passes (default), 1: direct")
+    ap.add_argument("--pass-variant", type=int, default=0, help="0: direct passes (default), 1: TMA-staged")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args.profile_case, args.profile_blocks, args.pass_variant)

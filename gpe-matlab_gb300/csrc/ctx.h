@@ -70,7 +70,7 @@ struct gpe_ctx {
   std::string err;
 
   int sms = 152;          // SM count of the device
-  int pass_variant = 0;   // 0: TMA-staged passes where they apply, 1: direct passes only
+  int pass_variant = 0;   // 0: direct passes, 1: TMA-staged passes where they apply
   bool prof = false;
   std::vector<gpe::ProfRec> prof_pending;
   std::vector<cudaEvent_t> ev_pool;

@@ -138,8 +138,9 @@ PlanInfo dispatch_plan(int N);
 
 // The TMA pass applies when every tile is one contiguous range (contiguous
 // axis) or N rows of FFTS contiguous, 16-byte aligned elements (strided
-// axes), and a CTA is at least two warps.  pass_variant: 0 = TMA where it
-// applies, 1 = always the direct pass.
+// axes), and a CTA is at least two warps.  pass_variant: 0 = the direct
+// pass everywhere (measured faster on GB300 for the 256^3 bench workload),
+// 1 = the TMA pass where it applies.
 template <typename R>
 size_t dispatch_tma_smem(int N, bool strided) {
   switch (N) {
@@ -154,7 +155,7 @@ size_t dispatch_tma_smem(int N, bool strided) {
 
 template <typename R>
 bool use_tma(const gpe_ctx* c, const AxisPass& ap) {
-  if (c->pass_variant == 1) return false;
+  if (c->pass_variant != 1) return false;
   if (dispatch_tma_smem<R>(ap.N, ap.strided) > 200 * 1024) return false;
   const int ffts = dispatch_tma_ffts<R>(ap.N, ap.strided);
   if (!ap.strided) return true;
@@ -1330,7 +1331,7 @@ gpe_status gpe_selftest_trig(const float* x, float* s, float* co, long long n) {
 
 gpe_status gpe_set_pass_variant(gpe_ctx* c, int variant) {
   CHECK(check_ctx(c));
-  if (variant < 0 || variant > 1) return fail(c, GPE_ERR_INVALID, "pass variant must be 0 (auto) or 1 (direct)");
+  if (variant < 0 || variant > 1) return fail(c, GPE_ERR_INVALID, "pass variant must be 0 (direct) or 1 (TMA)");
   c->pass_variant = variant;
   return GPE_OK;
 }

@@ -39,10 +39,15 @@ __host__ __device__ constexpr int padpos(int p) {
   else return p + (p >> PADSH);
 }
 
+// Threads per CTA of the direct passes (pencils per CTA follow from it).
+#ifndef GPE_DIRECT_CTA_THREADS
+#define GPE_DIRECT_CTA_THREADS 256
+#endif
+
 template <class P, typename R>
 struct ContigLayout {
   static constexpr int T = P::T;
-  static constexpr int FFTS = (T >= 256) ? 1 : 256 / T;
+  static constexpr int FFTS = (T >= GPE_DIRECT_CTA_THREADS) ? 1 : GPE_DIRECT_CTA_THREADS / T;
   static constexpr int THREADS = FFTS * T;
   static constexpr int REG0 = padpos<P::PADSH>(P::N - 1) + 1;
   static constexpr int REG = (REG0 % 2 == 0) ? REG0 + 1 : REG0;  // odd stride between pencils
@@ -70,7 +75,7 @@ template <class P, typename R>
 struct StridedLayout {
   static constexpr int T = P::T;
   static constexpr int G = 128 / (int)sizeof(cx<R>);  // pencils per 128-byte row
-  static constexpr int F0 = (256 / T > G) ? 256 / T : G;
+  static constexpr int F0 = (GPE_DIRECT_CTA_THREADS / T > G) ? GPE_DIRECT_CTA_THREADS / T : G;
   static constexpr int FFTS = (F0 * T > 1024) ? 1024 / T : F0;
   static constexpr int THREADS = FFTS * T;
   static constexpr size_t smem_bytes() { return sizeof(cx<R>) * (size_t)FFTS * P::N; }

@@ -98,7 +98,7 @@ class GPEtask:
 
     def _push_params(self):
         if self.omega != 0:
-            raise NotImplementedError("omega != 0 (rotating frame) is not supported by this build")
+            raise NotImplementedError("omega != 0 (rotating frame) is not supported by libgpe")
         p = L.gpe_params()
         p.g = float(self.g)
         p.gamma = float(self.gamma)
@@ -340,5 +340,5 @@ class GPEtask:
         return int(L.lib.gpe_kernel_launches(self._ctx))
 
     def set_pass_variant(self, variant: int):
-        """0: TMA-staged passes where they apply (default), 1: direct passes."""
+        """0: direct passes (default), 1: TMA-staged passes where they apply."""
         L.check(self._ctx, L.lib.gpe_set_pass_variant(self._ctx, int(variant)))

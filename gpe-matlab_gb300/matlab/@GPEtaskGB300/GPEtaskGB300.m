@@ -1,0 +1,140 @@
+classdef GPEtaskGB300 < GPEtask
+    %GPEtaskGB300 - GPEtask whose groundstate_itp and solve_split run on a
+    %GB300 GPU through libgpe (gpe_mex MEX gateway).
+    %
+    % Drop-in for GPEtask: construct it exactly like GPEtask(grid, V); all
+    % public properties (g, gamma, decay_rate, Ntotal, mu_init, n_recalc,
+    % Vtd, V0, init_state, current_*, history, user_callback, itp_*) keep
+    % their meaning.  A grid built from single-precision axes runs the split
+    % step in complex FP32 (FP64 reductions); double axes run FP64.
+    %
+    % UNVERIFIED: no MATLAB was available where this file was written; the
+    % library calls it makes are covered by the Python tests of the same ABI.
+
+    properties (Hidden, SetAccess = protected)
+        gb300_handle = uint64(0)
+        gb300_npts = 0
+        gb300_class = 'double'
+    end
+
+    methods
+        function obj = GPEtaskGB300(grid, trappot)
+            obj@GPEtask(grid, trappot);
+            x = gather(grid.x);
+            y = gather(grid.y);
+            obj.gb300_class = class(x);
+            if grid.ndims == 3
+                z = gather(grid.z);
+                n = [numel(x) numel(y) numel(z)];
+                dx = double([x(2)-x(1), y(2)-y(1), z(2)-z(1)]);
+                span = double([x(end)-x(1), y(end)-y(1), z(end)-z(1)]);
+            else
+                n = [numel(x) numel(y) 1];
+                dx = double([x(2)-x(1), y(2)-y(1), 1]);
+                span = double([x(end)-x(1), y(end)-y(1), 0]);
+            end
+            obj.gb300_npts = prod(n);
+            obj.gb300_handle = gpe_mex('create', grid.ndims, n, dx, span, obj.gb300_class);
+        end
+
+        function delete(obj)
+            if obj.gb300_handle ~= 0
+                gpe_mex('destroy', obj.gb300_handle);
+                obj.gb300_handle = uint64(0);
+            end
+        end
+
+        function [phi, varargout] = groundstate_itp(task, dt, eps, phi0)
+            % groundstate_itp.m semantics, executed by libgpe.
+            if nargin < 4
+                phi0 = 'rand';
+            end
+            task.gb300_push();
+            gpe_mex('set_potential', task.gb300_handle, double(gather(task.getVtotal(0))));
+            phi = task.process_init_state(phi0);
+            gpe_mex('set_state', task.gb300_handle, complex(gather(phi)));
+            [MU, MU2, EE] = gpe_mex('itp', task.gb300_handle, dt, eps, nargout >= 3, nargout >= 4);
+            phi = task.gb300_state();
+            if nargout >= 2
+                varargout{1} = MU;
+                if task.Ntotal > 0
+                    task.current_mu = MU(end);
+                    task.current_n = task.Ntotal;
+                end
+            end
+            if nargout >= 3
+                varargout{2} = MU2;
+                if task.Ntotal <= 0
+                    task.current_mu = MU2(end);
+                    task.current_n = MU(end);
+                end
+            end
+            if nargout >= 4
+                varargout{3} = EE;
+            end
+            task.init_state = phi;
+            task.current_state = phi;
+        end
+
+        function phi = solve_split(task, ddt, niter_inner, niter_outer)
+            % solve_split.m semantics, executed by libgpe; ext_callback and
+            % user_callback run in MATLAB after every outer step.
+            task.dispstat('', 'init');
+            tic;
+            task.gb300_push();
+            if task.current_iter > 0
+                phi = task.current_state;
+            else
+                phi = task.init_state;
+            end
+            gpe_mex('set_state', task.gb300_handle, complex(gather(phi)));
+            timedep = isa(task.Vtd, 'function_handle') || numel(task.V0) > 1;
+            if ~timedep
+                gpe_mex('set_potential', task.gb300_handle, double(gather(task.Vtrap)));
+            end
+            gpe_mex('split', task.gb300_handle, ddt, niter_inner, niter_outer, task, timedep);
+            phi = task.current_state;
+        end
+
+        function V = gb300_vtotal(task, time)
+            % getVtotal(time) as a host double array (called once per block).
+            V = double(gather(task.getVtotal(time)));
+        end
+
+        function gb300_step(task, step, time, mu, n)
+            % Called by the gateway after each outer step (solve_split.m:80).
+            phi = task.gb300_state();
+            task.ext_callback(phi, step, time, mu, n);
+        end
+
+        function E = get_energy(task, phi, time)
+            % GPEtask.m:97-107 on the GPU (current V).
+            if nargin >= 2
+                gpe_mex('set_state', task.gb300_handle, complex(gather(phi)));
+            end
+            o = gpe_mex('observables', task.gb300_handle);
+            E = o(6);
+        end
+    end
+
+    methods (Access = protected)
+        function gb300_push(task)
+            gpe_mex('set_params', task.gb300_handle, task.g, task.gamma, task.decay_rate, ...
+                task.Ntotal, task.mu_init, task.n_recalc, task.itp_max_iter, task.itp_min_iter, ...
+                double(task.itp_adjust_stepsize));
+            n = task.current_n;
+            if isempty(n)
+                n = 0;
+            end
+            gpe_mex('set_current', task.gb300_handle, task.current_iter, task.current_time, ...
+                task.current_mu, n);
+        end
+
+        function phi = gb300_state(task)
+            phi = gpe_mex('get_state', task.gb300_handle, task.gb300_class, size(task.grid.mesh.x));
+            if isa(task.grid.x, 'gpuArray')
+                phi = gpuArray(phi);
+            end
+        end
+    end
+end

@@ -1,0 +1,232 @@
+// gpe_mex.cpp - MEX gateway from MATLAB's GPEtask class to libgpe (C ABI,
+// include/gpe.h).  Build (MATLAB R2018a+, interleaved complex API):
+//
+//   mex -R2018a -I../../include gpe_mex.cpp -L.. -lgpe
+//
+// UNVERIFIED: this machine has no MATLAB (no mex.h, no libmx), so this file
+// has not been compiled.  It uses only documented MEX C API calls, and every
+// libgpe call it makes is exercised by the Python tests through the same ABI.
+//
+// Usage (see @GPEtaskGB300):
+//   h = gpe_mex('create', ndims, n, dx, span, precision)   % precision 'single'|'double'
+//   gpe_mex('destroy', h)
+//   gpe_mex('set_params', h, g, gamma, decay_rate, Ntotal, mu_init, n_recalc,
+//           itp_max_iter, itp_min_iter, itp_adjust_stepsize)
+//   gpe_mex('set_current', h, iter, time, mu, n)
+//   [iter, time, mu, n] = gpe_mex('current', h)
+//   [mu, n] = gpe_mex('history', h)
+//   gpe_mex('set_potential', h, V)                    % real double, grid size
+//   gpe_mex('set_state', h, psi)                      % complex double or single
+//   psi = gpe_mex('get_state', h, 'double'|'single')
+//   [MU, MU2, EE, iters, converged] = gpe_mex('itp', h, dt, eps, want_mu2, want_energy)
+//   gpe_mex('split', h, ddt, niter_inner, niter_outer, task)
+//       task: the calling GPEtaskGB300 object; if it has a time-dependent
+//       potential the gateway calls task.getVtotal(time) once per block, and
+//       after every outer step it calls task.gb300_step(step, time, mu, n).
+//   obs = gpe_mex('observables', h)                   % [norm ekin epot eint mu_int energy]
+#include <string.h>
+
+#include <string>
+
+#include "gpe.h"
+#include "mex.h"
+
+namespace {
+
+gpe_ctx* handle(const mxArray* a) {
+  if (!mxIsUint64(a) || mxGetNumberOfElements(a) != 1) mexErrMsgIdAndTxt("gpe:handle", "invalid gpe handle");
+  return reinterpret_cast<gpe_ctx*>(*static_cast<uint64_t*>(mxGetData(a)));
+}
+
+void check(gpe_ctx* c, gpe_status st) {
+  if (st != GPE_OK) {
+    std::string id = "gpe:status" + std::to_string((int)st);
+    mexErrMsgIdAndTxt(id.c_str(), "%s", gpe_last_error(c));
+  }
+}
+
+double scalar(const mxArray* a) { return mxGetScalar(a); }
+
+std::string str(const mxArray* a) {
+  char buf[64];
+  if (mxGetString(a, buf, sizeof(buf)) != 0) mexErrMsgIdAndTxt("gpe:arg", "expected a string");
+  return buf;
+}
+
+struct SplitCtx {
+  const mxArray* task;
+  size_t npts;
+};
+
+// getVtotal(time) of the MATLAB task, once per block (solve_split.m:53-54).
+int vtd_cb(void* user, double time, double* V_out) {
+  SplitCtx* s = static_cast<SplitCtx*>(user);
+  mxArray* in[2] = {const_cast<mxArray*>(s->task), mxCreateDoubleScalar(time)};
+  mxArray* out[1] = {nullptr};
+  if (mexCallMATLAB(1, out, 2, in, "gb300_vtotal") != 0) return 1;
+  int rc = 0;
+  if (!mxIsDouble(out[0]) || mxIsComplex(out[0]) || mxGetNumberOfElements(out[0]) != s->npts) rc = 1;
+  else memcpy(V_out, mxGetDoubles(out[0]), s->npts * sizeof(double));
+  mxDestroyArray(in[1]);
+  mxDestroyArray(out[0]);
+  return rc;
+}
+
+// ext_callback bookkeeping in MATLAB (GPEtask.m:115-142).
+int step_cb(void* user, int step, double time, double mu, double n) {
+  SplitCtx* s = static_cast<SplitCtx*>(user);
+  mxArray* in[5] = {const_cast<mxArray*>(s->task), mxCreateDoubleScalar(step), mxCreateDoubleScalar(time),
+                    mxCreateDoubleScalar(mu), mxCreateDoubleScalar(n)};
+  const int rc = mexCallMATLAB(0, nullptr, 5, in, "gb300_step");
+  for (int i = 1; i < 5; ++i) mxDestroyArray(in[i]);
+  return rc;
+}
+
+}  // namespace
+
+void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
+  if (nrhs < 1) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex(command, ...)");
+  const std::string cmd = str(prhs[0]);
+
+  if (cmd == "create") {
+    if (nrhs != 6) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('create', ndims, n, dx, span, precision)");
+    gpe_grid_desc d;
+    memset(&d, 0, sizeof(d));
+    d.ndims = (int)scalar(prhs[1]);
+    const double* n = mxGetDoubles(prhs[2]);
+    const double* dx = mxGetDoubles(prhs[3]);
+    const double* span = mxGetDoubles(prhs[4]);
+    for (int a = 0; a < d.ndims && a < 3; ++a) {
+      d.n[a] = (int)n[a];
+      d.dx[a] = dx[a];
+      d.span[a] = span[a];
+    }
+    d.precision = str(prhs[5]) == "single" ? GPE_FP32 : GPE_FP64;
+    d.device = 0;
+    gpe_ctx* c = nullptr;
+    check(nullptr, gpe_create(&d, &c));
+    plhs[0] = mxCreateNumericMatrix(1, 1, mxUINT64_CLASS, mxREAL);
+    *static_cast<uint64_t*>(mxGetData(plhs[0])) = reinterpret_cast<uint64_t>(c);
+    return;
+  }
+
+  if (nrhs < 2) mexErrMsgIdAndTxt("gpe:usage", "missing handle");
+  gpe_ctx* c = handle(prhs[1]);
+
+  if (cmd == "destroy") {
+    gpe_destroy(c);
+  } else if (cmd == "set_params") {
+    if (nrhs != 11) mexErrMsgIdAndTxt("gpe:usage", "set_params needs 9 values");
+    gpe_params p;
+    gpe_default_params(&p);
+    p.g = scalar(prhs[2]);
+    p.gamma = scalar(prhs[3]);
+    p.decay_rate = scalar(prhs[4]);
+    p.Ntotal = scalar(prhs[5]);
+    p.mu_init = scalar(prhs[6]);
+    p.n_recalc = (int)scalar(prhs[7]);
+    p.itp_max_iter = (int)scalar(prhs[8]);
+    p.itp_min_iter = (int)scalar(prhs[9]);
+    p.itp_adjust_stepsize = (int)scalar(prhs[10]);
+    check(c, gpe_set_params(c, &p));
+  } else if (cmd == "set_current") {
+    gpe_current cur;
+    cur.current_iter = (int)scalar(prhs[2]);
+    cur.current_time = scalar(prhs[3]);
+    cur.current_mu = scalar(prhs[4]);
+    cur.current_n = scalar(prhs[5]);
+    check(c, gpe_set_current(c, &cur));
+  } else if (cmd == "current") {
+    gpe_current cur;
+    check(c, gpe_get_current(c, &cur));
+    plhs[0] = mxCreateDoubleScalar(cur.current_iter);
+    if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(cur.current_time);
+    if (nlhs > 2) plhs[2] = mxCreateDoubleScalar(cur.current_mu);
+    if (nlhs > 3) plhs[3] = mxCreateDoubleScalar(cur.current_n);
+  } else if (cmd == "history") {
+    int len = 0;
+    check(c, gpe_get_history(c, nullptr, nullptr, 0, &len));
+    plhs[0] = mxCreateDoubleMatrix(1, len, mxREAL);
+    mxArray* nn = mxCreateDoubleMatrix(1, len, mxREAL);
+    check(c, gpe_get_history(c, mxGetDoubles(plhs[0]), mxGetDoubles(nn), len, &len));
+    if (nlhs > 1) plhs[1] = nn;
+    else mxDestroyArray(nn);
+  } else if (cmd == "set_potential") {
+    if (!mxIsDouble(prhs[2]) || mxIsComplex(prhs[2])) mexErrMsgIdAndTxt("gpe:arg", "V must be real double");
+    check(c, gpe_set_potential(c, mxGetDoubles(prhs[2])));
+  } else if (cmd == "set_state") {
+    const mxArray* psi = prhs[2];
+    if (!mxIsComplex(psi)) mexErrMsgIdAndTxt("gpe:arg", "psi must be complex (use complex(psi))");
+    if (mxIsSingle(psi)) check(c, gpe_set_state_f32(c, reinterpret_cast<const float*>(mxGetComplexSingles(psi))));
+    else check(c, gpe_set_state(c, reinterpret_cast<const double*>(mxGetComplexDoubles(psi))));
+  } else if (cmd == "get_state") {
+    // dims come from the caller's grid: psi = gpe_mex('get_state', h, cls, size(grid.mesh.x))
+    const std::string cls = nrhs > 2 ? str(prhs[2]) : "double";
+    if (nrhs < 4) mexErrMsgIdAndTxt("gpe:usage", "get_state needs the grid size");
+    const double* sz = mxGetDoubles(prhs[3]);
+    mwSize dims[3] = {(mwSize)sz[0], (mwSize)sz[1], mxGetNumberOfElements(prhs[3]) > 2 ? (mwSize)sz[2] : 1};
+    const mwSize nd = mxGetNumberOfElements(prhs[3]) > 2 ? 3 : 2;
+    if (cls == "single") {
+      plhs[0] = mxCreateNumericArray(nd, dims, mxSINGLE_CLASS, mxCOMPLEX);
+      check(c, gpe_get_state_f32(c, reinterpret_cast<float*>(mxGetComplexSingles(plhs[0]))));
+    } else {
+      plhs[0] = mxCreateNumericArray(nd, dims, mxDOUBLE_CLASS, mxCOMPLEX);
+      check(c, gpe_get_state(c, reinterpret_cast<double*>(mxGetComplexDoubles(plhs[0]))));
+    }
+  } else if (cmd == "itp") {
+    gpe_itp_params p;
+    memset(&p, 0, sizeof(p));
+    p.dt = scalar(prhs[2]);
+    p.eps = scalar(prhs[3]);
+    p.want_mu2 = (int)scalar(prhs[4]);
+    p.want_energy = (int)scalar(prhs[5]);
+    p.fp64_polish = 1;
+    gpe_params prm;
+    check(c, gpe_get_params(c, &prm));
+    const int cap = prm.itp_max_iter;
+    mxArray* MU = mxCreateDoubleMatrix(cap, 1, mxREAL);
+    mxArray* MU2 = mxCreateDoubleMatrix(cap, 1, mxREAL);
+    mxArray* EE = mxCreateDoubleMatrix(cap, 1, mxREAL);
+    gpe_itp_result res;
+    check(c, gpe_groundstate_itp(c, &p, mxGetDoubles(MU), mxGetDoubles(MU2), mxGetDoubles(EE), cap, &res));
+    mxSetM(MU, res.iters);
+    mxSetM(MU2, res.iters);
+    mxSetM(EE, res.iters);
+    plhs[0] = MU;
+    if (nlhs > 1) plhs[1] = MU2;
+    else mxDestroyArray(MU2);
+    if (nlhs > 2) plhs[2] = EE;
+    else mxDestroyArray(EE);
+    if (nlhs > 3) plhs[3] = mxCreateDoubleScalar(res.iters);
+    if (nlhs > 4) plhs[4] = mxCreateDoubleScalar(res.converged);
+    if (!res.converged) mexWarnMsgIdAndTxt("gpe:itp", "Convergence not reached");
+  } else if (cmd == "split") {
+    if (nrhs != 7) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('split', h, ddt, nin, nout, task, timedep)");
+    SplitCtx s{prhs[5], (size_t)mxGetScalar(mxGetProperty(prhs[5], 0, "gb300_npts"))};
+    gpe_split_params p;
+    memset(&p, 0, sizeof(p));
+    p.ddt = scalar(prhs[2]);
+    p.niter_inner = (int)scalar(prhs[3]);
+    p.niter_outer = (int)scalar(prhs[4]);
+    if (scalar(prhs[6]) != 0) {
+      p.vtd = vtd_cb;
+      p.vtd_user = &s;
+    }
+    p.on_step = step_cb;
+    p.step_user = &s;
+    check(c, gpe_solve_split(c, &p));
+  } else if (cmd == "observables") {
+    gpe_obs o;
+    check(c, gpe_observables(c, &o));
+    plhs[0] = mxCreateDoubleMatrix(1, 6, mxREAL);
+    double* r = mxGetDoubles(plhs[0]);
+    r[0] = o.norm;
+    r[1] = o.ekin;
+    r[2] = o.epot;
+    r[3] = o.eint;
+    r[4] = o.mu_integral;
+    r[5] = o.energy;
+  } else {
+    mexErrMsgIdAndTxt("gpe:usage", "unknown command '%s'", cmd.c_str());
+  }
+}

@@ -208,9 +208,9 @@ GPE_API gpe_status gpe_timer_start(gpe_ctx *ctx);
 GPE_API gpe_status gpe_timer_stop(gpe_ctx *ctx, double *ms);
 GPE_API gpe_status gpe_profile_enable(gpe_ctx *ctx, int on);
 GPE_API gpe_status gpe_profile_read(gpe_ctx *ctx, gpe_kernel_stat *out, int cap, int *n);
-/* Axis-pass implementation: 0 (default) = TMA-staged persistent passes
- * where the tile geometry allows, 1 = direct-load passes everywhere.  Both
- * compute the same result; the knob exists for measurement. */
+/* Axis-pass implementation: 0 (default) = direct-load passes, 1 = TMA-staged
+ * persistent passes where the tile geometry allows.  Both compute the same
+ * result; the knob exists for measurement. */
 GPE_API gpe_status gpe_set_pass_variant(gpe_ctx *ctx, int variant);
 /* Diagnostic: the FP32 device sin/cos used by the phase factors, on n host
  * values (device 0).  Lets tests bound its error against FP64 references. */

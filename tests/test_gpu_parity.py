@@ -6,7 +6,7 @@ Tolerances (written per test):
   steps, scalars (MU, mu, n) <= 1e-11 relative - rounding-level agreement
   (different FFT factorisation and summation order than pocketfft).
 * FP32 kernels: relative L2 <= 2e-5 per 100 steps of smooth states,
-  ground-state energy / mu <= 1e-6 relative (the spec bar).
+  ground-state energy / mu <= 1e-6 relative.
 """
 import math
 
@@ -218,6 +218,30 @@ def test_gamma0_conserves_norm_fp32(gpe):
     # FP32 rounding of unit-modulus factors leaves a drift of a few 1e-8 per
     # step (the FP64 path conserves to ~1e-17 per step): bound 1e-7 per step.
     np.testing.assert_allclose(task.history["n"], n0, rtol=200 * 1e-7)
+
+
+@pytest.mark.parametrize("precision", ["double", "single"])
+def test_tma_pass_variant_matches_direct(gpe, precision):
+    """The TMA-staged passes run the same per-point arithmetic as the direct
+    passes; only the order of the norm/energy sums differs, so results agree
+    to rounding (3D, damping, renormalisation, ITP)."""
+    out = []
+    for variant in (0, 1):
+        grid = gpe.grid3d(6, 32, 6, 64, 6, 48, precision=precision)
+        task = gpe.GPEtask(grid, harmonic((1.0, 1.2, 1.7)))
+        task.set_pass_variant(variant)
+        task.Ntotal, task.g, task.gamma = 30.0, 1.0, 0.02
+        X, Y, Z = grid.mesh["x"], grid.mesh["y"], grid.mesh["z"]
+        psi0 = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 3).astype(complex)
+        task.itp_max_iter = 200
+        phi = task.groundstate_itp(0.01, 1e-12, psi0)
+        task.init_state = phi * np.exp(0.3j * X)
+        task.solve_split(0.002, 20, 2)
+        out.append((phi, task.current_state, np.array(task.history["mu"])))
+    tol = 1e-12 if precision == "double" else 2e-5
+    assert rel_l2(out[1][0], out[0][0]) < tol
+    assert rel_l2(out[1][1], out[0][1]) < tol
+    np.testing.assert_allclose(out[1][2], out[0][2], rtol=tol)
 
 
 def test_device_sincos_error_bound(gpe):
