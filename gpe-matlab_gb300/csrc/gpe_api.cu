@@ -1351,3 +1351,9 @@ gpe_status gpe_host_unregister(void* ptr) {
 }
 
 }  // extern "C"
+
+namespace gpe {
+// Lets the context-free entry point (noalloc.cu) report through
+// gpe_last_error(NULL).
+void set_thread_error(const std::string& msg) { g_create_err = msg; }
+}  // namespace gpe

@@ -212,6 +212,21 @@ GPE_API gpe_status gpe_profile_read(gpe_ctx *ctx, gpe_kernel_stat *out, int cap,
  * persistent passes where the tile geometry allows.  Both compute the same
  * result; the knob exists for measurement. */
 GPE_API gpe_status gpe_set_pass_variant(gpe_ctx *ctx, int variant);
+/* integrate(|psi|^2) = sum |psi_i|^2 * weight of a caller-owned device array
+ * d_psi (npoints interleaved complex values of `precision`, on the current
+ * device), written to the host double *norm_out, on `stream` (a
+ * cudaStream_t; NULL = default stream).  No counterpart in the reference:
+ * an addition for callers that cannot allocate device memory at that point
+ * (MEX code on gpuArray memory owned by MATLAB's allocator, code inside a
+ * solve_split callback, applications that own all device memory).  It
+ * allocates nothing: its partial sums live in a fixed 256 KB device array
+ * inside the library, so it accepts at most 134,217,728 points (512^3) and
+ * rejects larger inputs with GPE_ERR_INVALID.  The first call on each device
+ * looks up that array's address and should come before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  Errors: gpe_last_error(NULL). */
+GPE_API gpe_status gpe_norm_noalloc(const void *d_psi, long long npoints, int precision, double weight,
+                                    void *stream, double *norm_out);
 /* Diagnostic: the FP32 device sin/cos used by the phase factors, on n host
  * values (device 0).  Lets tests bound its error against FP64 references. */
 GPE_API gpe_status gpe_selftest_trig(const float *x, float *s, float *c, long long n);
