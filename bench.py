@@ -146,12 +146,14 @@ def ground_state(gpe, W, precision="single", device=0):
     return grid, task, phi
 
 
-def cpu_reference_steps(W, phi, steps: int, cores: int):
-    """Times `steps` inner split steps of the FP64 oracle (reference restatement)."""
+def cpu_reference_steps(W, phi, steps: int, cores: int, max_seconds: float = 25.0):
+    """Times up to `steps` inner split steps (at most ~max_seconds) of the FP64
+    oracle (the restatement of the reference's solve_split)."""
     from oracle import gpe_oracle as O
 
     O.set_workers(cores)
-    og = O.Grid(W.box[0], W.n[0], W.box[1], W.n[1], W.box[2], W.n[2])
+    gargs = [v for pair in zip(W.box, W.n) for v in pair]
+    og = O.Grid(*gargs)
     ot = O.GPEtask(og, W.potential())
     ot.Ntotal, ot.g, ot.gamma = W.Ntotal, W.g, W.gamma
     ot.init_state = np.asarray(phi, dtype=np.complex128)
@@ -162,7 +164,7 @@ def cpu_reference_steps(W, phi, steps: int, cores: int):
 
     def on_inner(i):
         stamps.append(time.perf_counter())
-        if len(stamps) > steps:
+        if len(stamps) > steps or stamps[-1] - t0 > max_seconds:
             raise Done
 
     t0 = time.perf_counter()
@@ -176,37 +178,60 @@ def cpu_reference_steps(W, phi, steps: int, cores: int):
 
 
 def run_reference(args, dist):
-    from gpe_gb300.workloads import DAMPED3D as W
+    from gpe_gb300.workloads import WORKLOADS
 
+    W = WORKLOADS[args.workload]
     if dist.rank != 0:
         return
     cores = os.cpu_count() or 1
     # Start state: the seeded Gaussian (the timed work does not depend on it).
     grid = W.make_grid("double")
     phi = W.initial_state(grid) * 10.0
-    val, n, t = cpu_reference_steps(W, phi, args.warmup + args.steps, cores)
+    val, n, t = cpu_reference_steps(W, phi, args.warmup + args.steps, cores, max_seconds=150.0)
     line = {
         "metric": METRIC, "value": val, "unit": UNIT, "impl": "reference", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t / max(n, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": W.name, "grid": list(W.n), "dt": W.dt, "gamma": W.gamma, "step": "1 split step"},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{n} split steps of the 256^3 FP64 oracle (numpy + scipy.fft, {cores} workers)"},
+                         "sample": f"{n} split steps of the {'x'.join(map(str, W.n))} FP64 oracle "
+                                   f"(numpy + scipy.fft, {cores} workers)"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_gpu(args, dist):
-    import gpe_gb300 as gpe
-    from gpe_gb300.workloads import DAMPED3D as W
+def l2_note(W):
+    mb = W.npoints * 12 / 1e6  # complex64 state + float32 potential
+    if mb > 129:
+        return f"inputs larger than L2 (state + V = {mb:.0f} MB > 129 MB L2)"
+    return f"inputs ({mb:.1f} MB) fit in L2: an L2-resident workload, not an HBM measurement"
 
+
+def imprint(gpe, W, grid, task, phi):
+    """The workload's defect on the ground state: a vortex at x0 (2D,
+    example1_vortex.m:26-30) or a vortex ring at ring_frac * R_TF (3D)."""
+    if W.vortex_x0 is not None:
+        return gpe.imprint_vortex(grid, phi, W.g, W.vortex_x0)
+    if W.ring_frac is not None:
+        r_tf = math.sqrt(2.0 * task.current_mu) / W.trap[0]
+        return gpe.imprint_vortex_ring(grid, phi, W.g, W.ring_frac * r_tf)
+    return phi
+
+
+def run_gpu(args, dist):
+    global INNER
+    import gpe_gb300 as gpe
+    from gpe_gb300.workloads import WORKLOADS
+
+    W = WORKLOADS[args.workload]
+    INNER = W.niter_inner
     dev = dist.local
     P = W.npoints
     grid, task, phi = ground_state(gpe, W, "single", device=dev)
     task.set_pass_variant(args.pass_variant)
     itp = task.last_itp
-    phi = np.asarray(phi)
+    phi = np.asarray(imprint(gpe, W, grid, task, np.asarray(phi, dtype=np.complex128)))
     # ---- FP32 timed region ------------------------------------------------
     task.init_state = phi
     task.current_iter = 0
@@ -240,7 +265,7 @@ def run_gpu(args, dist):
     achieved = top["bytes_per_launch"] / (avg_ms / 1e3) / 1e9
     traffic = None
     tf = ROOT / "profiles" / "pass_traffic_damped3d_256.json"
-    if tf.exists():
+    if tf.exists() and W.name == "damped3d_256":  # captured on this grid only
         d = json.loads(tf.read_text())
         traffic = d.get(top["name"], {}).get("bytes_per_launch_256cube")
     if args.quick:
@@ -286,19 +311,19 @@ def run_gpu(args, dist):
         cores = os.cpu_count() or 1
         cval, n, t = cpu_reference_steps(W, phi, args.cpu_steps, cores)
         cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{n} split steps of the same 256^3 workload in the FP64 oracle "
-                         f"(numpy + scipy.fft with {cores} workers), {t:.1f} s"}
+               "sample": f"{n} split steps of the same {'x'.join(map(str, W.n))} workload in the FP64 "
+                         f"oracle (numpy + scipy.fft with {cores} workers), {t:.1f} s"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms.value / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 (FP64 reductions)", "data": "synthetic (seeded Gaussian -> ITP ground state)",
-        "config": {"workload": W.name, "grid": list(W.n), "box": W.box[0], "trap_lambda": W.trap[2], "g": W.g,
+        "config": {"workload": W.name, "grid": list(W.n), "box": W.box[0], "trap_lambda": list(W.trap), "g": W.g,
                    "Ntotal": W.Ntotal, "dt": W.dt, "gamma": W.gamma, "step": f"{INNER} split steps (1 outer step)",
-                   "n_recalc": 10, "l2": "inputs larger than L2 (state 134 MB + V 67 MB per GPU)",
+                   "n_recalc": 10, "l2": l2_note(W),
                    "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU"},
         "fp64": {"value": value64, "unit": UNIT, "steps": INNER * k64, "ratio_fp32_over_fp64": value / dist.world / value64},
-        "error": {"fp32_vs_fp64_rel_l2_after_100_steps": err_l2,
-                  "mu_rel_after_100_steps": abs(mu32 - mu64) / abs(mu64),
+        "error": {"fp32_vs_fp64_rel_l2_after_outer_step": err_l2,
+                  "mu_rel_after_outer_step": abs(mu32 - mu64) / abs(mu64),
                   "itp_iters": itp.iters, "itp_fp32_iters": itp.fp32_iters, "itp_converged": bool(itp.converged)},
         "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
@@ -315,6 +340,50 @@ def run_gpu(args, dist):
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     task.close()
+
+
+def run_batch(args, dist):
+    """The batched workload: 64 uneven 2D grids advanced by solve_split_batch
+    (CUDA graph per block, grids' chains concurrent); device-timed with the
+    first task's CUDA events."""
+    import ctypes as C
+
+    import gpe_gb300 as gpe
+    from gpe_gb300 import _lib as L
+    from gpe_gb300.workloads import BATCH2D as B
+
+    tasks = B.make_tasks("single", device=dist.local)
+    P = sum(t.grid.npoints for t in tasks)
+    inner = B.niter_inner
+    gpe.solve_split_batch(tasks, B.dt, inner, args.warmup)
+    k0 = sum(t.kernel_launches() for t in tasks)
+    dist.barrier()
+    t0c = tasks[0]._ctx
+    with ClockSampler(dist.local) as clk:
+        L.check(t0c, L.lib.gpe_timer_start(t0c))
+        gpe.solve_split_batch(tasks, B.dt, inner, args.warmup + args.steps)
+        ms = C.c_double()
+        L.check(t0c, L.lib.gpe_timer_stop(t0c, C.byref(ms)))
+    launches = sum(t.kernel_launches() for t in tasks) - k0
+    t_s = dist.reduce(ms.value / 1e3, "max")
+    value = dist.reduce(float(P) * inner * args.steps, "sum") / t_s
+    sizes = {}
+    for t in tasks:
+        sizes[t.grid.nx] = sizes.get(t.grid.nx, 0) + 1
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms.value / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 (FP64 reductions)", "data": "synthetic (seeded realisations -> ITP)",
+        "config": {"workload": B.name, "realisations": len(tasks), "sizes": {f"{k}^2": v for k, v in sorted(sizes.items())},
+                   "points_total": P, "dt": B.dt, "step": f"{inner} split steps of every realisation",
+                   "execution": "one CUDA graph per block of 10 steps, realisations concurrent",
+                   "l2": f"all states ({P * 12 / 1e6:.0f} MB with V) fit in L2: L2-resident workload"},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    for t in tasks:
+        t.close()
 
 
 def run_profile_case(precision: str, blocks: int, variant: int = 0):
@@ -344,6 +413,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="FP32 timed region only (no FP64, e2e, CPU legs)")
     ap.add_argument("--pass-variant", type=int, default=0, help="0: direct passes (default), 1: TMA-staged")
+    ap.add_argument("--workload", default="damped3d_256",
+                    choices=["damped3d_256", "ring3d_512", "vortex2d_256", "batch2d_64"],
+                    help="damped3d_256 (default, the headline), ring3d_512, vortex2d_256 (L2-resident)")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args.profile_case, args.profile_blocks, args.pass_variant)
@@ -355,7 +427,10 @@ def main():
         if args.impl == "reference":
             run_reference(args, dist)
         else:
-            run_gpu(args, dist)
+            if args.workload == "batch2d_64":
+                run_batch(args, dist)
+            else:
+                run_gpu(args, dist)
     finally:
         dist.close()
 

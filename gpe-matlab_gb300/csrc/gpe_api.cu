@@ -755,8 +755,18 @@ gpe_status vtd_upload(gpe_ctx* c, const gpe_split_params* prm, double time, int&
   return GPE_OK;
 }
 
+// One solve_split run of one context: the values fixed at its start.
+struct SplitRun {
+  int n_rec = 1, start = 0, nout = 0, nb = 1;
+  double ddt = 0, dre = 0, dim = 0, dt_outer = 0;
+  bool feedback = false;
+  std::vector<AxisPass> passes;
+  size_t hist_off = 0;  // history slot of outer step j: d_hist + hist_off + 3*(j - start - 1)
+};
+
+// solve_split.m:13-47: NN0, n_rec, complex dt, kinetic factors, initial mu.
 template <typename R>
-gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
+gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, int& vk, size_t hist_extra) {
   Field& f = c->main;
   const double ddt = prm->ddt;
   const double gam = c->prm.gamma;
@@ -770,7 +780,6 @@ gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
   const std::complex<double> dtc = ddt * std::complex<double>(0.0, 1.0) / std::complex<double>(1.0, gam);
   const double dre = dtc.real(), dim = dtc.imag();
   CHECK(set_kinop<R>(c, f, dre, dim));
-  int vk = 0;
   DevScalars s0;
   CHECK(read_scalars(c, &s0));
   // NN0 (solve_split.m:17-21)
@@ -791,19 +800,102 @@ gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
   // muc/mu at the start (solve_split.m:40-46): applyham at current_time.
   if (prm->vtd) CHECK(vtd_upload<R>(c, prm, c->cur.current_time, vk));
   CHECK(observables_impl<R>(c, f, NN0, 1, nullptr));
-  const bool feedback = gam > 0 && c->prm.mu_init == 0;
-  const double dt_outer = ddt * prm->niter_inner;
-  const int nb = prm->niter_inner / n_rec;
-  auto passes = axis_passes(c);
+  run.n_rec = n_rec;
+  run.start = start;
+  run.nout = nout;
+  run.ddt = ddt;
+  run.dre = dre;
+  run.dim = dim;
+  run.feedback = gam > 0 && c->prm.mu_init == 0;
+  run.dt_outer = ddt * prm->niter_inner;
+  run.nb = prm->niter_inner / n_rec;
+  run.passes = axis_passes(c);
+  run.hist_off = hist_extra;
   const int nsteps_out = std::max(0, nout - start);
-  std::vector<double> dh(3 * (size_t)std::max(1, nsteps_out), 0.0);
-  if (c->d_hist_len < dh.size()) {
+  const size_t hlen = hist_extra + 3 * (size_t)std::max(1, nsteps_out);
+  if (c->d_hist_len < hlen) {
     cudaFree(c->d_hist);
     c->d_hist = nullptr;
-    CU(cudaMalloc(&c->d_hist, dh.size() * sizeof(double)));
-    c->d_hist_len = dh.size();
+    CU(cudaMalloc(&c->d_hist, hlen * sizeof(double)));
+    c->d_hist_len = hlen;
   }
-  CU(cudaMemsetAsync(c->d_hist, 0, dh.size() * sizeof(double), c->stream));
+  CU(cudaMemsetAsync(c->d_hist, 0, hlen * sizeof(double), c->stream));
+  return GPE_OK;
+}
+
+// One block of n_rec steps, solve_split.m:51-79 (VV refresh is the caller's).
+// hist: where the block-end finalizer stores (muc, ncur), or nullptr.
+template <typename R>
+gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool last_block, double* hist) {
+  Field& f = c->main;
+  int nb_epi = 0;
+  for (int i = 1; i <= run.n_rec; ++i) {
+    for (size_t k = 0; k < run.passes.size(); ++k) {
+      const bool first = k == 0, last = k + 1 == run.passes.size();
+      const int pro = first ? (i == 1 ? PRO_RT_HALF : PRO_RT_FULL) : PRO_NONE;
+      const int epi = (last && i == run.n_rec) ? EPI_RT_END : EPI_NONE;
+      CHECK(run_pass<R>(c, f, run.passes[k], KIND_STEP, pro, epi, 0, run.dre, run.dim,
+                        (last && i == run.n_rec) ? &nb_epi : nullptr));
+    }
+  }
+  const bool need_mu = run.feedback || last_block;
+  int nk[3] = {0, 0, 0};
+  if (need_mu) CHECK(energy_passes<R>(c, f, false, nk, nullptr));
+  BlockFinalArgs a;
+  a.partials = c->partials;
+  a.cap = c->cap;
+  a.nblk_epi = nb_epi;
+  a.nblk_kin[0] = nk[0];
+  a.nblk_kin[1] = nk[1];
+  a.nblk_kin[2] = nk[2];
+  a.weight = c->weight;
+  a.g = c->prm.g;
+  a.feedback = run.feedback;
+  a.tau = c->prm.decay_rate;
+  a.time2 = time2;
+  a.hist_mu = hist;
+  a.hist_n = hist ? hist + 1 : nullptr;
+  a.hist_ok = nullptr;
+  Launch L(c, PC_FINALIZE, 0);
+  launch_finalize_block(a, c->sc, c->stream);
+  CU(cudaGetLastError());
+  return GPE_OK;
+}
+
+// End of a run: status checks, history and current_* from the device.
+template <typename R>
+gpe_status split_finish(gpe_ctx* c, const SplitRun& run, int last_j, double last_time2) {
+  DevScalars h;
+  CHECK(read_scalars(c, &h));
+  if (h.timeout) return fail(c, GPE_ERR_TIMEOUT, "solve_split: a device-side wait for staged data expired");
+  if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
+  const int start = run.start;
+  if (last_j > start) {
+    std::vector<double> dh(3 * (size_t)(last_j - start));
+    CU(cudaMemcpy(dh.data(), c->d_hist + run.hist_off, dh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if ((int)c->hist_mu.size() < last_j) {
+      c->hist_mu.resize(last_j, 0.0);
+      c->hist_n.resize(last_j, 0.0);
+    }
+    for (int j = start + 1; j <= last_j; ++j) {
+      c->hist_mu[j - 1] = dh[3 * (size_t)(j - start - 1)];
+      c->hist_n[j - 1] = dh[3 * (size_t)(j - start - 1) + 1];
+    }
+    c->cur.current_iter = last_j;
+    c->cur.current_time = last_time2;
+    c->cur.current_mu = h.muc;
+    c->cur.current_n = h.ncur;
+  }
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
+  SplitRun run;
+  int vk = 0;
+  CHECK(split_setup<R>(c, prm, run, vk, 0));
+  const int start = run.start, nout = run.nout, nb = run.nb, n_rec = run.n_rec;
+  const double ddt = run.ddt, dt_outer = run.dt_outer;
   int last_j = start;
   double last_time2 = c->cur.current_time;
   bool stop_req = false;
@@ -813,38 +905,8 @@ gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
     for (int jj = 1; jj <= nb; ++jj) {
       time2 = time + (jj - 1) * ddt * n_rec;  // solve_split.m:53
       if (prm->vtd) CHECK(vtd_upload<R>(c, prm, time2, vk));
-      int nb_epi = 0;
-      for (int i = 1; i <= n_rec; ++i) {
-        for (size_t k = 0; k < passes.size(); ++k) {
-          const bool first = k == 0, last = k + 1 == passes.size();
-          const int pro = first ? (i == 1 ? PRO_RT_HALF : PRO_RT_FULL) : PRO_NONE;
-          const int epi = (last && i == n_rec) ? EPI_RT_END : EPI_NONE;
-          CHECK(run_pass<R>(c, f, passes[k], KIND_STEP, pro, epi, 0, dre, dim,
-                            (last && i == n_rec) ? &nb_epi : nullptr));
-        }
-      }
-      const bool need_mu = feedback || jj == nb;
-      int nk[3] = {0, 0, 0};
-      if (need_mu) CHECK(energy_passes<R>(c, f, false, nk, nullptr));
-      BlockFinalArgs a;
-      a.partials = c->partials;
-      a.cap = c->cap;
-      a.nblk_epi = nb_epi;
-      a.nblk_kin[0] = nk[0];
-      a.nblk_kin[1] = nk[1];
-      a.nblk_kin[2] = nk[2];
-      a.weight = c->weight;
-      a.g = c->prm.g;
-      a.feedback = feedback;
-      a.tau = c->prm.decay_rate;
-      a.time2 = time2;
       const size_t hj = (size_t)(j - start - 1);
-      a.hist_mu = (jj == nb) ? c->d_hist + 3 * hj : nullptr;
-      a.hist_n = (jj == nb) ? c->d_hist + 3 * hj + 1 : nullptr;
-      a.hist_ok = nullptr;
-      Launch L(c, PC_FINALIZE, 0);
-      launch_finalize_block(a, c->sc, c->stream);
-      CU(cudaGetLastError());
+      CHECK(enqueue_block<R>(c, run, time2, jj == nb, (jj == nb) ? c->d_hist + 3 * hj : nullptr));
     }
     last_j = j;
     last_time2 = time2;
@@ -865,24 +927,125 @@ gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
       if (prm->on_step(prm->step_user, j, time2, h.muc, h.ncur) != 0) stop_req = true;
     }
   }
-  DevScalars h;
-  CHECK(read_scalars(c, &h));
-  if (h.timeout) return fail(c, GPE_ERR_TIMEOUT, "solve_split: a device-side wait for staged data expired");
-  if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
-  if (last_j > start) {
-    CU(cudaMemcpy(dh.data(), c->d_hist, dh.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    if ((int)c->hist_mu.size() < last_j) {
-      c->hist_mu.resize(last_j, 0.0);
-      c->hist_n.resize(last_j, 0.0);
-    }
-    for (int j = start + 1; j <= last_j; ++j) {
-      c->hist_mu[j - 1] = dh[3 * (size_t)(j - start - 1)];
-      c->hist_n[j - 1] = dh[3 * (size_t)(j - start - 1) + 1];
-    }
-    c->cur.current_iter = last_j;
-    c->cur.current_time = last_time2;
-    c->cur.current_mu = h.muc;
-    c->cur.current_n = h.ncur;
+  return split_finish<R>(c, run, last_j, last_time2);
+}
+
+// ---- batched solve_split -------------------------------------------------------
+// Many independent contexts (grids of any sizes) advance together: one block
+// of n_rec steps of every context is captured once into a CUDA graph whose
+// per-context chains hang off a fork/join pair of events, so the chains run
+// concurrently on the GPU; the graph is then replayed block after block.
+// A second graph holds the last block of an outer step (with the kinetic-
+// energy passes and the history record).  Per-block host work (callbacks,
+// time-dependent V, the decay target exp(-t/tau)) cannot live in a replayed
+// graph, so those features are rejected here.
+struct BatchGraph {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t x = nullptr;
+  ~BatchGraph() {
+    if (x) cudaGraphExecDestroy(x);
+    if (g) cudaGraphDestroy(g);
+  }
+};
+
+gpe_status capture_blocks(gpe_ctx* c0, std::vector<gpe_ctx*>& cs, std::vector<SplitRun>& runs, bool last_block,
+                          cudaStream_t master, std::vector<cudaEvent_t>& evs, BatchGraph& out) {
+  gpe_ctx* c = c0;
+  CU(cudaStreamBeginCapture(master, cudaStreamCaptureModeThreadLocal));
+  gpe_status st = GPE_OK;
+  cudaError_t e = cudaEventRecord(evs[0], master);
+  for (size_t i = 0; i < cs.size() && st == GPE_OK && e == cudaSuccess; ++i) {
+    gpe_ctx* ci = cs[i];
+    e = cudaStreamWaitEvent(ci->stream, evs[0], 0);
+    if (e != cudaSuccess) break;
+    const bool prof = ci->prof;
+    const long long launches = ci->launches;
+    ci->prof = false;  // no profiling events inside a graph
+    if (ci->prec == GPE_FP32) st = enqueue_block<float>(ci, runs[i], 0.0, last_block, last_block ? ci->d_hist : nullptr);
+    else st = enqueue_block<double>(ci, runs[i], 0.0, last_block, last_block ? ci->d_hist : nullptr);
+    ci->prof = prof;
+    ci->launches = launches;  // counted per replay instead
+    if (st != GPE_OK) break;
+    e = cudaEventRecord(evs[1 + i], ci->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(master, evs[1 + i], 0);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(master, &g);
+  if (st != GPE_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(c, GPE_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+  }
+  out.g = g;
+  CU(cudaGraphInstantiate(&out.x, g, 0));
+  return GPE_OK;
+}
+
+gpe_status batch_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm) {
+  gpe_ctx* c = cs[0];
+  const size_t n = cs.size();
+  std::vector<SplitRun> runs(n);
+  for (size_t i = 0; i < n; ++i) {
+    int vk = 0;
+    gpe_ctx* ci = cs[i];
+    ci->err.clear();
+    gpe_status st = ci->prec == GPE_FP32 ? split_setup<float>(ci, prm, runs[i], vk, 3)
+                                         : split_setup<double>(ci, prm, runs[i], vk, 3);
+    if (st != GPE_OK) return fail(c, st, "batch: context " + std::to_string(i) + ": " + ci->err);
+    CU(cudaStreamSynchronize(ci->stream));
+  }
+  const SplitRun& r0 = runs[0];
+  for (size_t i = 1; i < n; ++i)
+    if (runs[i].n_rec != r0.n_rec || runs[i].start != r0.start)
+      return fail(c, GPE_ERR_INVALID, "batch: all contexts need the same n_recalc and current_iter");
+  // The graphs are launched on the first context's stream, so that context's
+  // timer (gpe_timer_start/stop) brackets a batched run.
+  cudaStream_t master = cs[0]->stream;
+  std::vector<cudaEvent_t> evs(n + 1, nullptr);
+  for (auto& ev : evs) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  auto cleanup = [&]() {
+    for (auto ev : evs)
+      if (ev) cudaEventDestroy(ev);
+  };
+  BatchGraph g_plain, g_last;
+  gpe_status st = GPE_OK;
+  if (r0.nb > 1) st = capture_blocks(c, cs, runs, false, master, evs, g_plain);
+  if (st == GPE_OK) st = capture_blocks(c, cs, runs, true, master, evs, g_last);
+  if (st != GPE_OK) {
+    cleanup();
+    return st;
+  }
+  // kernels per replay, for the launch counters
+  std::vector<long long> k_plain(n), k_last(n);
+  for (size_t i = 0; i < n; ++i) {
+    const long long steps = (long long)runs[i].n_rec * (long long)runs[i].passes.size();
+    k_plain[i] = steps + (runs[i].feedback ? (long long)runs[i].passes.size() : 0) + 1;
+    k_last[i] = steps + (long long)runs[i].passes.size() + 1;
+  }
+  int last_j = r0.start;
+  cudaError_t e = cudaSuccess;
+  for (int j = r0.start + 1; j <= r0.nout && e == cudaSuccess; ++j) {
+    for (int jj = 1; jj < r0.nb && e == cudaSuccess; ++jj) e = cudaGraphLaunch(g_plain.x, master);
+    if (e == cudaSuccess) e = cudaGraphLaunch(g_last.x, master);
+    // the last block left (muc, ncur) in each context's slot 0: file it
+    const size_t hj = (size_t)(j - r0.start - 1);
+    for (size_t i = 0; i < n && e == cudaSuccess; ++i)
+      e = cudaMemcpyAsync(cs[i]->d_hist + 3 + 3 * hj, cs[i]->d_hist, 2 * sizeof(double), cudaMemcpyDeviceToDevice,
+                          master);
+    for (size_t i = 0; i < n; ++i) cs[i]->launches += (long long)(r0.nb - 1) * k_plain[i] + k_last[i];
+    last_j = j;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(master);
+  cleanup();
+  if (e != cudaSuccess) return fail(c, GPE_ERR_CUDA, std::string("batch replay: ") + cudaGetErrorString(e));
+  for (size_t i = 0; i < n; ++i) {
+    const double time2 = (last_j - 1) * runs[i].dt_outer + (runs[i].nb - 1) * runs[i].ddt * runs[i].n_rec;
+    gpe_status st2 = cs[i]->prec == GPE_FP32 ? split_finish<float>(cs[i], runs[i], last_j, time2)
+                                             : split_finish<double>(cs[i], runs[i], last_j, time2);
+    if (st2 != GPE_OK) return fail(c, st2, "batch: context " + std::to_string(i) + ": " + cs[i]->err);
   }
   return GPE_OK;
 }
@@ -1237,6 +1400,30 @@ gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
   c->err.clear();
   if (c->prec == GPE_FP32) return split_impl<float>(c, prm);
   return split_impl<double>(c, prm);
+}
+
+gpe_status gpe_solve_split_batch(gpe_ctx** ctxs, int count, const gpe_split_params* prm) {
+  if (!ctxs || count < 1 || !ctxs[0]) return fail(nullptr, GPE_ERR_INVALID, "solve_split_batch: no contexts");
+  gpe_ctx* c = ctxs[0];
+  CHECK(check_ctx(c));
+  if (!prm || !(prm->ddt > 0) || !std::isfinite(prm->ddt))
+    return fail(c, GPE_ERR_INVALID, "solve_split_batch: ddt must be positive");
+  if (prm->vtd || prm->on_step)
+    return fail(c, GPE_ERR_INVALID, "solve_split_batch: per-block host callbacks are not supported in batches");
+  std::vector<gpe_ctx*> cs;
+  for (int i = 0; i < count; ++i) {
+    gpe_ctx* ci = ctxs[i];
+    if (!ci) return fail(c, GPE_ERR_INVALID, "solve_split_batch: null context");
+    if (ci->device != c->device) return fail(c, GPE_ERR_INVALID, "solve_split_batch: contexts on different devices");
+    if (!ci->have_state || !ci->have_V) return fail(c, GPE_ERR_STATE, "solve_split_batch: a context lacks state or V");
+    if (ci->prm.decay_rate > 0)
+      return fail(c, GPE_ERR_INVALID, "solve_split_batch: decay_rate > 0 needs per-block host times");
+    for (auto* cj : cs)
+      if (cj == ci) return fail(c, GPE_ERR_INVALID, "solve_split_batch: a context appears twice");
+    cs.push_back(ci);
+  }
+  c->err.clear();
+  return batch_impl(cs, prm);
 }
 
 gpe_status gpe_observables(gpe_ctx* c, gpe_obs* o) {

@@ -96,6 +96,7 @@ PROTOTYPES = {
     "gpe_groundstate_itp": (C.c_int, [_P, C.POINTER(gpe_itp_params), _D, _D, _D, C.c_int,
                                       C.POINTER(gpe_itp_result)]),
     "gpe_solve_split": (C.c_int, [_P, C.POINTER(gpe_split_params)]),
+    "gpe_solve_split_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(gpe_split_params)]),
     "gpe_observables": (C.c_int, [_P, C.POINTER(gpe_obs)]),
     "gpe_synchronize": (C.c_int, [_P]),
     "gpe_timer_start": (C.c_int, [_P]),

@@ -227,8 +227,8 @@ class GPEtask:
         outs = (phi, MU[:n].copy(), MU2[:n].copy(), EE[:n].copy())
         return phi if nargout <= 1 else outs[:nargout]
 
-    def solve_split(self, ddt, niter_inner, niter_outer):
-        """solve_split.m:1-84: run outer steps current_iter+1 .. niter_outer."""
+    def _prepare_split(self):
+        """Parameters and the start state on the device (solve_split.m:29,34-38)."""
         self._push_params()
         start = int(self.current_iter)
         if start > 0:
@@ -238,6 +238,19 @@ class GPEtask:
                 self._upload_state(self._current_state)
         else:
             self._upload_state(self.init_state)
+
+    def _after_split(self):
+        cur = L.gpe_current()
+        L.check(self._ctx, L.lib.gpe_get_current(self._ctx, C.byref(cur)))
+        self.current_iter, self.current_time = cur.current_iter, cur.current_time
+        self.current_mu, self.current_n = cur.current_mu, cur.current_n
+        self._sync_history()
+        self._current_state = None
+        self._state_on_device = "current"
+
+    def solve_split(self, ddt, niter_inner, niter_outer):
+        """solve_split.m:1-84: run outer steps current_iter+1 .. niter_outer."""
+        self._prepare_split()
         errors = []
         vtd_cb = L.VTD_FN()
         if self._time_dependent():
@@ -276,13 +289,7 @@ class GPEtask:
         if errors:
             raise errors[0]
         L.check(self._ctx, st)
-        cur = L.gpe_current()
-        L.check(self._ctx, L.lib.gpe_get_current(self._ctx, C.byref(cur)))
-        self.current_iter, self.current_time = cur.current_iter, cur.current_time
-        self.current_mu, self.current_n = cur.current_mu, cur.current_n
-        self._sync_history()
-        self._current_state = None
-        self._state_on_device = "current"
+        self._after_split()
         return self.current_state
 
     def _sync_history(self):
@@ -342,3 +349,28 @@ class GPEtask:
     def set_pass_variant(self, variant: int):
         """0: direct passes (default), 1: TMA-staged passes where they apply."""
         L.check(self._ctx, L.lib.gpe_set_pass_variant(self._ctx, int(variant)))
+
+
+def solve_split_batch(tasks, ddt, niter_inner, niter_outer):
+    """solve_split(ddt, niter_inner, niter_outer) of many independent GPEtask
+    objects at once, through gpe_solve_split_batch: grids of any sizes, one
+    CUDA graph per block of n_recalc steps with the tasks' chains running
+    concurrently.  Each task keeps its own properties, state, history and
+    current_*.  Tasks need static potentials (no Vtd / V0), no user_callback,
+    no decay, the same n_recalc and the same current_iter."""
+    tasks = list(tasks)
+    if not tasks:
+        return
+    for t in tasks:
+        if t._time_dependent() or t.user_callback is not None:
+            raise ValueError("solve_split_batch: tasks need a static potential and no user_callback")
+        t._prepare_split()
+        t._upload_V(t.Vtrap)
+    arr = (C.c_void_p * len(tasks))(*[t._ctx.value for t in tasks])
+    prm = L.gpe_split_params()
+    prm.ddt = float(ddt)
+    prm.niter_inner = int(niter_inner)
+    prm.niter_outer = int(niter_outer)
+    L.check(tasks[0]._ctx, L.lib.gpe_solve_split_batch(arr, len(tasks), C.byref(prm)))
+    for t in tasks:
+        t._after_split()

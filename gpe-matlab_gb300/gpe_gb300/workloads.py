@@ -106,3 +106,69 @@ RING3D = Workload(
     notes=["box +-24 assumed", "ITP dt 0.004 and eps 1e-6 assumed"])
 
 WORKLOADS = {w.name: w for w in (VORTEX2D, DAMPED3D, RING3D)}
+
+
+@dataclass
+class BatchWorkload:
+    """Many independent 2D realisations of uneven sizes, advanced together.
+
+    Sizes uniform in {128^2, 192^2, 256^2, 384^2}, trap V = 0.5 (x^2 + (lam y)^2)
+    with lam ~ U(1, 2), g ~ U(0.02, 0.2), and 1-3 vortices at seeded positions
+    within 0.6 of the Thomas-Fermi radii; 5000 steps of dt = 0.004.  Assumed:
+    box +-16, Ntotal = 2e4, ITP dt = 0.01 (mu*dt <= 0.5), 100 steps per outer step.
+    """
+
+    name: str = "batch2d_64"
+    count: int = 64
+    sizes: tuple = (128, 192, 256, 384)
+    box: float = 16.0
+    Ntotal: float = 2e4
+    itp_dt: float = 0.01
+    itp_eps: float = 1e-6
+    dt: float = 0.004
+    steps: int = 5000
+    niter_inner: int = 100
+    seed: int = 3
+
+    def realisations(self):
+        rng = np.random.default_rng(self.seed)
+        out = []
+        for _ in range(self.count):
+            n = int(rng.choice(self.sizes))
+            lam = float(rng.uniform(1.0, 2.0))
+            g = float(rng.uniform(0.02, 0.2))
+            nv = int(rng.integers(1, 4))
+            out.append({"n": n, "lam": lam, "g": g, "nv": nv, "u": rng.random((nv, 2))})
+        return out
+
+    @property
+    def npoints(self) -> int:
+        return int(sum(r["n"] ** 2 for r in self.realisations()))
+
+    def make_tasks(self, precision: str = "single", device: int = 0):
+        """Tasks holding their ground state with the vortices imprinted."""
+        from .imprint import imprint_vortex
+        from .task import GPEtask
+
+        tasks = []
+        for r in self.realisations():
+            grid = grid2d(self.box, r["n"], self.box, r["n"], precision=precision)
+            lam = r["lam"]
+            task = GPEtask(grid, lambda X, Y, Z, lam=lam: 0.5 * (X ** 2 + (lam * Y) ** 2), device=device)
+            task.Ntotal, task.g = self.Ntotal, r["g"]
+            X, Y = grid.mesh["x"], grid.mesh["y"]
+            phi0 = np.exp(-(X ** 2 + (lam * Y) ** 2) / 32.0).astype(np.complex128)
+            phi = np.asarray(task.groundstate_itp(self.itp_dt, self.itp_eps, phi0, nargout=2)[0],
+                             dtype=np.complex128)
+            rx = np.sqrt(2.0 * task.current_mu)
+            ry = rx / lam
+            for u1, u2 in r["u"]:
+                rad, th = 0.6 * np.sqrt(u1), 2.0 * np.pi * u2
+                phi = imprint_vortex(grid, phi, r["g"], rad * rx * np.cos(th), rad * ry * np.sin(th))
+            task.init_state = phi
+            task.current_iter = 0
+            tasks.append(task)
+        return tasks
+
+
+BATCH2D = BatchWorkload()

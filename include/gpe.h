@@ -199,6 +199,14 @@ GPE_API gpe_status gpe_groundstate_itp(gpe_ctx *ctx, const gpe_itp_params *prm,
                                gpe_itp_result *res);
 /* solve_split.m:1-84 from the current state; resumes at current_iter. */
 GPE_API gpe_status gpe_solve_split(gpe_ctx *ctx, const gpe_split_params *prm);
+/* solve_split on `count` independent contexts (any grid sizes, same device,
+ * same n_recalc and current_iter) advanced together: one block of n_recalc
+ * steps of every context is captured into a CUDA graph whose per-context
+ * chains run concurrently, and replayed.  Each context keeps its own state,
+ * V, parameters, history and current_*.  Not available in a batch: vtd and
+ * on_step callbacks (must be NULL) and decay_rate > 0.  Errors are reported
+ * on ctxs[0]. */
+GPE_API gpe_status gpe_solve_split_batch(gpe_ctx **ctxs, int count, const gpe_split_params *prm);
 /* applyham / get_energy pieces for the current state at the current V. */
 GPE_API gpe_status gpe_observables(gpe_ctx *ctx, gpe_obs *obs);
 

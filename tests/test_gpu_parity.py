@@ -221,6 +221,44 @@ def test_gamma0_conserves_norm_fp32(gpe):
 
 
 @pytest.mark.parametrize("precision", ["double", "single"])
+def test_batched_uneven_grids_match_individual_runs(gpe, precision):
+    """solve_split_batch (one CUDA graph per block, chains of all grids run
+    concurrently) gives each task exactly what its own solve_split gives."""
+    specs = [((4.0, 32, 4.0, 32), 0.8, 0.0), ((5.0, 48, 4.0, 64), 1.5, 0.02),
+             ((6.0, 64, 6.0, 24), 0.5, 0.0), ((3.0, 24, 3.0, 32), 2.0, 0.05)]
+
+    def make(spec):
+        axes, g, gam = spec
+        grid = gpe.grid2d(*axes, precision=precision)
+        t = gpe.GPEtask(grid, harmonic((1.0, 1.3)))
+        t.g, t.gamma, t.Ntotal = g, gam, 5.0
+        X, Y = grid.mesh["x"], grid.mesh["y"]
+        t.init_state = np.sqrt(5.0) * grid.normalize(np.exp(-(X ** 2 + Y ** 2) / 2 + 0.4j * X))
+        return t
+
+    singles = [make(s) for s in specs]
+    for t in singles:
+        t.solve_split(0.003, 20, 3)
+    batch = [make(s) for s in specs]
+    gpe.solve_split_batch(batch, 0.003, 20, 3)
+    tol = 1e-12 if precision == "double" else 1e-6
+    for a, b in zip(singles, batch):
+        assert b.current_iter == 3 and b.current_time == pytest.approx(a.current_time)
+        assert rel_l2(b.current_state, a.current_state) < tol
+        np.testing.assert_allclose(b.history["mu"], a.history["mu"], rtol=tol)
+        np.testing.assert_allclose(b.history["n"], a.history["n"], rtol=tol)
+
+
+def test_batched_rejects_host_callbacks(gpe):
+    grid = gpe.grid2d(3, 16, 3, 16)
+    t = gpe.GPEtask(grid, harmonic((1.0, 1.0)))
+    t.init_state = np.ones(grid.shape, complex)
+    t.decay_rate = 1.0
+    with pytest.raises(gpe.GPEError):
+        gpe.solve_split_batch([t], 0.01, 10, 1)
+
+
+@pytest.mark.parametrize("precision", ["double", "single"])
 def test_tma_pass_variant_matches_direct(gpe, precision):
     """The TMA-staged passes run the same per-point arithmetic as the direct
     passes; only the order of the norm/energy sums differs, so results agree
