@@ -180,9 +180,13 @@ def cpu_reference_steps(W, phi, steps: int, cores: int, max_seconds: float = 25.
 def run_reference(args, dist):
     from gpe_gb300.workloads import WORKLOADS
 
-    W = WORKLOADS[args.workload]
     if dist.rank != 0:
         return
+    if args.workload not in WORKLOADS:
+        print(json.dumps({"impl": "reference", "unavailable": f"{args.workload}: the reference has no gradient or "
+                          "batched path; the FP64 oracle adjoint is timed as cpu_baseline of the gb300 arm"}))
+        return
+    W = WORKLOADS[args.workload]
     cores = os.cpu_count() or 1
     # Start state: the seeded Gaussian (the timed work does not depend on it).
     grid = W.make_grid("double")
@@ -386,6 +390,106 @@ def run_batch(args, dist):
         t.close()
 
 
+ADJ_METRIC = "adjoint grid-pt-steps/s (loss + dloss/dV through the window, per second)"
+
+
+def adjoint_case(gpe, name, dev):
+    """(task, psi0, target, V, nsteps, checkpoint_every, basis, describe) of an adjoint workload."""
+    if name == "adjoint2d_256":
+        from gpe_gb300.workloads import ADJOINT2D as W
+
+        grid = W.make_grid("single")
+        task = gpe.GPEtask(grid, lambda X, Y, Z: W.trap(grid), device=dev)
+        task.Ntotal, task.g = W.Ntotal, W.g
+        X, Y = grid.mesh["x"], grid.mesh["y"]
+        psi0 = np.asarray(task.groundstate_itp(W.itp_dt, W.itp_eps, np.exp(-(X ** 2 + Y ** 2) / 32).astype(complex)),
+                          dtype=np.complex128)
+        tgt = gpe.imprint_vortex(grid, psi0, W.g, W.vortex_x0)
+        a, basis = W.bumps(grid)
+        V = W.trap(grid) + sum(aj * b for aj, b in zip(a, basis))
+        cfg = {"workload": W.name, "grid": [W.n, W.n], "box": W.box, "g": W.g, "Ntotal": W.Ntotal, "dt": W.dt,
+               "window_steps": W.steps, "checkpoint_every": W.checkpoint_every,
+               "potential": "0.5 r^2 + 16 seeded Gaussian bumps", "target": f"vortex imprinted at x0 = {W.vortex_x0}"}
+        return task, psi0, tgt, V, W.steps, W.checkpoint_every, basis, cfg
+    from gpe_gb300.workloads import RING3D as W
+
+    grid, task, phi = ground_state(gpe, W, "single", device=dev)
+    psi0 = np.asarray(imprint(gpe, W, grid, task, np.asarray(phi, dtype=np.complex128)))
+    tgt = np.asarray(phi, dtype=np.complex128)
+    V = np.ascontiguousarray(task.Vtrap)
+    cfg = {"workload": "adjoint3d_512", "grid": list(W.n), "box": W.box[0], "trap_lambda": list(W.trap), "g": W.g,
+           "Ntotal": W.Ntotal, "dt": W.dt, "window_steps": 500, "checkpoint_every": "auto (sqrt rule)",
+           "mem_budget_GB": 60, "start": "vortex ring (0.5 R_TF) on the ITP ground state",
+           "target": "the ground state without the ring"}
+    return task, psi0, tgt, V, 500, 0, None, cfg
+
+
+def run_adjoint(args, dist):
+    """Gradient workloads: one bench step = one gpe_adjoint_grad call (forward
+    window with checkpoints, loss, backward sweep with segment recompute),
+    device-timed with CUDA events on the context stream."""
+    import ctypes as C
+
+    import gpe_gb300 as gpe
+    from gpe_gb300 import _lib as L
+
+    dev = dist.local
+    task, psi0, tgt, V, M, K, basis, cfg = adjoint_case(gpe, args.workload, dev)
+    P = task.grid.npoints
+    budget = 60e9
+    precision = "double" if args.adjoint_fp64 else None
+    kw = dict(phi0=psi0, V=V, checkpoint_every=K, mem_budget=budget, precision=precision)
+    for _ in range(1 if P > 1e7 else args.warmup):
+        task.adjoint_grad(tgt, cfg["dt"], M, **kw)
+    steps = min(args.steps, 2) if P > 1e7 else args.steps
+    task._upload_state(psi0)  # the timed calls run on a device-resident start state
+    k0 = task.kernel_launches()
+    task.profile(True)
+    dist.barrier()
+    with ClockSampler(dev) as clk:
+        L.check(task._ctx, L.lib.gpe_timer_start(task._ctx))
+        for _ in range(steps):
+            loss, dV = task.adjoint_grad(tgt, cfg["dt"], M, **kw)
+        ms = C.c_double()
+        L.check(task._ctx, L.lib.gpe_timer_stop(task._ctx, C.byref(ms)))
+    stats = task.profile_read()
+    task.profile(False)
+    launches = task.kernel_launches() - k0
+    t_s = dist.reduce(ms.value / 1e3, "max")
+    value = dist.reduce(float(P) * M * steps, "sum") / t_s
+    hbm, peak_kind = peaks()
+    top = max(stats, key=lambda s: s["total_ms"])
+    avg_ms = top["total_ms"] / top["launches"]
+    achieved = top["bytes_per_launch"] / (avg_ms / 1e3) / 1e9
+    line = {
+        "metric": ADJ_METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": ms.value / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if precision else "c64 (FP64 dL/dV accumulation)",
+        "data": "synthetic (seeded, ITP ground state)", "config": cfg, "loss": loss,
+        "grad_norm": float(np.linalg.norm(dV)),
+        "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": top["bytes_per_launch"], "avg_launch_ms": avg_ms},
+        "kernels": stats, "gpu_launches": int(launches), "clocks": clk.summary(),
+    }
+    if basis is not None:
+        line["dloss_da"] = [float(v) for v in task.project_gradient(dV, basis)]
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu and basis is not None:
+        from oracle import gpe_oracle as O
+
+        O.set_workers(os.cpu_count() or 1)
+        og = O.Grid(cfg["box"], cfg["grid"][0], cfg["box"], cfg["grid"][1])
+        n_cpu = 200
+        t0 = time.perf_counter()
+        O.adjoint_grad(og, V, task.g, psi0, tgt, cfg["dt"], n_cpu)
+        tc = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": P * n_cpu / tc, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": f"FP64 oracle adjoint over {n_cpu} steps of the same grid, {tc:.1f} s"}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    task.close()
+
+
 def run_profile_case(precision: str, blocks: int, variant: int = 0):
     """Small fixed case for ncu captures: the bench workload's grid and
     parameters from the seeded Gaussian (no ITP), `blocks` blocks of 10 steps."""
@@ -414,8 +518,11 @@ def main():
     ap.add_argument("--quick", action="store_true", help="FP32 timed region only (no FP64, e2e, CPU legs)")
     ap.add_argument("--pass-variant", type=int, default=0, help="0: direct passes (default), 1: TMA-staged")
     ap.add_argument("--workload", default="damped3d_256",
-                    choices=["damped3d_256", "ring3d_512", "vortex2d_256", "batch2d_64"],
-                    help="damped3d_256 (default, the headline), ring3d_512, vortex2d_256 (L2-resident)")
+                    choices=["damped3d_256", "ring3d_512", "vortex2d_256", "batch2d_64", "adjoint2d_256",
+                             "adjoint3d_512"],
+                    help="damped3d_256 (default, the headline), ring3d_512, vortex2d_256 (L2-resident), "
+                         "batch2d_64 (64 uneven grids), adjoint2d_256 / adjoint3d_512 (gradients)")
+    ap.add_argument("--adjoint-fp64", action="store_true", help="adjoint workloads: FP64 sweep of the FP32 context")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args.profile_case, args.profile_blocks, args.pass_variant)
@@ -429,6 +536,8 @@ def main():
         else:
             if args.workload == "batch2d_64":
                 run_batch(args, dist)
+            elif args.workload.startswith("adjoint"):
+                run_adjoint(args, dist)
             else:
                 run_gpu(args, dist)
     finally:

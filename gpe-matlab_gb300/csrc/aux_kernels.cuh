@@ -68,6 +68,17 @@ void launch_reset_scalars(DevScalars* sc, cudaStream_t s);
 void launch_set_scale_one(DevScalars* sc, cudaStream_t s);
 cudaError_t launch_selftest_trig(const float* x, float* s, float* c, long long n, cudaStream_t st);
 
+// Discrete adjoint pieces (adjoint_kernels.cu).
+template <typename R>
+void launch_nl_phase(cx<R>* psi, const R* V, long long n, double g, double h, cudaStream_t s);
+template <typename R>
+void launch_adj_nl(cx<R>* lam, const cx<R>* x, const R* V, double* dLdV, long long n, double g, double h,
+                   int first, int second, int conj_in, int conj_out, cudaStream_t s);
+template <typename R>
+int launch_inner(const cx<R>* a, const cx<R>* b, long long n, double* partials, cudaStream_t s);
+template <typename R>
+void launch_cscale(cx<R>* out, const cx<R>* in, long long n, double cr, double ci, cudaStream_t s);
+
 template <typename R>
 int launch_norm(const cx<R>* psi, long long n, DevScalars* sc, double* partials, int cap, cudaStream_t s);
 template <typename R>

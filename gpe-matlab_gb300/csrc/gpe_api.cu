@@ -188,11 +188,11 @@ size_t rsize() {
 // ---- profiling --------------------------------------------------------------
 enum ProfCls {
   PC_PASS_Y, PC_PASS_X, PC_PASS_Z, PC_ENERGY_Y, PC_ENERGY_X, PC_ENERGY_Z, PC_FINALIZE, PC_ITP_CHECK,
-  PC_NORM, PC_ELEMENTWISE, PC_COUNT
+  PC_NORM, PC_ELEMENTWISE, PC_NL_PHASE, PC_ADJ_NL, PC_COPY, PC_COUNT
 };
-const char* kProfNames[PC_COUNT] = {"pass_y",   "pass_x",    "pass_z",    "energy_y",
-                                    "energy_x", "energy_z",  "finalize",  "itp_check",
-                                    "norm",     "elementwise"};
+const char* kProfNames[PC_COUNT] = {"pass_y",   "pass_x",    "pass_z",      "energy_y",  "energy_x",
+                                    "energy_z", "finalize",  "itp_check",   "norm",      "elementwise",
+                                    "nl_phase", "adjoint_nl", "state_copy"};
 
 cudaEvent_t pool_event(gpe_ctx* c) {
   if (!c->ev_pool.empty()) {
@@ -419,9 +419,9 @@ gpe_status write_scalars(gpe_ctx* c, const DevScalars& v) {
 // ---- passes ---------------------------------------------------------------------
 template <typename R>
 gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro, int epi, int energy_pot,
-                    double dre, double dim, int* nblk) {
+                    double dre, double dim, int* nblk, void* psi_buf = nullptr) {
   PassArgs<R> a;
-  a.psi = (cx<R>*)f.psi;
+  a.psi = (cx<R>*)(psi_buf ? psi_buf : f.psi);  // psi_buf: another array of the grid's shape
   a.V = (const R*)f.V;
   a.aux = (R*)f.aux;
   a.php = (const cx<R>*)f.php[ap.axis];
@@ -930,6 +930,175 @@ gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
   return split_finish<R>(c, run, last_j, last_time2);
 }
 
+// ---- adjoint: dL/dV of L = 1 - |<target|psi(T)>|^2 / (|target|^2 |psi0|^2) ------
+// Forward: M steps S = N K N from the current state (the gamma = 0 form of
+// solve_split.m:55-64, adjoint_kernels.cu).  States are kept every K steps
+// (checkpoints); the backward sweep recomputes each segment's K step-start
+// states from its checkpoint, then walks the steps in reverse:
+//   phi2 = K N x0;  lam <- adjN(lam; phi2);  lam <- K^H lam;  lam <- adjN(lam; x0).
+gpe_status io_buffer(gpe_ctx* c, void** out);
+
+template <typename R>
+gpe_status kinetic_on(gpe_ctx* c, Field& f, void* buf, double ddt) {
+  for (auto& ap : axis_passes(c)) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, 0.0, ddt, nullptr, buf));
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status strang_step(gpe_ctx* c, Field& f, cx<R>* x, double ddt) {
+  const double h = 0.5 * ddt;
+  {
+    Launch L(c, PC_NL_PHASE, (double)c->P * (4 * sizeof(R) + sizeof(R)));
+    launch_nl_phase<R>(x, (const R*)f.V, c->P, c->prm.g, h, c->stream);
+  }
+  CHECK(kinetic_on<R>(c, f, x, ddt));
+  {
+    Launch L(c, PC_NL_PHASE, (double)c->P * (4 * sizeof(R) + sizeof(R)));
+    launch_nl_phase<R>(x, (const R*)f.V, c->P, c->prm.g, h, c->stream);
+  }
+  CU(cudaGetLastError());
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status inner_impl(gpe_ctx* c, const cx<R>* a, const cx<R>* b, std::complex<double>* out) {
+  const int nb = launch_inner<R>(a, b, c->P, c->partials, c->stream);
+  c->launches++;
+  std::vector<double> h(2 * (size_t)nb);
+  CU(cudaMemcpyAsync(h.data(), c->partials, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  double re = 0.0, im = 0.0;
+  for (int i = 0; i < nb; ++i) {
+    re += h[2 * i];
+    im += h[2 * i + 1];
+  }
+  *out = std::complex<double>(re, im) * c->weight;
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status adjoint_impl(gpe_ctx* c, Field& f, const gpe_adjoint_params* prm, const double* target,
+                        double* dLdV_out, double* loss_out) {
+  // f: the context's own field, or the FP64 field of an FP32 context.  The
+  // start state is read from the context state (with its pending scale),
+  // which is left as it is.
+  launch_reset_scalars(c->sc, c->stream);  // passes skip their work while sc->stop is set
+  const long long P = c->P;
+  const size_t S = (size_t)P * 2 * sizeof(R);
+  const int M = prm->nsteps;
+  const double budget = prm->mem_budget > 0 ? prm->mem_budget : 60e9;
+  // checkpoint interval: the caller's, or the one minimising stored states.
+  // Stored: ceil(M/K)+1 checkpoints (the last is psi(T)), K-1 recomputed
+  // states of one segment (K slots), x, lam, target, and dL/dV in FP64.
+  int K = prm->checkpoint_every;
+  auto bytes_for = [&](int k) { return ((double)((M + k - 1) / k + k + 4)) * S + (double)P * 8.0; };
+  if (K <= 0) {
+    K = 1;
+    for (int k = 1; k <= M; ++k)
+      if (bytes_for(k) < bytes_for(K)) K = k;
+  }
+  if (K > M) K = M;
+  if (bytes_for(K) > budget)
+    return fail(c, GPE_ERR_ALLOC, "adjoint: " + std::to_string(bytes_for(K) / 1e9) +
+                                      " GB of states exceed the memory budget; raise mem_budget or change checkpoint_every");
+  const int nck = (M + K - 1) / K;
+  std::vector<void*> bufs;
+  auto cleanup = [&]() {
+    for (void* p : bufs) cudaFree(p);
+  };
+  auto alloc = [&](void** p, size_t bytes) -> bool {
+    if (cudaMalloc(p, bytes) != cudaSuccess) return false;
+    bufs.push_back(*p);
+    return true;
+  };
+  void *ck = nullptr, *seg = nullptr, *x = nullptr, *lam = nullptr, *tgt = nullptr;
+  double* dV = nullptr;
+  if (!alloc(&ck, (size_t)(nck + 1) * S) || !alloc(&seg, (size_t)K * S) || !alloc(&x, S) || !alloc(&lam, S) ||
+      !alloc(&tgt, S) || !alloc((void**)&dV, (size_t)P * sizeof(double))) {
+    cleanup();
+    return fail(c, GPE_ERR_ALLOC, "adjoint: device allocation of the checkpoint store failed");
+  }
+  auto st_at = [&](void* base, int i) { return (cx<R>*)((char*)base + (size_t)i * S); };
+  gpe_status st = GPE_OK;
+  auto run = [&]() -> gpe_status {
+    CHECK(set_kinop<R>(c, f, 0.0, prm->ddt));
+    // target in the field's precision
+    if constexpr (sizeof(R) == 8) {
+      CU(cudaMemcpyAsync(tgt, target, (size_t)P * 16, cudaMemcpyHostToDevice, c->stream));
+    } else {
+      void* io = nullptr;
+      CHECK(io_buffer(c, &io));
+      CU(cudaMemcpyAsync(io, target, (size_t)P * 16, cudaMemcpyHostToDevice, c->stream));
+      launch_convert_cx<double, R>((const cx<double>*)io, (cx<R>*)tgt, P, nullptr, c->stream);
+      CU(cudaStreamSynchronize(c->stream));
+      if (io != c->polish.psi) cudaFree(io);
+    }
+    // forward with checkpoints, from the context state times its pending scale
+    if (c->prec == GPE_FP32)
+      launch_convert_cx<float, R>((const cx<float>*)c->main.psi, (cx<R>*)x, P, c->sc, c->stream);
+    else
+      launch_convert_cx<double, R>((const cx<double>*)c->main.psi, (cx<R>*)x, P, c->sc, c->stream);
+    c->launches++;
+    for (int m = 0; m < M; ++m) {
+      if (m % K == 0) {
+        Launch L(c, PC_COPY, 2.0 * S);
+        CU(cudaMemcpyAsync(st_at(ck, m / K), x, S, cudaMemcpyDeviceToDevice, c->stream));
+      }
+      CHECK(strang_step<R>(c, f, (cx<R>*)x, prm->ddt));
+    }
+    {
+      Launch L(c, PC_COPY, 2.0 * S);
+      CU(cudaMemcpyAsync(st_at(ck, nck), x, S, cudaMemcpyDeviceToDevice, c->stream));  // x_M
+    }
+    // loss
+    std::complex<double> ov, n0c, ntc;
+    CHECK(inner_impl<R>(c, (const cx<R>*)tgt, (const cx<R>*)x, &ov));
+    CHECK(inner_impl<R>(c, st_at(ck, 0), st_at(ck, 0), &n0c));
+    CHECK(inner_impl<R>(c, (const cx<R>*)tgt, (const cx<R>*)tgt, &ntc));
+    const double denom = std::sqrt(n0c.real() * ntc.real());
+    const std::complex<double> cc = ov / denom;
+    if (loss_out) *loss_out = 1.0 - std::norm(cc);
+    // lam_T = dL/dpsi(T)* = -c * target * w / denom
+    const std::complex<double> coef = -cc * (c->weight / denom);
+    launch_cscale<R>((cx<R>*)lam, (const cx<R>*)tgt, P, coef.real(), coef.imag(), c->stream);
+    CU(cudaMemsetAsync(dV, 0, (size_t)P * sizeof(double), c->stream));
+    const double h = 0.5 * prm->ddt;
+    const double adj_bytes = (double)P * (4.0 * sizeof(R) + sizeof(R) + 16.0);
+    auto adj_nl = [&](const cx<R>* xm, int first, int second, int conj_in, int conj_out) {
+      Launch L(c, PC_ADJ_NL, adj_bytes);
+      launch_adj_nl<R>((cx<R>*)lam, xm, (const R*)f.V, dV, P, c->prm.g, h, first, second, conj_in, conj_out,
+                       c->stream);
+    };
+    // adjoint of the last step's closing half: its output is x_M (slot nck)
+    adj_nl(st_at(ck, nck), 0, 1, 0, 1);
+    for (int s = nck - 1; s >= 0; --s) {
+      const int m0 = s * K, m1 = std::min(M, m0 + K);
+      // step-start states x_m0 .. x_{m1-1}; x_m1 is checkpoint s+1
+      CU(cudaMemcpyAsync(x, st_at(ck, s), S, cudaMemcpyDeviceToDevice, c->stream));
+      for (int m = m0 + 1; m < m1; ++m) {
+        CHECK(strang_step<R>(c, f, (cx<R>*)x, prm->ddt));
+        Launch L(c, PC_COPY, 2.0 * S);
+        CU(cudaMemcpyAsync(st_at(seg, m - m0), x, S, cudaMemcpyDeviceToDevice, c->stream));
+      }
+      for (int m = m1 - 1; m >= m0; --m) {
+        CHECK(kinetic_on<R>(c, f, lam, prm->ddt));  // conj(K^H lam), lam held conjugated
+        const cx<R>* xm = m == m0 ? st_at(ck, s) : st_at(seg, m - m0);
+        // opening half of step m and, for m > 0, closing half of step m-1:
+        // both are phases of |x_m|^2, applied in one pass
+        adj_nl(xm, 1, m > 0, 1, m > 0);
+        CU(cudaGetLastError());
+      }
+    }
+    CU(cudaMemcpyAsync(dLdV_out, dV, (size_t)P * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return GPE_OK;
+  };
+  st = run();
+  cudaStreamSynchronize(c->stream);
+  cleanup();
+  return st;
+}
+
 // ---- batched solve_split -------------------------------------------------------
 // Many independent contexts (grids of any sizes) advance together: one block
 // of n_rec steps of every context is captured once into a CUDA graph whose
@@ -1400,6 +1569,29 @@ gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
   c->err.clear();
   if (c->prec == GPE_FP32) return split_impl<float>(c, prm);
   return split_impl<double>(c, prm);
+}
+
+gpe_status gpe_adjoint_grad(gpe_ctx* c, const gpe_adjoint_params* prm, const double* psi_target, double* dLdV,
+                            double* loss) {
+  CHECK(check_ctx(c));
+  CHECK(need_state(c));
+  CHECK(need_V(c));
+  if (!prm || !psi_target || !dLdV) return fail(c, GPE_ERR_INVALID, "adjoint: null argument");
+  if (!(prm->ddt > 0) || prm->nsteps < 1) return fail(c, GPE_ERR_INVALID, "adjoint: ddt > 0 and nsteps >= 1 needed");
+  if (c->prm.gamma != 0.0 || c->prm.decay_rate > 0)
+    return fail(c, GPE_ERR_UNSUPPORTED,
+                "adjoint: only gamma = 0 and decay_rate = 0 (conservative dynamics) are differentiated");
+  const int prec = prm->precision ? prm->precision : c->prec;
+  if (prec != GPE_FP32 && prec != GPE_FP64) return fail(c, GPE_ERR_INVALID, "adjoint: precision must be 0, GPE_FP32 or GPE_FP64");
+  if (prec == GPE_FP32 && c->prec == GPE_FP64)
+    return fail(c, GPE_ERR_UNSUPPORTED, "adjoint: an FP64 context has no FP32 tables; use precision 0");
+  c->err.clear();
+  if (prec == GPE_FP32) return adjoint_impl<float>(c, c->main, prm, psi_target, dLdV, loss);
+  if (c->prec == GPE_FP32) {
+    CHECK(ensure_polish(c));
+    return adjoint_impl<double>(c, c->polish, prm, psi_target, dLdV, loss);
+  }
+  return adjoint_impl<double>(c, c->main, prm, psi_target, dLdV, loss);
 }
 
 gpe_status gpe_solve_split_batch(gpe_ctx** ctxs, int count, const gpe_split_params* prm) {

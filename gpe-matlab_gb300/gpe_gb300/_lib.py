@@ -52,6 +52,11 @@ class gpe_split_params(C.Structure):
                 ("vtd_user", C.c_void_p), ("on_step", STEP_FN), ("step_user", C.c_void_p)]
 
 
+class gpe_adjoint_params(C.Structure):
+    _fields_ = [("ddt", C.c_double), ("nsteps", C.c_int), ("checkpoint_every", C.c_int),
+                ("mem_budget", C.c_double), ("precision", C.c_int)]
+
+
 class gpe_current(C.Structure):
     _fields_ = [("current_iter", C.c_int), ("current_time", C.c_double), ("current_mu", C.c_double),
                 ("current_n", C.c_double)]
@@ -97,6 +102,7 @@ PROTOTYPES = {
                                       C.POINTER(gpe_itp_result)]),
     "gpe_solve_split": (C.c_int, [_P, C.POINTER(gpe_split_params)]),
     "gpe_solve_split_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(gpe_split_params)]),
+    "gpe_adjoint_grad": (C.c_int, [_P, C.POINTER(gpe_adjoint_params), _D, _D, _D]),
     "gpe_observables": (C.c_int, [_P, C.POINTER(gpe_obs)]),
     "gpe_synchronize": (C.c_int, [_P]),
     "gpe_timer_start": (C.c_int, [_P]),

@@ -331,6 +331,41 @@ class GPEtask:
         """real(inner(phi, applyham(phi))) (GPEtask.m:73-78 with grid.inner)."""
         return self.observables(phi if phi is not None else self.current_state)["mu_integral"]
 
+    # ---- gradient ------------------------------------------------------------
+    def adjoint_grad(self, psi_target, ddt, nsteps, phi0=None, V=None, checkpoint_every=0, mem_budget=0.0,
+                     precision=None):
+        """dloss/dV through `nsteps` gamma = 0 split steps of ddt from phi0
+        (default init_state) in the static potential V (default Vtrap), with
+        loss = 1 - |<target|psi(T)>|^2 / (<target|target> <phi0|phi0>).
+
+        Returns (loss, dLdV): dLdV[i] is the derivative with respect to the
+        potential's value at grid point i (same shape as the grid).  The
+        derivative with respect to a parameter a of V(x; a) is
+        sum(dLdV * dV/da), see ``project_gradient``.  precision "double" on a
+        single-precision grid runs the sweep in FP64 from the FP32 state."""
+        self._push_params()
+        V = self.Vtrap if V is None else V
+        self._upload_V(np.ascontiguousarray(np.broadcast_to(np.asarray(V, dtype=np.float64), self.grid.shape)))
+        self._upload_state(self.init_state if phi0 is None else phi0)
+        self._state_on_device = None
+        tgt = np.ascontiguousarray(np.broadcast_to(psi_target, self.grid.shape), dtype=np.complex128)
+        prm = L.gpe_adjoint_params()
+        prm.ddt = float(ddt)
+        prm.nsteps = int(nsteps)
+        prm.checkpoint_every = int(checkpoint_every)
+        prm.mem_budget = float(mem_budget)
+        prm.precision = {None: 0, "single": L.GPE_FP32, "double": L.GPE_FP64}[precision]
+        dLdV = np.zeros(self.grid.shape)
+        loss = C.c_double()
+        L.check(self._ctx, L.lib.gpe_adjoint_grad(self._ctx, C.byref(prm), L.dptr(tgt.view(np.float64)),
+                                                  L.dptr(dLdV), C.byref(loss)))
+        return loss.value, dLdV
+
+    @staticmethod
+    def project_gradient(dLdV, basis):
+        """dloss/da_j = sum_i dLdV[i] * basis[j][i] for V = V_0 + sum_j a_j basis[j]."""
+        return np.array([float(np.sum(dLdV * b)) for b in basis])
+
     # ---- profiling -----------------------------------------------------------
     def profile(self, on: bool = True):
         L.check(self._ctx, L.lib.gpe_profile_enable(self._ctx, int(on)))

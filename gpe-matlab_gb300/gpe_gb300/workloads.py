@@ -172,3 +172,55 @@ class BatchWorkload:
 
 
 BATCH2D = BatchWorkload()
+
+
+@dataclass
+class AdjointWorkload:
+    """Gradient of an overlap loss through gamma = 0 split steps.
+
+    256^2, V = 0.5 r^2 + sum_{j=1..16} a_j exp(-|r - c_j|^2 / 2) with
+    a_j ~ N(0, 0.1) and c_j uniform in the Thomas-Fermi disc (seed 4), 2000
+    steps of 0.002 with checkpoints every 50; loss 1 - |<target|psi(T)>|^2 with
+    the target a vortex imprinted at x0 = 3.  Assumed: box +-17, g = 0.06,
+    Ntotal = 1e5 (the 2D vortex example's values); psi0 and the target's base
+    are the ground state of 0.5 r^2 alone (ITP dt 0.02, eps 1e-6), so the 16
+    bumps drive the dynamics whose dloss/da_j is measured.
+    """
+
+    name: str = "adjoint2d_256"
+    n: int = 256
+    box: float = 17.0
+    g: float = 0.06
+    Ntotal: float = 1e5
+    nbumps: int = 16
+    a_sigma: float = 0.1
+    dt: float = 0.002
+    steps: int = 2000
+    checkpoint_every: int = 50
+    vortex_x0: float = 3.0
+    itp_dt: float = 0.02
+    itp_eps: float = 1e-6
+    seed: int = 4
+
+    def make_grid(self, precision: str = "single", n=None):
+        n = n or self.n
+        return grid2d(self.box, n, self.box, n, precision=precision)
+
+    def bumps(self, grid, mu_tf=None):
+        """(a, basis): a_j and the 16 Gaussians exp(-|r - c_j|^2 / 2) on grid."""
+        rng = np.random.default_rng(self.seed)
+        a = rng.normal(0.0, self.a_sigma, self.nbumps)
+        mu = mu_tf if mu_tf is not None else np.sqrt(self.g * self.Ntotal / np.pi)  # 2D TF, V = r^2/2
+        R = np.sqrt(2.0 * mu)
+        rad = R * np.sqrt(rng.random(self.nbumps))
+        th = 2.0 * np.pi * rng.random(self.nbumps)
+        X, Y = grid.mesh["x"], grid.mesh["y"]
+        basis = [np.exp(-((X - r * np.cos(t)) ** 2 + (Y - r * np.sin(t)) ** 2) / 2.0) for r, t in zip(rad, th)]
+        return a, basis
+
+    def trap(self, grid):
+        X, Y = grid.mesh["x"], grid.mesh["y"]
+        return 0.5 * (X ** 2 + Y ** 2)
+
+
+ADJOINT2D = AdjointWorkload()

@@ -122,6 +122,17 @@ typedef struct {
     void *step_user;
 } gpe_split_params;
 
+/* Gradient of an overlap loss through the split step (no counterpart in the
+ * reference; differentiates the gamma = 0 step of solve_split.m:55-64). */
+typedef struct {
+    double ddt;             /* real time step                                    */
+    int nsteps;             /* steps of the forward window                       */
+    int checkpoint_every;   /* states kept every K steps; <= 0: K ~ sqrt(nsteps) */
+    double mem_budget;      /* device bytes for stored states; <= 0: 60e9        */
+    int precision;          /* 0: the context's; GPE_FP64 on an FP32 context runs
+                             * the sweep in FP64 from the FP32 state             */
+} gpe_adjoint_params;
+
 /* Dynamics bookkeeping properties, GPEtask.m:18-24. */
 typedef struct {
     int current_iter;
@@ -207,6 +218,19 @@ GPE_API gpe_status gpe_solve_split(gpe_ctx *ctx, const gpe_split_params *prm);
  * on_step callbacks (must be NULL) and decay_rate > 0.  Errors are reported
  * on ctxs[0]. */
 GPE_API gpe_status gpe_solve_split_batch(gpe_ctx **ctxs, int count, const gpe_split_params *prm);
+/* Discrete adjoint of `nsteps` split steps (the gamma = 0 operator sequence
+ * of solve_split.m:55-64: per step exp(-i(V+g|psi|^2)ddt/2), kinetic
+ * exp(-i k^2 ddt/2), the nonlinear half again; mu is a global phase and is
+ * left out) from the current state psi0 at the current V:
+ *   loss = 1 - |<target|psi(T)>|^2 / (<target|target> <psi0|psi0>)
+ * with <a|b> = integrate(conj(a) b).  psi_target: nx*ny*nz interleaved
+ * complex doubles; dLdV: nx*ny*nz doubles, dloss/dV at each grid point;
+ * loss may be NULL.  Forward states are kept every checkpoint_every steps
+ * and each segment is recomputed once in the backward sweep; the stored
+ * states must fit mem_budget (else GPE_ERR_ALLOC).  The context state,
+ * current_* and history are left unchanged.  gamma must be 0. */
+GPE_API gpe_status gpe_adjoint_grad(gpe_ctx *ctx, const gpe_adjoint_params *prm, const double *psi_target,
+                                    double *dLdV, double *loss);
 /* applyham / get_energy pieces for the current state at the current V. */
 GPE_API gpe_status gpe_observables(gpe_ctx *ctx, gpe_obs *obs);
 

@@ -381,6 +381,72 @@ class GPEtask:
         return phi
 
 
+# ---------------------------------------------------------------------------
+# Discrete adjoint of the gamma = 0 split step.  Not in the reference: the
+# forward operator is solve_split.m:55-64 at gamma = 0, where every nonlinear
+# factor is a pure phase, so a block of n_recalc steps equals
+# (N_h K N_h)^n_recalc with N_h(phi) = exp(-i (V - mu + g|phi|^2) ddt/2) phi and
+# K = ifft(exp(-i kk ddt) fft(.)) (set_kinop.m:9 with dt = i ddt).  mu is a
+# global phase that the overlap loss does not see and is left out.
+# ---------------------------------------------------------------------------
+def _nl_half(V, g, h, phi):
+    return np.exp(-1j * (V + g * np.real(phi * np.conj(phi))) * h) * phi
+
+
+def split_forward(grid: Grid, V, g, psi0, ddt, nsteps, keep_states=False):
+    """psi(T) after nsteps steps N_h K N_h; with keep_states also every
+    step-start state."""
+    kin = np.exp(-1j * grid.kk * ddt)
+    h = 0.5 * ddt
+    phi = np.asarray(psi0, dtype=np.complex128)
+    states = []
+    for _ in range(nsteps):
+        if keep_states:
+            states.append(phi)
+        phi = _nl_half(V, g, h, phi)
+        phi = grid.ifft(kin * grid.fft(phi))
+        phi = _nl_half(V, g, h, phi)
+    return phi, states
+
+
+def overlap_loss(grid: Grid, target, psiT, psi0):
+    """1 - |<target|psi(T)>|^2 / (<target|target> <psi0|psi0>), and the
+    normalised overlap c."""
+    denom = math.sqrt(grid.integrate(np.abs(target) ** 2) * grid.integrate(np.abs(psi0) ** 2))
+    c = grid.inner(target, psiT) / denom
+    return 1.0 - abs(c) ** 2, c
+
+
+def _adj_nl(V, g, h, lam, x):
+    """Adjoint of y = exp(-i th) x, th = (V + g|x|^2) h, for lam = dL/dy*
+    (Wirtinger): returns dL/dx* and the contribution to dL/dV."""
+    u = np.exp(1j * (V + g * np.real(x * np.conj(x))) * h) * lam
+    s = 2.0 * np.imag(np.conj(u) * x)
+    return u + g * h * s * x, s * h
+
+
+def adjoint_grad(grid: Grid, V, g, psi0, target, ddt, nsteps):
+    """(loss, dL/dV) of overlap_loss after split_forward, by the reverse sweep
+    of the same operator sequence; dL/dV[i] is the derivative with respect to
+    the potential's value at grid point i."""
+    V = np.asarray(V, dtype=np.float64)
+    psiT, states = split_forward(grid, V, g, psi0, ddt, nsteps, keep_states=True)
+    loss, c = overlap_loss(grid, target, psiT, psi0)
+    denom = math.sqrt(grid.integrate(np.abs(target) ** 2) * grid.integrate(np.abs(psi0) ** 2))
+    lam = -c * grid.weight / denom * np.asarray(target, dtype=np.complex128)
+    kin = np.exp(-1j * grid.kk * ddt)
+    h = 0.5 * ddt
+    dLdV = np.zeros(grid.shape)
+    for x0 in reversed(states):
+        phi2 = grid.ifft(kin * grid.fft(_nl_half(V, g, h, x0)))
+        lam, d = _adj_nl(V, g, h, lam, phi2)
+        dLdV += d
+        lam = grid.ifft(np.conj(kin) * grid.fft(lam))
+        lam, d = _adj_nl(V, g, h, lam, x0)
+        dLdV += d
+    return loss, dLdV
+
+
 def _set_hist(lst, step, val):
     """MATLAB ``history.mu(step) = mu`` grows the row vector with zeros."""
     while len(lst) < step:

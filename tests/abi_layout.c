@@ -17,6 +17,8 @@ int main(void) {
     S(gpe_itp_params); F(gpe_itp_params, fp64_polish); F(gpe_itp_params, switch_delta);
     S(gpe_itp_result); F(gpe_itp_result, final_dt); F(gpe_itp_result, last_delta);
     S(gpe_split_params); F(gpe_split_params, vtd); F(gpe_split_params, on_step); F(gpe_split_params, step_user);
+    S(gpe_adjoint_params); F(gpe_adjoint_params, checkpoint_every); F(gpe_adjoint_params, mem_budget);
+    F(gpe_adjoint_params, precision);
     S(gpe_current); F(gpe_current, current_time);
     S(gpe_obs); F(gpe_obs, energy);
     S(gpe_kernel_stat); F(gpe_kernel_stat, launches); F(gpe_kernel_stat, bytes_per_launch);

@@ -141,6 +141,28 @@ def test_vortex_imprint_matches_example():
     np.testing.assert_allclose(np.angle(out[5, 20]), np.arctan2(X[5, 20] - 1, Y[5, 20]))
 
 
+@pytest.mark.parametrize("axes", [(8, 32, 8, 32), (6, 16, 6, 12, 4, 8)], ids=["2d", "3d"])
+def test_oracle_adjoint_matches_central_differences(axes):
+    """The oracle's reverse sweep against central differences of its own
+    forward (step 1e-5): directional derivatives within 1e-7 relative."""
+    g = O.Grid(*axes)
+    X, Y, Z = g.mesh["x"], g.mesh["y"], g.mesh["z"]
+    V = 0.5 * (X ** 2 + Y ** 2 + (Z ** 2 if len(axes) == 6 else 0.0))
+    psi0 = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 4).astype(complex) * (1 + 0.1j * X)
+    tgt = np.exp(-((X - 1) ** 2 + Y ** 2) / 4).astype(complex) * np.exp(1j * np.arctan2(X - 1, Y))
+    coupling, ddt, M = 0.5, 0.01, 20
+    loss, dV = O.adjoint_grad(g, V, coupling, psi0, tgt, ddt, M)
+    assert 0 < loss < 1
+    rng = np.random.default_rng(7)
+    eps = 1e-5
+    for _ in range(3):
+        d = rng.standard_normal(g.shape)
+        lp = O.overlap_loss(g, tgt, O.split_forward(g, V + eps * d, coupling, psi0, ddt, M)[0], psi0)[0]
+        lm = O.overlap_loss(g, tgt, O.split_forward(g, V - eps * d, coupling, psi0, ddt, M)[0], psi0)[0]
+        ad = float(np.sum(dV * d))
+        assert abs((lp - lm) / (2 * eps) - ad) < 1e-7 * abs(ad)
+
+
 def test_golden_fixtures_reproduce():
     from tests.golden import make_golden as MG
 
