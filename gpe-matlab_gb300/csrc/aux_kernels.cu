@@ -12,13 +12,18 @@ namespace gpe {
 
 static int g_sm_count = 0;
 
-int elem_grid(long long n, int threads) {
+int device_sm_count() {
   if (g_sm_count == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
     if (g_sm_count <= 0) g_sm_count = 152;
   }
+  return g_sm_count;
+}
+
+int elem_grid(long long n, int threads) {
+  device_sm_count();
   long long want = (n + threads - 1) / threads;
   long long cap = (long long)g_sm_count * 8;
   if (want > cap) want = cap;
@@ -28,24 +33,52 @@ int elem_grid(long long n, int threads) {
 
 constexpr int FIN_THREADS = 256;
 
-// Deterministic block-wide Kahan sum of p[0..n) by FIN_THREADS threads.
+// Deterministic block-wide Kahan sums of K arrays p[k][0..n[k]) by
+// FIN_THREADS threads in one sweep (the K chains interleave, so the loads of
+// all arrays are in flight together); fixed-order warp and CTA combination.
+// Every thread returns the K sums.
+template <int K>
+__device__ void block_sums(const double* const* p, const int* n, double* out) {
+  __shared__ double sh[K][FIN_THREADS / 32];
+  double s[K], c[K];
+  int nmax = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    s[k] = c[k] = 0.0;
+    nmax = n[k] > nmax ? n[k] : nmax;
+  }
+  for (int i = threadIdx.x; i < nmax; i += FIN_THREADS) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (i < n[k]) {
+        const double y = __ldcg(p[k] + i) - c[k];  // written by other CTAs: read from L2
+        const double t = s[k] + y;
+        c[k] = (t - s[k]) - y;
+        s[k] = t;
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double x = s[k] - c[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[k][warp] = x;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double r = 0.0;
+    for (int w = 0; w < FIN_THREADS / 32; ++w) r += sh[k][w];
+    out[k] = r;
+  }
+  __syncthreads();
+}
+
 __device__ double block_sum(const double* p, int n) {
-  __shared__ double sh[FIN_THREADS];
-  double s = 0.0, c = 0.0;
-  for (int i = threadIdx.x; i < n; i += FIN_THREADS) {
-    double y = p[i] - c;
-    double t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-  sh[threadIdx.x] = s - c;
-  __syncthreads();
-  for (int o = FIN_THREADS / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
-  }
-  double r = sh[0];
-  __syncthreads();
+  double r;
+  block_sums<1>(&p, &n, &r);
   return r;
 }
 
@@ -71,15 +104,55 @@ __device__ __forceinline__ void flag_nonfinite(DevScalars* sc) {
 }
 
 // solve_split.m:65-78 for one block.
+// Up to FIN_GRID CTAs (one per FIN_CHUNK partials of the longest slot): CTA b
+// sums chunk b of every slot's partials; the last CTA to finish sums the
+// chunk results (fixed chunking and order: deterministic) and runs the
+// scalar logic.  Spreading the FP64 Kahan sums over SMs keeps the finalizer
+// short on a GPU whose FP64 rate per SM is low; small grids use one CTA.
+constexpr int FIN_GRID = 32;
+constexpr int FIN_CHUNK = 256;
+
 __global__ void k_finalize_block(const BlockFinalArgs a, DevScalars* sc) {
-  if (sc->stop) return;
+  if (sc->stop) return;  // set only by earlier kernels: the same for every CTA
   const int cap = a.cap;
-  const double n = block_sum(a.partials + S_N * cap, a.nblk_epi);
-  const double vn = block_sum(a.partials + S_VN * cap, a.nblk_epi);
-  const double n2 = block_sum(a.partials + S_N2 * cap, a.nblk_epi);
-  double kin = 0.0;
-  for (int ax = 0; ax < 3; ++ax)
-    if (a.nblk_kin[ax] > 0) kin += block_sum(a.partials + (S_KX + ax) * cap, a.nblk_kin[ax]);
+  const double* p[6] = {a.partials + S_N * cap,        a.partials + S_VN * cap,       a.partials + S_N2 * cap,
+                        a.partials + (S_KX + 0) * cap, a.partials + (S_KX + 1) * cap, a.partials + (S_KX + 2) * cap};
+  const int cnt[6] = {a.nblk_epi, a.nblk_epi, a.nblk_epi, a.nblk_kin[0], a.nblk_kin[1], a.nblk_kin[2]};
+  const double* pc[6];
+  int nc[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const int chunk = (cnt[k] + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int lo = min(cnt[k], (int)blockIdx.x * chunk), hi = min(cnt[k], lo + chunk);
+    pc[k] = p[k] + lo;
+    nc[k] = hi - lo;
+  }
+  double sums[6];
+  block_sums<6>(pc, nc, sums);
+  // [6][FIN_GRID] chunk sums, in the buffer's scratch slot (the slots read
+  // above stay read-only)
+  double* scratch = const_cast<double*>(a.partials) + (size_t)S_FIN * cap;
+  __shared__ int last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) scratch[k * FIN_GRID + blockIdx.x] = sums[k];
+    __threadfence();
+    last = atomicAdd(&sc->fin_count, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const double* q[6];
+  int nq[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    q[k] = scratch + k * FIN_GRID;
+    nq[k] = (int)gridDim.x;
+  }
+  block_sums<6>(q, nq, sums);
+  if (threadIdx.x == 0) sc->fin_count = 0;
+  const double n = sums[0], vn = sums[1], n2 = sums[2];
+  const double kin = sums[3] + sums[4] + sums[5];  // axes without a pass contribute 0
   if (threadIdx.x != 0) return;
   const double w = a.weight;
   const double ncur = n * w;  // solve_split.m:67
@@ -235,7 +308,11 @@ __global__ void k_reset_scalars(DevScalars* sc) {
 __global__ void k_set_scale_one(DevScalars* sc) { sc->scale = 1.0; }
 
 void launch_finalize_block(const BlockFinalArgs& a, DevScalars* sc, cudaStream_t s) {
-  k_finalize_block<<<1, FIN_THREADS, 0, s>>>(a, sc);
+  int longest = a.nblk_epi;
+  for (int ax = 0; ax < 3; ++ax) longest = a.nblk_kin[ax] > longest ? a.nblk_kin[ax] : longest;
+  int grid = (longest + FIN_CHUNK - 1) / FIN_CHUNK;
+  grid = grid < 1 ? 1 : grid > FIN_GRID ? FIN_GRID : grid;
+  k_finalize_block<<<grid, FIN_THREADS, 0, s>>>(a, sc);
 }
 void launch_finalize_itp(const ItpFinalArgs& a, DevScalars* sc, cudaStream_t s) {
   k_finalize_itp<<<1, FIN_THREADS, 0, s>>>(a, sc);

@@ -50,6 +50,36 @@ __device__ __forceinline__ cx<double> ldg(const cx<double>* p) {
   return mk<double>(v.x, v.y);
 }
 
+// Loads of streamed data (state, potential) that a pass reads once: marked
+// evict-first so they do not push the FFT tables out of L1.
+#ifndef GPE_STREAM_LOADS
+#define GPE_STREAM_LOADS 1
+#endif
+__device__ __forceinline__ cx<float> ld_stream(const cx<float>* p) {
+#if GPE_STREAM_LOADS
+  float2 v = __ldcs(reinterpret_cast<const float2*>(p));
+  return mk<float>(v.x, v.y);
+#else
+  return *p;
+#endif
+}
+__device__ __forceinline__ cx<double> ld_stream(const cx<double>* p) {
+#if GPE_STREAM_LOADS
+  double2 v = __ldcs(reinterpret_cast<const double2*>(p));
+  return mk<double>(v.x, v.y);
+#else
+  return *p;
+#endif
+}
+template <typename R>
+__device__ __forceinline__ R ld_stream(const R* p) {
+#if GPE_STREAM_LOADS
+  return __ldcs(p);
+#else
+  return *p;
+#endif
+}
+
 // sin and cos of x in FP32.  For |x| <= 65536 (any physically meaningful
 // phase per step): Cody-Waite reduction x = q*pi/2 + r with pi/2 split into
 // two floats (q*hi is exact inside the FMA), then the Taylor series of sin
@@ -123,7 +153,8 @@ struct DevScalars {
   int status;         // StopReason
   int nonfinite;      // a reduction produced NaN/Inf
   int timeout;        // a bounded device-side wait gave up
-  int pad_[2];
+  int fin_count;      // CTAs of a multi-CTA finalizer that are done (0 between launches)
+  int pad_;
 };
 
 enum StopReason { RUNNING = 0, CONVERGED = 1, SWITCH_FP64 = 2, HALVE_DT = 3, NONFINITE = 4 };
@@ -138,7 +169,8 @@ enum Slot {
   S_KZ = 5,
   S_MAXD = 6,  // max | |psi| - |psi_prev| |
   S_MAXA = 7,  // max |psi|
-  NSLOTS = 8
+  NSLOTS = 8,
+  S_FIN = 8,   // scratch of the multi-CTA finalizer (chunk sums); buffer has NSLOTS + 1 slots
 };
 
 // Prologue applied right after a pencil is loaded (first axis pass).
@@ -181,6 +213,8 @@ struct PassArgs {
   int energy_pot;          // energy pass: also accumulate n, Vn, n^2
   double g;                // coupling
   double dre, dim;         // time step (real, imag) of the phase factors
+  int prefetch = 0;        // direct pass: 1 = prefetch the tile one wave ahead into L2
+  int pf_ahead = 0;        // set by the launcher: resident CTAs of the launch (one wave)
 };
 
 }  // namespace gpe

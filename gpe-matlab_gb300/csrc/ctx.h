@@ -25,6 +25,7 @@ struct Field {
   double phase_dt[2] = {0.0, 0.0};               // dt the phase tables hold
   bool phase_valid = false;
   bool V_valid = false;
+  int plan_var[3] = {0, 0, 0};                   // per axis: FFT plan variant (plans.cuh PlanSel)
 };
 
 struct ProfRec {
@@ -70,7 +71,9 @@ struct gpe_ctx {
   std::string err;
 
   int sms = 152;          // SM count of the device
-  int pass_variant = 0;   // 0: direct passes, 1: TMA-staged passes where they apply
+  int pass_variant = 0;   // 0: direct passes + L2 prefetch, 1: TMA-staged where they apply, 2: direct
+  int tune_mode = 2;      // FFT plan autotuner: 0 off, 1 explicit only, 2 on the first hot-path call
+  bool tuned = false;     // the autotuner has set main.plan_var
   bool prof = false;
   std::vector<gpe::ProfRec> prof_pending;
   std::vector<cudaEvent_t> ev_pool;

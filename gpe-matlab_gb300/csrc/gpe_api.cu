@@ -10,11 +10,13 @@
 // time-dependent potential is evaluated on the host.
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -56,8 +58,33 @@ bool supported_n(int n) {
   }
 }
 
+// Axis lengths with an alternative plan (FP32 direct passes).
+bool has_alt_plan(int n) {
+  switch (n) {
+#define X(v) case v:
+    GPE_FOR_EACH_ALT(X)
+#undef X
+    return true;
+    default:
+      return false;
+  }
+}
+
+// var: plan variant (0 = Plan<N>; 1 = PlanAlt<N>, FP32 and has_alt_plan(N) only).
 template <typename R>
-cudaError_t dispatch_pass(int N, const PassArgs<R>& a, bool strided, cudaStream_t s) {
+cudaError_t dispatch_pass(int N, int var, const PassArgs<R>& a, bool strided, cudaStream_t s) {
+  if constexpr (sizeof(R) == 4) {
+    if (var == 1) {
+      switch (N) {
+#define X(v) \
+  case v:    \
+    return launch_pass<float, v, 1>(a, strided, s);
+        GPE_FOR_EACH_ALT(X)
+#undef X
+      }
+      return cudaErrorInvalidValue;
+    }
+  }
   switch (N) {
 #define X(v) \
   case v:    \
@@ -69,7 +96,19 @@ cudaError_t dispatch_pass(int N, const PassArgs<R>& a, bool strided, cudaStream_
 }
 
 template <typename R>
-PassGeom dispatch_geom(int N, bool strided) {
+PassGeom dispatch_geom(int N, int var, bool strided) {
+  if constexpr (sizeof(R) == 4) {
+    if (var == 1) {
+      switch (N) {
+#define X(v) \
+  case v:    \
+    return pass_geom<float, v, 1>(strided);
+        GPE_FOR_EACH_ALT(X)
+#undef X
+      }
+      return PassGeom{0, 1, 0};
+    }
+  }
   switch (N) {
 #define X(v) \
   case v:    \
@@ -139,8 +178,9 @@ PlanInfo dispatch_plan(int N);
 // The TMA pass applies when every tile is one contiguous range (contiguous
 // axis) or N rows of FFTS contiguous, 16-byte aligned elements (strided
 // axes), and a CTA is at least two warps.  pass_variant: 0 = the direct
-// pass everywhere (measured faster on GB300 for the 256^3 bench workload),
-// 1 = the TMA pass where it applies.
+// pass everywhere, with L2 prefetch of the next wave's tiles (measured
+// fastest on GB300 for the 256^3 and 512^3 workloads), 1 = the TMA pass
+// where it applies, 2 = the direct pass without prefetch.
 template <typename R>
 size_t dispatch_tma_smem(int N, bool strided) {
   switch (N) {
@@ -154,8 +194,9 @@ size_t dispatch_tma_smem(int N, bool strided) {
 }
 
 template <typename R>
-bool use_tma(const gpe_ctx* c, const AxisPass& ap) {
+bool use_tma(const gpe_ctx* c, const Field& f, const AxisPass& ap) {
   if (c->pass_variant != 1) return false;
+  if (f.plan_var[ap.axis] != 0) return false;  // TMA passes are built on Plan<N> only
   if (dispatch_tma_smem<R>(ap.N, ap.strided) > 200 * 1024) return false;
   const int ffts = dispatch_tma_ffts<R>(ap.N, ap.strided);
   if (!ap.strided) return true;
@@ -163,7 +204,17 @@ bool use_tma(const gpe_ctx* c, const AxisPass& ap) {
   return ap.inner % ffts == 0 && ap.stride % ffts == 0 && ffts * pi.T >= 64 && (ffts * pi.T) % 32 == 0;
 }
 
-PlanInfo dispatch_plan(int N) {
+PlanInfo dispatch_plan(int N, int var) {
+  if (var == 1) {
+    switch (N) {
+#define X(v) \
+  case v:    \
+    return plan_info<v, 1>();
+      GPE_FOR_EACH_ALT(X)
+#undef X
+    }
+    return PlanInfo{};
+  }
   switch (N) {
 #define X(v) \
   case v:    \
@@ -173,10 +224,11 @@ PlanInfo dispatch_plan(int N) {
   }
   return PlanInfo{};
 }
+PlanInfo dispatch_plan(int N) { return dispatch_plan(N, 0); }
 
 template <typename R>
-long long pass_blocks(const AxisPass& p) {
-  PassGeom g = dispatch_geom<R>(p.N, p.strided);
+long long pass_blocks(const AxisPass& p, int var) {
+  PassGeom g = dispatch_geom<R>(p.N, var, p.strided);
   return (p.n_batch + g.ffts - 1) / g.ffts;
 }
 
@@ -297,11 +349,17 @@ int slot_index(int T, int t, int m) {
 }
 
 // Tables of one axis: stage twiddle rows and k^2/2/N in spectrum-slot order.
+// Tables of axis ax for the plan variant f.plan_var[ax] (rebuilt when the
+// autotuner changes the variant; the kinetic factors follow in set_kinop).
 template <typename R>
-gpe_status build_static_tables(gpe_ctx* c, Field& f) {
-  for (int ax = 0; ax < c->ndims; ++ax) {
+gpe_status build_axis_tables(gpe_ctx* c, Field& f, int ax) {
+  {
     const int N = c->n[ax];
-    const PlanInfo pi = dispatch_plan(N);
+    const PlanInfo pi = dispatch_plan(N, f.plan_var[ax]);
+    if (f.tws[ax]) {
+      cudaFree(f.tws[ax]);
+      f.tws[ax] = nullptr;
+    }
     int total = 0, Ns = pi.radix[0];
     for (int s = 1; s < pi.nstages; ++s) {
       total += (Ns * pi.radix[s] + 1) & ~1;
@@ -321,8 +379,8 @@ gpe_status build_static_tables(gpe_ctx* c, Field& f) {
     }
     CU(cudaMalloc(&f.tws[ax], rows.size() * 2 * sizeof(R)));
     CHECK(upload_cx<R>(c, f.tws[ax], rows));
-    CU(cudaMalloc(&f.php[ax], N * 2 * sizeof(R)));
-    CU(cudaMalloc(&f.k2p[ax], N * sizeof(R)));
+    if (!f.php[ax]) CU(cudaMalloc(&f.php[ax], N * 2 * sizeof(R)));
+    if (!f.k2p[ax]) CU(cudaMalloc(&f.k2p[ax], N * sizeof(R)));
     std::vector<R> k2(N);
     for (int t = 0; t < pi.T; ++t)
       for (int m = 0; m < pi.E; ++m) {
@@ -335,6 +393,12 @@ gpe_status build_static_tables(gpe_ctx* c, Field& f) {
   return GPE_OK;
 }
 
+template <typename R>
+gpe_status build_static_tables(gpe_ctx* c, Field& f) {
+  for (int ax = 0; ax < c->ndims; ++ax) CHECK(build_axis_tables<R>(c, f, ax));
+  return GPE_OK;
+}
+
 // kinop = exp(-kk*dt) (set_kinop.m:9), as one factor per axis with the 1/N of
 // ifft folded in: exp(-k^2/2*dt)/N, dt = dre + i*dim, evaluated in FP64 and
 // stored in the threads' spectrum-slot order.
@@ -343,7 +407,7 @@ gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
   if (f.phase_valid && f.phase_dt[0] == dre && f.phase_dt[1] == dim) return GPE_OK;
   for (int ax = 0; ax < c->ndims; ++ax) {
     const int N = c->n[ax];
-    const PlanInfo pi = dispatch_plan(N);
+    const PlanInfo pi = dispatch_plan(N, f.plan_var[ax]);
     std::vector<std::complex<double>> ph(N);
     for (int t = 0; t < pi.T; ++t)
       for (int m = 0; m < pi.E; ++m) {
@@ -442,6 +506,7 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.g = c->prm.g;
   a.dre = dre;
   a.dim = dim;
+  a.prefetch = c->pass_variant == 0;
   const double P = (double)c->P;
   double bytes = (kind == KIND_ENERGY ? 1.0 : 2.0) * P * 2 * sizeof(R);
   const bool useV = pro == PRO_RT_HALF || pro == PRO_RT_FULL || pro == PRO_ITP || epi == EPI_RT_END ||
@@ -455,15 +520,16 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
             (kind == KIND_ENERGY && energy_pot))
                ? 1
                : (epi == EPI_ITP ? 2 : 0);
-  if (use_tma<R>(c, ap)) {
+  if (use_tma<R>(c, f, ap)) {
     const int grid = dispatch_tma_grid<R>(ap.N, a, ap.strided, c->sms);
     if (nblk) *nblk = grid;
     Launch L(c, cls, bytes);
     CU(dispatch_tma<R>(ap.N, a, ap.strided, c->stream, c->sms));
   } else {
-    if (nblk) *nblk = (int)pass_blocks<R>(ap);
+    const int var = f.plan_var[ap.axis];
+    if (nblk) *nblk = (int)pass_blocks<R>(ap, var);
     Launch L(c, cls, bytes);
-    CU(dispatch_pass<R>(ap.N, a, ap.strided, c->stream));
+    CU(dispatch_pass<R>(ap.N, var, a, ap.strided, c->stream));
   }
   return GPE_OK;
 }
@@ -1258,6 +1324,104 @@ gpe_status io_buffer(gpe_ctx* c, void** out) {
   return GPE_OK;
 }
 
+// ---- FFT plan autotuner ------------------------------------------------------
+// For every FP32 axis pass whose length has two plans (plans.cuh Plan /
+// PlanAlt), time both on a scratch array shaped like the state and keep the
+// faster; the alternative must win by 5% so near-ties keep the default plan
+// (and the choice does not flip between runs).  Choices are cached per
+// device and pass geometry for the process, so contexts of one shape are
+// timed once.
+struct TuneKey {
+  int dev, N, strided;
+  long long n_batch, stride, inner, outer;
+  bool operator==(const TuneKey& o) const {
+    return dev == o.dev && N == o.N && strided == o.strided && n_batch == o.n_batch && stride == o.stride &&
+           inner == o.inner && outer == o.outer;
+  }
+};
+std::mutex g_tune_mu;
+std::vector<std::pair<TuneKey, int>> g_tune_cache;
+
+// Best of 3 launches of one axis pass on buf, in ms.  The contiguous pass
+// runs with the real-time phase prologue it carries in every split step
+// (when the context has a potential); the others run bare.
+gpe_status time_axis_pass(gpe_ctx* c, Field& f, const AxisPass& ap, void* buf, float* ms) {
+  const int pro = (!ap.strided && c->have_V && f.V) ? PRO_RT_FULL : PRO_NONE;
+  cudaEvent_t e0 = pool_event(c), e1 = pool_event(c);
+  float best = 1e30f;
+  CHECK(run_pass<float>(c, f, ap, KIND_STEP, pro, EPI_NONE, 0, 0.0, 1e-3, nullptr, buf));  // warm-up
+  for (int r = 0; r < 3; ++r) {
+    CU(cudaEventRecord(e0, c->stream));
+    CHECK(run_pass<float>(c, f, ap, KIND_STEP, pro, EPI_NONE, 0, 0.0, 1e-3, nullptr, buf));
+    CU(cudaEventRecord(e1, c->stream));
+    CU(cudaEventSynchronize(e1));
+    float t = 0.0f;
+    CU(cudaEventElapsedTime(&t, e0, e1));
+    best = std::min(best, t);
+  }
+  c->ev_pool.push_back(e0);
+  c->ev_pool.push_back(e1);
+  *ms = best;
+  return GPE_OK;
+}
+
+// chosen[ax]: the variant of axis ax, -1 where the length has one plan.
+gpe_status autotune_main(gpe_ctx* c, int chosen[3]) {
+  for (int ax = 0; ax < 3; ++ax) chosen[ax] = -1;
+  c->tuned = true;
+  if (c->prec != GPE_FP32) return GPE_OK;  // FP64 passes use Plan<N>
+  Field& f = c->main;
+  std::vector<AxisPass> todo;
+  for (auto& ap : axis_passes(c))
+    if (has_alt_plan(ap.N)) todo.push_back(ap);
+  if (todo.empty()) return GPE_OK;
+  void* buf = nullptr;
+  CU(cudaMalloc(&buf, (size_t)c->P * 2 * sizeof(float)));
+  gpe_status st = GPE_OK;
+  auto tune = [&]() -> gpe_status {
+    CU(cudaMemsetAsync(buf, 0, (size_t)c->P * 2 * sizeof(float), c->stream));
+    launch_reset_scalars(c->sc, c->stream);  // passes skip their work while sc->stop is set
+    for (auto& ap : todo) {
+      const TuneKey key{c->device, ap.N, ap.strided ? 1 : 0, ap.n_batch, ap.stride, ap.inner, ap.outer};
+      int var = -1;
+      {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        for (auto& e : g_tune_cache)
+          if (e.first == key) var = e.second;
+      }
+      if (var < 0) {
+        float t[2];
+        for (int v = 0; v < 2; ++v) {
+          f.plan_var[ap.axis] = v;
+          CHECK(build_axis_tables<float>(c, f, ap.axis));
+          CHECK(set_kinop<float>(c, f, 0.0, 1e-3));  // any unit-modulus factor: timing only
+          CHECK(time_axis_pass(c, f, ap, buf, &t[v]));
+        }
+        var = t[1] < 0.95f * t[0] ? 1 : 0;
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache.push_back({key, var});
+      }
+      f.plan_var[ap.axis] = var;
+      CHECK(build_axis_tables<float>(c, f, ap.axis));
+      chosen[ap.axis] = var;
+    }
+    f.phase_valid = false;  // the next run builds its own kinetic factors
+    return GPE_OK;
+  };
+  st = tune();
+  cudaStreamSynchronize(c->stream);
+  cudaFree(buf);
+  return st;
+}
+
+// Automatic tuning on the first hot-path call of a large FP32 context.
+gpe_status maybe_autotune(gpe_ctx* c) {
+  if (c->tuned || c->tune_mode != 2 || c->prec != GPE_FP32 || c->pass_variant == 1) return GPE_OK;
+  if (c->P < (1LL << 20)) return GPE_OK;
+  int chosen[3];
+  return autotune_main(c, chosen);
+}
+
 }  // namespace
 
 // =============================================================================
@@ -1343,15 +1507,22 @@ gpe_status gpe_create(const gpe_grid_desc* d, gpe_ctx** out) {
   }
   cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
   if (c->sms <= 0) c->sms = 152;
+  // GPE_AUTOTUNE=0|1|2 sets the initial autotuner mode (gpe_autotune) of new contexts.
+  if (const char* e = getenv("GPE_AUTOTUNE")) {
+    const int m = atoi(e);
+    if (m >= 0 && m <= 2) c->tune_mode = m;
+  }
   // partial-sum capacity: the largest grid of any pass in either precision
+  // and any plan variant
   long long cap = 8LL * 1024;
   for (auto& ap : axis_passes(c)) {
-    cap = std::max(cap, pass_blocks<float>(ap));
-    cap = std::max(cap, pass_blocks<double>(ap));
+    cap = std::max(cap, pass_blocks<float>(ap, 0));
+    if (has_alt_plan(ap.N)) cap = std::max(cap, pass_blocks<float>(ap, 1));
+    cap = std::max(cap, pass_blocks<double>(ap, 0));
   }
   c->cap = (int)cap;
   gpe_status st = GPE_OK;
-  if (cudaMalloc(&c->partials, (size_t)NSLOTS * c->cap * sizeof(double)) != cudaSuccess ||
+  if (cudaMalloc(&c->partials, (size_t)(NSLOTS + 1) * c->cap * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&c->sc, sizeof(DevScalars)) != cudaSuccess ||
       cudaMallocHost(&c->sc_host, 2 * sizeof(DevScalars)) != cudaSuccess ||
       cudaMalloc(&c->V64, (size_t)c->P * sizeof(double)) != cudaSuccess) {
@@ -1556,6 +1727,7 @@ gpe_status gpe_groundstate_itp(gpe_ctx* c, const gpe_itp_params* prm, double* MU
     return fail(c, GPE_ERR_INVALID, "groundstate_itp: dt and eps must be positive");
   if (cap < 0) return fail(c, GPE_ERR_INVALID, "negative cap");
   c->err.clear();
+  CHECK(maybe_autotune(c));
   if (c->prec == GPE_FP32) return itp_impl<float>(c, prm, MU, MU2, EE, cap, res);
   return itp_impl<double>(c, prm, MU, MU2, EE, cap, res);
 }
@@ -1567,6 +1739,7 @@ gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
     return fail(c, GPE_ERR_INVALID, "solve_split: ddt must be positive");
   if (!prm->vtd) CHECK(need_V(c));
   c->err.clear();
+  CHECK(maybe_autotune(c));
   if (c->prec == GPE_FP32) return split_impl<float>(c, prm);
   return split_impl<double>(c, prm);
 }
@@ -1586,6 +1759,7 @@ gpe_status gpe_adjoint_grad(gpe_ctx* c, const gpe_adjoint_params* prm, const dou
   if (prec == GPE_FP32 && c->prec == GPE_FP64)
     return fail(c, GPE_ERR_UNSUPPORTED, "adjoint: an FP64 context has no FP32 tables; use precision 0");
   c->err.clear();
+  CHECK(maybe_autotune(c));
   if (prec == GPE_FP32) return adjoint_impl<float>(c, c->main, prm, psi_target, dLdV, loss);
   if (c->prec == GPE_FP32) {
     CHECK(ensure_polish(c));
@@ -1615,7 +1789,43 @@ gpe_status gpe_solve_split_batch(gpe_ctx** ctxs, int count, const gpe_split_para
     cs.push_back(ci);
   }
   c->err.clear();
+  // Batched contexts are tuned whatever their size (one timing per distinct
+  // grid shape), before any graph is captured.
+  for (auto* ci : cs) {
+    if (ci->tuned || ci->tune_mode != 2 || ci->prec != GPE_FP32 || ci->pass_variant == 1) continue;
+    int chosen[3];
+    if (autotune_main(ci, chosen) != GPE_OK) return fail(c, GPE_ERR_CUDA, "solve_split_batch: autotune: " + ci->err);
+  }
   return batch_impl(cs, prm);
+}
+
+gpe_status gpe_autotune(gpe_ctx* c, int mode, int* chosen) {
+  CHECK(check_ctx(c));
+  if (mode < 0 || mode > 3)
+    return fail(c, GPE_ERR_INVALID, "autotune mode must be 0 (off), 1 (now), 2 (auto) or 3 (alternative plans)");
+  int ch[3] = {-1, -1, -1};
+  if (mode == 0 || mode == 3) {
+    // fixed plans: the defaults, or (mode 3, FP32) the alternative wherever one exists
+    c->tune_mode = mode == 0 ? 0 : 1;
+    c->tuned = mode == 3;
+    for (int ax = 0; ax < c->ndims; ++ax) {
+      const int v = (mode == 3 && c->prec == GPE_FP32 && has_alt_plan(c->n[ax])) ? 1 : 0;
+      if (c->main.plan_var[ax] == v) continue;
+      c->main.plan_var[ax] = v;
+      if (c->prec == GPE_FP32) CHECK(build_axis_tables<float>(c, c->main, ax));
+      else CHECK(build_axis_tables<double>(c, c->main, ax));
+    }
+    c->main.phase_valid = false;
+  } else if (mode == 1) {
+    c->tune_mode = 1;
+    CHECK(autotune_main(c, ch));
+  } else {
+    c->tune_mode = 2;
+  }
+  if (chosen)
+    for (int ax = 0; ax < 3; ++ax)
+      chosen[ax] = (mode == 1) ? ch[ax] : (ax < c->ndims && has_alt_plan(c->n[ax]) ? c->main.plan_var[ax] : -1);
+  return GPE_OK;
 }
 
 gpe_status gpe_observables(gpe_ctx* c, gpe_obs* o) {
@@ -1623,6 +1833,7 @@ gpe_status gpe_observables(gpe_ctx* c, gpe_obs* o) {
   CHECK(need_state(c));
   CHECK(need_V(c));
   if (!o) return fail(c, GPE_ERR_INVALID, "null output");
+  CHECK(maybe_autotune(c));
   DevScalars h;
   if (c->prec == GPE_FP32) CHECK(observables_impl<float>(c, c->main, 0.0, 0, &h));
   else CHECK(observables_impl<double>(c, c->main, 0.0, 0, &h));
@@ -1710,7 +1921,8 @@ gpe_status gpe_selftest_trig(const float* x, float* s, float* co, long long n) {
 
 gpe_status gpe_set_pass_variant(gpe_ctx* c, int variant) {
   CHECK(check_ctx(c));
-  if (variant < 0 || variant > 1) return fail(c, GPE_ERR_INVALID, "pass variant must be 0 (direct) or 1 (TMA)");
+  if (variant < 0 || variant > 2)
+    return fail(c, GPE_ERR_INVALID, "pass variant must be 0 (direct + L2 prefetch), 1 (TMA) or 2 (direct)");
   c->pass_variant = variant;
   return GPE_OK;
 }

@@ -18,8 +18,15 @@
 //    interleaved [position][pencil], which makes every exchange conflict-free.
 #pragma once
 #include "plans.cuh"
+#include "tma.cuh"
 
 namespace gpe {
+
+// Side array of a pass (V for the phase factors, aux for the ITP factor).
+template <typename R>
+__device__ __forceinline__ const R* side_array(const PassArgs<R>& a) {
+  return a.side == 2 ? a.aux : a.V;
+}
 
 template <typename R>
 struct Kahan {
@@ -69,6 +76,22 @@ struct ContigLayout {
     return b * (long long)P::N;
   }
   static __device__ __forceinline__ long long step(const PassArgs<R>&) { return 1; }
+  // L2 prefetch of pencils b0 .. b0+cnt-1 (one contiguous run; with the side
+  // array's run when the pass reads one).  N*sizeof(R) is a multiple of 16
+  // for every planned N, so every chunk is 16-byte aligned and sized.
+  static __device__ __forceinline__ void prefetch(const PassArgs<R>& a, long long b0, long long cnt) {
+    constexpr size_t CH = 4096;
+    const size_t bytes = (size_t)cnt * P::N * sizeof(cx<R>);
+    const char* p = reinterpret_cast<const char*>(a.psi + b0 * P::N);
+    for (size_t off = (size_t)threadIdx.x * CH; off < bytes; off += (size_t)THREADS * CH)
+      prefetch_l2_bulk(p + off, (uint32_t)(bytes - off < CH ? bytes - off : CH));
+    if (a.side != 0) {
+      const size_t sb = (size_t)cnt * P::N * sizeof(R);
+      const char* s = reinterpret_cast<const char*>(side_array(a) + b0 * P::N);
+      for (size_t off = (size_t)threadIdx.x * CH; off < sb; off += (size_t)THREADS * CH)
+        prefetch_l2_bulk(s + off, (uint32_t)(sb - off < CH ? sb - off : CH));
+    }
+  }
 };
 
 template <class P, typename R>
@@ -93,10 +116,87 @@ struct StridedLayout {
     return (b % a.inner) + (b / a.inner) * a.outer;
   }
   static __device__ __forceinline__ long long step(const PassArgs<R>& a) { return a.stride; }
+  // L2 prefetch of pencils b0 .. b0+cnt-1: N rows of cnt adjacent elements,
+  // one line-sized hint per 128 bytes of each row (and of the side array's
+  // rows).  Skipped when a tile's pencils could straddle two row groups.
+  static __device__ __forceinline__ void prefetch(const PassArgs<R>& a, long long b0, long long cnt) {
+    if (a.inner % FFTS != 0) return;
+    const long long o = base(a, b0);
+    const int lines = (int)((cnt * (long long)sizeof(cx<R>) + 127) / 128);
+    for (int i = threadIdx.x; i < P::N * lines; i += THREADS) {
+      const int r = i / lines, l = i % lines;
+      prefetch_l2_line(reinterpret_cast<const char*>(a.psi + o + (long long)r * a.stride) + l * 128);
+    }
+    if (a.side != 0) {
+      const R* s = side_array(a);
+      const int sl = (int)((cnt * (long long)sizeof(R) + 127) / 128);
+      for (int i = threadIdx.x; i < P::N * sl; i += THREADS) {
+        const int r = i / sl, l = i % sl;
+        prefetch_l2_line(reinterpret_cast<const char*>(s + o + (long long)r * a.stride) + l * 128);
+      }
+    }
+  }
 };
+
+// Error-free float addition (Knuth's TwoSum): a + b = s + e exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+// (h, l) += (h2, l2) for unevaluated float pairs h + l (double-float add).
+__device__ __forceinline__ void pair_add(float& h, float& l, float h2, float l2) {
+  float s, e;
+  two_sum(h, h2, s, e);
+  e += l + l2;
+  h = s + e;
+  l = e - (h - s);
+}
 
 // Sum `nred` per-thread values over the CTA in FP64 and store the CTA's
 // partial of each to partials[slot*cap + blockIdx.x].
+template <int THREADS>
+__device__ __forceinline__ void cta_reduce_store(double* vals, const int* slots, int nred,
+                                                 double* partials, int cap);
+
+// The same for per-thread compensated sums.  FP32: each thread's Kahan sum
+// s - c is kept as the float pair (s, -c) and the warp combines pairs with
+// double-float additions (FP32 pipe; the GPU's FP64 rate is a small fraction
+// of its FP32 rate), converting to FP64 once per warp.
+template <int THREADS, typename R>
+__device__ __forceinline__ void cta_reduce_store(const Kahan<R>* acc, const int* slots, int nred,
+                                                 double* partials, int cap) {
+  if constexpr (sizeof(R) == 8) {
+    double vals[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) vals[i] = i < nred ? acc[i].value() : 0.0;
+    cta_reduce_store<THREADS>(vals, slots, nred, partials, cap);
+  } else {
+    __shared__ double red[THREADS / 32 > 0 ? THREADS / 32 : 1][4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i >= nred) break;
+      float h = acc[i].s, l = -acc[i].c;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, h, o);
+        const float l2 = __shfl_down_sync(0xffffffffu, l, o);
+        pair_add(h, l, h2, l2);
+      }
+      if (lane == 0) red[warp][i] = (double)h + (double)l;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < nred; ++i) {
+        double s = 0.0;
+        for (int w = 0; w < (THREADS + 31) / 32; ++w) s += red[w][i];
+        partials[(size_t)slots[i] * cap + blockIdx.x] = s;
+      }
+    }
+  }
+}
+
 template <int THREADS>
 __device__ __forceinline__ void cta_reduce_store(double* vals, const int* slots, int nred,
                                                  double* partials, int cap) {
@@ -144,10 +244,12 @@ __device__ __forceinline__ void apply_phase(cx<double>* v, const cx<double>* __r
 #ifndef GPE_FP32_THREADS_PER_SM
 #define GPE_FP32_THREADS_PER_SM 768  // 80 registers: no spills; 1024 (64) spilled heavily
 #endif
-template <typename R, class L>
+// Plans with at most 8 points per thread hold half the data in registers and
+// aim at 1024 threads per SM (64 registers).
+template <typename R, class P, class L>
 struct MinBlocks {
-  static constexpr int value =
-      (sizeof(R) == 4 && L::THREADS <= 256) ? GPE_FP32_THREADS_PER_SM / L::THREADS : 1;
+  static constexpr int TPS = P::E <= 8 ? 1024 : GPE_FP32_THREADS_PER_SM;
+  static constexpr int value = (sizeof(R) == 4 && L::THREADS <= TPS) ? TPS / L::THREADS : 1;
 };
 
 // Prologue of the first pass on one pencil's E values (sv: V for the phase
@@ -227,7 +329,7 @@ __device__ __forceinline__ void epilogue(cx<R>* v, const R* sv, const PassArgs<R
 // KIND is a template parameter so the step and energy variants are separate
 // kernels, each with only its own live ranges and code.
 template <typename R, class P, class L, int KIND>
-__global__ void __launch_bounds__(L::THREADS, MinBlocks<R, L>::value) pass_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_kernel(const PassArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);
   // An earlier finalizer (or a timed-out pass) ended the run; the block-wide
@@ -250,7 +352,13 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, L>::value) pass_kerne
   {
     const cx<R>* __restrict__ src = a.psi + first;
 #pragma unroll
-    for (int m = 0; m < E; ++m) v[m] = valid ? src[m * dm] : mk<R>(R(0), R(0));
+    for (int m = 0; m < E; ++m) v[m] = valid ? ld_stream(src + m * dm) : mk<R>(R(0), R(0));
+  }
+  // With the own loads in flight, hint the tile of the CTA one wave of
+  // resident CTAs later into L2, so that CTA's loads hit L2.
+  if (a.pf_ahead > 0) {
+    const long long b0 = ((long long)blockIdx.x + a.pf_ahead) * L::FFTS;
+    if (b0 < a.n_batch) L::prefetch(a, b0, a.n_batch - b0 < L::FFTS ? a.n_batch - b0 : (long long)L::FFTS);
   }
 
   if constexpr (KIND == KIND_ENERGY) {
@@ -265,7 +373,7 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, L>::value) pass_kerne
       v[m] = rmul(v[m], s);
       if (pot) {
         const R n = norm2(v[m]);
-        const R Vm = valid ? vs[m * dm] : R(0);
+        const R Vm = valid ? ld_stream(vs + m * dm) : R(0);
         acc[0].add(n);
         acc[1].add(Vm * n);
         acc[2].add(n * n);
@@ -275,22 +383,24 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, L>::value) pass_kerne
     Kahan<R> kin;
 #pragma unroll
     for (int m = 0; m < E; ++m) kin.add(__ldg(a.k2p + m * T + t) * norm2(v[m]));
-    double vals[4];
+    Kahan<R> sums[4];
     int slots[4];
     int nred;
     if (pot) {
-      vals[0] = valid ? acc[0].value() : 0.0;
-      vals[1] = valid ? acc[1].value() : 0.0;
-      vals[2] = valid ? acc[2].value() : 0.0;
-      vals[3] = valid ? kin.value() : 0.0;
+      if (valid) {
+        sums[0] = acc[0];
+        sums[1] = acc[1];
+        sums[2] = acc[2];
+        sums[3] = kin;
+      }
       slots[0] = S_N; slots[1] = S_VN; slots[2] = S_N2; slots[3] = a.kin_slot;
       nred = 4;
     } else {
-      vals[0] = valid ? kin.value() : 0.0;
+      if (valid) sums[0] = kin;
       slots[0] = a.kin_slot;
       nred = 1;
     }
-    cta_reduce_store<L::THREADS>(vals, slots, nred, a.partials, a.cap);
+    cta_reduce_store<L::THREADS>(sums, slots, nred, a.partials, a.cap);
   } else {
     // The side array (V for the phase factors, or the ITP factors) is read
     // right before the phase that uses it: a pass has a prologue or an
@@ -299,7 +409,7 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, L>::value) pass_kerne
     auto load_side = [&]() {
       const R* __restrict__ ss = (a.side == 2 ? a.aux : a.V) + first;
 #pragma unroll
-      for (int m = 0; m < E; ++m) sv[m] = valid ? ss[m * dm] : R(0);
+      for (int m = 0; m < E; ++m) sv[m] = valid ? ld_stream(ss + m * dm) : R(0);
     };
     if (a.pro != PRO_NONE) {
       if (a.side != 0) load_side();
@@ -320,9 +430,8 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, L>::value) pass_kerne
     }
     const int nred = a.epi == EPI_RT_END ? 3 : a.epi == EPI_ITP ? 1 : 0;
     if (nred > 0) {
-      double vals[4] = {acc[0].value(), acc[1].value(), acc[2].value(), 0.0};
       const int slots[4] = {S_N, S_VN, S_N2, 0};
-      cta_reduce_store<L::THREADS>(vals, slots, nred, a.partials, a.cap);
+      cta_reduce_store<L::THREADS>(acc, slots, nred, a.partials, a.cap);
     }
   }
 }
@@ -334,10 +443,11 @@ struct PassGeom {
   size_t smem;
 };
 
-template <typename R, int N>
+// V: plan variant (plans.cuh PlanSel): 0 = Plan<N>, 1 = PlanAlt<N>.
+template <typename R, int N, int V = 0>
 PassGeom pass_geom(bool strided);
 
-template <int N>
+template <int N, int V = 0>
 PlanInfo plan_info();
 
 template <typename R, int N>
@@ -349,7 +459,7 @@ int pass_tma_ffts(bool strided);
 template <typename R, int N>
 size_t pass_tma_smem(bool strided);
 
-template <typename R, int N>
+template <typename R, int N, int V = 0>
 cudaError_t launch_pass(const PassArgs<R>& a, bool strided, cudaStream_t s);
 
 }  // namespace gpe

@@ -6,9 +6,9 @@
 
 namespace gpe {
 
-template <typename R, int N>
+template <typename R, int N, int V>
 PassGeom pass_geom(bool strided) {
-  using P = Plan<N>;
+  using P = typename PlanSel<N, V>::type;
   if (strided) {
     using L = StridedLayout<P, R>;
     return PassGeom{L::THREADS, L::FFTS, L::smem_bytes()};
@@ -17,9 +17,9 @@ PassGeom pass_geom(bool strided) {
   return PassGeom{L::THREADS, L::FFTS, L::smem_bytes()};
 }
 
-template <int N>
+template <int N, int V>
 PlanInfo plan_info() {
-  using P = Plan<N>;
+  using P = typename PlanSel<N, V>::type;
   PlanInfo pi{};
   pi.N = P::N;
   pi.T = P::T;
@@ -28,6 +28,12 @@ PlanInfo plan_info() {
   for (int s = 0; s < P::NSTAGES; ++s) pi.radix[s] = P::radix[s];
   return pi;
 }
+
+// Resident CTAs per SM of a kernel at a given dynamic shared-memory size,
+// cached (the occupancy query costs a few microseconds of host time).
+int resident_ctas(const void* kern, int threads, size_t smem);
+// SMs of the current device (cached).
+int device_sm_count();
 
 template <typename R, class P, class L>
 static cudaError_t launch_layout(const PassArgs<R>& a, cudaStream_t s) {
@@ -41,21 +47,24 @@ static cudaError_t launch_layout(const PassArgs<R>& a, cudaStream_t s) {
   }
   const long long blocks = (a.n_batch + L::FFTS - 1) / L::FFTS;
   if (blocks > a.cap || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  kern<<<(unsigned)blocks, L::THREADS, smem, s>>>(a);
+  PassArgs<R> b = a;
+  b.pf_ahead = 0;
+  if (a.prefetch) {
+    const int wave = resident_ctas((const void*)kern, L::THREADS, smem) * device_sm_count();
+    if (wave > 0 && blocks > wave) b.pf_ahead = wave;
+  }
+  kern<<<(unsigned)blocks, L::THREADS, smem, s>>>(b);
   return cudaGetLastError();
 }
 
-template <typename R, int N>
+template <typename R, int N, int V>
 cudaError_t launch_pass(const PassArgs<R>& a, bool strided, cudaStream_t s) {
-  using P = Plan<N>;
+  using P = typename PlanSel<N, V>::type;
   if (strided) return launch_layout<R, P, StridedLayout<P, R>>(a, s);
   return launch_layout<R, P, ContigLayout<P, R>>(a, s);
 }
 
 // ---- TMA-staged persistent variant --------------------------------------
-// Resident CTAs per SM of a kernel at a given dynamic shared-memory size,
-// cached (the occupancy query costs a few microseconds of host time).
-int resident_ctas(const void* kern, int threads, size_t smem);
 
 template <typename R, class P, class L>
 static cudaError_t launch_tma_layout(const PassArgs<R>& a, cudaStream_t s, int sms) {
@@ -134,5 +143,11 @@ size_t pass_tma_smem(bool strided) {
 
 // Plan descriptions are precision independent: instantiated once (FP32 files).
 #define GPE_INST_PLAN(N) template PlanInfo plan_info<N>();
+
+// The alternative plan of N (FP32 direct passes only).
+#define GPE_INST_PASS_ALT(N)                                                              \
+  template PassGeom pass_geom<float, N, 1>(bool);                                         \
+  template cudaError_t launch_pass<float, N, 1>(const PassArgs<float>&, bool, cudaStream_t); \
+  template PlanInfo plan_info<N, 1>();
 
 }  // namespace gpe

@@ -44,6 +44,31 @@ template <> struct Plan<512>  : PlanT<512, 32, 4, 16, 16, 2> {};
 template <> struct Plan<768>  : PlanT<768, 32, 4, 8, 8, 6, 2> {};
 template <> struct Plan<1024> : PlanT<1024, 64, 4, 16, 16, 4> {};
 
+// Alternative plans: twice the threads per pencil, half the points per thread
+// (fewer registers, more resident warps; one more shared-memory exchange).
+// The autotuner times both plans of an axis pass and keeps the faster one
+// (FP32 passes; FP64 passes use Plan<N>).
+template <int N>
+struct PlanAlt;
+template <> struct PlanAlt<128> : PlanT<128, 16, 4, 8, 4, 4> {};
+template <> struct PlanAlt<192> : PlanT<192, 16, 4, 4, 4, 4, 3> {};
+template <> struct PlanAlt<256> : PlanT<256, 32, 4, 8, 8, 4> {};
+template <> struct PlanAlt<384> : PlanT<384, 32, 4, 4, 4, 4, 6> {};
+template <> struct PlanAlt<512> : PlanT<512, 64, 4, 8, 8, 8> {};
+
+// Plan variant V of length N: 0 = Plan<N>, 1 = PlanAlt<N>.
+template <int N, int V>
+struct PlanSel {
+  using type = Plan<N>;
+};
+template <int N>
+struct PlanSel<N, 1> {
+  using type = PlanAlt<N>;
+};
+
+// The axis lengths with an alternative plan.
+#define GPE_FOR_EACH_ALT(X) X(128) X(192) X(256) X(384) X(512)
+
 // Host-side description of a plan: the tables the pass kernels read are
 // built from it (stage twiddle rows, per-thread permuted kinetic factors).
 struct PlanInfo {

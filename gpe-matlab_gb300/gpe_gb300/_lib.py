@@ -111,6 +111,7 @@ PROTOTYPES = {
     "gpe_profile_read": (C.c_int, [_P, C.POINTER(gpe_kernel_stat), C.c_int, C.POINTER(C.c_int)]),
     "gpe_kernel_launches": (C.c_longlong, [_P]),
     "gpe_set_pass_variant": (C.c_int, [_P, C.c_int]),
+    "gpe_autotune": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int)]),
     "gpe_selftest_trig": (C.c_int, [_F, _F, _F, C.c_longlong]),
     "gpe_norm_noalloc": (C.c_int, [_P, C.c_longlong, C.c_int, C.c_double, _P, _D]),
     "gpe_host_register": (C.c_int, [_P, C.c_size_t]),

@@ -381,8 +381,17 @@ class GPEtask:
     def kernel_launches(self) -> int:
         return int(L.lib.gpe_kernel_launches(self._ctx))
 
+    def autotune(self, mode: int = 1):
+        """FFT plan autotuner (gpe_autotune): 0 default plans, 1 tune now,
+        2 automatic (default), 3 alternative plans.  Returns the plan variant
+        per axis (x, y, z); -1 where an axis has a single plan."""
+        ch = (C.c_int * 3)()
+        L.check(self._ctx, L.lib.gpe_autotune(self._ctx, int(mode), ch))
+        return tuple(ch)
+
     def set_pass_variant(self, variant: int):
-        """0: direct passes (default), 1: TMA-staged passes where they apply."""
+        """0: direct passes with L2 prefetch (default), 1: TMA-staged passes where
+        they apply, 2: direct passes without prefetch."""
         L.check(self._ctx, L.lib.gpe_set_pass_variant(self._ctx, int(variant)))
 
 

@@ -240,9 +240,10 @@ GPE_API gpe_status gpe_timer_start(gpe_ctx *ctx);
 GPE_API gpe_status gpe_timer_stop(gpe_ctx *ctx, double *ms);
 GPE_API gpe_status gpe_profile_enable(gpe_ctx *ctx, int on);
 GPE_API gpe_status gpe_profile_read(gpe_ctx *ctx, gpe_kernel_stat *out, int cap, int *n);
-/* Axis-pass implementation: 0 (default) = direct-load passes, 1 = TMA-staged
- * persistent passes where the tile geometry allows.  Both compute the same
- * result; the knob exists for measurement. */
+/* Axis-pass implementation: 0 (default) = direct-load passes that also
+ * prefetch the next wave's tiles into L2, 1 = TMA-staged persistent passes
+ * where the tile geometry allows, 2 = direct-load passes without prefetch.
+ * All compute the same result; the knob exists for measurement. */
 GPE_API gpe_status gpe_set_pass_variant(gpe_ctx *ctx, int variant);
 /* integrate(|psi|^2) = sum |psi_i|^2 * weight of a caller-owned device array
  * d_psi (npoints interleaved complex values of `precision`, on the current
@@ -259,6 +260,17 @@ GPE_API gpe_status gpe_set_pass_variant(gpe_ctx *ctx, int variant);
  * serialised by the caller.  Errors: gpe_last_error(NULL). */
 GPE_API gpe_status gpe_norm_noalloc(const void *d_psi, long long npoints, int precision, double weight,
                                     void *stream, double *norm_out);
+/* FFT plan autotuner (FP32 contexts).  Axis lengths 128, 192, 256, 384 and
+ * 512 have two FFT plans (threads per pencil T and radix schedule); the tuner
+ * times both on each axis pass of this grid and keeps the faster (the
+ * alternative must win by 5%), caching choices per device and grid shape.
+ * mode 0: default plans, no tuning; 1: tune now; 2 (default): tune on the
+ * first groundstate_itp / solve_split / observables / adjoint call when the
+ * grid has >= 2^20 points, and for every context of solve_split_batch;
+ * 3: use the alternative plan wherever one exists (testing, measurement).
+ * chosen (may be NULL) receives the plan variant of axes x, y, z (0 default,
+ * 1 alternative, -1 for a length with one plan, FP64 contexts, 2D z). */
+GPE_API gpe_status gpe_autotune(gpe_ctx *ctx, int mode, int *chosen);
 /* Diagnostic: the FP32 device sin/cos used by the phase factors, on n host
  * values (device 0).  Lets tests bound its error against FP64 references. */
 GPE_API gpe_status gpe_selftest_trig(const float *x, float *s, float *c, long long n);

@@ -142,6 +142,43 @@ def test_every_axis_length_contig_and_strided(gpe, n, precision):
         np.testing.assert_allclose(task.history["mu"], ot.history["mu"], rtol=tol)
 
 
+@pytest.mark.parametrize("n", [128, 192, 256, 384, 512])
+def test_alternative_fft_plans_contig_and_strided(gpe, n):
+    """The autotuner's alternative plans (twice the threads per pencil) give
+    the same step as the oracle on both pass layouts (FP32 tolerance)."""
+    rng = np.random.default_rng(n + 1)
+    for nx, ny in ((n, 8), (8, n)):
+        grid, task, og, ot = make_pair(gpe, (3.0, nx, 2.0, ny), harmonic((1.0, 1.7)), "single", g=0.7)
+        chosen = task.autotune(3)
+        assert chosen[0] == (1 if nx == n else -1) and chosen[1] == (1 if ny == n else -1)
+        X, Y = og.mesh["x"], og.mesh["y"]
+        psi0 = np.exp(-(X ** 2 + Y ** 2)) * (1 + 0.05 * rng.standard_normal(og.shape)) * np.exp(0.3j * X)
+        task.init_state = psi0
+        ot.init_state = psi0
+        task.solve_split(0.002, 3, 2)
+        ot.solve_split(0.002, 3, 2)
+        assert rel_l2(task.current_state, ot.current_state) < 2e-5, (nx, ny)
+        np.testing.assert_allclose(task.history["mu"], ot.history["mu"], rtol=2e-5)
+
+
+def test_autotuner_choices_and_results(gpe):
+    """Tuning picks a plan per axis (cached per shape), and the tuned context
+    reproduces the oracle; mode 0 restores the default plans."""
+    axes = (6.0, 128, 6.0, 256, 4.0, 64)
+    grid, task, og, ot = make_pair(gpe, axes, harmonic((1.0, 1.0, 1.5)), "single", g=0.5)
+    chosen = task.autotune(1)
+    assert chosen[0] in (0, 1) and chosen[1] in (0, 1) and chosen[2] == -1
+    assert task.autotune(1) == chosen  # cached per device and shape
+    X, Y, Z = og.mesh["x"], og.mesh["y"], og.mesh["z"]
+    psi0 = (np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 2) * np.exp(0.2j * Y)).astype(complex)
+    task.init_state = psi0
+    ot.init_state = psi0
+    task.solve_split(0.002, 10, 1)
+    ot.solve_split(0.002, 10, 1)
+    assert rel_l2(task.current_state, ot.current_state) < 2e-5
+    assert task.autotune(0) == (0, 0, -1)  # x = 128 and y = 256 have two plans, z = 64 one
+
+
 # ---- semantics -----------------------------------------------------------------
 def test_observables_match_applyham_and_get_energy(gpe):
     grid, task, og, ot = make_pair(gpe, (4.0, 32, 3.0, 48, 2.0, 24), harmonic((1.0, 1.2, 2.0)), "double", g=1.3)
@@ -280,6 +317,31 @@ def test_tma_pass_variant_matches_direct(gpe, precision):
     assert rel_l2(out[1][0], out[0][0]) < tol
     assert rel_l2(out[1][1], out[0][1]) < tol
     np.testing.assert_allclose(out[1][2], out[0][2], rtol=tol)
+
+
+@pytest.mark.parametrize("precision", ["double", "single"])
+def test_l2_prefetch_variant_is_bit_identical(gpe, precision):
+    """Variant 0 only adds L2 prefetch hints to variant 2's passes: the
+    arithmetic and the reduction order are those of the direct passes, so the
+    results are identical.  The grid is large enough that every axis pass
+    launches more CTAs than one resident wave (the prefetch path runs)."""
+    out = []
+    for variant in (0, 2):
+        grid = gpe.grid3d(8, 256, 8, 256, 8, 64, precision=precision)
+        task = gpe.GPEtask(grid, harmonic((1.0, 1.0, 2.0)))
+        task.set_pass_variant(variant)
+        task.Ntotal, task.g, task.gamma = 1e3, 0.5, 0.01
+        X, Y, Z = grid.mesh["x"], grid.mesh["y"], grid.mesh["z"]
+        psi0 = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 4).astype(complex)
+        task.itp_max_iter = 60
+        task.itp_min_iter = 10
+        phi = task.groundstate_itp(0.005, 1e-12, psi0)
+        task.init_state = phi * np.exp(0.3j * X)
+        task.solve_split(0.002, 20, 2)
+        out.append((phi, task.current_state, np.array(task.history["mu"])))
+    np.testing.assert_array_equal(out[1][0], out[0][0])
+    np.testing.assert_array_equal(out[1][1], out[0][1])
+    np.testing.assert_array_equal(out[1][2], out[0][2])
 
 
 def test_device_sincos_error_bound(gpe):
