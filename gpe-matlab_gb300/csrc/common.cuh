@@ -50,6 +50,28 @@ __device__ __forceinline__ cx<double> ldg(const cx<double>* p) {
   return mk<double>(v.x, v.y);
 }
 
+// Loads of FFT table entries (twiddle rows, kinetic factors): SMT = the
+// tables were copied to shared memory (plain loads), else global memory
+// through the read-only data cache.  GPE_SMEM_TABLES=0 disables the copy.
+#ifndef GPE_SMEM_TABLES
+#define GPE_SMEM_TABLES 1
+#endif
+template <bool SMT, typename T>
+__device__ __forceinline__ T ld_tab(const T* p) {
+  if constexpr (SMT) return *p;
+  else return __ldg(p);
+}
+template <bool SMT>
+__device__ __forceinline__ cx<float> ld_tab(const cx<float>* p) {
+  const float2 v = ld_tab<SMT>(reinterpret_cast<const float2*>(p));
+  return mk<float>(v.x, v.y);
+}
+template <bool SMT>
+__device__ __forceinline__ cx<double> ld_tab(const cx<double>* p) {
+  const double2 v = ld_tab<SMT>(reinterpret_cast<const double2*>(p));
+  return mk<double>(v.x, v.y);
+}
+
 // Loads of streamed data (state, potential) that a pass reads once: marked
 // evict-first so they do not push the FFT tables out of L1.
 #ifndef GPE_STREAM_LOADS

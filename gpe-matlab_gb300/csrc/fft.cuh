@@ -202,34 +202,35 @@ __device__ __forceinline__ int scatter_pos(int j, int r) {
 // rows are stored k-fastest so that adjacent lanes (adjacent k) read adjacent
 // addresses: FP32 stages of even radix as [r/2][k] pairs of entries (one
 // 16-byte vector load gives w_{2i}, w_{2i+1}), otherwise as [r][k] entries.
-template <int Ns, int RAD, int DIR>
+// SMT: the rows are in shared memory (plain loads), else in global memory.
+template <int Ns, int RAD, int DIR, bool SMT>
 __device__ __forceinline__ void apply_row(cx<float>* u, const cx<float>* __restrict__ rows, int k) {
   if constexpr (RAD % 2 == 0) {
     const float4* r4 = reinterpret_cast<const float4*>(rows) + k;
 #pragma unroll
     for (int i = 0; i < RAD / 2; ++i) {
-      const float4 q = __ldg(r4 + i * Ns);
+      const float4 q = ld_tab<SMT>(r4 + i * Ns);
       if (i > 0) u[2 * i] = DIR < 0 ? cmul(u[2 * i], mk<float>(q.x, q.y)) : cmulc(u[2 * i], mk<float>(q.x, q.y));
       u[2 * i + 1] = DIR < 0 ? cmul(u[2 * i + 1], mk<float>(q.z, q.w)) : cmulc(u[2 * i + 1], mk<float>(q.z, q.w));
     }
   } else {
 #pragma unroll
     for (int r = 1; r < RAD; ++r) {
-      const cx<float> w = ldg(rows + r * Ns + k);
+      const cx<float> w = ld_tab<SMT>(rows + r * Ns + k);
       u[r] = DIR < 0 ? cmul(u[r], w) : cmulc(u[r], w);
     }
   }
 }
-template <int Ns, int RAD, int DIR>
+template <int Ns, int RAD, int DIR, bool SMT>
 __device__ __forceinline__ void apply_row(cx<double>* u, const cx<double>* __restrict__ rows, int k) {
 #pragma unroll
   for (int r = 1; r < RAD; ++r) {
-    const cx<double> w = ldg(rows + r * Ns + k);
+    const cx<double> w = ld_tab<SMT>(rows + r * Ns + k);
     u[r] = DIR < 0 ? cmul(u[r], w) : cmulc(u[r], w);
   }
 }
 
-template <typename R, int N, int T, int Ns, int RAD>
+template <typename R, int N, int T, int Ns, int RAD, bool SMT>
 __device__ __forceinline__ void fwd_stage(cx<R>* v, int t, const cx<R>* __restrict__ rows) {
   constexpr int E = N / T;
   constexpr int NB = E / RAD;
@@ -238,14 +239,14 @@ __device__ __forceinline__ void fwd_stage(cx<R>* v, int t, const cx<R>* __restri
     cx<R> u[RAD];
 #pragma unroll
     for (int r = 0; r < RAD; ++r) u[r] = v[b + r * NB];
-    if constexpr (Ns > 1) apply_row<Ns, RAD, -1>(u, rows, (t + T * b) % Ns);
+    if constexpr (Ns > 1) apply_row<Ns, RAD, -1, SMT>(u, rows, (t + T * b) % Ns);
     dft<R, RAD, -1>(u);
 #pragma unroll
     for (int r = 0; r < RAD; ++r) v[b + r * NB] = u[r];
   }
 }
 
-template <typename R, int N, int T, int Ns, int RAD>
+template <typename R, int N, int T, int Ns, int RAD, bool SMT>
 __device__ __forceinline__ void inv_stage(cx<R>* v, int t, const cx<R>* __restrict__ rows) {
   constexpr int E = N / T;
   constexpr int NB = E / RAD;
@@ -255,7 +256,7 @@ __device__ __forceinline__ void inv_stage(cx<R>* v, int t, const cx<R>* __restri
 #pragma unroll
     for (int r = 0; r < RAD; ++r) u[r] = v[b + r * NB];
     dft<R, RAD, +1>(u);
-    if constexpr (Ns > 1) apply_row<Ns, RAD, +1>(u, rows, (t + T * b) % Ns);
+    if constexpr (Ns > 1) apply_row<Ns, RAD, +1, SMT>(u, rows, (t + T * b) % Ns);
 #pragma unroll
     for (int r = 0; r < RAD; ++r) v[b + r * NB] = u[r];
   }
@@ -295,23 +296,24 @@ __device__ __forceinline__ void xchg_own_to_scatter(cx<R>* v, cx<R>* sm, const S
 template <typename R, int N, int T, int Ns, int OFF, int RAD, int... REST>
 struct Stages {
   static constexpr int NEXT_OFF = (Ns > 1) ? OFF + ((Ns * RAD + 1) & ~1) : OFF;
-  template <class SM>
+  // SMT: tws points to shared memory.
+  template <bool SMT, class SM>
   static __device__ __forceinline__ void forward(cx<R>* v, cx<R>* sm, const SM& pol, int t,
                                                  const cx<R>* __restrict__ tws) {
-    fwd_stage<R, N, T, Ns, RAD>(v, t, tws + OFF);
+    fwd_stage<R, N, T, Ns, RAD, SMT>(v, t, tws + OFF);
     if constexpr (sizeof...(REST) > 0) {
       xchg_scatter_to_own<R, N, T, Ns, RAD>(v, sm, pol, t);
-      Stages<R, N, T, Ns * RAD, NEXT_OFF, REST...>::forward(v, sm, pol, t, tws);
+      Stages<R, N, T, Ns * RAD, NEXT_OFF, REST...>::template forward<SMT>(v, sm, pol, t, tws);
     }
   }
-  template <class SM>
+  template <bool SMT, class SM>
   static __device__ __forceinline__ void inverse(cx<R>* v, cx<R>* sm, const SM& pol, int t,
                                                  const cx<R>* __restrict__ tws) {
     if constexpr (sizeof...(REST) > 0) {
-      Stages<R, N, T, Ns * RAD, NEXT_OFF, REST...>::inverse(v, sm, pol, t, tws);
+      Stages<R, N, T, Ns * RAD, NEXT_OFF, REST...>::template inverse<SMT>(v, sm, pol, t, tws);
       xchg_own_to_scatter<R, N, T, Ns, RAD>(v, sm, pol, t);
     }
-    inv_stage<R, N, T, Ns, RAD>(v, t, tws + OFF);
+    inv_stage<R, N, T, Ns, RAD, SMT>(v, t, tws + OFF);
   }
 };
 

@@ -58,7 +58,7 @@ struct ContigLayout {
   static constexpr int THREADS = FFTS * T;
   static constexpr int REG0 = padpos<P::PADSH>(P::N - 1) + 1;
   static constexpr int REG = (REG0 % 2 == 0) ? REG0 + 1 : REG0;  // odd stride between pencils
-  static constexpr size_t smem_bytes() { return sizeof(cx<R>) * (size_t)FFTS * REG; }
+  __host__ __device__ static constexpr size_t smem_bytes() { return sizeof(cx<R>) * (size_t)FFTS * REG; }
   struct Pol {
     int off;
     __device__ __forceinline__ int idx(int p) const { return off + padpos<P::PADSH>(p); }
@@ -101,7 +101,7 @@ struct StridedLayout {
   static constexpr int F0 = (GPE_DIRECT_CTA_THREADS / T > G) ? GPE_DIRECT_CTA_THREADS / T : G;
   static constexpr int FFTS = (F0 * T > 1024) ? 1024 / T : F0;
   static constexpr int THREADS = FFTS * T;
-  static constexpr size_t smem_bytes() { return sizeof(cx<R>) * (size_t)FFTS * P::N; }
+  __host__ __device__ static constexpr size_t smem_bytes() { return sizeof(cx<R>) * (size_t)FFTS * P::N; }
   struct Pol {
     int f;
     __device__ __forceinline__ int idx(int p) const { return p * FFTS + f; }
@@ -112,6 +112,8 @@ struct StridedLayout {
     t = tid / FFTS;
   }
   static __device__ __forceinline__ Pol pol(int f) { return Pol{f}; }
+  // (A 32-bit or shift form of this division made ptxas schedule the table
+  // loads earlier and spill ~150 bytes in the step kernel: measured slower.)
   static __device__ __forceinline__ long long base(const PassArgs<R>& a, long long b) {
     return (b % a.inner) + (b / a.inner) * a.outer;
   }
@@ -223,20 +225,21 @@ __device__ __forceinline__ void cta_reduce_store(double* vals, const int* slots,
 // Multiply v[0..E) by the thread's kinetic factors.  The permuted table is
 // stored slot-major so adjacent lanes read adjacent addresses: FP32 as
 // [m/2][t] pairs of entries (16-byte vectors), FP64 as [m][t] entries.
-template <int T, int E>
+// SMT: php points to shared memory.
+template <int T, int E, bool SMT = false>
 __device__ __forceinline__ void apply_phase(cx<float>* v, const cx<float>* __restrict__ php, int t) {
   const float4* r4 = reinterpret_cast<const float4*>(php) + t;
 #pragma unroll
   for (int i = 0; i < E / 2; ++i) {
-    const float4 q = __ldg(r4 + i * T);
+    const float4 q = ld_tab<SMT>(r4 + i * T);
     v[2 * i] = cmul(v[2 * i], mk<float>(q.x, q.y));
     v[2 * i + 1] = cmul(v[2 * i + 1], mk<float>(q.z, q.w));
   }
 }
-template <int T, int E>
+template <int T, int E, bool SMT = false>
 __device__ __forceinline__ void apply_phase(cx<double>* v, const cx<double>* __restrict__ php, int t) {
 #pragma unroll
-  for (int m = 0; m < E; ++m) v[m] = cmul(v[m], ldg(php + m * T + t));
+  for (int m = 0; m < E; ++m) v[m] = cmul(v[m], ld_tab<SMT>(php + m * T + t));
 }
 
 // Occupancy hint: FP32 passes aim at GPE_FP32_THREADS_PER_SM resident
@@ -244,6 +247,18 @@ __device__ __forceinline__ void apply_phase(cx<double>* v, const cx<double>* __r
 #ifndef GPE_FP32_THREADS_PER_SM
 #define GPE_FP32_THREADS_PER_SM 768  // 80 registers: no spills; 1024 (64) spilled heavily
 #endif
+// FP32 step passes of length <= 256 keep their twiddle rows and kinetic
+// factors in shared memory (after the exchange buffer): measured 4% faster
+// at 256^3; at 512 the larger buffers cost occupancy and it was slower.
+template <typename R, class P, int KIND>
+struct SmemTables {
+  static constexpr bool value = GPE_SMEM_TABLES && sizeof(R) == 4 && KIND == KIND_STEP && P::N <= 256;
+};
+template <typename R, class P, class L, int KIND>
+constexpr size_t pass_smem_bytes() {
+  return L::smem_bytes() + (SmemTables<R, P, KIND>::value ? sizeof(cx<R>) * (size_t)(P::TW_LEN + P::N) : 0);
+}
+
 // Plans with at most 8 points per thread hold half the data in registers and
 // aim at 1024 threads per SM (64 registers).
 template <typename R, class P, class L>
@@ -360,6 +375,22 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
     const long long b0 = ((long long)blockIdx.x + a.pf_ahead) * L::FFTS;
     if (b0 < a.n_batch) L::prefetch(a, b0, a.n_batch - b0 < L::FFTS ? a.n_batch - b0 : (long long)L::FFTS);
   }
+  // Step-pass tables in shared memory (SmemTables): copied while the pencil
+  // loads are in flight, then read from shared memory.
+  const cx<R>* tws = a.tws;
+  const cx<R>* php = a.php;
+  if constexpr (SmemTables<R, P, KIND>::value) {
+    cx<R>* tab = reinterpret_cast<cx<R>*>(smem_raw + L::smem_bytes());  // 16-byte aligned
+    const float4* g1 = reinterpret_cast<const float4*>(a.tws);
+    float4* s1 = reinterpret_cast<float4*>(tab);
+    for (int i = threadIdx.x; i < P::TW_LEN / 2; i += L::THREADS) s1[i] = __ldg(g1 + i);
+    const float4* g2 = reinterpret_cast<const float4*>(a.php);
+    float4* s2 = reinterpret_cast<float4*>(tab + P::TW_LEN);
+    for (int i = threadIdx.x; i < P::N / 2; i += L::THREADS) s2[i] = __ldg(g2 + i);
+    __syncthreads();
+    tws = tab;
+    php = tab + P::TW_LEN;
+  }
 
   if constexpr (KIND == KIND_ENERGY) {
     // <psi|L_axis psi> (+ the n, Vn, n^2 sums on request) of the state times
@@ -379,7 +410,7 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
         acc[2].add(n * n);
       }
     }
-    St::forward(v, sm, pol, t, a.tws);
+    St::template forward<false>(v, sm, pol, t, a.tws);
     Kahan<R> kin;
 #pragma unroll
     for (int m = 0; m < E; ++m) kin.add(__ldg(a.k2p + m * T + t) * norm2(v[m]));
@@ -415,9 +446,10 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
       if (a.side != 0) load_side();
       prologue<R, E>(v, sv, a, valid, first, dm);
     }
-    St::forward(v, sm, pol, t, a.tws);
-    apply_phase<T, E>(v, a.php, t);
-    St::inverse(v, sm, pol, t, a.tws);
+    constexpr bool SMT = SmemTables<R, P, KIND>::value;
+    St::template forward<SMT>(v, sm, pol, t, tws);
+    apply_phase<T, E, SMT>(v, php, t);
+    St::template inverse<SMT>(v, sm, pol, t, tws);
     Kahan<R> acc[3];
     if (a.epi != EPI_NONE) {
       load_side();

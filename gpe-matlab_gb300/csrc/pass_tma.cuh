@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value) pass_tm
           acc[2].add(n * n);
         }
       }
-      St::forward(v, xb, pol, t, a.tws);
+      St::template forward<false>(v, xb, pol, t, a.tws);
       if (valid) {
 #pragma unroll
         for (int m = 0; m < E; ++m) acc[3].add(__ldg(a.k2p + m * T + t) * norm2(v[m]));
@@ -201,9 +201,9 @@ __global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value) pass_tm
         if (side) load_side();
         prologue<R, E>(v, sv, a, valid, first, dm);
       }
-      St::forward(v, xb, pol, t, a.tws);
+      St::template forward<false>(v, xb, pol, t, a.tws);
       apply_phase<T, E>(v, a.php, t);
-      St::inverse(v, xb, pol, t, a.tws);
+      St::template inverse<false>(v, xb, pol, t, a.tws);
       if (a.epi != EPI_NONE) {
         load_side();
         epilogue<R, E>(v, sv, a, acc, valid);

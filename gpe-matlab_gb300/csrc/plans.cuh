@@ -21,6 +21,18 @@ struct PlanT {
   template <typename R>
   using St = Stages<R, N_, T_, 1, 0, RADS...>;
   static constexpr int prod() { return (RADS * ...); }
+  // Complex entries of the stage twiddle rows (the layout the host builds:
+  // stage s >= 1 takes even(Ns * R_s) entries), at least 2.
+  static constexpr int tw_len() {
+    const int r[] = {RADS...};
+    int off = 0, Ns = r[0];
+    for (int s = 1; s < (int)sizeof...(RADS); ++s) {
+      off += (Ns * r[s] + 1) & ~1;
+      Ns *= r[s];
+    }
+    return off < 2 ? 2 : off;
+  }
+  static constexpr int TW_LEN = tw_len();
   static_assert(prod() == N_, "radices must multiply to N");
   static_assert((((N_ / T_) % RADS == 0) && ...), "every radix must divide E");
 };
