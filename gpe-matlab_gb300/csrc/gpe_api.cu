@@ -1740,6 +1740,14 @@ gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
   if (!prm->vtd) CHECK(need_V(c));
   c->err.clear();
   CHECK(maybe_autotune(c));
+  // Small grids are launch-bound: run their blocks as replayed CUDA graphs
+  // (the batched path with one context) when no per-block host work is
+  // needed (no Vtd or outer-step callback, no decay target) and no per-launch
+  // profiling events are requested.
+  if (!prm->vtd && !prm->on_step && !(c->prm.decay_rate > 0) && !c->prof && c->P <= (1LL << 20)) {
+    std::vector<gpe_ctx*> one{c};
+    return batch_impl(one, prm);
+  }
   if (c->prec == GPE_FP32) return split_impl<float>(c, prm);
   return split_impl<double>(c, prm);
 }
