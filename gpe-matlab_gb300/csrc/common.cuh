@@ -235,6 +235,7 @@ struct PassArgs {
   int energy_pot;          // energy pass: also accumulate n, Vn, n^2
   double g;                // coupling
   double dre, dim;         // time step (real, imag) of the phase factors
+  R gr, drer, dimr;        // g, dre, dim rounded to R by the host (no FP64 work per thread)
   int prefetch = 0;        // direct pass: 1 = prefetch the tile one wave ahead into L2
   int pf_ahead = 0;        // set by the launcher: resident CTAs of the launch (one wave)
 };

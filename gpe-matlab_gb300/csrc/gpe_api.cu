@@ -506,6 +506,9 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.g = c->prm.g;
   a.dre = dre;
   a.dim = dim;
+  a.gr = (R)a.g;
+  a.drer = (R)dre;
+  a.dimr = (R)dim;
   a.prefetch = c->pass_variant == 0;
   const double P = (double)c->P;
   double bytes = (kind == KIND_ENERGY ? 1.0 : 2.0) * P * 2 * sizeof(R);

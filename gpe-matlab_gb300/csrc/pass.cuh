@@ -271,12 +271,11 @@ struct MinBlocks {
 // modes, unused otherwise).  The mode switch sits outside the unrolled loops
 // so only the selected variant executes (branches inside an unrolled loop
 // are if-converted, which ran every variant).
+// s, mu: the pending scale and mu in R (read once per CTA).
 template <typename R, int E>
 __device__ __forceinline__ void prologue(cx<R>* v, const R* sv, const PassArgs<R>& a, bool valid,
-                                         long long first, long long dm) {
-  const R s = (R)a.sc->scale;
-  const R mu = (R)a.sc->mu;
-  const R g = (R)a.g, dre = (R)a.dre, dim = (R)a.dim;
+                                         long long first, long long dm, R s, R mu) {
+  const R g = a.gr, dre = a.drer, dim = a.dimr;
   switch (a.pro) {
     case PRO_SCALE:
 #pragma unroll
@@ -314,10 +313,9 @@ __device__ __forceinline__ void prologue(cx<R>* v, const R* sv, const PassArgs<R
 // Epilogue of the last pass; sums of valid pencils go to acc.
 template <typename R, int E>
 __device__ __forceinline__ void epilogue(cx<R>* v, const R* sv, const PassArgs<R>& a, Kahan<R>* acc,
-                                         bool valid) {
+                                         bool valid, R mu) {
   if (a.epi == EPI_RT_END) {
-    const R mu = (R)a.sc->mu;
-    const R g = (R)a.g, dre = (R)a.dre, dim = (R)a.dim;
+    const R g = a.gr, dre = a.drer, dim = a.dimr;
 #pragma unroll
     for (int m = 0; m < E; ++m) {
       cx<R> p = v[m];
@@ -347,8 +345,15 @@ template <typename R, class P, class L, int KIND>
 __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_kernel(const PassArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);
+  // The pending scale and mu, converted to R once per CTA (the FP64 pipe of
+  // this GPU is narrow: per-thread conversions showed up in the pass time).
+  __shared__ R scal[2];
+  if (threadIdx.x == 0) {
+    scal[0] = (R)a.sc->scale;
+    scal[1] = (R)a.sc->mu;
+  }
   // An earlier finalizer (or a timed-out pass) ended the run; the block-wide
-  // vote keeps the decision uniform within the CTA.
+  // vote keeps the decision uniform within the CTA (and publishes scal).
   if (__syncthreads_or(a.sc->stop != 0)) return;
 
   constexpr int T = P::T, E = P::E;
@@ -395,7 +400,7 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
   if constexpr (KIND == KIND_ENERGY) {
     // <psi|L_axis psi> (+ the n, Vn, n^2 sums on request) of the state times
     // the pending scale (PRO_SCALE) or as stored (PRO_NONE).
-    const R s = a.pro == PRO_SCALE ? (R)a.sc->scale : R(1);
+    const R s = a.pro == PRO_SCALE ? scal[0] : R(1);
     Kahan<R> acc[3];
     const bool pot = a.energy_pot != 0;
     const R* __restrict__ vs = a.V + first;
@@ -444,7 +449,7 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
     };
     if (a.pro != PRO_NONE) {
       if (a.side != 0) load_side();
-      prologue<R, E>(v, sv, a, valid, first, dm);
+      prologue<R, E>(v, sv, a, valid, first, dm, scal[0], scal[1]);
     }
     constexpr bool SMT = SmemTables<R, P, KIND>::value;
     St::template forward<SMT>(v, sm, pol, t, tws);
@@ -453,7 +458,7 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
     Kahan<R> acc[3];
     if (a.epi != EPI_NONE) {
       load_side();
-      epilogue<R, E>(v, sv, a, acc, valid);
+      epilogue<R, E>(v, sv, a, acc, valid, scal[1]);
     }
     if (valid) {
       cx<R>* __restrict__ dst = a.psi + first;

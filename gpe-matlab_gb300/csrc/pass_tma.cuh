@@ -199,14 +199,14 @@ __global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value) pass_tm
     } else {
       if (a.pro != PRO_NONE) {
         if (side) load_side();
-        prologue<R, E>(v, sv, a, valid, first, dm);
+        prologue<R, E>(v, sv, a, valid, first, dm, (R)a.sc->scale, (R)a.sc->mu);
       }
       St::template forward<false>(v, xb, pol, t, a.tws);
       apply_phase<T, E>(v, a.php, t);
       St::template inverse<false>(v, xb, pol, t, a.tws);
       if (a.epi != EPI_NONE) {
         load_side();
-        epilogue<R, E>(v, sv, a, acc, valid);
+        epilogue<R, E>(v, sv, a, acc, valid, (R)a.sc->mu);
       }
       if (valid) {
         cx<R>* __restrict__ dst = a.psi + first;
