@@ -107,6 +107,20 @@ classdef GPEtaskGB300 < GPEtask
             task.ext_callback(phi, step, time, mu, n);
         end
 
+        function [loss, dLdV] = adjoint_grad(task, target, ddt, nsteps, phi0, K, budget, fp64)
+            % dloss/dV of loss = 1 - |<target|psi(T)>|^2/(|target|^2 |phi0|^2)
+            % after nsteps gamma = 0 split steps from phi0 in Vtrap (GPU discrete
+            % adjoint with checkpoints every K steps, K = 0: about sqrt(nsteps)).
+            if nargin < 6, K = 0; end
+            if nargin < 7, budget = 60e9; end
+            if nargin < 8, fp64 = false; end
+            task.gb300_push();
+            gpe_mex('set_potential', task.gb300_handle, double(gather(task.Vtrap)));
+            gpe_mex('set_state', task.gb300_handle, complex(gather(phi0)));
+            [loss, dLdV] = gpe_mex('adjoint', task.gb300_handle, complex(double(gather(target))), ...
+                ddt, nsteps, K, budget, 2 * double(fp64));
+        end
+
         function E = get_energy(task, phi, time)
             % GPEtask.m:97-107 on the GPU (current V).
             if nargin >= 2

@@ -226,6 +226,32 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     r[3] = o.eint;
     r[4] = o.mu_integral;
     r[5] = o.energy;
+  } else if (cmd == "adjoint") {
+    // [loss, dLdV] = gpe_mex('adjoint', h, target, ddt, nsteps, K, budget, precision)
+    // precision: 0 = the context's, 2 = FP64 sweep.  dLdV has the grid's shape.
+    if (nrhs != 8) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('adjoint', h, target, ddt, nsteps, K, budget, prec)");
+    const mxArray* tg = prhs[2];
+    if (!mxIsDouble(tg) || !mxIsComplex(tg)) mexErrMsgIdAndTxt("gpe:arg", "target must be complex double");
+    gpe_adjoint_params p;
+    memset(&p, 0, sizeof(p));
+    p.ddt = scalar(prhs[3]);
+    p.nsteps = (int)scalar(prhs[4]);
+    p.checkpoint_every = (int)scalar(prhs[5]);
+    p.mem_budget = scalar(prhs[6]);
+    p.precision = (int)scalar(prhs[7]);
+    mxArray* g = mxCreateNumericArray(mxGetNumberOfDimensions(tg), mxGetDimensions(tg), mxDOUBLE_CLASS, mxREAL);
+    double loss = 0.0;
+    check(c, gpe_adjoint_grad(c, &p, reinterpret_cast<const double*>(mxGetComplexDoubles(tg)), mxGetDoubles(g),
+                              &loss));
+    plhs[0] = mxCreateDoubleScalar(loss);
+    if (nlhs > 1) plhs[1] = g;
+    else mxDestroyArray(g);
+  } else if (cmd == "autotune") {
+    // chosen = gpe_mex('autotune', h, mode): FFT plan per axis (x, y, z)
+    int ch[3];
+    check(c, gpe_autotune(c, (int)scalar(prhs[2]), ch));
+    plhs[0] = mxCreateDoubleMatrix(1, 3, mxREAL);
+    for (int k = 0; k < 3; ++k) mxGetDoubles(plhs[0])[k] = ch[k];
   } else {
     mexErrMsgIdAndTxt("gpe:usage", "unknown command '%s'", cmd.c_str());
   }
