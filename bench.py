@@ -513,12 +513,15 @@ def run_adjoint(args, dist):
     task.close()
 
 
-def run_profile_case(precision: str, blocks: int, variant: int = 0):
+def run_profile_case(precision: str, blocks: int, variant: int = 0, plans: int = 0):
     """Small fixed case for ncu captures: the bench workload's grid and
-    parameters from the seeded Gaussian (no ITP), `blocks` blocks of 10 steps."""
+    parameters from the seeded Gaussian (no ITP), `blocks` blocks of 10 steps.
+    The FFT plans are fixed (no autotuning under the profiler): `plans` = bit
+    mask of the axes (bit 0 = x) that use the alternative plan."""
     from gpe_gb300.workloads import DAMPED3D as W
 
     grid, task = W.make_task(precision)
+    task.autotune(16 + plans)
     task.set_pass_variant(variant)
     task.init_state = W.initial_state(grid) * 30.0
     task.solve_split(W.dt, 10, blocks)
@@ -532,6 +535,8 @@ def main():
     ap.add_argument("--profile-case", choices=["single", "double"], default=None,
                     help="run the small fixed case used for ncu captures and exit")
     ap.add_argument("--profile-blocks", type=int, default=2)
+    ap.add_argument("--profile-plans", type=int, default=0,
+                    help="profile case: bit mask of axes (bit 0 = x) on the alternative FFT plan")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -548,7 +553,7 @@ def main():
     ap.add_argument("--adjoint-fp64", action="store_true", help="adjoint workloads: FP64 sweep of the FP32 context")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args.profile_case, args.profile_blocks, args.pass_variant)
+        run_profile_case(args.profile_case, args.profile_blocks, args.pass_variant, args.profile_plans)
         return
     if args.warmup < 3:
         args.warmup = 3

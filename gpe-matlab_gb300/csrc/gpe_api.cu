@@ -1812,15 +1812,18 @@ gpe_status gpe_solve_split_batch(gpe_ctx** ctxs, int count, const gpe_split_para
 
 gpe_status gpe_autotune(gpe_ctx* c, int mode, int* chosen) {
   CHECK(check_ctx(c));
-  if (mode < 0 || mode > 3)
-    return fail(c, GPE_ERR_INVALID, "autotune mode must be 0 (off), 1 (now), 2 (auto) or 3 (alternative plans)");
+  if (mode < 0 || (mode > 3 && (mode < 16 || mode > 23)))
+    return fail(c, GPE_ERR_INVALID,
+                "autotune mode must be 0 (off), 1 (now), 2 (auto), 3 (alternative plans) or 16 + axis mask");
   int ch[3] = {-1, -1, -1};
-  if (mode == 0 || mode == 3) {
-    // fixed plans: the defaults, or (mode 3, FP32) the alternative wherever one exists
+  if (mode == 0 || mode == 3 || mode >= 16) {
+    // fixed plans: the defaults, the alternative wherever one exists (3), or
+    // the alternative on the axes of bit mask mode - 16 (bit 0 = x) (FP32)
+    const int mask = mode == 3 ? 7 : mode >= 16 ? mode - 16 : 0;
     c->tune_mode = mode == 0 ? 0 : 1;
-    c->tuned = mode == 3;
+    c->tuned = mode != 0;
     for (int ax = 0; ax < c->ndims; ++ax) {
-      const int v = (mode == 3 && c->prec == GPE_FP32 && has_alt_plan(c->n[ax])) ? 1 : 0;
+      const int v = ((mask >> ax) & 1) && c->prec == GPE_FP32 && has_alt_plan(c->n[ax]) ? 1 : 0;
       if (c->main.plan_var[ax] == v) continue;
       c->main.plan_var[ax] = v;
       if (c->prec == GPE_FP32) CHECK(build_axis_tables<float>(c, c->main, ax));

@@ -97,7 +97,10 @@ struct ContigLayout {
 template <class P, typename R>
 struct StridedLayout {
   static constexpr int T = P::T;
-  static constexpr int G = 128 / (int)sizeof(cx<R>);  // pencils per 128-byte row
+  // Adjacent pencils per CTA: one 128-byte row.  (64-byte rows, which halve
+  // the CTA of T > 16 plans, measured 5% faster on the 512^3 x pass and 28%
+  // slower on the z pass, whose rows are 2 MB apart.)
+  static constexpr int G = 128 / (int)sizeof(cx<R>);
   static constexpr int F0 = (GPE_DIRECT_CTA_THREADS / T > G) ? GPE_DIRECT_CTA_THREADS / T : G;
   static constexpr int FFTS = (F0 * T > 1024) ? 1024 / T : F0;
   static constexpr int THREADS = FFTS * T;
@@ -112,8 +115,8 @@ struct StridedLayout {
     t = tid / FFTS;
   }
   static __device__ __forceinline__ Pol pol(int f) { return Pol{f}; }
-  // (A 32-bit or shift form of this division made ptxas schedule the table
-  // loads earlier and spill ~150 bytes in the step kernel: measured slower.)
+  // (32-bit and shift forms of this division made ptxas spill 130-150 bytes
+  // in the strided step kernel, and it measured slower.)
   static __device__ __forceinline__ long long base(const PassArgs<R>& a, long long b) {
     return (b % a.inner) + (b / a.inner) * a.outer;
   }

@@ -267,7 +267,9 @@ GPE_API gpe_status gpe_norm_noalloc(const void *d_psi, long long npoints, int pr
  * mode 0: default plans, no tuning; 1: tune now; 2 (default): tune on the
  * first groundstate_itp / solve_split / observables / adjoint call when the
  * grid has >= 2^20 points, and for every context of solve_split_batch;
- * 3: use the alternative plan wherever one exists (testing, measurement).
+ * 3: use the alternative plan wherever one exists (testing, measurement);
+ * 16 + m (m = 0..7): the alternative plan on the axes of bit mask m (bit 0 =
+ * x, 1 = y, 2 = z), the default elsewhere (reproducing a tuned choice).
  * chosen (may be NULL) receives the plan variant of axes x, y, z (0 default,
  * 1 alternative, -1 for a length with one plan, FP64 contexts, 2D z). */
 GPE_API gpe_status gpe_autotune(gpe_ctx *ctx, int mode, int *chosen);
