@@ -26,6 +26,11 @@ struct Field {
   bool phase_valid = false;
   bool V_valid = false;
   int plan_var[3] = {0, 0, 0};                   // per axis: FFT plan variant (plans.cuh PlanSel)
+  // Rotating frame (scalar omega): per axis x (0) and y (1)
+  void* kp[3] = {nullptr, nullptr, nullptr};     // permuted k/N, N real (energy weights)
+  void* rot[2] = {nullptr, nullptr};             // [transverse index][slot] complex factors of the step
+  void* rotw[2] = {nullptr, nullptr};            // per transverse index: -omega*y (x) / +omega*x (y)
+  double rotw_omega = 0.0;                       // omega the rotw arrays hold
 };
 
 struct ProfRec {

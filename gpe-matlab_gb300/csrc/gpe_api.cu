@@ -124,16 +124,38 @@ struct AxisPass {
   int N;
   bool strided;
   long long n_batch, stride, inner, outer;
+  int rot = 0;  // rotating frame: 1 = x pass with exp(+kx y omega dt/2), 2 = y pass with exp(-ky x omega dt)
 };
 
 // Pass order: y (contiguous, carries the prologue), x, then z (3D).  The
-// last pass carries the epilogue.
+// last pass carries the epilogue.  Rotating frame (scalar omega,
+// ssft_kin_step.m:12-15): x half step, y (and z), x half step again.
 std::vector<AxisPass> axis_passes(const gpe_ctx* c) {
   const long long nx = c->n[0], ny = c->n[1], nz = c->ndims == 3 ? c->n[2] : 1;
+  const AxisPass py{1, (int)ny, false, nx * nz, 1, 1, 0};
+  const AxisPass px{0, (int)nx, true, ny * nz, ny, ny, nx * ny};
+  const AxisPass pz{2, (int)nz, true, nx * ny, nx * ny, nx * ny, 0};
   std::vector<AxisPass> v;
-  v.push_back({1, (int)ny, false, nx * nz, 1, 1, 0});
-  v.push_back({0, (int)nx, true, ny * nz, ny, ny, nx * ny});
-  if (c->ndims == 3) v.push_back({2, (int)nz, true, nx * ny, nx * ny, nx * ny, 0});
+  if (c->prm.omega != 0.0) {
+    AxisPass rx = px, ry = py;
+    rx.rot = 1;
+    ry.rot = 2;
+    v.push_back(rx);
+    v.push_back(ry);
+    if (c->ndims == 3) v.push_back(pz);
+    v.push_back(rx);
+    return v;
+  }
+  v.push_back(py);
+  v.push_back(px);
+  if (c->ndims == 3) v.push_back(pz);
+  return v;
+}
+
+// One pass per axis (energy sums): the axis passes without the second x half.
+std::vector<AxisPass> energy_axes(const gpe_ctx* c) {
+  std::vector<AxisPass> v = axis_passes(c);
+  if (c->prm.omega != 0.0) v.pop_back();
   return v;
 }
 
@@ -197,6 +219,7 @@ template <typename R>
 bool use_tma(const gpe_ctx* c, const Field& f, const AxisPass& ap) {
   if (c->pass_variant != 1) return false;
   if (f.plan_var[ap.axis] != 0) return false;  // TMA passes are built on Plan<N> only
+  if (ap.rot != 0) return false;                // and without the rotating-frame terms
   if (dispatch_tma_smem<R>(ap.N, ap.strided) > 200 * 1024) return false;
   const int ffts = dispatch_tma_ffts<R>(ap.N, ap.strided);
   if (!ap.strided) return true;
@@ -381,15 +404,40 @@ gpe_status build_axis_tables(gpe_ctx* c, Field& f, int ax) {
     CHECK(upload_cx<R>(c, f.tws[ax], rows));
     if (!f.php[ax]) CU(cudaMalloc(&f.php[ax], N * 2 * sizeof(R)));
     if (!f.k2p[ax]) CU(cudaMalloc(&f.k2p[ax], N * sizeof(R)));
-    std::vector<R> k2(N);
+    if (!f.kp[ax]) CU(cudaMalloc(&f.kp[ax], N * sizeof(R)));
+    std::vector<R> k2(N), k1(N);
     for (int t = 0; t < pi.T; ++t)
       for (int m = 0; m < pi.E; ++m) {
         const double k = kval(c, ax, plan_spec_pos(pi, t, m));
         k2[m * pi.T + t] = (R)(k * k / 2.0 / N);
+        k1[m * pi.T + t] = (R)(k / N);
       }
     CU(cudaMemcpy(f.k2p[ax], k2.data(), N * sizeof(R), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(f.kp[ax], k1.data(), N * sizeof(R), cudaMemcpyHostToDevice));
   }
   f.phase_valid = false;
+  return GPE_OK;
+}
+
+// Coordinate of grid index i along axis ax: linspace(-xmax, xmax, n)
+// (grid2d/init.m:12-13), xmax = span/2.
+double coord(const gpe_ctx* c, int ax, int i) { return -0.5 * c->span[ax] + i * c->dx[ax]; }
+
+// Rotating-frame weights of the energy sums (lap.m:8-10): the x pass adds
+// -omega*y*kx, the y pass +omega*x*ky, y and x being the pencil's transverse
+// coordinate: rotw[0][iy] = -omega*y(iy), rotw[1][ix] = +omega*x(ix).
+template <typename R>
+gpe_status ensure_rot_weights(gpe_ctx* c, Field& f) {
+  const double om = c->prm.omega;
+  if (om == 0.0 || (f.rotw[0] && f.rotw_omega == om)) return GPE_OK;
+  for (int r = 0; r < 2; ++r) {
+    const int tax = r == 0 ? 1 : 0;  // transverse axis: y for x pencils, x for y pencils
+    std::vector<R> w(c->n[tax]);
+    for (int i = 0; i < c->n[tax]; ++i) w[i] = (R)((r == 0 ? -om : om) * coord(c, tax, i));
+    if (!f.rotw[r]) CU(cudaMalloc(&f.rotw[r], w.size() * sizeof(R)));
+    CU(cudaMemcpy(f.rotw[r], w.data(), w.size() * sizeof(R), cudaMemcpyHostToDevice));
+  }
+  f.rotw_omega = om;
   return GPE_OK;
 }
 
@@ -402,21 +450,49 @@ gpe_status build_static_tables(gpe_ctx* c, Field& f) {
 // kinop = exp(-kk*dt) (set_kinop.m:9), as one factor per axis with the 1/N of
 // ifft folded in: exp(-k^2/2*dt)/N, dt = dre + i*dim, evaluated in FP64 and
 // stored in the threads' spectrum-slot order.
+//
+// Rotating frame (scalar omega, set_kinop.m:5-7): the x factor is taken over
+// half a step, exp(-(kx^2/2 - kx y omega) dt/2) (applied twice per step), the
+// y factor exp(-(ky^2/2 + ky x omega) dt) and z as without rotation.  The
+// k^2 part stays in the per-axis table; the cross term, which depends on the
+// pencil's transverse coordinate, is a second table rot[ax][i][slot] =
+// exp(+kx y(i) omega dt/2) (x) or exp(-ky x(i) omega dt) (y).
 template <typename R>
 gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
   if (f.phase_valid && f.phase_dt[0] == dre && f.phase_dt[1] == dim) return GPE_OK;
+  const double om = c->prm.omega;
   for (int ax = 0; ax < c->ndims; ++ax) {
     const int N = c->n[ax];
     const PlanInfo pi = dispatch_plan(N, f.plan_var[ax]);
+    const double h = (om != 0.0 && ax == 0) ? 0.5 : 1.0;  // x takes half steps in the rotating frame
     std::vector<std::complex<double>> ph(N);
     for (int t = 0; t < pi.T; ++t)
       for (int m = 0; m < pi.E; ++m) {
         const double k = kval(c, ax, plan_spec_pos(pi, t, m));
         const double kk = k * k / 2.0;
-        const double mag = std::exp(-kk * dre) / N;
-        ph[slot_index<R>(pi.T, t, m)] = std::complex<double>(mag * std::cos(kk * dim), -mag * std::sin(kk * dim));
+        const double mag = std::exp(-kk * dre * h) / N;
+        ph[slot_index<R>(pi.T, t, m)] =
+            std::complex<double>(mag * std::cos(kk * dim * h), -mag * std::sin(kk * dim * h));
       }
     CHECK(upload_cx<R>(c, f.php[ax], ph));
+    if (om != 0.0 && ax < 2) {
+      const int tax = ax == 0 ? 1 : 0;  // transverse axis of the pencils
+      const int nt = c->n[tax];
+      const double s = ax == 0 ? 0.5 * om : -om;
+      std::vector<std::complex<double>> rt((size_t)nt * N);
+      for (int i = 0; i < nt; ++i) {
+        const double xc = coord(c, tax, i);
+        for (int t = 0; t < pi.T; ++t)
+          for (int m = 0; m < pi.E; ++m) {
+            const double a = s * kval(c, ax, plan_spec_pos(pi, t, m)) * xc;  // exp(a*(dre + i dim))
+            const double mag = std::exp(a * dre);
+            rt[(size_t)i * N + slot_index<R>(pi.T, t, m)] =
+                std::complex<double>(mag * std::cos(a * dim), mag * std::sin(a * dim));
+          }
+      }
+      if (!f.rot[ax]) CU(cudaMalloc(&f.rot[ax], rt.size() * 2 * sizeof(R)));
+      CHECK(upload_cx<R>(c, f.rot[ax], rt));
+    }
   }
   f.phase_dt[0] = dre;
   f.phase_dt[1] = dim;
@@ -453,6 +529,11 @@ void free_field(Field& f, const double* V64) {
     cudaFree(f.tws[i]);
     cudaFree(f.php[i]);
     cudaFree(f.k2p[i]);
+    cudaFree(f.kp[i]);
+  }
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(f.rot[i]);
+    cudaFree(f.rotw[i]);
   }
   f = Field();
 }
@@ -510,6 +591,18 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.drer = (R)dre;
   a.dimr = (R)dim;
   a.prefetch = c->pass_variant == 0;
+  if (ap.rot != 0) {
+    const int r = ap.rot - 1;  // 0: x pencils (transverse y), 1: y pencils (transverse x)
+    a.rot_period = c->n[r == 0 ? 1 : 0];
+    if (kind == KIND_STEP) {
+      a.rot = (const cx<R>*)f.rot[r];
+      if (!a.rot) return fail(c, GPE_ERR_STATE, "rotating frame: kinetic factors not set");
+    } else {
+      a.rotw = (const R*)f.rotw[r];
+      a.kp = (const R*)f.kp[ap.axis];
+      if (!a.rotw) return fail(c, GPE_ERR_STATE, "rotating frame: energy weights not set");
+    }
+  }
   const double P = (double)c->P;
   double bytes = (kind == KIND_ENERGY ? 1.0 : 2.0) * P * 2 * sizeof(R);
   const bool useV = pro == PRO_RT_HALF || pro == PRO_RT_FULL || pro == PRO_ITP || epi == EPI_RT_END ||
@@ -541,7 +634,8 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
 // also sums n, Vn, n^2 and every pass applies the pending scale.
 template <typename R>
 gpe_status energy_passes(gpe_ctx* c, Field& f, bool pot, int nblk_kin[3], int* nblk_pot) {
-  auto passes = axis_passes(c);
+  CHECK(ensure_rot_weights<R>(c, f));
+  auto passes = energy_axes(c);
   nblk_kin[0] = nblk_kin[1] = nblk_kin[2] = 0;
   for (auto& ap : passes) {
     int nb = 0;
@@ -1591,8 +1685,12 @@ gpe_status gpe_set_params(gpe_ctx* c, const gpe_params* p) {
   if (p->itp_max_iter < 1) return fail(c, GPE_ERR_INVALID, "itp_max_iter must be >= 1");
   if (p->itp_min_iter < 0) return fail(c, GPE_ERR_INVALID, "itp_min_iter must be >= 0");
   if (!std::isfinite(p->g) || !std::isfinite(p->gamma) || !std::isfinite(p->Ntotal) ||
-      !std::isfinite(p->mu_init) || !std::isfinite(p->decay_rate) || p->gamma < 0)
+      !std::isfinite(p->mu_init) || !std::isfinite(p->decay_rate) || p->gamma < 0 || !std::isfinite(p->omega))
     return fail(c, GPE_ERR_INVALID, "parameters must be finite, gamma >= 0");
+  if (p->omega != c->prm.omega) {  // the kinetic factors and rotation tables depend on omega
+    c->main.phase_valid = false;
+    c->polish.phase_valid = false;
+  }
   c->prm = *p;
   return GPE_OK;
 }
@@ -1765,6 +1863,7 @@ gpe_status gpe_adjoint_grad(gpe_ctx* c, const gpe_adjoint_params* prm, const dou
   if (c->prm.gamma != 0.0 || c->prm.decay_rate > 0)
     return fail(c, GPE_ERR_UNSUPPORTED,
                 "adjoint: only gamma = 0 and decay_rate = 0 (conservative dynamics) are differentiated");
+  if (c->prm.omega != 0.0) return fail(c, GPE_ERR_UNSUPPORTED, "adjoint: the rotating frame is not differentiated");
   const int prec = prm->precision ? prm->precision : c->prec;
   if (prec != GPE_FP32 && prec != GPE_FP64) return fail(c, GPE_ERR_INVALID, "adjoint: precision must be 0, GPE_FP32 or GPE_FP64");
   if (prec == GPE_FP32 && c->prec == GPE_FP64)

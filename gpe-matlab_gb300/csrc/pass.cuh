@@ -420,8 +420,16 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
     }
     St::template forward<false>(v, sm, pol, t, a.tws);
     Kahan<R> kin;
+    if (a.rotw) {
+      // rotating frame (lap.m:8-9): weight k^2/2 -+ omega * coordinate * k
+      const R w = valid ? a.rotw[(unsigned)b % (unsigned)a.rot_period] : R(0);
 #pragma unroll
-    for (int m = 0; m < E; ++m) kin.add(__ldg(a.k2p + m * T + t) * norm2(v[m]));
+      for (int m = 0; m < E; ++m)
+        kin.add((__ldg(a.k2p + m * T + t) + w * __ldg(a.kp + m * T + t)) * norm2(v[m]));
+    } else {
+#pragma unroll
+      for (int m = 0; m < E; ++m) kin.add(__ldg(a.k2p + m * T + t) * norm2(v[m]));
+    }
     Kahan<R> sums[4];
     int slots[4];
     int nred;
@@ -457,6 +465,11 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
     constexpr bool SMT = SmemTables<R, P, KIND>::value;
     St::template forward<SMT>(v, sm, pol, t, tws);
     apply_phase<T, E, SMT>(v, php, t);
+    if (a.rot) {
+      // rotating frame: the cross term of this pencil's transverse coordinate
+      const unsigned ci = valid ? (unsigned)b % (unsigned)a.rot_period : 0u;
+      apply_phase<T, E, false>(v, a.rot + (size_t)ci * P::N, t);
+    }
     St::template inverse<SMT>(v, sm, pol, t, tws);
     Kahan<R> acc[3];
     if (a.epi != EPI_NONE) {

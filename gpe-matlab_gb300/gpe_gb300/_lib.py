@@ -30,7 +30,7 @@ class gpe_grid_desc(C.Structure):
 class gpe_params(C.Structure):
     _fields_ = [("g", C.c_double), ("gamma", C.c_double), ("decay_rate", C.c_double), ("Ntotal", C.c_double),
                 ("mu_init", C.c_double), ("n_recalc", C.c_int), ("itp_max_iter", C.c_int),
-                ("itp_min_iter", C.c_int), ("itp_adjust_stepsize", C.c_int)]
+                ("itp_min_iter", C.c_int), ("itp_adjust_stepsize", C.c_int), ("omega", C.c_double)]
 
 
 class gpe_itp_params(C.Structure):

@@ -8,7 +8,8 @@ GPU; this class only packs properties, uploads arrays, evaluates host-side
 callbacks (time-dependent potential, user callback) and exposes the results.
 
 Differences from the reference, all deliberate:
-* ``omega`` (rotating frame) is not part of this hot path; nonzero values raise.
+* ``omega``: a scalar rotating frame runs on the GPU (set_kinop.m:5-7,
+  ssft_kin_step.m:12-15); the array-omega Lz Crank-Nicolson branch raises.
 * ``'rand'`` initial states use a seeded numpy generator (the reference calls
   an unseeded ``rand``, GPEtask.m:49-52).
 * ``show_image`` and the console status line are not implemented (UI).
@@ -97,9 +98,10 @@ class GPEtask:
         self._state_on_device = None
 
     def _push_params(self):
-        if self.omega != 0:
-            raise NotImplementedError("omega != 0 (rotating frame) is not supported by libgpe")
+        if np.size(self.omega) != 1:
+            raise NotImplementedError("array omega (Lz Crank-Nicolson, ssft_kin_step.m:3-11) is not supported")
         p = L.gpe_params()
+        p.omega = float(self.omega)
         p.g = float(self.g)
         p.gamma = float(self.gamma)
         p.decay_rate = float(self.decay_rate)

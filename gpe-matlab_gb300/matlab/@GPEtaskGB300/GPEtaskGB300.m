@@ -133,9 +133,12 @@ classdef GPEtaskGB300 < GPEtask
 
     methods (Access = protected)
         function gb300_push(task)
+            if ~isscalar(task.omega)
+                error('gpe:omega', 'array omega (Lz Crank-Nicolson) is not supported by libgpe');
+            end
             gpe_mex('set_params', task.gb300_handle, task.g, task.gamma, task.decay_rate, ...
                 task.Ntotal, task.mu_init, task.n_recalc, task.itp_max_iter, task.itp_min_iter, ...
-                double(task.itp_adjust_stepsize));
+                double(task.itp_adjust_stepsize), double(task.omega));
             n = task.current_n;
             if isempty(n)
                 n = 0;

@@ -116,7 +116,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (cmd == "destroy") {
     gpe_destroy(c);
   } else if (cmd == "set_params") {
-    if (nrhs != 11) mexErrMsgIdAndTxt("gpe:usage", "set_params needs 9 values");
+    if (nrhs != 11 && nrhs != 12) mexErrMsgIdAndTxt("gpe:usage", "set_params needs 9 or 10 values");
     gpe_params p;
     gpe_default_params(&p);
     p.g = scalar(prhs[2]);
@@ -128,6 +128,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     p.itp_max_iter = (int)scalar(prhs[8]);
     p.itp_min_iter = (int)scalar(prhs[9]);
     p.itp_adjust_stepsize = (int)scalar(prhs[10]);
+    if (nrhs == 12) p.omega = scalar(prhs[11]);  // scalar rotating frame
     check(c, gpe_set_params(c, &p));
   } else if (cmd == "set_current") {
     gpe_current cur;

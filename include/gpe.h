@@ -79,6 +79,9 @@ typedef struct {
     int itp_max_iter;       /* ITP iteration cap                         [5000] */
     int itp_min_iter;       /* ITP iterations before the first check     [50]   */
     int itp_adjust_stepsize;/* halve dt on convergence until dt < dtmin  [0]    */
+    double omega;           /* rotation frequency of a rotating frame    [0]:
+                               set_kinop.m:5-7, ssft_kin_step.m:12-15, lap.m:8-10
+                               (scalar omega; the adjoint needs omega = 0)       */
 } gpe_params;
 
 /* Imaginary-time propagation, lib/@GPEtask/groundstate_itp.m:1-112. */

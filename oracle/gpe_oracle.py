@@ -103,6 +103,8 @@ class Grid:
             self.mesh = {"x": X, "y": Y, "z": 0.0}
             self.weight = self.dx * self.dy                    # init.m:36
             self.shape = (self.nx, self.ny)
+            self.KX, self.KY, self.KZ = KX, KY, 0.0
+            self.axis = {"x": 0, "y": 1}
         else:
             KZ, KX, KY = np.meshgrid(kz, kx, ky, indexing="ij")
             self.kk = (KX ** 2 + KY ** 2 + KZ ** 2) / 2        # grid3d/init.m:76
@@ -110,6 +112,8 @@ class Grid:
             self.mesh = {"x": X, "y": Y, "z": Z}               # grid3d/init.m:79-82
             self.weight = self.dx * self.dy * self.dz          # grid3d/init.m:83
             self.shape = (self.nz, self.nx, self.ny)
+            self.KX, self.KY, self.KZ = KX, KY, KZ
+            self.axis = {"x": 1, "y": 2, "z": 0}
 
     # lib/@grid2d/fft.m:11, lib/@grid3d/fft.m:11
     def fft(self, f):
@@ -135,16 +139,33 @@ class Grid:
     def normalize(self, psi):
         return psi * (1.0 / self.norm(psi))
 
-    # lib/@grid2d/lap.m:5-6, lib/@grid3d/lap.m:5-6 (omega == 0 branch)
-    def lap(self, phi):
-        return self.ifft(self.kk * self.fft(phi))
+    # lib/@grid2d/fftx.m:11 (dim 2 = x), ffty.m:11 (dim 1 = y),
+    # lib/@grid3d/fftz.m:11 (dim 3 = z) and the ifftx/iffty/ifftz files:
+    # 1D transforms along one axis, same conventions as fft/ifft.
+    def fft1(self, f, ax):
+        return sfft.fft(f, axis=self.axis[ax], workers=_WORKERS)
+
+    def ifft1(self, f, ax):
+        return sfft.ifft(f, axis=self.axis[ax], workers=_WORKERS)
+
+    # lib/@grid2d/lap.m:5-10, lib/@grid3d/lap.m:5-11
+    def lap(self, phi, omega=0.0):
+        if omega == 0:
+            return self.ifft(self.kk * self.fft(phi))
+        Y, X = self.mesh["y"], self.mesh["x"]
+        res = self.ifft1((self.KX ** 2 / 2 - self.KX * Y * omega) * self.fft1(phi, "x"), "x") + \
+            self.ifft1((self.KY ** 2 / 2 + self.KY * X * omega) * self.fft1(phi, "y"), "y")
+        if self.ndims == 3:
+            res = res + self.ifft1((self.KZ ** 2 / 2) * self.fft1(phi, "z"), "z")
+        return res
 
 
 # ---------------------------------------------------------------------------
 # Solver: lib/@GPEtask
 # ---------------------------------------------------------------------------
 class GPEtask:
-    """lib/@GPEtask/GPEtask.m:1-167, omega == 0 branch only."""
+    """lib/@GPEtask/GPEtask.m:1-167: omega == 0 and scalar omega (rotating
+    frame); the array-omega (Lz Crank-Nicolson) branches are not restated."""
 
     def __init__(self, grid: Grid, trappot):
         # GPEtask.m:41-60 (rng('shuffle') and the FFTW planner are not numerics)
@@ -191,11 +212,11 @@ class GPEtask:
             time = self.current_time
         return self.applyh0(phi, time) + self.g * np.abs(phi) ** 2 * phi
 
-    # GPEtask.m:80-95 (omega == 0)
+    # GPEtask.m:80-95 (scalar omega; the array-omega Lz term :92-94 is not restated)
     def applyh0(self, phi, time=None):
         if time is None:
             time = self.current_time
-        return self.getVtotal(time) * phi + self.grid.lap(phi)
+        return self.getVtotal(time) * phi + self.grid.lap(phi, self.omega)
 
     # GPEtask.m:97-107
     def get_energy(self, phi=None, time=None):
@@ -258,13 +279,26 @@ class GPEtask:
             mu = (mul + mur) / 2
         return np.sqrt(vvv / self.g), mu
 
-    # lib/@GPEtask/set_kinop.m:1-11 (omega == 0 branch, :9)
+    # lib/@GPEtask/set_kinop.m:1-11 (scalar omega: :5-7, omega == 0: :9)
     def set_kinop(self, dt):
-        self.kinop = np.exp(-self.grid.kk * dt)
+        grid = self.grid
+        if self.omega != 0:
+            self.kinop = np.exp(-(grid.KX ** 2 / 2 - grid.KX * grid.mesh["y"] * self.omega) * dt / 2)
+            self.kinop2 = np.exp(-(grid.KY ** 2 / 2 + grid.KZ ** 2 / 2 + grid.KY * grid.mesh["x"] * self.omega) * dt)
+        else:
+            self.kinop = np.exp(-grid.kk * dt)
 
-    # lib/@GPEtask/ssft_kin_step.m:17
+    # lib/@GPEtask/ssft_kin_step.m:12-17
     def ssft_kin_step(self, phi, dt):
-        return self.grid.ifft(self.kinop * self.grid.fft(phi))
+        grid = self.grid
+        if self.omega != 0:
+            phi = grid.ifft1(self.kinop * grid.fft1(phi, "x"), "x")                 # :13
+            if grid.ndims == 3:                                                      # :14
+                phi = grid.ifft1(grid.ifft1(self.kinop2 * grid.fft1(grid.fft1(phi, "y"), "z"), "z"), "y")
+            else:
+                phi = grid.ifft1(self.kinop2 * grid.fft1(phi, "y"), "y")
+            return grid.ifft1(self.kinop * grid.fft1(phi, "x"), "x")                # :15
+        return grid.ifft(self.kinop * grid.fft(phi))
 
     # lib/@GPEtask/groundstate_itp.m:1-112
     def groundstate_itp(self, dt, eps, phi0="rand", nargout=4, rng=None):

@@ -13,7 +13,7 @@ int main(void) {
     printf("{");
     S(gpe_grid_desc); F(gpe_grid_desc, n); F(gpe_grid_desc, dx); F(gpe_grid_desc, span);
     F(gpe_grid_desc, precision); F(gpe_grid_desc, device);
-    S(gpe_params); F(gpe_params, n_recalc); F(gpe_params, itp_adjust_stepsize);
+    S(gpe_params); F(gpe_params, n_recalc); F(gpe_params, itp_adjust_stepsize); F(gpe_params, omega);
     S(gpe_itp_params); F(gpe_itp_params, fp64_polish); F(gpe_itp_params, switch_delta);
     S(gpe_itp_result); F(gpe_itp_result, final_dt); F(gpe_itp_result, last_delta);
     S(gpe_split_params); F(gpe_split_params, vtd); F(gpe_split_params, on_step); F(gpe_split_params, step_user);

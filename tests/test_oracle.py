@@ -163,6 +163,37 @@ def test_oracle_adjoint_matches_central_differences(axes):
         assert abs((lp - lm) / (2 * eps) - ad) < 1e-7 * abs(ad)
 
 
+def test_rotating_frame_keeps_the_isotropic_ground_state():
+    """Scalar omega (set_kinop.m:5-7, ssft_kin_step.m:12-15, lap.m:8-9): the
+    nodeless ground state of an isotropic trap has Lz psi = 0, so a slowly
+    rotating frame leaves the ITP fixed point and its energy unchanged."""
+    g = O.Grid(6, 32, 6, 32)
+    X, Y = g.mesh["x"], g.mesh["y"]
+    out = []
+    for om in (0.0, 0.3):
+        t = O.GPEtask(g, lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2))
+        t.Ntotal, t.g, t.omega = 10.0, 1.0, om
+        phi = t.groundstate_itp(0.01, 1e-9, np.exp(-(X ** 2 + Y ** 2) / 2).astype(complex), nargout=1)[0]
+        out.append((phi, t.get_energy(phi)))
+    assert np.linalg.norm(out[1][0] - out[0][0]) / np.linalg.norm(out[0][0]) < 1e-5
+    assert out[1][1] == pytest.approx(out[0][1], rel=1e-9)
+
+
+def test_rotating_frame_dynamics_conserve_norm_and_energy():
+    """gamma = 0 in a rotating anisotropic trap: the split step conserves the
+    norm exactly and the rotating-frame energy to the splitting error."""
+    g = O.Grid(6, 32, 6, 32, 4, 16)
+    t = O.GPEtask(g, lambda X, Y, Z: 0.5 * (X ** 2 + 1.2 * Y ** 2 + Z ** 2))
+    t.g, t.omega = 1.0, 0.4
+    X, Y, Z = g.mesh["x"], g.mesh["y"], g.mesh["z"]
+    psi = np.exp(-((X - 1) ** 2 + Y ** 2 + Z ** 2) / 2).astype(complex) * np.exp(0.2j * Y)
+    t.init_state = psi
+    E0 = t.get_energy(psi)
+    phi = t.solve_split(0.002, 20, 2)
+    assert g.integrate(np.abs(phi) ** 2) == pytest.approx(g.integrate(np.abs(psi) ** 2), rel=1e-12)
+    assert t.get_energy(phi) == pytest.approx(E0, rel=1e-6)
+
+
 def test_golden_fixtures_reproduce():
     from tests.golden import make_golden as MG
 
