@@ -137,12 +137,62 @@ void launch_cscale(cx<R>* out, const cx<R>* in, long long n, double cr, double c
   k_cscale<R><<<elem_grid(n, ADJ_THREADS), ADJ_THREADS, 0, s>>>(out, in, n, cr, ci);
 }
 
+// ---- stochastic GPE (lib/@SGPEtask/solve_split.m:57-66) ----------------------
+// psi <- exp((mu - V - g|s psi|^2) dt') s psi with dt' = (dre + i dim) * frac
+// (frac = 1/2 at a block start, 1 after a kinetic step), s = the pending scale
+// at a block start, then psi <- psi + sigma (n1 + i n2) with n1, n2 the
+// normal variates of gauss2(seed, step, point index).
+template <typename R>
+__global__ void k_sgpe_nl_noise(cx<R>* __restrict__ psi, const R* __restrict__ V, long long n, DevScalars* sc,
+                                R g, R dre, R dim, int half, R sigma, unsigned long long seed,
+                                unsigned long long step) {
+  if (sc->stop) return;
+  const R s = half ? (R)sc->scale : R(1);
+  const R mu = (R)sc->mu;
+  const R f = half ? R(0.5) : R(1);
+  for (long long i = (long long)blockIdx.x * ADJ_THREADS + threadIdx.x; i < n;
+       i += (long long)gridDim.x * ADJ_THREADS) {
+    cx<R> p = psi[i];
+    p = mk<R>(p.x * s, p.y * s);
+    const R a = (mu - V[i] - g * norm2(p)) * f;
+    p = cmul(cexp_real_times(a, dre, dim), p);
+    if (sigma != R(0)) {
+      const cx<R> z = gauss2<R>(seed, step, (unsigned long long)i);
+      p = mk<R>(p.x + sigma * z.x, p.y + sigma * z.y);
+    }
+    psi[i] = p;
+  }
+}
+
+template <typename R>
+void launch_sgpe_nl_noise(cx<R>* psi, const R* V, long long n, DevScalars* sc, double g, double dre, double dim,
+                          int half, double sigma, unsigned long long seed, unsigned long long step, cudaStream_t s) {
+  k_sgpe_nl_noise<R><<<elem_grid(n, ADJ_THREADS), ADJ_THREADS, 0, s>>>(psi, V, n, sc, (R)g, (R)dre, (R)dim, half,
+                                                                      (R)sigma, seed, step);
+}
+
+__global__ void k_selftest_noise(float* out, long long n, unsigned long long seed, unsigned long long step) {
+  for (long long i = (long long)blockIdx.x * ADJ_THREADS + threadIdx.x; i < n;
+       i += (long long)gridDim.x * ADJ_THREADS) {
+    const cx<float> z = gauss2<float>(seed, step, (unsigned long long)i);
+    out[2 * i] = z.x;
+    out[2 * i + 1] = z.y;
+  }
+}
+cudaError_t launch_selftest_noise(float* out, long long n, unsigned long long seed, unsigned long long step,
+                                  cudaStream_t s) {
+  k_selftest_noise<<<elem_grid(n, ADJ_THREADS), ADJ_THREADS, 0, s>>>(out, n, seed, step);
+  return cudaGetLastError();
+}
+
 #define INST_ADJ(R)                                                                                     \
   template void launch_nl_phase<R>(cx<R>*, const R*, long long, double, double, cudaStream_t);         \
   template void launch_adj_nl<R>(cx<R>*, const cx<R>*, const R*, double*, long long, double, double,   \
                                  int, int, int, int, cudaStream_t);                                    \
   template int launch_inner<R>(const cx<R>*, const cx<R>*, long long, double*, cudaStream_t);          \
-  template void launch_cscale<R>(cx<R>*, const cx<R>*, long long, double, double, cudaStream_t);
+  template void launch_cscale<R>(cx<R>*, const cx<R>*, long long, double, double, cudaStream_t);        \
+  template void launch_sgpe_nl_noise<R>(cx<R>*, const R*, long long, DevScalars*, double, double, double, int, \
+                                        double, unsigned long long, unsigned long long, cudaStream_t);
 INST_ADJ(float)
 INST_ADJ(double)
 

@@ -165,6 +165,8 @@ __global__ void k_finalize_block(const BlockFinalArgs a, DevScalars* sc) {
     const double s2 = scale * scale;
     muc = (s2 * (kin + vn) * w + s2 * s2 * a.g * n2 * w) / NNN;
     sc->mu = muc;
+  } else if (a.fixed_mu) {  // SGPEtask solve_split.m:52,78
+    muc = sc->mu;
   } else {  // solve_split.m:76-77
     muc = (kin + vn + a.g * n2) * w / ncur;
   }

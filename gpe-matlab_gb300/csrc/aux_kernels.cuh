@@ -20,6 +20,7 @@ struct BlockFinalArgs {
   double* hist_mu;       // nullptr or &history[j]
   double* hist_n;
   int* hist_ok;
+  int fixed_mu = 0;      // report sc->mu (the stochastic GPE's mu_init) instead of <psi|H psi>/N
 };
 
 struct ItpFinalArgs {
@@ -78,6 +79,13 @@ template <typename R>
 int launch_inner(const cx<R>* a, const cx<R>* b, long long n, double* partials, cudaStream_t s);
 template <typename R>
 void launch_cscale(cx<R>* out, const cx<R>* in, long long n, double cr, double ci, cudaStream_t s);
+
+// Stochastic GPE nonlinear factor + noise (adjoint_kernels.cu).
+template <typename R>
+void launch_sgpe_nl_noise(cx<R>* psi, const R* V, long long n, DevScalars* sc, double g, double dre, double dim,
+                          int half, double sigma, unsigned long long seed, unsigned long long step, cudaStream_t s);
+cudaError_t launch_selftest_noise(float* out, long long n, unsigned long long seed, unsigned long long step,
+                                  cudaStream_t s);
 
 template <typename R>
 int launch_norm(const cx<R>* psi, long long n, DevScalars* sc, double* partials, int cap, cudaStream_t s);

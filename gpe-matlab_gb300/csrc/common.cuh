@@ -72,6 +72,51 @@ __device__ __forceinline__ cx<double> ld_tab(const cx<double>* p) {
   return mk<double>(v.x, v.y);
 }
 
+// Counter-based random numbers for the stochastic GPE: Philox4x32 with 10
+// rounds (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as
+// 1, 2, 3", SC'11): round = two 32x32->64 multiplies by M0, M1 and xors with
+// the key, which is bumped by the Weyl constants W0, W1 between rounds.
+struct Philox4 {
+  unsigned x, y, z, w;
+};
+__host__ __device__ inline void mulhilo32(unsigned a, unsigned b, unsigned& hi, unsigned& lo) {
+  const unsigned long long p = (unsigned long long)a * b;
+  hi = (unsigned)(p >> 32);
+  lo = (unsigned)p;
+}
+__host__ __device__ inline Philox4 philox4x32_10(Philox4 c, unsigned k0, unsigned k1) {
+  const unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    unsigned hi0, lo0, hi1, lo1;
+    mulhilo32(M0, c.x, hi0, lo0);
+    mulhilo32(M1, c.z, hi1, lo1);
+    c = Philox4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+// Two standard normal variates for (seed, step, point index) by Box-Muller
+// on 24-bit uniforms u1 in (0, 1], u2 in [0, 1) from the first two words.
+template <typename R>
+__device__ __forceinline__ cx<R> gauss2(unsigned long long seed, unsigned long long step, unsigned long long idx) {
+  const Philox4 r = philox4x32_10(Philox4{(unsigned)idx, (unsigned)(idx >> 32), (unsigned)step, (unsigned)(step >> 32)},
+                                  (unsigned)seed, (unsigned)(seed >> 32));
+  const R u1 = (R)((r.x >> 8) + 1u) * (R)5.9604644775390625e-08;  // 2^-24
+  const R u2 = (R)(r.y >> 8) * (R)5.9604644775390625e-08;
+  R s, c;
+  if constexpr (sizeof(R) == 4) {
+    sincospif(2.0f * u2, &s, &c);
+    const float rad = sqrtf(-2.0f * logf(u1));
+    return mk<float>(rad * c, rad * s);
+  } else {
+    sincospi(2.0 * u2, &s, &c);
+    const double rad = sqrt(-2.0 * log(u1));
+    return mk<double>(rad * c, rad * s);
+  }
+}
+
 // Loads of streamed data (state, potential) that a pass reads once: marked
 // evict-first so they do not push the FFT tables out of L1.
 #ifndef GPE_STREAM_LOADS

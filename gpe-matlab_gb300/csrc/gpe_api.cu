@@ -925,11 +925,18 @@ struct SplitRun {
   bool feedback = false;
   std::vector<AxisPass> passes;
   size_t hist_off = 0;  // history slot of outer step j: d_hist + hist_off + 3*(j - start - 1)
+  // Stochastic GPE (SGPEtask.solve_split): mu fixed at mu_init, no
+  // renormalisation, noise sigma * (n1 + i n2) before every kinetic step.
+  bool sgpe = false;
+  double sigma = 0.0;          // sqrt(T gamma ddt / weight), solve_split.m:49
+  unsigned long long seed = 0;
+  int niter_inner = 1;         // for the global step index of the noise counter
 };
 
 // solve_split.m:13-47: NN0, n_rec, complex dt, kinetic factors, initial mu.
 template <typename R>
-gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, int& vk, size_t hist_extra) {
+gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, int& vk, size_t hist_extra,
+                       const gpe_sgpe_params* sg = nullptr) {
   Field& f = c->main;
   const double ddt = prm->ddt;
   const double gam = c->prm.gamma;
@@ -959,17 +966,24 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
   s0.nonfinite = 0;
   s0.NN0 = NN0;
   s0.NNN = NN0;
+  if (sg) s0.mu = c->prm.mu_init;  // SGPE: mu = mu_init throughout (SGPEtask solve_split.m:52)
   CHECK(write_scalars(c, s0));
   // muc/mu at the start (solve_split.m:40-46): applyham at current_time.
   if (prm->vtd) CHECK(vtd_upload<R>(c, prm, c->cur.current_time, vk));
-  CHECK(observables_impl<R>(c, f, NN0, 1, nullptr));
+  if (!sg) CHECK(observables_impl<R>(c, f, NN0, 1, nullptr));
   run.n_rec = n_rec;
   run.start = start;
   run.nout = nout;
   run.ddt = ddt;
   run.dre = dre;
   run.dim = dim;
-  run.feedback = gam > 0 && c->prm.mu_init == 0;
+  run.feedback = gam > 0 && c->prm.mu_init == 0 && !sg;
+  run.niter_inner = prm->niter_inner;
+  if (sg) {
+    run.sgpe = true;
+    run.sigma = std::sqrt(sg->T * gam * ddt / c->weight);
+    run.seed = sg->seed;
+  }
   run.dt_outer = ddt * prm->niter_inner;
   run.nb = prm->niter_inner / n_rec;
   run.passes = axis_passes(c);
@@ -989,19 +1003,28 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
 // One block of n_rec steps, solve_split.m:51-79 (VV refresh is the caller's).
 // hist: where the block-end finalizer stores (muc, ncur), or nullptr.
 template <typename R>
-gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool last_block, double* hist) {
+gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool last_block, double* hist,
+                         unsigned long long step0 = 0) {
   Field& f = c->main;
   int nb_epi = 0;
   for (int i = 1; i <= run.n_rec; ++i) {
+    if (run.sgpe) {
+      // SGPE (solve_split.m:57-66): the nonlinear factor (half at the block
+      // start, else the full one of the previous step) and the noise of step
+      // step0 + i - 1 come before the kinetic passes, in one elementwise pass
+      Launch L(c, PC_NL_PHASE, (double)c->P * (4 * sizeof(R) + sizeof(R)));
+      launch_sgpe_nl_noise<R>((cx<R>*)f.psi, (const R*)f.V, c->P, c->sc, c->prm.g, run.dre, run.dim, i == 1,
+                              run.sigma, run.seed, step0 + (unsigned long long)(i - 1), c->stream);
+    }
     for (size_t k = 0; k < run.passes.size(); ++k) {
       const bool first = k == 0, last = k + 1 == run.passes.size();
-      const int pro = first ? (i == 1 ? PRO_RT_HALF : PRO_RT_FULL) : PRO_NONE;
+      const int pro = (first && !run.sgpe) ? (i == 1 ? PRO_RT_HALF : PRO_RT_FULL) : PRO_NONE;
       const int epi = (last && i == run.n_rec) ? EPI_RT_END : EPI_NONE;
       CHECK(run_pass<R>(c, f, run.passes[k], KIND_STEP, pro, epi, 0, run.dre, run.dim,
                         (last && i == run.n_rec) ? &nb_epi : nullptr));
     }
   }
-  const bool need_mu = run.feedback || last_block;
+  const bool need_mu = (run.feedback || last_block) && !run.sgpe;
   int nk[3] = {0, 0, 0};
   if (need_mu) CHECK(energy_passes<R>(c, f, false, nk, nullptr));
   BlockFinalArgs a;
@@ -1019,6 +1042,7 @@ gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool las
   a.hist_mu = hist;
   a.hist_n = hist ? hist + 1 : nullptr;
   a.hist_ok = nullptr;
+  a.fixed_mu = run.sgpe;  // SGPE reports mu = mu_init (solve_split.m:78)
   Launch L(c, PC_FINALIZE, 0);
   launch_finalize_block(a, c->sc, c->stream);
   CU(cudaGetLastError());
@@ -1053,10 +1077,10 @@ gpe_status split_finish(gpe_ctx* c, const SplitRun& run, int last_j, double last
 }
 
 template <typename R>
-gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
+gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm, const gpe_sgpe_params* sg = nullptr) {
   SplitRun run;
   int vk = 0;
-  CHECK(split_setup<R>(c, prm, run, vk, 0));
+  CHECK(split_setup<R>(c, prm, run, vk, 0, sg));
   const int start = run.start, nout = run.nout, nb = run.nb, n_rec = run.n_rec;
   const double ddt = run.ddt, dt_outer = run.dt_outer;
   int last_j = start;
@@ -1069,7 +1093,10 @@ gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm) {
       time2 = time + (jj - 1) * ddt * n_rec;  // solve_split.m:53
       if (prm->vtd) CHECK(vtd_upload<R>(c, prm, time2, vk));
       const size_t hj = (size_t)(j - start - 1);
-      CHECK(enqueue_block<R>(c, run, time2, jj == nb, (jj == nb) ? c->d_hist + 3 * hj : nullptr));
+      // global index of the block's first step: distinct noise for every step of every run
+      const unsigned long long step0 =
+          (unsigned long long)(j - 1) * (unsigned long long)run.niter_inner + (unsigned long long)(jj - 1) * n_rec;
+      CHECK(enqueue_block<R>(c, run, time2, jj == nb, (jj == nb) ? c->d_hist + 3 * hj : nullptr, step0));
     }
     last_j = j;
     last_time2 = time2;
@@ -2030,6 +2057,36 @@ gpe_status gpe_selftest_trig(const float* x, float* s, float* co, long long n) {
   cudaFree(d);
   if (e != cudaSuccess) return fail(c, GPE_ERR_CUDA, std::string("gpe_selftest_trig: ") + cudaGetErrorString(e));
   return GPE_OK;
+}
+
+gpe_status gpe_selftest_noise(unsigned long long seed, unsigned long long step, long long n, float* out) {
+  gpe_ctx* c = nullptr;
+  if (!out || n <= 0) return fail(c, GPE_ERR_INVALID, "gpe_selftest_noise: bad arguments");
+  float* d = nullptr;
+  CU(cudaMalloc(&d, 2 * (size_t)n * sizeof(float)));
+  cudaError_t e = launch_selftest_noise(d, n, seed, step, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, 2 * (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(c, GPE_ERR_CUDA, std::string("gpe_selftest_noise: ") + cudaGetErrorString(e));
+  return GPE_OK;
+}
+
+gpe_status gpe_solve_sgpe(gpe_ctx* c, const gpe_split_params* prm, const gpe_sgpe_params* sg) {
+  CHECK(check_ctx(c));
+  CHECK(need_state(c));
+  if (!prm || !sg || !(prm->ddt > 0) || !std::isfinite(prm->ddt))
+    return fail(c, GPE_ERR_INVALID, "solve_sgpe: ddt must be positive");
+  if (!(sg->T >= 0) || !std::isfinite(sg->T) || !(sg->ecut >= 0))
+    return fail(c, GPE_ERR_INVALID, "solve_sgpe: T and ecut must be >= 0");
+  if (sg->ecut > 0 && sg->T > 0)
+    return fail(c, GPE_ERR_UNSUPPORTED, "solve_sgpe: the energy cut-off mask (ecut > 0 with T > 0) is not supported");
+  if (c->prm.omega != 0.0)
+    return fail(c, GPE_ERR_UNSUPPORTED, "solve_sgpe: omega != 0 (the reference's Lz Crank-Nicolson branch)");
+  if (!prm->vtd) CHECK(need_V(c));
+  c->err.clear();
+  CHECK(maybe_autotune(c));
+  if (c->prec == GPE_FP32) return split_impl<float>(c, prm, sg);
+  return split_impl<double>(c, prm, sg);
 }
 
 gpe_status gpe_set_pass_variant(gpe_ctx* c, int variant) {

@@ -57,6 +57,10 @@ class gpe_adjoint_params(C.Structure):
                 ("mem_budget", C.c_double), ("precision", C.c_int)]
 
 
+class gpe_sgpe_params(C.Structure):
+    _fields_ = [("T", C.c_double), ("ecut", C.c_double), ("seed", C.c_ulonglong)]
+
+
 class gpe_current(C.Structure):
     _fields_ = [("current_iter", C.c_int), ("current_time", C.c_double), ("current_mu", C.c_double),
                 ("current_n", C.c_double)]
@@ -113,6 +117,8 @@ PROTOTYPES = {
     "gpe_set_pass_variant": (C.c_int, [_P, C.c_int]),
     "gpe_autotune": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int)]),
     "gpe_selftest_trig": (C.c_int, [_F, _F, _F, C.c_longlong]),
+    "gpe_selftest_noise": (C.c_int, [C.c_ulonglong, C.c_ulonglong, C.c_longlong, _F]),
+    "gpe_solve_sgpe": (C.c_int, [_P, C.POINTER(gpe_split_params), C.POINTER(gpe_sgpe_params)]),
     "gpe_norm_noalloc": (C.c_int, [_P, C.c_longlong, C.c_int, C.c_double, _P, _D]),
     "gpe_host_register": (C.c_int, [_P, C.c_size_t]),
     "gpe_host_unregister": (C.c_int, [_P]),

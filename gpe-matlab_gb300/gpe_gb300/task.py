@@ -252,6 +252,11 @@ class GPEtask:
 
     def solve_split(self, ddt, niter_inner, niter_outer):
         """solve_split.m:1-84: run outer steps current_iter+1 .. niter_outer."""
+        return self._run_split(ddt, niter_inner, niter_outer, None)
+
+    def _run_split(self, ddt, niter_inner, niter_outer, sgpe):
+        """The shared driver of solve_split and SGPEtask.solve_split (sgpe:
+        a gpe_sgpe_params, or None)."""
         self._prepare_split()
         errors = []
         vtd_cb = L.VTD_FN()
@@ -287,7 +292,10 @@ class GPEtask:
         prm.niter_outer = int(niter_outer)
         prm.vtd = vtd_cb
         prm.on_step = step_cb
-        st = L.lib.gpe_solve_split(self._ctx, C.byref(prm))
+        if sgpe is None:
+            st = L.lib.gpe_solve_split(self._ctx, C.byref(prm))
+        else:
+            st = L.lib.gpe_solve_sgpe(self._ctx, C.byref(prm), C.byref(sgpe))
         if errors:
             raise errors[0]
         L.check(self._ctx, st)
@@ -395,6 +403,35 @@ class GPEtask:
         """0: direct passes with L2 prefetch (default), 1: TMA-staged passes where
         they apply, 2: direct passes without prefetch."""
         L.check(self._ctx, L.lib.gpe_set_pass_variant(self._ctx, int(variant)))
+
+
+class SGPEtask(GPEtask):
+    """SGPEtask (lib/@SGPEtask/SGPEtask.m:1-48): GPEtask with temperature T,
+    noise cut-off ecut and (an addition) the noise seed.  solve_split runs
+    SGPEtask.solve_split on the GPU: mu = mu_init, no renormalisation, noise
+    sqrt(T*gamma*ddt/weight)*(n1 + 1i*n2) before every kinetic step."""
+
+    def __init__(self, grid: _GridBase, trappot, device: int = 0):
+        super().__init__(grid, trappot, device=device)
+        self.T = 0.0
+        self.ecut = 0.0
+        self.seed = 0
+
+    def solve_split(self, ddt, niter_inner, niter_outer):
+        """lib/@SGPEtask/solve_split.m:1-81."""
+        sg = L.gpe_sgpe_params()
+        sg.T = float(self.T)
+        sg.ecut = float(self.ecut)
+        sg.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        return self._run_split(ddt, niter_inner, niter_outer, sg)
+
+
+def noise_variates(seed, step, n):
+    """The stochastic GPE's noise for points 0..n-1 of `step` (device FP32):
+    an (n, 2) array of standard normal pairs (gpe_selftest_noise)."""
+    out = np.empty(2 * int(n), dtype=np.float32)
+    L.check(None, L.lib.gpe_selftest_noise(int(seed), int(step), int(n), L.fptr(out)))
+    return out.reshape(-1, 2)
 
 
 def solve_split_batch(tasks, ddt, niter_inner, niter_outer):

@@ -136,6 +136,16 @@ typedef struct {
                              * the sweep in FP64 from the FP32 state             */
 } gpe_adjoint_params;
 
+/* Stochastic GPE, lib/@SGPEtask (SGPEtask.m:1-48, solve_split.m:1-81). */
+typedef struct {
+    double T;                  /* temperature                                   [0] */
+    double ecut;               /* noise energy cut-off; with T > 0 only 0 (none) is
+                                  supported (the k-space mask of solve_split.m:41-46
+                                  does not factorise over axes)                     */
+    unsigned long long seed;   /* noise stream: Philox4x32-10 keyed by seed with the
+                                  counter (grid point, global step index)           */
+} gpe_sgpe_params;
+
 /* Dynamics bookkeeping properties, GPEtask.m:18-24. */
 typedef struct {
     int current_iter;
@@ -234,6 +244,13 @@ GPE_API gpe_status gpe_solve_split_batch(gpe_ctx **ctxs, int count, const gpe_sp
  * current_* and history are left unchanged.  gamma must be 0. */
 GPE_API gpe_status gpe_adjoint_grad(gpe_ctx *ctx, const gpe_adjoint_params *prm, const double *psi_target,
                                     double *dLdV, double *loss);
+/* SGPEtask.solve_split (lib/@SGPEtask/solve_split.m:1-81) from the current
+ * state: mu = mu_init throughout, no renormalisation, and before every
+ * kinetic step psi += sqrt(T*gamma*ddt/weight) * (n1 + i*n2) with n1, n2
+ * standard normal variates (solve_split.m:49,55).  history.mu holds mu_init,
+ * history.n the norm.  Vtd and on_step work as in gpe_solve_split; omega must
+ * be 0 (the reference's rotating SGPE uses the Lz Crank-Nicolson branch). */
+GPE_API gpe_status gpe_solve_sgpe(gpe_ctx *ctx, const gpe_split_params *prm, const gpe_sgpe_params *sg);
 /* applyham / get_energy pieces for the current state at the current V. */
 GPE_API gpe_status gpe_observables(gpe_ctx *ctx, gpe_obs *obs);
 
@@ -276,6 +293,9 @@ GPE_API gpe_status gpe_norm_noalloc(const void *d_psi, long long npoints, int pr
  * chosen (may be NULL) receives the plan variant of axes x, y, z (0 default,
  * 1 alternative, -1 for a length with one plan, FP64 contexts, 2D z). */
 GPE_API gpe_status gpe_autotune(gpe_ctx *ctx, int mode, int *chosen);
+/* Diagnostic: the stochastic GPE's noise variates for points 0..n-1 of step
+ * `step` (FP32, interleaved n1, n2 per point), on device 0. */
+GPE_API gpe_status gpe_selftest_noise(unsigned long long seed, unsigned long long step, long long n, float *out);
 /* Diagnostic: the FP32 device sin/cos used by the phase factors, on n host
  * values (device 0).  Lets tests bound its error against FP64 references. */
 GPE_API gpe_status gpe_selftest_trig(const float *x, float *s, float *c, long long n);

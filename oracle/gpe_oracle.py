@@ -489,6 +489,60 @@ def _set_hist(lst, step, val):
 
 
 # ---------------------------------------------------------------------------
+# Stochastic GPE: lib/@SGPEtask/solve_split.m:1-81 (scalar omega = 0)
+# ---------------------------------------------------------------------------
+class SGPEtask(GPEtask):
+    """SGPEtask (lib/@SGPEtask/SGPEtask.m:1-48): GPEtask with temperature T and
+    energy cut-off ecut.  ``noise(shape)`` supplies the complex standard
+    normal variates randn + 1i*randn of solve_split.m:55 (the reference draws
+    them from MATLAB's generator; a seeded numpy generator by default)."""
+
+    def __init__(self, grid, trappot):
+        super().__init__(grid, trappot)
+        self.T = 0.0
+        self.ecut = 0.0
+        self.noise = None
+
+    def solve_split(self, ddt, niter_inner, niter_outer, rng=None):
+        grid = self.grid
+        g = self.g
+        NN0 = self.Ntotal if self.Ntotal > 0 else grid.integrate(np.abs(self.init_state) ** 2)  # :19-23
+        gam = self.gamma
+        n_rec = self.n_recalc
+        start = self.current_iter
+        dt = ddt * 1j / (1 + 1j * gam)                                   # :31
+        phi = self.current_state if start > 0 else self.init_state       # :33-37
+        tmp2 = np.real(phi * np.conj(phi))                               # :39
+        if self.ecut > 0 and self.T > 0:                                 # :41-46
+            mask = grid.kk < self.ecut
+            ekk = np.exp(-grid.kk * dt) * mask
+        else:
+            ekk = np.exp(-grid.kk * dt)
+        dt_outer = ddt * niter_inner
+        variance = math.sqrt(self.T * gam * ddt / grid.weight)          # :49
+        rng = rng or np.random.default_rng(0)
+        noise = self.noise or (lambda shape: rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+        ncur = time2 = None
+        mu = self.mu_init
+        for j in range(start + 1, niter_outer + 1):                     # :51
+            mu = self.mu_init                                            # :52
+            time = (j - 1) * dt_outer
+            for jj in range(1, niter_inner // n_rec + 1):                # :54
+                time2 = time + (jj - 1) * ddt * n_rec
+                VV = self.getVtotal(time2)
+                phi = np.exp((mu - VV - g * tmp2) * dt / 2) * phi        # :57
+                for _ in range(n_rec):                                   # :59-70
+                    phi = phi + variance * noise(phi.shape)
+                    phi = grid.ifft(ekk * grid.fft(phi))
+                    phi = np.exp((mu - VV - g * phi * np.conj(phi)) * dt) * phi
+                phi = np.exp((VV - mu + g * phi * np.conj(phi)) * dt / 2) * phi  # :73
+                tmp2 = np.real(phi * np.conj(phi))
+                ncur = grid.integrate(tmp2)                              # :76
+            self.ext_callback(phi, j, time2, mu, ncur)                   # :78
+        return phi
+
+
+# ---------------------------------------------------------------------------
 # Vortex imprint: examples/example1_vortex.m:26-30 (also README.md:93-97)
 # ---------------------------------------------------------------------------
 def imprint_vortex(grid: Grid, phi, g, x0, y0=0.0):

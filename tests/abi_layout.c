@@ -19,6 +19,7 @@ int main(void) {
     S(gpe_split_params); F(gpe_split_params, vtd); F(gpe_split_params, on_step); F(gpe_split_params, step_user);
     S(gpe_adjoint_params); F(gpe_adjoint_params, checkpoint_every); F(gpe_adjoint_params, mem_budget);
     F(gpe_adjoint_params, precision);
+    S(gpe_sgpe_params); F(gpe_sgpe_params, ecut); F(gpe_sgpe_params, seed);
     S(gpe_current); F(gpe_current, current_time);
     S(gpe_obs); F(gpe_obs, energy);
     S(gpe_kernel_stat); F(gpe_kernel_stat, launches); F(gpe_kernel_stat, bytes_per_launch);

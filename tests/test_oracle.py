@@ -194,6 +194,24 @@ def test_rotating_frame_dynamics_conserve_norm_and_energy():
     assert t.get_energy(phi) == pytest.approx(E0, rel=1e-6)
 
 
+def test_sgpe_zero_temperature_is_gpe_up_to_a_global_phase():
+    """SGPEtask at T = 0, gamma = 0 (lib/@SGPEtask/solve_split.m): mu stays at
+    mu_init while GPEtask uses <psi|H psi>/N; mu only adds a global phase at
+    gamma = 0, so |psi| agrees with GPEtask's."""
+    g = O.Grid(5, 32, 4, 24)
+    V = lambda X, Y, Z: 0.5 * (X ** 2 + 1.3 * Y ** 2)
+    X, Y = g.mesh["x"], g.mesh["y"]
+    psi0 = (np.exp(-((X - 0.5) ** 2 + Y ** 2) / 2) * np.exp(0.3j * Y)).astype(complex)
+    a, b = O.GPEtask(g, V), O.SGPEtask(g, V)
+    for t in (a, b):
+        t.g = 1.0
+        t.init_state = psi0
+    pa = a.solve_split(0.005, 10, 2)
+    pb = b.solve_split(0.005, 10, 2)
+    np.testing.assert_allclose(np.abs(pb), np.abs(pa), rtol=0, atol=1e-12)
+    assert b.history["mu"] == [0.0, 0.0]
+
+
 def test_golden_fixtures_reproduce():
     from tests.golden import make_golden as MG
 
