@@ -58,6 +58,40 @@ struct ObsFinalArgs {
   double mu_init;
 };
 
+// Two-component (spinor) split step, spinor_kernels.cu.
+template <typename R>
+struct SpinorNL {
+  R g11, g12, g21, g22;         // interaction matrix
+  R dre, dim;                   // complex time step dt
+  cx<R> cosom, sinomm, sinomp;  // step-constant coupling factors (nl == 0)
+  int nl;                       // nlincpl != 0: per-point factors of cre + i cim + nlincpl*n
+  R nlincpl, cre, cim;
+};
+constexpr int SP_NSUMS = 9;     // n1 n2 V1n1 V2n2 n1^2 n2^2 n1n2 Re/Im conj(psi1)psi2
+struct SpinorFinalArgs {
+  const double* sums;           // [SP_NSUMS][nsum] partials of launch_spinor_sums
+  int nsum;
+  const double* partials;       // kinetic partials (slots S_KX..S_KZ)
+  int cap;
+  int nblk_kin[3];
+  double weight;
+  double g[4];
+  double cre, cim;
+  int mode;                     // 0: run start, 1: block end, 2: observables
+  double Ntotal;                // mode 0
+  int renorm;                   // mode 1: gamma > 0
+  double tau, time2;
+  double* hist;                 // mode 1: (mu, ncur) or nullptr
+  double* obs;                  // mode 2: norm, ekin, epot, eint, ecpl
+};
+template <typename R>
+void launch_spinor_nl(cx<R>* psi, const R* V, long long P, const DevScalars* sc, int first, const SpinorNL<R>& q,
+                      cudaStream_t s);
+template <typename R>
+int launch_spinor_sums(const cx<R>* psi, const R* V, long long P, const DevScalars* sc, double* out,
+                       cudaStream_t s);
+void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream_t s);
+
 void launch_finalize_block(const BlockFinalArgs& a, DevScalars* sc, cudaStream_t s);
 void launch_finalize_itp(const ItpFinalArgs& a, DevScalars* sc, cudaStream_t s);
 void launch_finalize_check(const CheckFinalArgs& a, DevScalars* sc, cudaStream_t s);

@@ -256,7 +256,10 @@ enum Epilogue {
   EPI_ITP = 2      // psi *= aux, sum n (groundstate_itp.m:42-44)
 };
 
-enum PassKind { KIND_STEP = 0, KIND_ENERGY = 1 };
+// KIND_STEP_EXT: a step pass with the rotating-frame cross terms, the energy
+// cut-off mask or only one of its halves; a separate kernel, so that the
+// plain step kernel keeps its register allocation.
+enum PassKind { KIND_STEP = 0, KIND_ENERGY = 1, KIND_STEP_EXT = 2 };
 
 template <typename R>
 struct PassArgs {
@@ -289,6 +292,19 @@ struct PassArgs {
   const R* rotw = nullptr;     // energy: per transverse index weight (-+omega * coordinate)
   const R* kp = nullptr;       // energy: k/N in the spectrum-slot order
   int rot_period = 0;
+  // Non-separable kinetic factor (the stochastic GPE's energy cut-off): a
+  // step pass may run only its forward half (skip_inv: position m*T+t of the
+  // pencil then holds spectrum slot m*T+t) or only its inverse half
+  // (skip_fwd, reading that order back), and the middle pass zeroes the
+  // modes with kk >= ecut, kk = mask_a[b % mask_pa] + mask_b[b / mask_pa]
+  // (the pencil's transverse axes, by stored position; mask_b optional) +
+  // mask_c[slot] (the pass's own axis).  Tables hold k^2/2 in slot order.
+  int skip_fwd = 0, skip_inv = 0;
+  const R* mask_a = nullptr;
+  const R* mask_b = nullptr;
+  const R* mask_c = nullptr;
+  long long mask_pa = 1;
+  R ecut = R(0);
 };
 
 }  // namespace gpe

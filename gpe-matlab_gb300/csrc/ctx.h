@@ -31,6 +31,8 @@ struct Field {
   void* rot[2] = {nullptr, nullptr};             // [transverse index][slot] complex factors of the step
   void* rotw[2] = {nullptr, nullptr};            // per transverse index: -omega*y (x) / +omega*x (y)
   double rotw_omega = 0.0;                       // omega the rotw arrays hold
+  void* kks[3] = {nullptr, nullptr, nullptr};    // per axis: permuted k^2/2, N real (energy cut-off)
+  void* php2[3] = {nullptr, nullptr, nullptr};   // spinor: the kinetic factors of half a step
 };
 
 struct ProfRec {
@@ -54,6 +56,15 @@ struct gpe_ctx {
   int n[3] = {1, 1, 1};  // nx, ny, nz
   double dx[3] = {1, 1, 1}, span[3] = {1, 1, 1};
   long long P = 0;
+  // Components of the state (1; 2 for a spinor context).  State, potential
+  // and their staging buffers hold PS = ncomp*P points, component after
+  // component; the axis passes run over all components in one launch.
+  int ncomp = 1;
+  long long PS = 0;
+  gpe_spinor_params spin{};
+  double* Vmu = nullptr;  // spinor with a time-dependent V: getVtotal(current_time) (FP64 copy)
+  void* VmuR = nullptr;   // the same in the context precision
+  double* spin_part = nullptr;  // spinor sums: [SP_NSUMS][grid] partials, then 8 observables
   double weight = 1.0;
   int prec = GPE_FP64;
   gpe_params prm{};

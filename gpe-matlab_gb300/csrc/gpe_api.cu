@@ -119,23 +119,53 @@ PassGeom dispatch_geom(int N, int var, bool strided) {
   return PassGeom{0, 1, 0};
 }
 
+enum { SPLIT_FULL = 0, SPLIT_FWD = 1, SPLIT_INV = 2, SPLIT_MASKED = 3 };
+
 struct AxisPass {
   int axis;  // 0 = x, 1 = y, 2 = z
   int N;
   bool strided;
   long long n_batch, stride, inner, outer;
   int rot = 0;  // rotating frame: 1 = x pass with exp(+kx y omega dt/2), 2 = y pass with exp(-ky x omega dt)
+  int split = SPLIT_FULL;  // energy cut-off chain: forward half only, inverse half only, or the masked pass
+  double ecut = 0.0;
+  int half = 0;  // spinor contexts: the half-step kinetic factors exp(-k^2/2 dt/2)
 };
 
 // Pass order: y (contiguous, carries the prologue), x, then z (3D).  The
 // last pass carries the epilogue.  Rotating frame (scalar omega,
 // ssft_kin_step.m:12-15): x half step, y (and z), x half step again.
-std::vector<AxisPass> axis_passes(const gpe_ctx* c) {
-  const long long nx = c->n[0], ny = c->n[1], nz = c->ndims == 3 ? c->n[2] : 1;
-  const AxisPass py{1, (int)ny, false, nx * nz, 1, 1, 0};
-  const AxisPass px{0, (int)nx, true, ny * nz, ny, ny, nx * ny};
-  const AxisPass pz{2, (int)nz, true, nx * ny, nx * ny, nx * ny, 0};
+//
+// Energy cut-off (ecut > 0, SGPEtask/solve_split.m:40-42): the mask kk < ecut
+// does not factor over the axes, so the kinetic step becomes y and x forward
+// halves (spectra stored in slot order), the last axis whole with the mask
+// between its halves, then the x and y inverse halves: 2D y x~ y, 3D y x z~ x y.
+//
+// Spinor contexts: the components lie one after the other, so the pencils of
+// every component are one batch (pencil index b = pencil + component * count;
+// for z pencils outer = P steps to the next component).
+std::vector<AxisPass> axis_passes(const gpe_ctx* c, double ecut = 0.0) {
+  const long long nx = c->n[0], ny = c->n[1], nz = c->ndims == 3 ? c->n[2] : 1, nc = c->ncomp;
+  const AxisPass py{1, (int)ny, false, nx * nz * nc, 1, 1, 0};
+  const AxisPass px{0, (int)nx, true, ny * nz * nc, ny, ny, nx * ny};
+  const AxisPass pz{2, (int)nz, true, nx * ny * nc, nx * ny, nx * ny, c->P};
   std::vector<AxisPass> v;
+  if (ecut > 0.0) {
+    std::vector<AxisPass> fw{py, px};
+    if (c->ndims == 3) fw.push_back(pz);
+    for (size_t k = 0; k + 1 < fw.size(); ++k) {
+      v.push_back(fw[k]);
+      v.back().split = SPLIT_FWD;
+    }
+    v.push_back(fw.back());
+    v.back().split = SPLIT_MASKED;
+    v.back().ecut = ecut;
+    for (size_t k = fw.size() - 1; k-- > 0;) {
+      v.push_back(fw[k]);
+      v.back().split = SPLIT_INV;
+    }
+    return v;
+  }
   if (c->prm.omega != 0.0) {
     AxisPass rx = px, ry = py;
     rx.rot = 1;
@@ -220,6 +250,8 @@ bool use_tma(const gpe_ctx* c, const Field& f, const AxisPass& ap) {
   if (c->pass_variant != 1) return false;
   if (f.plan_var[ap.axis] != 0) return false;  // TMA passes are built on Plan<N> only
   if (ap.rot != 0) return false;                // and without the rotating-frame terms
+  if (ap.split != SPLIT_FULL) return false;     // or the energy cut-off chain
+  if (ap.half != 0) return false;               // or the spinor's half steps
   if (dispatch_tma_smem<R>(ap.N, ap.strided) > 200 * 1024) return false;
   const int ffts = dispatch_tma_ffts<R>(ap.N, ap.strided);
   if (!ap.strided) return true;
@@ -405,15 +437,18 @@ gpe_status build_axis_tables(gpe_ctx* c, Field& f, int ax) {
     if (!f.php[ax]) CU(cudaMalloc(&f.php[ax], N * 2 * sizeof(R)));
     if (!f.k2p[ax]) CU(cudaMalloc(&f.k2p[ax], N * sizeof(R)));
     if (!f.kp[ax]) CU(cudaMalloc(&f.kp[ax], N * sizeof(R)));
-    std::vector<R> k2(N), k1(N);
+    if (!f.kks[ax]) CU(cudaMalloc(&f.kks[ax], N * sizeof(R)));
+    std::vector<R> k2(N), k1(N), kk(N);
     for (int t = 0; t < pi.T; ++t)
       for (int m = 0; m < pi.E; ++m) {
         const double k = kval(c, ax, plan_spec_pos(pi, t, m));
         k2[m * pi.T + t] = (R)(k * k / 2.0 / N);
         k1[m * pi.T + t] = (R)(k / N);
+        kk[m * pi.T + t] = (R)(k * k / 2.0);
       }
     CU(cudaMemcpy(f.k2p[ax], k2.data(), N * sizeof(R), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(f.kp[ax], k1.data(), N * sizeof(R), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(f.kks[ax], kk.data(), N * sizeof(R), cudaMemcpyHostToDevice));
   }
   f.phase_valid = false;
   return GPE_OK;
@@ -475,6 +510,19 @@ gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
             std::complex<double>(mag * std::cos(kk * dim * h), -mag * std::sin(kk * dim * h));
       }
     CHECK(upload_cx<R>(c, f.php[ax], ph));
+    if (c->ncomp == 2) {
+      // GPEtaskSpinor/solve_split.m:44-45: ekkp = exp(-kk dt/2) at block starts;
+      // the last step's ekk times ekkm = exp(+kk dt/2) is exp(-kk dt/2) too
+      for (int t = 0; t < pi.T; ++t)
+        for (int m = 0; m < pi.E; ++m) {
+          const double k = kval(c, ax, plan_spec_pos(pi, t, m));
+          const double kk = k * k / 4.0;
+          const double mag = std::exp(-kk * dre) / N;
+          ph[slot_index<R>(pi.T, t, m)] = std::complex<double>(mag * std::cos(kk * dim), -mag * std::sin(kk * dim));
+        }
+      if (!f.php2[ax]) CU(cudaMalloc(&f.php2[ax], N * 2 * sizeof(R)));
+      CHECK(upload_cx<R>(c, f.php2[ax], ph));
+    }
     if (om != 0.0 && ax < 2) {
       const int tax = ax == 0 ? 1 : 0;  // transverse axis of the pencils
       const int nt = c->n[tax];
@@ -504,11 +552,11 @@ gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
 template <typename R>
 gpe_status alloc_field(gpe_ctx* c, Field& f, int prec, bool share_V64) {
   f.prec = prec;
-  CU(cudaMalloc(&f.psi, (size_t)c->P * 2 * sizeof(R)));
+  CU(cudaMalloc(&f.psi, (size_t)c->PS * 2 * sizeof(R)));
   if (share_V64) {
     f.V = c->V64;
   } else {
-    CU(cudaMalloc(&f.V, (size_t)c->P * sizeof(R)));
+    CU(cudaMalloc(&f.V, (size_t)c->PS * sizeof(R)));
   }
   return build_static_tables<R>(c, f);
 }
@@ -530,6 +578,8 @@ void free_field(Field& f, const double* V64) {
     cudaFree(f.php[i]);
     cudaFree(f.k2p[i]);
     cudaFree(f.kp[i]);
+    cudaFree(f.kks[i]);
+    cudaFree(f.php2[i]);
   }
   for (int i = 0; i < 2; ++i) {
     cudaFree(f.rot[i]);
@@ -569,7 +619,8 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.psi = (cx<R>*)(psi_buf ? psi_buf : f.psi);  // psi_buf: another array of the grid's shape
   a.V = (const R*)f.V;
   a.aux = (R*)f.aux;
-  a.php = (const cx<R>*)f.php[ap.axis];
+  a.php = (const cx<R>*)(ap.half ? f.php2[ap.axis] : f.php[ap.axis]);
+  if (!a.php) return fail(c, GPE_ERR_STATE, "kinetic factors not set");
   a.tws = (const cx<R>*)f.tws[ap.axis];
   a.k2p = (const R*)f.k2p[ap.axis];
   a.partials = c->partials;
@@ -579,7 +630,8 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.inner = ap.inner;
   a.outer = ap.outer;
   a.cap = c->cap;
-  a.kind = kind;
+  // rotating-frame terms and the cut-off chain run in the extended step kernel
+  a.kind = (kind == KIND_STEP && (ap.rot != 0 || ap.split != SPLIT_FULL)) ? KIND_STEP_EXT : kind;
   a.pro = pro;
   a.epi = epi;
   a.kin_slot = S_KX + ap.axis;
@@ -602,6 +654,16 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
       a.kp = (const R*)f.kp[ap.axis];
       if (!a.rotw) return fail(c, GPE_ERR_STATE, "rotating frame: energy weights not set");
     }
+  }
+  if (ap.split == SPLIT_FWD) a.skip_inv = 1;
+  if (ap.split == SPLIT_INV) a.skip_fwd = 1;
+  if (ap.split == SPLIT_MASKED) {
+    // transverse axes of the last axis' pencils: y (b % ny) and, in 3D, x (b / ny)
+    a.mask_a = (const R*)f.kks[1];
+    a.mask_b = c->ndims == 3 ? (const R*)f.kks[0] : nullptr;
+    a.mask_c = (const R*)f.kks[ap.axis];
+    a.mask_pa = c->n[1];
+    a.ecut = (R)ap.ecut;
   }
   const double P = (double)c->P;
   double bytes = (kind == KIND_ENERGY ? 1.0 : 2.0) * P * 2 * sizeof(R);
@@ -893,11 +955,11 @@ gpe_status itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* M
 // ---- solve_split -----------------------------------------------------------------
 template <typename R>
 gpe_status upload_V_double(gpe_ctx* c, const double* hostV, bool async_pinned) {
-  const size_t bytes = (size_t)c->P * sizeof(double);
+  const size_t bytes = (size_t)c->PS * sizeof(double);
   CU(cudaMemcpyAsync(c->V64, hostV, bytes, cudaMemcpyHostToDevice, c->stream));
   if (c->prec == GPE_FP32) {
-    Launch L(c, PC_ELEMENTWISE, (double)c->P * 12);
-    launch_convert_re<double, float>(c->V64, (float*)c->main.V, c->P, c->stream);
+    Launch L(c, PC_ELEMENTWISE, (double)c->PS * 12);
+    launch_convert_re<double, float>(c->V64, (float*)c->main.V, c->PS, c->stream);
     CU(cudaGetLastError());
   }
   if (!async_pinned) CU(cudaStreamSynchronize(c->stream));
@@ -907,7 +969,7 @@ gpe_status upload_V_double(gpe_ctx* c, const double* hostV, bool async_pinned) {
 
 template <typename R>
 gpe_status vtd_upload(gpe_ctx* c, const gpe_split_params* prm, double time, int& k) {
-  const size_t bytes = (size_t)c->P * sizeof(double);
+  const size_t bytes = (size_t)c->PS * sizeof(double);
   if (!c->pinned_V[k]) CU(cudaMallocHost(&c->pinned_V[k], bytes));
   CU(cudaEventSynchronize(c->ev_V[k]));  // the previous copy out of this buffer is done
   if (prm->vtd(prm->vtd_user, time, c->pinned_V[k]) != 0)
@@ -943,7 +1005,14 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
   int n_rec = c->prm.n_recalc;
   if (n_rec < 1) return fail(c, GPE_ERR_INVALID, "n_recalc must be >= 1");
   if (prm->niter_inner < 1) return fail(c, GPE_ERR_INVALID, "niter_inner must be >= 1");
-  if (prm->niter_inner % n_rec != 0) n_rec = 1;  // solve_split.m:25-27
+  if (prm->niter_inner % n_rec != 0) {
+    // GPEtask: n_rec = 1 (solve_split.m:25-27).  SGPEtask keeps n_rec and runs
+    // floor(niter_inner/n_rec) blocks (its loop 1:niter_inner/n_rec,
+    // @SGPEtask/solve_split.m:54), none at all (an error there) below n_rec.
+    if (!sg) n_rec = 1;
+    else if (prm->niter_inner < n_rec)
+      return fail(c, GPE_ERR_INVALID, "solve_sgpe: niter_inner < n_recalc runs no block (solve_split.m:54)");
+  }
   const int start = c->cur.current_iter;
   const int nout = prm->niter_outer;
   // dt = ddt*1i/(1+1i*gam) (solve_split.m:31)
@@ -986,7 +1055,8 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
   }
   run.dt_outer = ddt * prm->niter_inner;
   run.nb = prm->niter_inner / n_rec;
-  run.passes = axis_passes(c);
+  // the cut-off mask applies only with noise (SGPEtask/solve_split.m:40)
+  run.passes = axis_passes(c, (sg && sg->T > 0 && sg->ecut > 0) ? sg->ecut : 0.0);
   run.hist_off = hist_extra;
   const int nsteps_out = std::max(0, nout - start);
   const size_t hlen = hist_extra + 3 * (size_t)std::max(1, nsteps_out);
@@ -1411,8 +1481,8 @@ gpe_status batch_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm) {
 
 template <typename R>
 gpe_status materialize(gpe_ctx* c) {
-  Launch L(c, PC_ELEMENTWISE, (double)c->P * 4 * sizeof(R));
-  launch_apply_scale<R>((cx<R>*)c->main.psi, c->P, c->sc, c->stream);
+  Launch L(c, PC_ELEMENTWISE, (double)c->PS * 4 * sizeof(R));
+  launch_apply_scale<R>((cx<R>*)c->main.psi, c->PS, c->sc, c->stream);
   launch_set_scale_one(c->sc, c->stream);
   CU(cudaGetLastError());
   return GPE_OK;
@@ -1443,7 +1513,7 @@ gpe_status io_buffer(gpe_ctx* c, void** out) {
     return GPE_OK;
   }
   void* p = nullptr;
-  CU(cudaMalloc(&p, (size_t)c->P * 16));
+  CU(cudaMalloc(&p, (size_t)c->PS * 16));
   *out = p;
   return GPE_OK;
 }
@@ -1540,7 +1610,7 @@ gpe_status autotune_main(gpe_ctx* c, int chosen[3]) {
 
 // Automatic tuning on the first hot-path call of a large FP32 context.
 gpe_status maybe_autotune(gpe_ctx* c) {
-  if (c->tuned || c->tune_mode != 2 || c->prec != GPE_FP32 || c->pass_variant == 1) return GPE_OK;
+  if (c->tuned || c->tune_mode != 2 || c->prec != GPE_FP32 || c->pass_variant == 1 || c->ncomp != 1) return GPE_OK;
   if (c->P < (1LL << 20)) return GPE_OK;
   int chosen[3];
   return autotune_main(c, chosen);
@@ -1551,6 +1621,8 @@ gpe_status maybe_autotune(gpe_ctx* c) {
 // =============================================================================
 // C ABI
 // =============================================================================
+#include "spinor_driver.cuh"
+
 extern "C" {
 
 int gpe_abi_version(void) { return GPE_ABI_VERSION; }
@@ -1580,7 +1652,7 @@ void gpe_default_params(gpe_params* p) {
   p->itp_min_iter = 50;
 }
 
-gpe_status gpe_create(const gpe_grid_desc* d, gpe_ctx** out) {
+static gpe_status create_impl(const gpe_grid_desc* d, gpe_ctx** out, int ncomp) {
   gpe_ctx* c = nullptr;
   if (!d || !out) return fail(nullptr, GPE_ERR_INVALID, "gpe_create: null argument");
   *out = nullptr;
@@ -1607,6 +1679,7 @@ gpe_status gpe_create(const gpe_grid_desc* d, gpe_ctx** out) {
     return fail(nullptr, GPE_ERR_NO_DEVICE,
                 "libgpe is built for sm_103a (GB300); device is sm_" + std::to_string(maj * 10 + min));
   c = new gpe_ctx();
+  c->ncomp = ncomp;
   c->device = d->device;
   c->ndims = d->ndims;
   for (int a = 0; a < 3; ++a) {
@@ -1615,6 +1688,7 @@ gpe_status gpe_create(const gpe_grid_desc* d, gpe_ctx** out) {
     c->span[a] = (a < d->ndims) ? d->span[a] : 0.0;
   }
   c->P = (long long)c->n[0] * c->n[1] * c->n[2];
+  c->PS = c->P * c->ncomp;
   c->weight = c->dx[0] * c->dx[1] * (d->ndims == 3 ? c->dx[2] : 1.0);  // init.m:36, grid3d/init.m:83
   c->prec = d->precision;
   gpe_default_params(&c->prm);
@@ -1649,7 +1723,8 @@ gpe_status gpe_create(const gpe_grid_desc* d, gpe_ctx** out) {
   if (cudaMalloc(&c->partials, (size_t)(NSLOTS + 1) * c->cap * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&c->sc, sizeof(DevScalars)) != cudaSuccess ||
       cudaMallocHost(&c->sc_host, 2 * sizeof(DevScalars)) != cudaSuccess ||
-      cudaMalloc(&c->V64, (size_t)c->P * sizeof(double)) != cudaSuccess) {
+      cudaMalloc(&c->V64, (size_t)c->PS * sizeof(double)) != cudaSuccess ||
+      (ncomp == 2 && cudaMalloc(&c->spin_part, ((size_t)SP_NSUMS * 8 * c->sms + 8) * sizeof(double)) != cudaSuccess)) {
     c->err = "device allocation failed";
     return cleanup(GPE_ERR_ALLOC);
   }
@@ -1678,6 +1753,35 @@ gpe_status gpe_create(const gpe_grid_desc* d, gpe_ctx** out) {
   return GPE_OK;
 }
 
+gpe_status gpe_create(const gpe_grid_desc* d, gpe_ctx** out) { return create_impl(d, out, 1); }
+
+gpe_status gpe_create_spinor(const gpe_grid_desc* d, gpe_ctx** out) {
+  const gpe_status st = create_impl(d, out, 2);
+  if (st == GPE_OK) {
+    gpe_ctx* c = *out;
+    c->spin.g[0] = c->spin.g[1] = c->spin.g[2] = c->spin.g[3] = 0.0;
+    c->spin.coupling_re = c->spin.coupling_im = c->spin.nlincpl = 0.0;
+  }
+  return st;
+}
+
+gpe_status gpe_set_spinor_params(gpe_ctx* c, const gpe_spinor_params* p) {
+  CHECK(check_ctx(c));
+  if (c->ncomp != 2) return fail(c, GPE_ERR_STATE, "gpe_set_spinor_params: not a spinor context");
+  if (!p) return fail(c, GPE_ERR_INVALID, "null spinor params");
+  for (double v : {p->g[0], p->g[1], p->g[2], p->g[3], p->coupling_re, p->coupling_im, p->nlincpl})
+    if (!std::isfinite(v)) return fail(c, GPE_ERR_INVALID, "spinor params must be finite");
+  c->spin = *p;
+  return GPE_OK;
+}
+
+gpe_status gpe_get_spinor_params(const gpe_ctx* c, gpe_spinor_params* p) {
+  if (!c || !p) return fail(nullptr, GPE_ERR_INVALID, "null argument");
+  if (c->ncomp != 2) return GPE_ERR_STATE;
+  *p = c->spin;
+  return GPE_OK;
+}
+
 void gpe_destroy(gpe_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
@@ -1685,6 +1789,9 @@ void gpe_destroy(gpe_ctx* c) {
   free_field(c->main, c->V64);
   free_field(c->polish, c->V64);
   cudaFree(c->V64);
+  cudaFree(c->Vmu);
+  cudaFree(c->VmuR);
+  cudaFree(c->spin_part);
   cudaFree(c->partials);
   cudaFree(c->sc);
   cudaFree(c->d_hist);
@@ -1771,14 +1878,14 @@ gpe_status gpe_set_potential(gpe_ctx* c, const double* V) {
 gpe_status gpe_set_potential_f32(gpe_ctx* c, const float* V) {
   CHECK(check_ctx(c));
   if (!V) return fail(c, GPE_ERR_INVALID, "null potential");
-  std::vector<double> tmp(V, V + c->P);
+  std::vector<double> tmp(V, V + c->PS);
   return gpe_set_potential(c, tmp.data());
 }
 
 static gpe_status set_state_any(gpe_ctx* c, const void* src, int src_prec, cudaMemcpyKind kind) {
   CHECK(check_ctx(c));
   if (!src) return fail(c, GPE_ERR_INVALID, "null state");
-  const size_t n = (size_t)c->P;
+  const size_t n = (size_t)c->PS;
   if (src_prec == c->prec) {
     CU(cudaMemcpyAsync(c->main.psi, src, n * 2 * (src_prec == GPE_FP32 ? 4 : 8), kind, c->stream));
   } else {
@@ -1786,9 +1893,9 @@ static gpe_status set_state_any(gpe_ctx* c, const void* src, int src_prec, cudaM
     CHECK(io_buffer(c, &io));
     CU(cudaMemcpyAsync(io, src, n * 2 * (src_prec == GPE_FP32 ? 4 : 8), kind, c->stream));
     if (src_prec == GPE_FP64)
-      launch_convert_cx<double, float>((const cx<double>*)io, (cx<float>*)c->main.psi, c->P, nullptr, c->stream);
+      launch_convert_cx<double, float>((const cx<double>*)io, (cx<float>*)c->main.psi, c->PS, nullptr, c->stream);
     else
-      launch_convert_cx<float, double>((const cx<float>*)io, (cx<double>*)c->main.psi, c->P, nullptr, c->stream);
+      launch_convert_cx<float, double>((const cx<float>*)io, (cx<double>*)c->main.psi, c->PS, nullptr, c->stream);
     c->launches++;
     CU(cudaStreamSynchronize(c->stream));
     if (io != c->polish.psi) cudaFree(io);
@@ -1804,7 +1911,7 @@ static gpe_status get_state_any(gpe_ctx* c, void* dst, int dst_prec, cudaMemcpyK
   CHECK(check_ctx(c));
   CHECK(need_state(c));
   if (!dst) return fail(c, GPE_ERR_INVALID, "null output");
-  const size_t n = (size_t)c->P;
+  const size_t n = (size_t)c->PS;
   if (c->prec == GPE_FP32) CHECK(materialize<float>(c));
   else CHECK(materialize<double>(c));
   if (dst_prec == c->prec) {
@@ -1814,9 +1921,9 @@ static gpe_status get_state_any(gpe_ctx* c, void* dst, int dst_prec, cudaMemcpyK
     void* io = nullptr;
     CHECK(io_buffer(c, &io));
     if (dst_prec == GPE_FP64)
-      launch_convert_cx<float, double>((const cx<float>*)c->main.psi, (cx<double>*)io, c->P, nullptr, c->stream);
+      launch_convert_cx<float, double>((const cx<float>*)c->main.psi, (cx<double>*)io, c->PS, nullptr, c->stream);
     else
-      launch_convert_cx<double, float>((const cx<double>*)c->main.psi, (cx<float>*)io, c->P, nullptr, c->stream);
+      launch_convert_cx<double, float>((const cx<double>*)c->main.psi, (cx<float>*)io, c->PS, nullptr, c->stream);
     c->launches++;
     CU(cudaMemcpyAsync(dst, io, n * 2 * (dst_prec == GPE_FP32 ? 4 : 8), kind, c->stream));
     CU(cudaStreamSynchronize(c->stream));
@@ -1849,6 +1956,7 @@ gpe_status gpe_get_state_device(gpe_ctx* c, void* d, int precision) {
 gpe_status gpe_groundstate_itp(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* MU2, double* EE,
                                int cap, gpe_itp_result* res) {
   CHECK(check_ctx(c));
+  if (c->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "groundstate_itp: not available on a spinor context");
   CHECK(need_state(c));
   CHECK(need_V(c));
   if (!prm || !(prm->dt > 0) || !std::isfinite(prm->dt) || !(prm->eps > 0))
@@ -1867,6 +1975,12 @@ gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
     return fail(c, GPE_ERR_INVALID, "solve_split: ddt must be positive");
   if (!prm->vtd) CHECK(need_V(c));
   c->err.clear();
+  if (c->ncomp == 2) {
+    if (c->prm.omega != 0.0)
+      return fail(c, GPE_ERR_UNSUPPORTED, "solve_split (spinor): omega != 0 is not supported");
+    if (c->prec == GPE_FP32) return spinor_split_impl<float>(c, prm);
+    return spinor_split_impl<double>(c, prm);
+  }
   CHECK(maybe_autotune(c));
   // Small grids are launch-bound: run their blocks as replayed CUDA graphs
   // (the batched path with one context) when no per-block host work is
@@ -1883,6 +1997,7 @@ gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
 gpe_status gpe_adjoint_grad(gpe_ctx* c, const gpe_adjoint_params* prm, const double* psi_target, double* dLdV,
                             double* loss) {
   CHECK(check_ctx(c));
+  if (c->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "adjoint_grad: not available on a spinor context");
   CHECK(need_state(c));
   CHECK(need_V(c));
   if (!prm || !psi_target || !dLdV) return fail(c, GPE_ERR_INVALID, "adjoint: null argument");
@@ -1919,6 +2034,7 @@ gpe_status gpe_solve_split_batch(gpe_ctx** ctxs, int count, const gpe_split_para
     if (!ci) return fail(c, GPE_ERR_INVALID, "solve_split_batch: null context");
     if (ci->device != c->device) return fail(c, GPE_ERR_INVALID, "solve_split_batch: contexts on different devices");
     if (!ci->have_state || !ci->have_V) return fail(c, GPE_ERR_STATE, "solve_split_batch: a context lacks state or V");
+    if (ci->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "solve_split_batch: spinor contexts are not batched");
     if (ci->prm.decay_rate > 0)
       return fail(c, GPE_ERR_INVALID, "solve_split_batch: decay_rate > 0 needs per-block host times");
     for (auto* cj : cs)
@@ -1938,6 +2054,7 @@ gpe_status gpe_solve_split_batch(gpe_ctx** ctxs, int count, const gpe_split_para
 
 gpe_status gpe_autotune(gpe_ctx* c, int mode, int* chosen) {
   CHECK(check_ctx(c));
+  if (c->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "autotune: not available on a spinor context");
   if (mode < 0 || (mode > 3 && (mode < 16 || mode > 23)))
     return fail(c, GPE_ERR_INVALID,
                 "autotune mode must be 0 (off), 1 (now), 2 (auto), 3 (alternative plans) or 16 + axis mask");
@@ -1973,6 +2090,12 @@ gpe_status gpe_observables(gpe_ctx* c, gpe_obs* o) {
   CHECK(need_state(c));
   CHECK(need_V(c));
   if (!o) return fail(c, GPE_ERR_INVALID, "null output");
+  o->ecpl = 0.0;
+  if (c->ncomp == 2) {
+    if (c->prm.omega != 0.0) return fail(c, GPE_ERR_UNSUPPORTED, "observables (spinor): omega != 0");
+    if (c->prec == GPE_FP32) return spinor_observables<float>(c, o);
+    return spinor_observables<double>(c, o);
+  }
   CHECK(maybe_autotune(c));
   DevScalars h;
   if (c->prec == GPE_FP32) CHECK(observables_impl<float>(c, c->main, 0.0, 0, &h));
@@ -2073,13 +2196,12 @@ gpe_status gpe_selftest_noise(unsigned long long seed, unsigned long long step, 
 
 gpe_status gpe_solve_sgpe(gpe_ctx* c, const gpe_split_params* prm, const gpe_sgpe_params* sg) {
   CHECK(check_ctx(c));
+  if (c->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "solve_sgpe: not available on a spinor context");
   CHECK(need_state(c));
   if (!prm || !sg || !(prm->ddt > 0) || !std::isfinite(prm->ddt))
     return fail(c, GPE_ERR_INVALID, "solve_sgpe: ddt must be positive");
   if (!(sg->T >= 0) || !std::isfinite(sg->T) || !(sg->ecut >= 0))
     return fail(c, GPE_ERR_INVALID, "solve_sgpe: T and ecut must be >= 0");
-  if (sg->ecut > 0 && sg->T > 0)
-    return fail(c, GPE_ERR_UNSUPPORTED, "solve_sgpe: the energy cut-off mask (ecut > 0 with T > 0) is not supported");
   if (c->prm.omega != 0.0)
     return fail(c, GPE_ERR_UNSUPPORTED, "solve_sgpe: omega != 0 (the reference's Lz Crank-Nicolson branch)");
   if (!prm->vtd) CHECK(need_V(c));

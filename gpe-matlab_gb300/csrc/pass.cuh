@@ -255,7 +255,7 @@ __device__ __forceinline__ void apply_phase(cx<double>* v, const cx<double>* __r
 // at 256^3; at 512 the larger buffers cost occupancy and it was slower.
 template <typename R, class P, int KIND>
 struct SmemTables {
-  static constexpr bool value = GPE_SMEM_TABLES && sizeof(R) == 4 && KIND == KIND_STEP && P::N <= 256;
+  static constexpr bool value = GPE_SMEM_TABLES && sizeof(R) == 4 && KIND != KIND_ENERGY && P::N <= 256;
 };
 template <typename R, class P, class L, int KIND>
 constexpr size_t pass_smem_bytes() {
@@ -463,14 +463,33 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
       prologue<R, E>(v, sv, a, valid, first, dm, scal[0], scal[1]);
     }
     constexpr bool SMT = SmemTables<R, P, KIND>::value;
-    St::template forward<SMT>(v, sm, pol, t, tws);
-    apply_phase<T, E, SMT>(v, php, t);
-    if (a.rot) {
-      // rotating frame: the cross term of this pencil's transverse coordinate
-      const unsigned ci = valid ? (unsigned)b % (unsigned)a.rot_period : 0u;
-      apply_phase<T, E, false>(v, a.rot + (size_t)ci * P::N, t);
+    if constexpr (KIND == KIND_STEP_EXT) {
+      if (!a.skip_fwd) {
+        St::template forward<SMT>(v, sm, pol, t, tws);
+        apply_phase<T, E, SMT>(v, php, t);
+        if (a.rot) {
+          // rotating frame: the cross term of this pencil's transverse coordinate
+          const unsigned ci = valid ? (unsigned)b % (unsigned)a.rot_period : 0u;
+          apply_phase<T, E, false>(v, a.rot + (size_t)ci * P::N, t);
+        }
+        if (a.mask_c) {
+          // energy cut-off, ekk .* (kk < ecut) (SGPEtask/solve_split.m:40-42)
+          R kab = R(0);
+          if (valid) {
+            kab = __ldg(a.mask_a + b % a.mask_pa);
+            if (a.mask_b) kab += __ldg(a.mask_b + b / a.mask_pa);
+          }
+#pragma unroll
+          for (int m = 0; m < E; ++m)
+            if (!(kab + __ldg(a.mask_c + m * T + t) < a.ecut)) v[m] = mk<R>(R(0), R(0));
+        }
+      }
+      if (!a.skip_inv) St::template inverse<SMT>(v, sm, pol, t, tws);
+    } else {
+      St::template forward<SMT>(v, sm, pol, t, tws);
+      apply_phase<T, E, SMT>(v, php, t);
+      St::template inverse<SMT>(v, sm, pol, t, tws);
     }
-    St::template inverse<SMT>(v, sm, pol, t, tws);
     Kahan<R> acc[3];
     if (a.epi != EPI_NONE) {
       load_side();

@@ -37,9 +37,12 @@ int device_sm_count();
 
 template <typename R, class P, class L>
 static cudaError_t launch_layout(const PassArgs<R>& a, cudaStream_t s) {
-  auto kern = a.kind == KIND_ENERGY ? pass_kernel<R, P, L, KIND_ENERGY> : pass_kernel<R, P, L, KIND_STEP>;
-  const size_t smem =
-      a.kind == KIND_ENERGY ? pass_smem_bytes<R, P, L, KIND_ENERGY>() : pass_smem_bytes<R, P, L, KIND_STEP>();
+  auto kern = a.kind == KIND_ENERGY     ? pass_kernel<R, P, L, KIND_ENERGY>
+              : a.kind == KIND_STEP_EXT ? pass_kernel<R, P, L, KIND_STEP_EXT>
+                                        : pass_kernel<R, P, L, KIND_STEP>;
+  const size_t smem = a.kind == KIND_ENERGY     ? pass_smem_bytes<R, P, L, KIND_ENERGY>()
+                      : a.kind == KIND_STEP_EXT ? pass_smem_bytes<R, P, L, KIND_STEP_EXT>()
+                                                : pass_smem_bytes<R, P, L, KIND_STEP>();
   // Above 32 KB of dynamic shared memory opt in explicitly: the static
   // reduction scratch counts toward the 48 KB default limit too.
   if (smem > 32 * 1024) {

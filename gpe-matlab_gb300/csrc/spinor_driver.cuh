@@ -1,0 +1,222 @@
+// spinor_driver.cuh - host driver of the coherently coupled two-component
+// split step (GPEtaskSpinor.solve_split, lib/@GPEtaskSpinor/solve_split.m of
+// GPE-MATLAB) and its observables (GPEtaskSpinor.m:53-110).  Included by
+// gpe_api.cu after the single-component drivers, whose pass, table and
+// scalar helpers it uses.
+//
+// Per block of n_recalc steps (solve_split.m:66-113):
+//   K/2 passes | (NL+coupling, K passes) x n_rec, the last K taking the
+//   half-step factors (ekk .* ekkm = exp(-kk dt/2)) | kinetic sums, spinor
+//   sums, finalizer (ncur, renormalisation factor kept pending, mu)
+// The pending factor is applied by the next block's first NL kernel (the K/2
+// passes before it are linear) or by materialize() when the state is read.
+#pragma once
+
+// The step constants of solve_split.m:61-64: cosom = cosh(dt |c|),
+// sinomm/sinomp = sinh(dt |c|) exp(-/+ i angle(c)), in FP64, rounded once.
+template <typename R>
+SpinorNL<R> spinor_nl_consts(const gpe_ctx* c, double dre, double dim) {
+  const gpe_spinor_params& p = c->spin;
+  SpinorNL<R> q;
+  q.g11 = (R)p.g[0];
+  q.g12 = (R)p.g[1];
+  q.g21 = (R)p.g[2];
+  q.g22 = (R)p.g[3];
+  q.dre = (R)dre;
+  q.dim = (R)dim;
+  const std::complex<double> dt(dre, dim), cpl(p.coupling_re, p.coupling_im);
+  const double ac = std::abs(cpl), cang = std::arg(cpl);
+  const std::complex<double> co = std::cosh(dt * ac), sh = std::sinh(dt * ac);
+  const std::complex<double> sm = sh * std::exp(std::complex<double>(0.0, -cang));
+  const std::complex<double> sp = sh * std::exp(std::complex<double>(0.0, cang));
+  q.cosom = mk<R>((R)co.real(), (R)co.imag());
+  q.sinomm = mk<R>((R)sm.real(), (R)sm.imag());
+  q.sinomp = mk<R>((R)sp.real(), (R)sp.imag());
+  q.nl = p.nlincpl != 0.0;
+  q.nlincpl = (R)p.nlincpl;
+  q.cre = (R)p.coupling_re;
+  q.cim = (R)p.coupling_im;
+  return q;
+}
+
+// Kinetic sums over both components, the spinor sums against Vsum and the
+// finalizer in `mode` (0 run start, 1 block end, 2 observables).
+template <typename R>
+gpe_status spinor_finalize(gpe_ctx* c, Field& f, const R* Vsum, int mode, double time2, double* hist,
+                           bool renorm, double* obs) {
+  int nk[3] = {0, 0, 0};
+  CHECK(energy_passes<R>(c, f, false, nk, nullptr));
+  int ns;
+  {
+    Launch L(c, PC_NORM, (double)c->PS * (2 * sizeof(R) + sizeof(R)));
+    ns = launch_spinor_sums<R>((const cx<R>*)f.psi, Vsum, c->P, c->sc, c->spin_part, c->stream);
+    CU(cudaGetLastError());
+  }
+  SpinorFinalArgs a{};
+  a.sums = c->spin_part;
+  a.nsum = ns;
+  a.partials = c->partials;
+  a.cap = c->cap;
+  for (int k = 0; k < 3; ++k) a.nblk_kin[k] = nk[k];
+  a.weight = c->weight;
+  for (int k = 0; k < 4; ++k) a.g[k] = c->spin.g[k];
+  a.cre = c->spin.coupling_re;
+  a.cim = c->spin.coupling_im;
+  a.mode = mode;
+  a.Ntotal = c->prm.Ntotal;
+  a.renorm = renorm;
+  a.tau = c->prm.decay_rate;
+  a.time2 = time2;
+  a.hist = hist;
+  a.obs = obs;
+  Launch L(c, PC_FINALIZE, 0);
+  launch_finalize_spinor(a, c->sc, c->stream);
+  CU(cudaGetLastError());
+  return GPE_OK;
+}
+
+// getVtotal(time) of a time-dependent potential into the copy that the mu
+// sums read (GPEtaskSpinor.applyham evaluates V at current_time,
+// GPEtaskSpinor.m:53-58, while the step uses the block's time).
+template <typename R>
+gpe_status spinor_vmu(gpe_ctx* c, const gpe_split_params* prm, double time) {
+  const size_t n = (size_t)c->PS;
+  if (!c->Vmu) CU(cudaMalloc(&c->Vmu, n * sizeof(double)));
+  if (sizeof(R) == 8) c->VmuR = nullptr;
+  else if (!c->VmuR) CU(cudaMalloc(&c->VmuR, n * sizeof(R)));
+  std::vector<double> h(n);
+  if (prm->vtd(prm->vtd_user, time, h.data()) != 0)
+    return fail(c, GPE_ERR_CALLBACK, "solve_split: potential callback failed");
+  CU(cudaMemcpyAsync(c->Vmu, h.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (sizeof(R) == 4) {
+    Launch L(c, PC_ELEMENTWISE, (double)n * 12);
+    launch_convert_re<double, float>(c->Vmu, (float*)c->VmuR, (long long)n, c->stream);
+    CU(cudaGetLastError());
+  }
+  CU(cudaStreamSynchronize(c->stream));  // h is pageable and goes out of scope
+  return GPE_OK;
+}
+
+template <typename R>
+const R* spinor_vmu_ptr(gpe_ctx* c) {
+  return sizeof(R) == 8 ? (const R*)c->Vmu : (const R*)c->VmuR;
+}
+
+// GPEtaskSpinor.solve_split (solve_split.m:1-119) from the current state.
+template <typename R>
+gpe_status spinor_split_impl(gpe_ctx* c, const gpe_split_params* prm) {
+  Field& f = c->main;
+  const double ddt = prm->ddt, gam = c->prm.gamma;
+  const int n_rec = c->prm.n_recalc;
+  if (n_rec < 1) return fail(c, GPE_ERR_INVALID, "n_recalc must be >= 1");
+  // jj = 1:niter_inner/n_rec (solve_split.m:66): floor(niter_inner/n_rec) blocks
+  if (prm->niter_inner < n_rec)
+    return fail(c, GPE_ERR_INVALID, "solve_split (spinor): niter_inner < n_recalc runs no block (solve_split.m:66)");
+  const int nb = prm->niter_inner / n_rec;
+  const int start = c->cur.current_iter, nout = prm->niter_outer;
+  const std::complex<double> dtc = ddt * std::complex<double>(0.0, 1.0) / std::complex<double>(1.0, gam);  // :41
+  const double dre = dtc.real(), dim = dtc.imag();
+  CHECK(set_kinop<R>(c, f, dre, dim));
+  CHECK(materialize<R>(c));
+  launch_reset_scalars(c->sc, c->stream);
+  const bool vtd = prm->vtd != nullptr;
+  if (vtd) CHECK(spinor_vmu<R>(c, prm, c->cur.current_time));
+  // NN0 (:29-37) and mu = sum_j real(inner(phi_j, hphi_j))/NN0 (:52-57)
+  CHECK(spinor_finalize<R>(c, f, vtd ? spinor_vmu_ptr<R>(c) : (const R*)f.V, 0, 0.0, nullptr, false, nullptr));
+  const SpinorNL<R> q = spinor_nl_consts<R>(c, dre, dim);
+  const std::vector<AxisPass> full = axis_passes(c);
+  std::vector<AxisPass> half = full;
+  for (auto& ap : half) ap.half = 1;
+  const int nsteps_out = std::max(0, nout - start);
+  const size_t hlen = 2 * (size_t)std::max(1, nsteps_out);
+  if (c->d_hist_len < hlen) {
+    cudaFree(c->d_hist);
+    c->d_hist = nullptr;
+    CU(cudaMalloc(&c->d_hist, hlen * sizeof(double)));
+    c->d_hist_len = hlen;
+  }
+  CU(cudaMemsetAsync(c->d_hist, 0, hlen * sizeof(double), c->stream));
+  const double dt_outer = ddt * prm->niter_inner;
+  int vk = 0, last_j = start;
+  double time2 = c->cur.current_time;
+  bool stopped = false;
+  for (int j = start + 1; j <= nout && !stopped; ++j) {
+    const double time = (j - 1) * dt_outer;
+    for (int jj = 1; jj <= nb; ++jj) {
+      time2 = time + (jj - 1) * ddt * n_rec;
+      if (vtd) CHECK(vtd_upload<R>(c, prm, time2, vk));  // VV = getVtotal(time2) (:69)
+      for (const auto& ap : half) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dre, dim, nullptr));
+      for (int i = 1; i <= n_rec; ++i) {
+        {
+          Launch L(c, PC_NL_PHASE, (double)c->PS * (4 * sizeof(R) + sizeof(R)));
+          launch_spinor_nl<R>((cx<R>*)f.psi, (const R*)f.V, c->P, c->sc, i == 1, q, c->stream);
+          CU(cudaGetLastError());
+        }
+        for (const auto& ap : (i == n_rec ? half : full))
+          CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dre, dim, nullptr));
+      }
+      double* hist = (jj == nb) ? c->d_hist + 2 * (size_t)(j - start - 1) : nullptr;
+      CHECK(spinor_finalize<R>(c, f, vtd ? spinor_vmu_ptr<R>(c) : (const R*)f.V, 1, time2, hist, gam > 0,
+                               nullptr));
+    }
+    last_j = j;
+    // ext_callback (:115): current_time = time2 from here on
+    if (prm->on_step || vtd) {
+      DevScalars h;
+      CHECK(read_scalars(c, &h));
+      if (h.nonfinite) break;
+      c->cur.current_iter = j;
+      c->cur.current_time = time2;
+      c->cur.current_mu = h.muc;
+      c->cur.current_n = h.ncur;
+      if ((int)c->hist_mu.size() < j) {
+        c->hist_mu.resize(j, 0.0);
+        c->hist_n.resize(j, 0.0);
+      }
+      c->hist_mu[j - 1] = h.muc;
+      c->hist_n[j - 1] = h.ncur;
+      if (prm->on_step && prm->on_step(prm->step_user, j, time2, h.muc, h.ncur) != 0) stopped = true;
+      if (vtd && !stopped && j < nout) CHECK(spinor_vmu<R>(c, prm, time2));
+    }
+  }
+  DevScalars h;
+  CHECK(read_scalars(c, &h));
+  if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
+  if (last_j > start) {
+    std::vector<double> dh(2 * (size_t)(last_j - start));
+    CU(cudaMemcpy(dh.data(), c->d_hist, dh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if ((int)c->hist_mu.size() < last_j) {
+      c->hist_mu.resize(last_j, 0.0);
+      c->hist_n.resize(last_j, 0.0);
+    }
+    for (int j = start + 1; j <= last_j; ++j) {
+      c->hist_mu[j - 1] = dh[2 * (size_t)(j - start - 1)];
+      c->hist_n[j - 1] = dh[2 * (size_t)(j - start - 1) + 1];
+    }
+    c->cur.current_iter = last_j;
+    c->cur.current_time = time2;
+    c->cur.current_mu = h.muc;
+    c->cur.current_n = h.ncur;
+  }
+  return GPE_OK;
+}
+
+// applyham / get_energy pieces of both components at the current V.
+template <typename R>
+gpe_status spinor_observables(gpe_ctx* c, gpe_obs* o) {
+  CHECK(materialize<R>(c));
+  launch_reset_scalars(c->sc, c->stream);
+  double* obs = c->spin_part + (size_t)SP_NSUMS * 8 * c->sms;
+  CHECK(spinor_finalize<R>(c, c->main, (const R*)c->main.V, 2, 0.0, nullptr, false, obs));
+  double v[5];
+  CU(cudaMemcpyAsync(v, obs, sizeof(v), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  o->norm = v[0];
+  o->ekin = v[1];
+  o->epot = v[2];
+  o->eint = v[3];
+  o->ecpl = v[4];
+  o->mu_integral = v[1] + v[2] + v[3] + v[4];
+  o->energy = v[1] + v[2] + 0.5 * v[3] + v[4];  // get_energy halves g (GPEtaskSpinor.m:98-110)
+  return GPE_OK;
+}

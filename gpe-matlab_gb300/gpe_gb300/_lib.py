@@ -68,7 +68,12 @@ class gpe_current(C.Structure):
 
 class gpe_obs(C.Structure):
     _fields_ = [("norm", C.c_double), ("ekin", C.c_double), ("epot", C.c_double), ("eint", C.c_double),
-                ("mu_integral", C.c_double), ("energy", C.c_double)]
+                ("mu_integral", C.c_double), ("energy", C.c_double), ("ecpl", C.c_double)]
+
+
+class gpe_spinor_params(C.Structure):
+    _fields_ = [("g", C.c_double * 4), ("coupling_re", C.c_double), ("coupling_im", C.c_double),
+                ("nlincpl", C.c_double)]
 
 
 class gpe_kernel_stat(C.Structure):
@@ -83,6 +88,9 @@ _F = C.POINTER(C.c_float)
 # name -> (restype, argtypes); exactly the functions include/gpe.h declares.
 PROTOTYPES = {
     "gpe_create": (C.c_int, [C.POINTER(gpe_grid_desc), C.POINTER(_P)]),
+    "gpe_create_spinor": (C.c_int, [C.POINTER(gpe_grid_desc), C.POINTER(_P)]),
+    "gpe_set_spinor_params": (C.c_int, [_P, C.POINTER(gpe_spinor_params)]),
+    "gpe_get_spinor_params": (C.c_int, [_P, C.POINTER(gpe_spinor_params)]),
     "gpe_destroy": (None, [_P]),
     "gpe_last_error": (C.c_char_p, [_P]),
     "gpe_abi_version": (C.c_int, []),

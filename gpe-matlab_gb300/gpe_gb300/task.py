@@ -102,7 +102,7 @@ class GPEtask:
             raise NotImplementedError("array omega (Lz Crank-Nicolson, ssft_kin_step.m:3-11) is not supported")
         p = L.gpe_params()
         p.omega = float(self.omega)
-        p.g = float(self.g)
+        p.g = self._g_scalar()
         p.gamma = float(self.gamma)
         p.decay_rate = float(self.decay_rate)
         p.Ntotal = float(self.Ntotal)
@@ -118,6 +118,9 @@ class GPEtask:
         cur.current_mu = float(self.current_mu)
         cur.current_n = float(self.current_n)
         L.check(self._ctx, L.lib.gpe_set_current(self._ctx, C.byref(cur)))
+
+    def _g_scalar(self):
+        return float(self.g)
 
     def _upload_V(self, V):
         key = (id(V), V.ctypes.data)
@@ -261,12 +264,10 @@ class GPEtask:
         errors = []
         vtd_cb = L.VTD_FN()
         if self._time_dependent():
-            P = self.grid.npoints
 
             def _vtd(user, time, out):
                 try:
-                    v = np.asarray(self.getVtotal(time), dtype=np.float64)
-                    np.ctypeslib.as_array(out, shape=(P,))[:] = np.broadcast_to(v, self.grid.shape).ravel()
+                    self._vtd_fill(time, out)
                     return 0
                 except BaseException as e:  # surfaced after the call returns
                     errors.append(e)
@@ -301,6 +302,11 @@ class GPEtask:
         L.check(self._ctx, st)
         self._after_split()
         return self.current_state
+
+    def _vtd_fill(self, time, out):
+        """getVtotal(time) into the library's buffer (P doubles)."""
+        v = np.asarray(self.getVtotal(time), dtype=np.float64)
+        np.ctypeslib.as_array(out, shape=(self.grid.npoints,))[:] = np.broadcast_to(v, self.grid.shape).ravel()
 
     def _sync_history(self):
         n = C.c_int()
@@ -424,6 +430,147 @@ class SGPEtask(GPEtask):
         sg.ecut = float(self.ecut)
         sg.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
         return self._run_split(ddt, niter_inner, niter_outer, sg)
+
+
+class GPEtaskSpinor(GPEtask):
+    """GPEtaskSpinor(grid, {V1, V2}) (lib/@GPEtaskSpinor/GPEtaskSpinor.m:1-147):
+    two coherently coupled components.  ``trappot`` is a pair of arrays or
+    V(X, Y, Z) callables; ``g`` a 2x2 matrix; ``coupling`` the (complex) Rabi
+    coupling, ``nlincpl`` its density-dependent part.  States are pairs
+    [phi1, phi2].  solve_split runs GPEtaskSpinor.solve_split on the GPU
+    (one context holding both components); ``Vtd`` is a callable added to
+    both potentials or a pair of callables (GPEtaskSpinor.m:23-42).  The
+    spinor's groundstate_itp is not built; omega must be 0."""
+
+    def __init__(self, grid: _GridBase, trappot, device: int = 0):
+        self.grid = grid
+        self._ctx = C.c_void_p()
+        L.check(None, L.lib.gpe_create_spinor(C.byref(grid.desc(device)), C.byref(self._ctx)))
+        self.g = np.zeros((2, 2))
+        self.coupling = 0.0
+        self.nlincpl = 0.0
+        self.ncomp = 2
+        self.omega = 0.0
+        self.n_recalc = 10
+        self.gamma = 0.0
+        self.decay_rate = 0.0
+        self.Ntotal = 0.0
+        self.mu_init = 0.0
+        self.Vtd = None
+        self.V0 = 0
+        self.user_callback = None
+        self.history = {"mu": np.zeros(0), "n": np.zeros(0)}
+        self.current_time = 0.0
+        self.current_iter = 0
+        self.current_mu = 0.0
+        self.current_n = 0.0
+        self.init_state = [np.zeros(grid.shape, np.complex128), np.zeros(grid.shape, np.complex128)]
+        self._current_state = None
+        self._state_on_device = None
+        self._V_key = None
+        if len(trappot) != 2:
+            raise ValueError("GPEtaskSpinor: two trap potentials (one per component)")
+        X, Y, Z = grid.mesh["x"], grid.mesh["y"], grid.mesh["z"]
+        self.Vtrap = [f(X, Y, Z) if callable(f) else f for f in trappot]
+
+    @property
+    def Vtrap(self):
+        return self._Vtrap
+
+    @Vtrap.setter
+    def Vtrap(self, v):
+        self._Vtrap = [np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), self.grid.shape))
+                       for x in v]
+        self._V_key = None
+
+    @property
+    def current_state(self):
+        if self._state_on_device == "current" and self._current_state is None:
+            self._current_state = self._download()
+        return self._current_state
+
+    @current_state.setter
+    def current_state(self, v):
+        self._current_state = None if v is None else [np.asarray(x, dtype=np.complex128) for x in v]
+        self._state_on_device = None
+
+    def _g_scalar(self):
+        return 0.0  # the matrix goes through gpe_set_spinor_params
+
+    def _push_params(self):
+        super()._push_params()
+        p = L.gpe_spinor_params()
+        g = np.broadcast_to(np.asarray(self.g, dtype=np.float64), (2, 2))
+        for k in range(4):
+            p.g[k] = float(g[k // 2, k % 2])
+        cpl = complex(self.coupling)
+        p.coupling_re, p.coupling_im = cpl.real, cpl.imag
+        p.nlincpl = float(self.nlincpl)
+        L.check(self._ctx, L.lib.gpe_set_spinor_params(self._ctx, C.byref(p)))
+
+    def _pair(self, v, dtype):
+        return np.ascontiguousarray(np.concatenate([np.broadcast_to(np.asarray(x), self.grid.shape).ravel()
+                                                    for x in v]), dtype=dtype)
+
+    def _upload_V(self, V):
+        key = tuple((id(x), x.ctypes.data) for x in V)
+        if key == self._V_key:
+            return
+        flat = self._pair(V, np.float64)
+        L.check(self._ctx, L.lib.gpe_set_potential(self._ctx, L.dptr(flat)))
+        self._V_key = key
+        self._V_keep = V
+
+    def _upload_state(self, phi):
+        flat = self._pair(phi, np.complex128)
+        L.check(self._ctx, L.lib.gpe_set_state(self._ctx, L.dptr(flat.view(np.float64))))
+
+    def _download(self, out=None):
+        dt = np.complex64 if self.grid.precision == "single" else np.complex128
+        flat = np.empty(2 * self.grid.npoints, dtype=dt)
+        if dt == np.complex64:
+            L.check(self._ctx, L.lib.gpe_get_state_f32(self._ctx, L.fptr(flat.view(np.float32))))
+        else:
+            L.check(self._ctx, L.lib.gpe_get_state(self._ctx, L.dptr(flat.view(np.float64))))
+        n = self.grid.npoints
+        return [flat[:n].reshape(self.grid.shape), flat[n:].reshape(self.grid.shape)]
+
+    def getVtotal(self, time):
+        """GPEtaskSpinor.m:23-42 (the internal V0 branch is not mirrored)."""
+        if callable(self.Vtd):
+            return [V + self.Vtd(self, time) for V in self.Vtrap]
+        if isinstance(self.Vtd, (list, tuple)):
+            return [V + f(self, time) for V, f in zip(self.Vtrap, self.Vtd)]
+        return self.Vtrap
+
+    def _time_dependent(self):
+        return self.Vtd is not None
+
+    def _vtd_fill(self, time, out):
+        P = self.grid.npoints
+        V = self.getVtotal(time)
+        arr = np.ctypeslib.as_array(out, shape=(2 * P,))
+        for k in range(2):
+            arr[k * P:(k + 1) * P] = np.broadcast_to(np.asarray(V[k], dtype=np.float64), self.grid.shape).ravel()
+
+    def groundstate_itp(self, *args, **kwargs):
+        raise NotImplementedError("GPEtaskSpinor.groundstate_itp is not built (split-step dynamics only)")
+
+    def observables(self, phi=None):
+        """<psi|H psi> pieces of the pair (default: the current device state),
+        V at current_time (GPEtaskSpinor.applyham)."""
+        self._push_params()
+        self._upload_V(self.getVtotal(self.current_time))
+        if phi is not None:
+            self._upload_state(phi)
+            self._state_on_device = None
+        o = L.gpe_obs()
+        L.check(self._ctx, L.lib.gpe_observables(self._ctx, C.byref(o)))
+        return {k: getattr(o, k) for k, _ in L.gpe_obs._fields_}
+
+    def get_energy(self, phi=None):
+        """GPEtaskSpinor.m:98-110."""
+        return self.observables(phi if phi is not None else self.current_state)["energy"]
 
 
 def noise_variates(seed, step, n):

@@ -216,6 +216,27 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     p.on_step = step_cb;
     p.step_user = &s;
     check(c, gpe_solve_split(c, &p));
+  } else if (cmd == "sgpe") {
+    // gpe_mex('sgpe', h, ddt, nin, nout, task, timedep, T, ecut, seed): SGPEtask.solve_split
+    if (nrhs != 10) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('sgpe', h, ddt, nin, nout, task, timedep, T, ecut, seed)");
+    SplitCtx s{prhs[5], (size_t)mxGetScalar(mxGetProperty(prhs[5], 0, "gb300_npts"))};
+    gpe_split_params p;
+    memset(&p, 0, sizeof(p));
+    p.ddt = scalar(prhs[2]);
+    p.niter_inner = (int)scalar(prhs[3]);
+    p.niter_outer = (int)scalar(prhs[4]);
+    if (scalar(prhs[6]) != 0) {
+      p.vtd = vtd_cb;
+      p.vtd_user = &s;
+    }
+    p.on_step = step_cb;
+    p.step_user = &s;
+    gpe_sgpe_params sg;
+    memset(&sg, 0, sizeof(sg));
+    sg.T = scalar(prhs[7]);
+    sg.ecut = scalar(prhs[8]);
+    sg.seed = (unsigned long long)scalar(prhs[9]);
+    check(c, gpe_solve_sgpe(c, &p, &sg));
   } else if (cmd == "observables") {
     gpe_obs o;
     check(c, gpe_observables(c, &o));

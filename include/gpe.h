@@ -139,9 +139,9 @@ typedef struct {
 /* Stochastic GPE, lib/@SGPEtask (SGPEtask.m:1-48, solve_split.m:1-81). */
 typedef struct {
     double T;                  /* temperature                                   [0] */
-    double ecut;               /* noise energy cut-off; with T > 0 only 0 (none) is
-                                  supported (the k-space mask of solve_split.m:41-46
-                                  does not factorise over axes)                     */
+    double ecut;               /* energy cut-off: with T > 0 and ecut > 0 the kinetic
+                                  factor is exp(-kk*dt) .* (kk < ecut)
+                                  (solve_split.m:40-42); 0: no cut-off              */
     unsigned long long seed;   /* noise stream: Philox4x32-10 keyed by seed with the
                                   counter (grid point, global step index)           */
 } gpe_sgpe_params;
@@ -154,15 +154,31 @@ typedef struct {
     double current_n;
 } gpe_current;
 
-/* <psi|H psi> pieces, GPEtask.m:73-107 (omega = 0). */
+/* <psi|H psi> pieces, GPEtask.m:73-107 (omega = 0).  Spinor contexts
+ * (GPEtaskSpinor.m:53-110): sums over both components, eint =
+ * sum_jk g(j,k) integrate(|psi_j|^2 |psi_k|^2), ecpl = the coupling term
+ * 2 Re(coupling * inner(psi_1, psi_2)); 0 for one component. */
 typedef struct {
     double norm;            /* integrate(|psi|^2)                                */
     double ekin;            /* real(inner(psi, lap(psi)))                        */
     double epot;            /* integrate(V |psi|^2)                              */
     double eint;            /* g * integrate(|psi|^4)                            */
-    double mu_integral;     /* real(inner(psi, applyham(psi))) = ekin+epot+eint  */
-    double energy;          /* get_energy(psi) = ekin + epot + eint/2            */
+    double mu_integral;     /* real(inner(psi, applyham(psi)))
+                               = ekin + epot + eint + ecpl                       */
+    double energy;          /* get_energy(psi) = ekin + epot + eint/2 + ecpl     */
+    double ecpl;            /* coherent coupling energy (spinor)                 */
 } gpe_obs;
+
+/* Coherently coupled two-component condensate, lib/@GPEtaskSpinor
+ * (GPEtaskSpinor.m:4-8; solve_split.m:61-91).  The other properties
+ * (gamma, decay_rate, Ntotal, n_recalc; omega must be 0) come from
+ * gpe_set_params, whose g is not used by a spinor context. */
+typedef struct {
+    double g[4];            /* interaction matrix g(j,k) at g[2*(j-1)+(k-1)]     */
+    double coupling_re;     /* coupling (Rabi frequency), complex      [0]       */
+    double coupling_im;
+    double nlincpl;         /* density-dependent coupling               [0]       */
+} gpe_spinor_params;
 
 /* Per-kernel-class timings collected while profiling is enabled. */
 typedef struct {
@@ -175,6 +191,15 @@ typedef struct {
 /* ---- context ---------------------------------------------------------- */
 /* grid2d/grid3d init + GPEtask constructor (GPEtask.m:41-60). */
 GPE_API gpe_status gpe_create(const gpe_grid_desc *desc, gpe_ctx **out);
+/* A two-component (GPEtaskSpinor) context on the same grid.  Its state,
+ * potential and Vtd buffers hold both components, component 1 then 2
+ * (2*nx*ny*nz points: MATLAB's {phi1, phi2} / {V1, V2} concatenated);
+ * gpe_solve_split runs GPEtaskSpinor.solve_split and gpe_observables its
+ * applyham/get_energy.  ITP, the adjoint, SGPE, batching and the autotuner
+ * return GPE_ERR_UNSUPPORTED on it. */
+GPE_API gpe_status gpe_create_spinor(const gpe_grid_desc *desc, gpe_ctx **out);
+GPE_API gpe_status gpe_set_spinor_params(gpe_ctx *ctx, const gpe_spinor_params *p);
+GPE_API gpe_status gpe_get_spinor_params(const gpe_ctx *ctx, gpe_spinor_params *p);
 GPE_API void gpe_destroy(gpe_ctx *ctx);
 /* Message of the last failed call on ctx (ctx may be NULL: last failure of
  * gpe_create on this thread). Never NULL. */
@@ -221,7 +246,14 @@ GPE_API gpe_status gpe_host_unregister(void *ptr);
 GPE_API gpe_status gpe_groundstate_itp(gpe_ctx *ctx, const gpe_itp_params *prm,
                                double *MU, double *MU2, double *EE, int cap,
                                gpe_itp_result *res);
-/* solve_split.m:1-84 from the current state; resumes at current_iter. */
+/* solve_split.m:1-84 from the current state; resumes at current_iter.
+ * Spinor context: lib/@GPEtaskSpinor/solve_split.m:1-119 (kinetic half step
+ * at each block start, per step the nonlinear and coupling factor then the
+ * kinetic step, the inverse half step at the block end; blocks of n_recalc
+ * steps, floor(niter_inner/n_recalc) of them; renormalised to Ntotal (with
+ * decay) when gamma > 0; mu = <psi|H psi>/N at each block end with V at
+ * current_time, as GPEtaskSpinor.applyham evaluates it).  vtd fills 2*P
+ * doubles (V1 then V2). */
 GPE_API gpe_status gpe_solve_split(gpe_ctx *ctx, const gpe_split_params *prm);
 /* solve_split on `count` independent contexts (any grid sizes, same device,
  * same n_recalc and current_iter) advanced together: one block of n_recalc
@@ -247,8 +279,11 @@ GPE_API gpe_status gpe_adjoint_grad(gpe_ctx *ctx, const gpe_adjoint_params *prm,
 /* SGPEtask.solve_split (lib/@SGPEtask/solve_split.m:1-81) from the current
  * state: mu = mu_init throughout, no renormalisation, and before every
  * kinetic step psi += sqrt(T*gamma*ddt/weight) * (n1 + i*n2) with n1, n2
- * standard normal variates (solve_split.m:49,55).  history.mu holds mu_init,
- * history.n the norm.  Vtd and on_step work as in gpe_solve_split; omega must
+ * standard normal variates (solve_split.m:49,55).  With T > 0 and ecut > 0
+ * the modes with kk >= ecut are zeroed in every kinetic step (five axis
+ * passes in 3D, three in 2D, instead of three and two; kk is summed in the
+ * context's precision, so a mode within rounding of ecut may fall either
+ * way).  history.mu holds mu_init, history.n the norm.  Vtd and on_step work as in gpe_solve_split; omega must
  * be 0 (the reference's rotating SGPE uses the Lz Crank-Nicolson branch). */
 GPE_API gpe_status gpe_solve_sgpe(gpe_ctx *ctx, const gpe_split_params *prm, const gpe_sgpe_params *sg);
 /* applyham / get_energy pieces for the current state at the current V. */

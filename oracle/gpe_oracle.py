@@ -543,6 +543,133 @@ class SGPEtask(GPEtask):
 
 
 # ---------------------------------------------------------------------------
+# Coherently coupled two-component condensate: lib/@GPEtaskSpinor
+# ---------------------------------------------------------------------------
+class GPEtaskSpinor(GPEtask):
+    """GPEtaskSpinor (lib/@GPEtaskSpinor/GPEtaskSpinor.m:1-147): states and
+    potentials are lists of two arrays, g a 2x2 matrix, ``coupling`` the
+    (complex) Rabi coupling and ``nlincpl`` its density-dependent part.
+    omega == 0 only.  (lib/@GPEtask2comp/solve_split.m is the same loop; that
+    class declares no coupling/nlincpl properties, so it is this one with
+    coupling = nlincpl = 0.)"""
+
+    def __init__(self, grid, trappot):
+        super().__init__(grid, lambda X, Y, Z: 0.0 * X)
+        self.coupling = 0.0
+        self.nlincpl = 0.0
+        self.ncomp = len(trappot)                                        # :13-20
+        X, Y, Z = grid.mesh["x"], grid.mesh["y"], grid.mesh["z"]
+        self.Vtrap = [np.broadcast_to(f(X, Y, Z) if callable(f) else np.asarray(f, np.float64),
+                                      grid.shape).astype(np.float64) for f in trappot]
+        self.g = np.zeros((self.ncomp, self.ncomp))
+        self.init_state = [np.zeros(grid.shape, np.complex128) for _ in range(self.ncomp)]
+
+    # GPEtaskSpinor.m:23-42 (the internal V0 branch is not restated)
+    def getVtotal(self, time):
+        if callable(self.Vtd):
+            return [V + self.Vtd(self, time) for V in self.Vtrap]
+        if isinstance(self.Vtd, (list, tuple)):
+            return [V + f(self, time) for V, f in zip(self.Vtrap, self.Vtd)]
+        return self.Vtrap
+
+    # GPEtaskSpinor.m:53-72 (omega == 0)
+    def applyham1c(self, phi, j, time=None):
+        if time is None:
+            time = self.current_time
+        res = self.getVtotal(time)[j]
+        for k in range(self.ncomp):
+            res = res + self.g[j, k] * np.abs(phi[k]) ** 2
+        res = res * phi[j] + self.grid.lap(phi[j])
+        if j == 0:
+            res = res + self.coupling * phi[1]
+        else:
+            res = res + np.conj(self.coupling) * phi[0]
+        return res
+
+    # GPEtaskSpinor.m:74-82
+    def applyham(self, phi, time=None):
+        return [self.applyham1c(phi, j, time) for j in range(self.ncomp)]
+
+    # GPEtaskSpinor.m:84-89
+    def inner(self, left, right):
+        return sum(self.grid.inner(a, b) for a, b in zip(left, right))
+
+    # GPEtaskSpinor.m:98-110
+    def get_energy(self, phi=None, time=None):
+        if phi is None:
+            phi = self.current_state
+        tmp = self.g
+        self.g = 0.5 * self.g
+        try:
+            res = np.real(self.inner(phi, self.applyham(phi, time)))
+        finally:
+            self.g = tmp
+        return res
+
+    # lib/@GPEtaskSpinor/solve_split.m:1-119
+    def solve_split(self, ddt, niter_inner, niter_outer):
+        grid = self.grid
+        ncomp = self.g.shape[0]                                          # :14
+        g = self.g
+        gam = self.gamma
+        n_rec = self.n_recalc
+        tau = self.decay_rate
+        start = self.current_iter
+        phi = list(self.current_state) if start > 0 else list(self.init_state)  # :23-27
+        if self.Ntotal > 0:                                              # :29-37
+            NN0 = self.Ntotal
+        else:
+            # :33-35; the reference then overwrites NN0 with
+            # integrate(abs(init_state).^2) (:36), which errors on a cell array
+            NN0 = sum(grid.integrate(np.real(p * np.conj(p))) for p in phi)
+        NNN = NN0
+        ncur = NN0
+        dt = ddt * 1j / (1 + 1j * gam)                                   # :41
+        ekk = np.exp(-grid.kk * dt)
+        ekkp = np.exp(-grid.kk * dt * 0.5)
+        ekkm = np.exp(grid.kk * dt * 0.5)
+        tmp2 = [None] * ncomp
+        hphi = self.applyham(phi)                                        # :52-57
+        mu = sum(np.real(grid.inner(phi[j], hphi[j])) for j in range(ncomp)) / NN0
+        dt_outer = ddt * niter_inner
+        time2 = None
+        for j in range(start + 1, niter_outer + 1):                     # :59
+            coupl = self.coupling
+            cang = np.angle(coupl)
+            cosom = np.cosh(dt * abs(coupl))
+            sinomm = np.sinh(dt * abs(coupl)) * np.exp(-1j * cang)
+            sinomp = np.sinh(dt * abs(coupl)) * np.exp(1j * cang)
+            time = (j - 1) * dt_outer
+            for jj in range(1, niter_inner // n_rec + 1):                # :66
+                time2 = time + (jj - 1) * ddt * n_rec
+                VV = self.getVtotal(time2)
+                phi = [grid.ifft(ekkp * grid.fft(p)) for p in phi]       # :72-74
+                for _ in range(n_rec):                                   # :75-96
+                    for i in range(ncomp):
+                        tmp2[i] = VV[i] - mu
+                        for k in range(ncomp):
+                            tmp2[i] = tmp2[i] + g[i, k] * np.abs(phi[k]) ** 2
+                    if self.nlincpl != 0:                                # :84-89
+                        tmp3 = coupl + self.nlincpl * (np.abs(phi[0]) ** 2 + np.abs(phi[1]) ** 2)
+                        cosom = np.cosh(dt * tmp3)
+                        sinomm = np.sinh(dt * tmp3)
+                        sinomp = sinomm
+                    t0 = np.exp(-tmp2[0] * dt) * (cosom * phi[0] - sinomp * phi[1])  # :90-91
+                    t1 = np.exp(-tmp2[1] * dt) * (cosom * phi[1] - sinomm * phi[0])
+                    phi = [grid.ifft(ekk * grid.fft(t)) for t in (t0, t1)]  # :92-94
+                phi = [grid.ifft(ekkm * grid.fft(p)) for p in phi]       # :97-99
+                ncur = np.real(grid.integrate(phi[0] * np.conj(phi[0]) + phi[1] * np.conj(phi[1])))  # :105,111
+                if gam > 0:                                              # :100-109
+                    if tau > 0:
+                        NNN = NN0 * math.exp(-time2 / tau)
+                    phi = [p * math.sqrt(NNN / ncur) for p in phi]
+                hphi = self.applyham(phi)     # at current_time (:107, :112)
+                mu = self.inner(phi, hphi) / NNN
+            self.ext_callback(phi, j, time2, mu, ncur)                   # :115
+        return phi
+
+
+# ---------------------------------------------------------------------------
 # Vortex imprint: examples/example1_vortex.m:26-30 (also README.md:93-97)
 # ---------------------------------------------------------------------------
 def imprint_vortex(grid: Grid, phi, g, x0, y0=0.0):

@@ -21,7 +21,8 @@ int main(void) {
     F(gpe_adjoint_params, precision);
     S(gpe_sgpe_params); F(gpe_sgpe_params, ecut); F(gpe_sgpe_params, seed);
     S(gpe_current); F(gpe_current, current_time);
-    S(gpe_obs); F(gpe_obs, energy);
+    S(gpe_obs); F(gpe_obs, energy); F(gpe_obs, ecpl);
+    S(gpe_spinor_params); F(gpe_spinor_params, coupling_re); F(gpe_spinor_params, nlincpl);
     S(gpe_kernel_stat); F(gpe_kernel_stat, launches); F(gpe_kernel_stat, bytes_per_launch);
     printf("\"end\": 0}\n");
     return 0;

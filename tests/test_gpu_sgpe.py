@@ -8,6 +8,10 @@
 * T > 0: the oracle fed the device's own noise variates: FP32 <= 2e-5.
 * The noise amplitude of one step from a zero state: within 5% of
   sqrt(T gamma ddt / weight) propagated through the kinetic factor.
+* Energy cut-off (ecut > 0 with T > 0, solve_split.m:40-42): the oracle fed
+  the device's noise (a numpy restatement of the generator in FP64), 2D and
+  3D, FP64 <= 1e-11 and FP32 <= 2e-5; one step of pure noise leaves no mode
+  with kk >= ecut.
 """
 import math
 
@@ -37,6 +41,23 @@ def gauss2(seed, step, idx):
     u2 = (r[1] >> 8) * 2.0 ** -24
     rad = math.sqrt(-2.0 * math.log(u1))
     return rad * math.cos(2 * math.pi * u2), rad * math.sin(2 * math.pi * u2)
+
+
+def gauss2_np(seed, step, n):
+    """gauss2 for points 0..n-1 in FP64 (numpy uint64 products)."""
+    i = np.arange(n, dtype=np.uint64)
+    m32 = np.uint64(MASK)
+    c = [i & m32, i >> np.uint64(32), np.full(n, step & MASK, np.uint64), np.full(n, step >> 32, np.uint64)]
+    k0, k1 = seed & MASK, seed >> 32
+    for _ in range(10):
+        p0, p1 = np.uint64(M0) * c[0], np.uint64(M1) * c[2]
+        c = [((p1 >> np.uint64(32)) ^ c[1] ^ np.uint64(k0)) & m32, p1 & m32,
+             ((p0 >> np.uint64(32)) ^ c[3] ^ np.uint64(k1)) & m32, p0 & m32]
+        k0, k1 = (k0 + W0) & MASK, (k1 + W1) & MASK
+    u1 = ((c[0] >> np.uint64(8)) + np.uint64(1)).astype(np.float64) * 2.0 ** -24
+    u2 = (c[1] >> np.uint64(8)).astype(np.float64) * 2.0 ** -24
+    rad = np.sqrt(-2.0 * np.log(u1))
+    return rad * np.cos(2 * np.pi * u2) + 1j * rad * np.sin(2 * np.pi * u2)
 
 
 def rel_l2(a, b):
@@ -134,12 +155,83 @@ def test_sgpe_noise_amplitude(gpe):
 def test_sgpe_unsupported_options(gpe):
     from gpe_gb300 import _lib as L
 
-    task, og, ot = make_pair(gpe, (4.0, 32, 3.5, 32), "single", g=1.0, gamma=0.1, T=1.0, ecut=5.0)
+    task, og, ot = make_pair(gpe, (4.0, 32, 3.5, 32), "single", g=1.0, gamma=0.1, T=1.0, omega=0.5)
     task.init_state = np.ones(og.shape, complex)
     with pytest.raises(gpe.GPEError) as e:
         task.solve_split(0.004, 10, 1)
     assert e.value.status == L.GPE_ERR_UNSUPPORTED
-    task.ecut, task.omega = 0.0, 0.5
+    task.omega, task.ecut = 0.0, float("nan")
     with pytest.raises(gpe.GPEError) as e:
         task.solve_split(0.004, 10, 1)
-    assert e.value.status == L.GPE_ERR_UNSUPPORTED
+    assert e.value.status == L.GPE_ERR_INVALID
+
+
+def cut_between_modes(og, frac):
+    """An ecut at the given fraction of max(kk), moved to the middle of the gap
+    between the two distinct mode energies around it (no mode within rounding)."""
+    kk = np.unique(np.round(og.kk.ravel(), 9))
+    i = np.searchsorted(kk, frac * kk[-1])
+    return 0.5 * (kk[i - 1] + kk[i])
+
+
+@pytest.mark.parametrize("axes", [(4.0, 48, 3.5, 32), (4.0, 32, 3.5, 24, 2.5, 16)], ids=["2d", "3d"])
+@pytest.mark.parametrize("precision", ["double", "single"])
+def test_sgpe_energy_cutoff_matches_oracle(gpe, axes, precision):
+    task, og, ot = make_pair(gpe, axes, precision, g=0.8, gamma=0.1, mu_init=2.0, T=0.5, n_recalc=5)
+    ecut = cut_between_modes(og, 0.3)
+    task.ecut = ot.ecut = ecut
+    task.seed = 99
+    steps = iter(range(10 ** 6))
+
+    def noise(shape):
+        return gauss2_np(task.seed, next(steps), int(np.prod(shape))).reshape(shape)
+
+    ot.noise = noise
+    X, Y = og.mesh["x"], og.mesh["y"]
+    psi0 = (np.exp(-((X - 0.3) ** 2 + Y ** 2) / 2) * np.exp(0.5j * X)).astype(complex)
+    task.init_state = psi0
+    ot.init_state = psi0
+    task.solve_split(0.004, 10, 2)
+    ot.solve_split(0.004, 10, 2)
+    tol = 1e-11 if precision == "double" else 2e-5
+    assert rel_l2(task.current_state, ot.current_state) < tol
+    np.testing.assert_allclose(task.history["n"], ot.history["n"], rtol=tol)
+
+
+@pytest.mark.parametrize("axes", [(8.0, 64, 8.0, 64), (8.0, 32, 8.0, 32, 8.0, 32)], ids=["2d", "3d"])
+def test_sgpe_energy_cutoff_empties_the_high_modes(gpe, axes):
+    """One step of pure noise (V = g = mu = 0) from psi = 0: psi =
+    ifft(ekk .* mask .* fft(noise)), so fft(psi) vanishes where kk >= ecut."""
+    grid = gpe.grid2d(*axes, precision="single") if len(axes) == 4 else gpe.grid3d(*axes, precision="single")
+    task = gpe.SGPEtask(grid, lambda X, Y, Z: 0 * X)
+    og = O.Grid(*axes)
+    task.gamma, task.T, task.seed, task.n_recalc = 0.2, 3.0, 5, 1
+    task.ecut = cut_between_modes(og, 0.25)
+    task.init_state = np.zeros(grid.shape, complex)
+    task.solve_split(0.01, 1, 1)
+    spec = np.abs(og.fft(task.current_state))
+    kept = og.kk < task.ecut
+    assert 0 < kept.sum() < kept.size
+    assert spec[~kept].max() < 1e-5 * spec[kept].max()
+    assert spec[kept].min() > 0
+
+
+def test_sgpe_block_count_follows_sgpe_solve_split(gpe):
+    """@SGPEtask/solve_split.m:54 loops jj = 1:niter_inner/n_recalc without
+    GPEtask's n_recalc = 1 fallback: 15 inner steps at n_recalc = 10 run one
+    block of 10 (time still advances by 15 ddt); 5 < 10 runs none (an error)."""
+    from gpe_gb300 import _lib as L
+
+    task, og, ot = make_pair(gpe, (4.0, 32, 3.5, 24), "double", g=1.0, gamma=0.05, mu_init=1.2, n_recalc=10)
+    X, Y = og.mesh["x"], og.mesh["y"]
+    psi0 = np.exp(-(X ** 2 + Y ** 2) / 2).astype(complex)
+    task.init_state = psi0
+    ot.init_state = psi0
+    task.solve_split(0.004, 15, 2)
+    ot.solve_split(0.004, 15, 2)
+    assert rel_l2(task.current_state, ot.current_state) < 1e-11
+    assert task.current_time == pytest.approx(ot.current_time)
+    task.current_iter = 0
+    with pytest.raises(gpe.GPEError) as e:
+        task.solve_split(0.004, 5, 1)
+    assert e.value.status == L.GPE_ERR_INVALID

@@ -212,6 +212,79 @@ def test_sgpe_zero_temperature_is_gpe_up_to_a_global_phase():
     assert b.history["mu"] == [0.0, 0.0]
 
 
+def test_sgpe_energy_cutoff_masks_the_noise_spectrum():
+    """With T > 0 and ecut > 0 (solve_split.m:40-42) one step of pure noise
+    from psi = 0 (V = g = mu = 0) has no mode with kk >= ecut; with T = 0 the
+    cut-off is not applied."""
+    g = O.Grid(8, 32, 8, 32)
+    t = O.SGPEtask(g, lambda X, Y, Z: 0 * X)
+    t.gamma, t.T, t.ecut, t.n_recalc = 0.2, 2.0, 0.3 * g.kk.max(), 1
+    t.init_state = np.zeros(g.shape, complex)
+    spec = np.abs(g.fft(t.solve_split(0.01, 1, 1, rng=np.random.default_rng(3))))
+    kept = g.kk < t.ecut
+    assert 0 < kept.sum() < kept.size
+    assert spec[~kept].max() < 1e-12 * spec[kept].max()
+    t.T, t.current_iter = 0.0, 0
+    psi0 = np.exp(-(g.mesh["x"] ** 2 + g.mesh["y"] ** 2)).astype(complex)
+    t.init_state = psi0
+    a = t.solve_split(0.01, 2, 1)
+    t.ecut, t.current_iter = 0.0, 0
+    np.testing.assert_array_equal(t.solve_split(0.01, 2, 1), a)
+
+
+def test_spinor_rabi_oscillation_is_exact():
+    """GPEtaskSpinor.solve_split (lib/@GPEtaskSpinor/solve_split.m) with V = 0,
+    g = 0 and a uniform state: the kinetic factors leave k = 0 alone, mu is a
+    common phase, and the coupling matrix of each step is exp(-i H_c ddt),
+    H_c = [[0, c], [conj(c), 0]], so the populations follow cos^2(|c| t)."""
+    g = O.Grid(4, 16, 4, 16)
+    t = O.GPEtaskSpinor(g, [lambda X, Y, Z: 0 * X, lambda X, Y, Z: 0 * X])
+    t.coupling = 0.7 * np.exp(0.4j)
+    t.init_state = [np.ones(g.shape, complex), np.zeros(g.shape, complex)]
+    ddt, nin, nout = 0.01, 10, 3
+    t.solve_split(ddt, nin, nout)
+    N = g.integrate(np.ones(g.shape))
+    n1 = g.integrate(np.abs(t.current_state[0]) ** 2)
+    assert n1 / N == pytest.approx(math.cos(0.7 * ddt * nin * nout) ** 2, abs=1e-12)
+    ratio = t.current_state[1][3, 5] / t.current_state[0][3, 5]
+    # phi2/phi1 = -i tan(|c| t) exp(-i arg c)
+    assert ratio == pytest.approx(-1j * math.tan(0.7 * ddt * nin * nout) * np.exp(-0.4j), abs=1e-12)
+    np.testing.assert_allclose(t.history["n"], N, rtol=1e-12)
+
+
+def test_spinor_conserves_norm_and_matches_single_component_when_decoupled():
+    """gamma = 0: the step is unitary (real coupling with nlincpl as well).
+    Decoupled (coupling = nlincpl = 0, g diagonal, V2 = V1) with phi2 = 0, the
+    first component evolves as GPEtask with the kinetic-first splitting
+    K/2 (N K)^n K^-1/2 of solve_split.m:72-99."""
+    g = O.Grid(5, 32, 5, 24)
+    V = lambda X, Y, Z: 0.5 * (X ** 2 + 1.3 * Y ** 2)
+    X, Y = g.mesh["x"], g.mesh["y"]
+    p1 = np.exp(-((X - 0.4) ** 2 + Y ** 2) / 2) * np.exp(0.3j * Y)
+    p2 = 0.5 * np.exp(-(X ** 2 + (Y - 0.5) ** 2) / 3)
+    t = O.GPEtaskSpinor(g, [V, lambda X, Y, Z: V(X, Y, Z) + 0.2 * X])
+    t.g = np.array([[1.0, 0.6], [0.6, 0.8]])
+    t.coupling, t.nlincpl = 0.3, 0.2
+    t.init_state = [p1, p2]
+    t.solve_split(0.005, 10, 2)
+    N0 = g.integrate(np.abs(p1) ** 2 + np.abs(p2) ** 2)
+    np.testing.assert_allclose(t.history["n"], N0, rtol=1e-12)
+    # decoupled: one component against a direct restatement of the splitting
+    d = O.GPEtaskSpinor(g, [V, V])
+    d.g = np.diag([1.0, 0.5])
+    d.init_state = [p1, np.zeros(g.shape, complex)]
+    d.solve_split(0.005, 10, 1)
+    dt = 0.005j
+    mu = np.real(g.inner(p1, g.lap(p1) + (V(X, Y, 0) + np.abs(p1) ** 2) * p1)) / g.integrate(np.abs(p1) ** 2)
+    ph = g.ifft(np.exp(-g.kk * dt / 2) * g.fft(p1))
+    for _ in range(10):
+        ph = np.exp(-(V(X, Y, 0) - mu + np.abs(ph) ** 2) * dt) * ph
+        ph = g.ifft(np.exp(-g.kk * dt) * g.fft(ph))
+    ph = g.ifft(np.exp(g.kk * dt / 2) * g.fft(ph))
+    np.testing.assert_allclose(d.current_state[0], ph, rtol=0, atol=1e-12)
+    assert np.max(np.abs(d.current_state[1])) == 0
+
+
 def test_golden_fixtures_reproduce():
     from tests.golden import make_golden as MG
 
