@@ -459,6 +459,10 @@ class GPEtaskSpinor(GPEtask):
         self.Vtd = None
         self.V0 = 0
         self.user_callback = None
+        self.itp_max_iter = 5000
+        self.itp_min_iter = 50
+        self.itp_adjust_stepsize = False
+        self.last_itp = None
         self.history = {"mu": np.zeros(0), "n": np.zeros(0)}
         self.current_time = 0.0
         self.current_iter = 0
