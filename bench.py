@@ -513,6 +513,168 @@ def run_adjoint(args, dist):
     task.close()
 
 
+SPIN_METRIC = "spinor split-step grid-pt-steps/s (2 coupled components, complex FP32)"
+
+
+def spinor_cpu_steps(S, pair, cores: int):
+    """One outer step of 10 split steps (n_recalc 10) of the FP64 oracle's
+    GPEtaskSpinor.solve_split on the workload grid: (grid-pt-steps/s, steps, s)."""
+    from oracle import gpe_oracle as O
+
+    O.set_workers(cores)
+    og = O.Grid(S.box, S.n[0], S.box, S.n[1], S.box, S.n[2])
+    ot = O.GPEtaskSpinor(og, S.potentials())
+    S.configure(ot)
+    ot.init_state = [np.asarray(p, dtype=np.complex128) for p in pair]
+    t0 = time.perf_counter()
+    ot.solve_split(S.dt, 10, 1)
+    t = time.perf_counter() - t0
+    return S.npoints * 10 / t, 10, t
+
+
+def spinor_start(gpe, dev):
+    """The damped workload's ITP ground state (untimed), split into the pair."""
+    from gpe_gb300.workloads import DAMPED3D as W, SPINOR3D as S
+
+    _, t1, phi = ground_state(gpe, W, "single", device=dev)
+    phi = np.asarray(phi, dtype=np.complex128)
+    t1.close()
+    return S, S.initial_pair(phi)
+
+
+def run_spinor(args, dist):
+    """The two-component workload: one bench step = one outer step (100 split
+    steps) of GPEtaskSpinor.solve_split, device-timed with CUDA events."""
+    import ctypes as C
+
+    import gpe_gb300 as gpe
+    from gpe_gb300 import _lib as L
+
+    dev = dist.local
+    S, pair = spinor_start(gpe, dev)
+    P = S.npoints
+    inner = S.niter_inner
+    _, task = S.make_task("single", device=dev)
+    task.init_state = pair
+    task.solve_split(S.dt, inner, 1)
+    psi32_1 = [x.astype(np.complex128) for x in task.current_state]
+    mu32 = task.history["mu"][0]
+    task.solve_split(S.dt, inner, max(1, args.warmup))
+    k0 = task.kernel_launches()
+    dist.barrier()
+    with ClockSampler(dev) as clk:
+        L.check(task._ctx, L.lib.gpe_timer_start(task._ctx))
+        task.solve_split(S.dt, inner, int(task.current_iter) + args.steps)
+        ms = C.c_double()
+        L.check(task._ctx, L.lib.gpe_timer_stop(task._ctx, C.byref(ms)))
+    launches = task.kernel_launches() - k0
+    t_s = dist.reduce(ms.value / 1e3, "max")
+    value = dist.reduce(float(P) * inner * args.steps, "sum") / t_s
+    task.profile(True)
+    task.solve_split(S.dt, inner, int(task.current_iter) + min(args.steps, 2))
+    stats = task.profile_read()
+    task.profile(False)
+    hbm, peak_kind = peaks()
+    top = max(stats, key=lambda s: s["total_ms"])
+    avg_ms = top["total_ms"] / top["launches"]
+    achieved = top["bytes_per_launch"] / (avg_ms / 1e3) / 1e9
+    # FP64 arm on the same start
+    _, t64 = S.make_task("double", device=dev)
+    t64.init_state = pair
+    t64.solve_split(S.dt, inner, 1)
+    psi64_1 = t64.current_state
+    mu64 = t64.history["mu"][0]
+    L.check(t64._ctx, L.lib.gpe_timer_start(t64._ctx))
+    t64.solve_split(S.dt, inner, 2)
+    ms64 = C.c_double()
+    L.check(t64._ctx, L.lib.gpe_timer_stop(t64._ctx, C.byref(ms64)))
+    value64 = float(P) * inner / (ms64.value / 1e3)
+    t64.close()
+    a = np.concatenate([x.ravel() for x in psi32_1])
+    b = np.concatenate([x.ravel() for x in psi64_1])
+    err_l2 = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    # e2e: both components from and to pinned host buffers through the public API
+    host_in = np.ascontiguousarray(np.concatenate([p.ravel() for p in pair]).astype(np.complex64))
+    host_out = np.empty_like(host_in)
+    e2e_steps = max(1, min(args.steps, 3))
+    with gpe.pinned(host_in), gpe.pinned(host_out):
+        task.init_state = host_in
+        task.current_iter = 0
+        task.solve_split(S.dt, inner, 1)
+        task._download(host_out)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            task.init_state = host_in
+            task.current_iter = 0
+            task.solve_split(S.dt, inner, 1)
+            task._download(host_out)
+        e2e_t = time.perf_counter() - t0
+    e2e_t = dist.reduce(e2e_t, "max")
+    e2e_val = dist.reduce(float(P) * inner * e2e_steps, "sum") / e2e_t
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
+        cores = os.cpu_count() or 1
+        cval, n, t = spinor_cpu_steps(S, pair, cores)
+        cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{n} split steps (one block) of the same 256^3 two-component workload in the FP64 "
+                         f"oracle (numpy + scipy.fft with {cores} workers), {t:.1f} s"}
+    line = {
+        "metric": SPIN_METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms.value / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 (FP64 reductions)",
+        "data": "synthetic (ITP ground state of the damped workload split 70/30)",
+        "config": {"workload": S.name, "grid": list(S.n), "components": 2, "box": S.box, "g": [list(r) for r in S.g],
+                   "coupling": str(S.coupling), "Ntotal": S.Ntotal, "gamma": S.gamma, "dt": S.dt,
+                   "step": f"{inner} split steps (1 outer step)", "n_recalc": 10,
+                   "l2": f"inputs larger than L2 (2 states + 2 V = {P * 24 / 1e6:.0f} MB > 129 MB L2)",
+                   "points_counted": "grid points (each carries both components)"},
+        "fp64": {"value": value64, "unit": UNIT, "steps": inner, "ratio_fp32_over_fp64": value / dist.world / value64},
+        "error": {"fp32_vs_fp64_rel_l2_after_outer_step": err_l2, "mu_rel_after_outer_step": abs(mu32 - mu64) / abs(mu64)},
+        "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": top["bytes_per_launch"], "avg_launch_ms": avg_ms,
+                     "timing": "CUDA events around every launch on the context stream, in a profiled "
+                               "window of the same work right after the timed region"},
+        "kernels": stats,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(host_in.nbytes),
+                "d2h_bytes_per_step": int(host_out.nbytes), "steps": e2e_steps},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    task.close()
+
+
+def run_spinor_reference(args, dist):
+    """--impl reference for the spinor workload: the FP64 oracle restatement of
+    GPEtaskSpinor.solve_split on the host cores (the start state is the
+    seeded Gaussian pair; the timed work does not depend on it)."""
+    from gpe_gb300.workloads import DAMPED3D as W, SPINOR3D as S
+
+    if dist.rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    grid = W.make_grid("double")
+    pair = S.initial_pair(W.initial_state(grid) * 10.0)
+    vals = []
+    for _ in range(max(1, min(args.steps, 2))):
+        v, n, t = spinor_cpu_steps(S, pair, cores)
+        vals.append((v, n, t))
+    v = float(np.median([x[0] for x in vals]))
+    line = {
+        "metric": SPIN_METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": 1, "steps": len(vals),
+        "warmup": args.warmup, "ms_per_step": 1e3 * vals[-1][2] / vals[-1][1], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": S.name, "grid": list(S.n), "components": 2, "dt": S.dt, "step": "1 split step"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{len(vals)} x 10 split steps of the 256^3 two-component FP64 oracle"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_case(precision: str, blocks: int, variant: int = 0, plans: int = 0):
     """Small fixed case for ncu captures: the bench workload's grid and
     parameters from the seeded Gaussian (no ITP), `blocks` blocks of 10 steps.
@@ -547,9 +709,10 @@ def main():
     ap.add_argument("--pass-variant", type=int, default=0, help="0: direct + L2 prefetch (default), 1: TMA-staged, 2: direct")
     ap.add_argument("--workload", default="damped3d_256",
                     choices=["damped3d_256", "ring3d_512", "vortex2d_256", "batch2d_64", "adjoint2d_256",
-                             "adjoint3d_512"],
+                             "adjoint3d_512", "spinor3d_256"],
                     help="damped3d_256 (default, the headline), ring3d_512, vortex2d_256 (L2-resident), "
-                         "batch2d_64 (64 uneven grids), adjoint2d_256 / adjoint3d_512 (gradients)")
+                         "batch2d_64 (64 uneven grids), adjoint2d_256 / adjoint3d_512 (gradients), "
+                         "spinor3d_256 (two coupled components)")
     ap.add_argument("--adjoint-fp64", action="store_true", help="adjoint workloads: FP64 sweep of the FP32 context")
     args = ap.parse_args()
     if args.profile_case:
@@ -560,9 +723,14 @@ def main():
     dist = Dist()
     try:
         if args.impl == "reference":
-            run_reference(args, dist)
+            if args.workload == "spinor3d_256":
+                run_spinor_reference(args, dist)
+            else:
+                run_reference(args, dist)
         else:
-            if args.workload == "batch2d_64":
+            if args.workload == "spinor3d_256":
+                run_spinor(args, dist)
+            elif args.workload == "batch2d_64":
                 run_batch(args, dist)
             elif args.workload.startswith("adjoint"):
                 run_adjoint(args, dist)

@@ -665,7 +665,7 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
     a.mask_pa = c->n[1];
     a.ecut = (R)ap.ecut;
   }
-  const double P = (double)c->P;
+  const double P = (double)c->PS;  // points of every component the pass covers
   double bytes = (kind == KIND_ENERGY ? 1.0 : 2.0) * P * 2 * sizeof(R);
   const bool useV = pro == PRO_RT_HALF || pro == PRO_RT_FULL || pro == PRO_ITP || epi == EPI_RT_END ||
                     (kind == KIND_ENERGY && energy_pot);

@@ -112,24 +112,34 @@ __global__ void __launch_bounds__(SP_THREADS) k_spinor_sums(const cx<R>* __restr
   }
 }
 
-// Sum of n partials in a fixed order (one warp, deterministic).
-__device__ double warp_sum_fixed(const double* p, int n) {
+constexpr int FIN_T = 256;
+
+// Sum of n partials in a fixed order over the CTA (deterministic): strided
+// per-thread sums, then a shared-memory tree.  Every thread gets the result.
+__device__ double cta_sum_fixed(const double* p, int n, double* sh) {
   double v = 0.0;
-  for (int i = (int)threadIdx.x; i < n; i += 32) v += p[i];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return __shfl_sync(0xffffffffu, v, 0);
+  for (int i = (int)threadIdx.x; i < n; i += FIN_T) v += p[i];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = FIN_T / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
 }
 
 // Start of a run (mode 0, solve_split.m:29-37,52-57), block end (mode 1,
 // :100-113) or observables (mode 2): NN0, renormalisation, mu.
 __global__ void k_finalize_spinor(const SpinorFinalArgs a, DevScalars* sc) {
   if (a.mode != 2 && sc->stop) return;
+  __shared__ double sh[FIN_T];
   double s[SP_NSUMS];
-  for (int k = 0; k < SP_NSUMS; ++k) s[k] = warp_sum_fixed(a.sums + (size_t)k * a.nsum, a.nsum);
+  for (int k = 0; k < SP_NSUMS; ++k) s[k] = cta_sum_fixed(a.sums + (size_t)k * a.nsum, a.nsum, sh);
   double kin = 0.0;
   for (int ax = 0; ax < 3; ++ax)
-    if (a.nblk_kin[ax] > 0) kin += warp_sum_fixed(a.partials + (size_t)(S_KX + ax) * a.cap, a.nblk_kin[ax]);
+    if (a.nblk_kin[ax] > 0) kin += cta_sum_fixed(a.partials + (size_t)(S_KX + ax) * a.cap, a.nblk_kin[ax], sh);
   if (threadIdx.x != 0) return;
   const double w = a.weight;
   const double ncur = (s[0] + s[1]) * w;
@@ -197,7 +207,7 @@ int launch_spinor_sums(const cx<R>* psi, const R* V, long long P, const DevScala
 }
 
 void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream_t s) {
-  k_finalize_spinor<<<1, 32, 0, s>>>(a, sc);
+  k_finalize_spinor<<<1, FIN_T, 0, s>>>(a, sc);
 }
 
 #define INST_SPINOR(R)                                                                                     \

@@ -526,17 +526,33 @@ class GPEtaskSpinor(GPEtask):
         self._V_keep = V
 
     def _upload_state(self, phi):
-        flat = self._pair(phi, np.complex128)
-        L.check(self._ctx, L.lib.gpe_set_state(self._ctx, L.dptr(flat.view(np.float64))))
+        """A pair [phi1, phi2], or one contiguous array of both components
+        (2*npoints values, e.g. a pinned host buffer), uploaded as it is."""
+        n = self.grid.npoints
+        if isinstance(phi, np.ndarray) and phi.size == 2 * n and phi.flags.c_contiguous and \
+                phi.dtype in (np.complex64, np.complex128):
+            flat = phi
+        else:
+            flat = self._pair(phi, np.complex128)
+        if flat.dtype == np.complex64:
+            L.check(self._ctx, L.lib.gpe_set_state_f32(self._ctx, L.fptr(flat.view(np.float32))))
+        else:
+            L.check(self._ctx, L.lib.gpe_set_state(self._ctx, L.dptr(flat.view(np.float64))))
 
     def _download(self, out=None):
-        dt = np.complex64 if self.grid.precision == "single" else np.complex128
-        flat = np.empty(2 * self.grid.npoints, dtype=dt)
-        if dt == np.complex64:
+        """[phi1, phi2], or both components into `out` (2*npoints values)."""
+        n = self.grid.npoints
+        if out is None:
+            dt = np.complex64 if self.grid.precision == "single" else np.complex128
+            flat = np.empty(2 * n, dtype=dt)
+        else:
+            flat = out
+        if flat.dtype == np.complex64:
             L.check(self._ctx, L.lib.gpe_get_state_f32(self._ctx, L.fptr(flat.view(np.float32))))
         else:
             L.check(self._ctx, L.lib.gpe_get_state(self._ctx, L.dptr(flat.view(np.float64))))
-        n = self.grid.npoints
+        if out is not None:
+            return out
         return [flat[:n].reshape(self.grid.shape), flat[n:].reshape(self.grid.shape)]
 
     def getVtotal(self, time):

@@ -224,3 +224,59 @@ class AdjointWorkload:
 
 
 ADJOINT2D = AdjointWorkload()
+
+
+@dataclass
+class SpinorWorkload:
+    """Coherently coupled two-component dynamics (GPEtaskSpinor.solve_split)
+    on the damped 3D grid: 256^3, box +-12, V1 = 0.5 (x^2 + y^2 + (4 z)^2),
+    V2 = V1 with the trap centre moved to x = 0.5, g = [[0.5, 0.45],
+    [0.45, 0.5]], Rabi coupling 0.5, Ntotal = 1e5, gamma = 0.01, 100 steps of
+    0.002 per outer step (n_recalc = 10).  Start: the one-component ITP
+    ground state of the damped workload split 70/30 between the components
+    (component 2 with a phase 0.3).  All values are assumed: the reference
+    names no spinor workload."""
+
+    name: str = "spinor3d_256"
+    n: tuple = (256, 256, 256)
+    box: float = 12.0
+    lam_z: float = 4.0
+    shift2: float = 0.5
+    g: tuple = ((0.5, 0.45), (0.45, 0.5))
+    coupling: complex = 0.5
+    Ntotal: float = 1e5
+    gamma: float = 0.01
+    dt: float = 0.002
+    niter_inner: int = 100
+    frac1: float = 0.7
+
+    @property
+    def npoints(self) -> int:
+        return int(np.prod(self.n))
+
+    def potentials(self):
+        lz = self.lam_z
+        s = self.shift2
+        return [lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2 + (lz * Z) ** 2),
+                lambda X, Y, Z: 0.5 * ((X - s) ** 2 + Y ** 2 + (lz * Z) ** 2)]
+
+    def initial_pair(self, phi):
+        phi = np.asarray(phi, dtype=np.complex128)
+        return [np.sqrt(self.frac1) * phi, np.sqrt(1.0 - self.frac1) * np.exp(0.3j) * phi]
+
+    def configure(self, task):
+        task.g = np.array(self.g)
+        task.coupling = self.coupling
+        task.Ntotal = self.Ntotal
+        task.gamma = self.gamma
+        return task
+
+    def make_task(self, precision: str = "single", device: int = 0):
+        from .task import GPEtaskSpinor
+
+        b, n = self.box, self.n
+        grid = grid3d(b, n[0], b, n[1], b, n[2], precision=precision)
+        return grid, self.configure(GPEtaskSpinor(grid, self.potentials(), device=device))
+
+
+SPINOR3D = SpinorWorkload()

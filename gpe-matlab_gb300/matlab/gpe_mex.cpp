@@ -23,7 +23,12 @@
 //       task: the calling GPEtaskGB300 object; if it has a time-dependent
 //       potential the gateway calls task.getVtotal(time) once per block, and
 //       after every outer step it calls task.gb300_step(step, time, mu, n).
-//   obs = gpe_mex('observables', h)                   % [norm ekin epot eint mu_int energy]
+//   obs = gpe_mex('observables', h)                   % [norm ekin epot eint mu_int energy ecpl]
+//   gpe_mex('sgpe', h, ddt, nin, nout, task, timedep, T, ecut, seed)   % SGPEtask.solve_split
+//   h = gpe_mex('create_spinor', ndims, n, dx, span, precision)      % GPEtaskSpinor context
+//   gpe_mex('set_spinor_params', h, g, coupling, nlincpl)
+//       spinor contexts take [phi1(:); phi2(:)] and [V1(:); V2(:)] in set_state /
+//       set_potential / getVtotal, and get_state returns them stacked the same way
 #include <string.h>
 
 #include <string>
@@ -88,7 +93,9 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (nrhs < 1) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex(command, ...)");
   const std::string cmd = str(prhs[0]);
 
-  if (cmd == "create") {
+  if (cmd == "create" || cmd == "create_spinor") {
+    // create_spinor: a two-component (GPEtaskSpinor) context; its state, V and
+    // Vtd arrays are [phi1(:); phi2(:)] / [V1(:); V2(:)]
     if (nrhs != 6) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('create', ndims, n, dx, span, precision)");
     gpe_grid_desc d;
     memset(&d, 0, sizeof(d));
@@ -104,7 +111,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     d.precision = str(prhs[5]) == "single" ? GPE_FP32 : GPE_FP64;
     d.device = 0;
     gpe_ctx* c = nullptr;
-    check(nullptr, gpe_create(&d, &c));
+    check(nullptr, cmd == "create" ? gpe_create(&d, &c) : gpe_create_spinor(&d, &c));
     plhs[0] = mxCreateNumericMatrix(1, 1, mxUINT64_CLASS, mxREAL);
     *static_cast<uint64_t*>(mxGetData(plhs[0])) = reinterpret_cast<uint64_t>(c);
     return;
@@ -152,6 +159,26 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     check(c, gpe_get_history(c, mxGetDoubles(plhs[0]), mxGetDoubles(nn), len, &len));
     if (nlhs > 1) plhs[1] = nn;
     else mxDestroyArray(nn);
+  } else if (cmd == "set_spinor_params") {
+    // gpe_mex('set_spinor_params', h, g (2x2), coupling (complex scalar), nlincpl)
+    if (nrhs != 5) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('set_spinor_params', h, g, coupling, nlincpl)");
+    if (!mxIsDouble(prhs[2]) || mxGetNumberOfElements(prhs[2]) != 4) mexErrMsgIdAndTxt("gpe:arg", "g must be 2x2 double");
+    const double* g = mxGetDoubles(prhs[2]);  // column-major: g(1,1) g(2,1) g(1,2) g(2,2)
+    gpe_spinor_params sp;
+    memset(&sp, 0, sizeof(sp));
+    sp.g[0] = g[0];
+    sp.g[1] = g[2];
+    sp.g[2] = g[1];
+    sp.g[3] = g[3];
+    if (mxIsComplex(prhs[3])) {
+      const mxComplexDouble* cp = mxGetComplexDoubles(prhs[3]);
+      sp.coupling_re = cp[0].real;
+      sp.coupling_im = cp[0].imag;
+    } else {
+      sp.coupling_re = scalar(prhs[3]);
+    }
+    sp.nlincpl = scalar(prhs[4]);
+    check(c, gpe_set_spinor_params(c, &sp));
   } else if (cmd == "set_potential") {
     if (!mxIsDouble(prhs[2]) || mxIsComplex(prhs[2])) mexErrMsgIdAndTxt("gpe:arg", "V must be real double");
     check(c, gpe_set_potential(c, mxGetDoubles(prhs[2])));
@@ -240,7 +267,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   } else if (cmd == "observables") {
     gpe_obs o;
     check(c, gpe_observables(c, &o));
-    plhs[0] = mxCreateDoubleMatrix(1, 6, mxREAL);
+    plhs[0] = mxCreateDoubleMatrix(1, 7, mxREAL);
     double* r = mxGetDoubles(plhs[0]);
     r[0] = o.norm;
     r[1] = o.ekin;
@@ -248,6 +275,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     r[3] = o.eint;
     r[4] = o.mu_integral;
     r[5] = o.energy;
+    r[6] = o.ecpl;
   } else if (cmd == "adjoint") {
     // [loss, dLdV] = gpe_mex('adjoint', h, target, ddt, nsteps, K, budget, precision)
     // precision: 0 = the context's, 2 = FP64 sweep.  dLdV has the grid's shape.
