@@ -92,6 +92,29 @@ int launch_spinor_sums(const cx<R>* psi, const R* V, long long P, const DevScala
                        cudaStream_t s);
 void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream_t s);
 
+// On-device observables, observables.cu.
+struct CoreGeom {
+  double x0, y0;    // coordinates of column 0 and row 0 of the slice
+  double hxg, hyg;  // grid spacings (coordinate of column ix = x0 + ix*hxg)
+  double hx, hy;    // detect_core.m:13-14 spacings (del2 and the position offsets)
+  int refine;
+};
+struct CoreScratch {
+  double* blockmax;   // elem_grid(n) doubles
+  double* thr;        // 1 double
+  signed char* q;     // n charges
+  int* cnt;           // 2 * chunks
+  int* off;           // 2 * chunks + 2 (totals last)
+};
+int core_chunks(long long n);
+template <typename R>
+cudaError_t launch_detect_core(const cx<R>* slice, int nx, int ny, const CoreGeom& geo, CoreScratch& w,
+                               double* pos, int cap_pos, double* neg, int cap_neg, cudaStream_t st);
+int launch_minmax(const double* V, long long n, double* out, cudaStream_t st);
+int launch_tf_sum(const double* V, long long n, double mu, double* out, cudaStream_t st);
+template <typename R>
+void launch_tf_state(cx<R>* psi, const double* V, long long n, double mu, double g, cudaStream_t st);
+
 void launch_finalize_block(const BlockFinalArgs& a, DevScalars* sc, cudaStream_t s);
 void launch_finalize_itp(const ItpFinalArgs& a, DevScalars* sc, cudaStream_t s);
 void launch_finalize_check(const CheckFinalArgs& a, DevScalars* sc, cudaStream_t s);

@@ -65,6 +65,8 @@ struct gpe_ctx {
   double* Vmu = nullptr;  // spinor with a time-dependent V: getVtotal(current_time) (FP64 copy)
   void* VmuR = nullptr;   // the same in the context precision
   double* spin_part = nullptr;  // spinor sums: [SP_NSUMS][grid] partials, then 8 observables
+  void* obs_buf = nullptr;      // scratch of the on-device observables (vortex-core detection)
+  size_t obs_len = 0;
   double weight = 1.0;
   int prec = GPE_FP64;
   gpe_params prm{};

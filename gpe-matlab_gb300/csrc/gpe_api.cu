@@ -1622,6 +1622,7 @@ gpe_status maybe_autotune(gpe_ctx* c) {
 // C ABI
 // =============================================================================
 #include "spinor_driver.cuh"
+#include "observables_driver.cuh"
 
 extern "C" {
 
@@ -1792,6 +1793,7 @@ void gpe_destroy(gpe_ctx* c) {
   cudaFree(c->Vmu);
   cudaFree(c->VmuR);
   cudaFree(c->spin_part);
+  cudaFree(c->obs_buf);
   cudaFree(c->partials);
   cudaFree(c->sc);
   cudaFree(c->d_hist);
@@ -2107,6 +2109,32 @@ gpe_status gpe_observables(gpe_ctx* c, gpe_obs* o) {
   o->mu_integral = o->ekin + o->epot + o->eint;
   o->energy = o->ekin + o->epot + 0.5 * o->eint;
   return GPE_OK;
+}
+
+gpe_status gpe_detect_core(gpe_ctx* c, int component, int z_index, int refine, double* pos, int cap_pos,
+                           int* n_pos, double* neg, int cap_neg, int* n_neg) {
+  CHECK(check_ctx(c));
+  CHECK(need_state(c));
+  if (!n_pos || !n_neg || cap_pos < 0 || cap_neg < 0 || (cap_pos > 0 && !pos) || (cap_neg > 0 && !neg))
+    return fail(c, GPE_ERR_INVALID, "detect_core: bad output arguments");
+  if (component < 0 || component >= c->ncomp) return fail(c, GPE_ERR_INVALID, "detect_core: bad component");
+  const int nz = c->ndims == 3 ? c->n[2] : 1;
+  if (z_index < 0 || z_index >= nz) return fail(c, GPE_ERR_INVALID, "detect_core: z_index out of range");
+  if (c->prec == GPE_FP32)
+    return detect_core_impl<float>(c, component, z_index, refine, pos, cap_pos, n_pos, neg, cap_neg, n_neg);
+  return detect_core_impl<double>(c, component, z_index, refine, pos, cap_pos, n_pos, neg, cap_neg, n_neg);
+}
+
+gpe_status gpe_groundstate_tf(gpe_ctx* c, double eps, double N, const double* bounds, double* mu) {
+  CHECK(check_ctx(c));
+  if (c->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "groundstate_tf: not available on a spinor context");
+  CHECK(need_V(c));
+  if (!mu || !(eps > 0) || !std::isfinite(N)) return fail(c, GPE_ERR_INVALID, "groundstate_tf: bad arguments");
+  if (!(c->prm.g > 0)) return fail(c, GPE_ERR_INVALID, "groundstate_tf: g must be positive (phi = sqrt(vvv/g))");
+  if (bounds && !(bounds[0] < bounds[1])) return fail(c, GPE_ERR_INVALID, "groundstate_tf: need mul < mur");
+  c->err.clear();
+  if (c->prec == GPE_FP32) return groundstate_tf_impl<float>(c, eps, N, bounds, mu);
+  return groundstate_tf_impl<double>(c, eps, N, bounds, mu);
 }
 
 gpe_status gpe_synchronize(gpe_ctx* c) {

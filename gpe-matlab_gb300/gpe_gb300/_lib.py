@@ -116,6 +116,9 @@ PROTOTYPES = {
     "gpe_solve_split_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(gpe_split_params)]),
     "gpe_adjoint_grad": (C.c_int, [_P, C.POINTER(gpe_adjoint_params), _D, _D, _D]),
     "gpe_observables": (C.c_int, [_P, C.POINTER(gpe_obs)]),
+    "gpe_detect_core": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _D, C.c_int, C.POINTER(C.c_int), _D, C.c_int,
+                                  C.POINTER(C.c_int)]),
+    "gpe_groundstate_tf": (C.c_int, [_P, C.c_double, C.c_double, _D, _D]),
     "gpe_synchronize": (C.c_int, [_P]),
     "gpe_timer_start": (C.c_int, [_P]),
     "gpe_timer_stop": (C.c_int, [_P, _D]),

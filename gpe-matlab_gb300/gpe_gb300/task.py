@@ -179,23 +179,29 @@ class GPEtask:
         return np.asarray(phi0, dtype=np.complex128)
 
     def groundstate_tf(self, eps, N=None, V=None, mul=None, mur=None):
-        """Thomas-Fermi bisection, lib/@GPEtask/groundstate_tf.m:1-37 (host)."""
+        """Thomas-Fermi state and mu, lib/@GPEtask/groundstate_tf.m:1-37, on the
+        device (gpe_groundstate_tf): bisection against getVtotal(0) (or V),
+        phi = sqrt(vvv/g).  Returns (phi, mu); the device state holds phi."""
         N = self.Ntotal if N is None else N
-        V = self.getVtotal(0) if V is None else V
-        if mul is None:
-            mul, mur = float(np.min(V)), float(np.max(V))
-        NC = N * self.g
-        mu = (mul + mur) / 2
-        vvv = (mu - V) * (V < mu)
-        while (mur - mul) / mu > eps:
-            vvv = (mu - V) * (V < mu)
-            NN = self.grid.integrate(vvv)
-            if NN > NC:
-                mur = mu
-            else:
-                mul = mu
-            mu = (mul + mur) / 2
-        return np.sqrt(vvv / self.g), mu
+        self._push_params()
+        self._upload_V(np.ascontiguousarray(self.getVtotal(0) if V is None else
+                                            np.broadcast_to(np.asarray(V, dtype=np.float64), self.grid.shape)))
+        bounds = None
+        if mul is not None:
+            bounds = np.array([float(mul), float(mur)])
+        mu = C.c_double()
+        L.check(self._ctx, L.lib.gpe_groundstate_tf(self._ctx, float(eps), float(N),
+                                                    None if bounds is None else L.dptr(bounds), C.byref(mu)))
+        if V is not None:
+            self._V_key = None  # the next call uploads its own potential again
+        phi = np.real(self._download())
+        self._state_on_device = None
+        return phi, mu.value
+
+    def detect_core(self, refine=0, z_index=0, component=0, cap=4096):
+        """lib/util/detect_core.m on the current device state (slice z_index of
+        a 3D grid): (resp, resm), k x 2 arrays of [x, y]."""
+        return detect_core(self, refine=refine, z_index=z_index, component=component, cap=cap)
 
     def groundstate_itp(self, dt, eps, phi0="rand", nargout=1, rng=None):
         """groundstate_itp.m:1-112.  Returns phi, or (phi, MU, MU2, EE)[:nargout]."""
@@ -591,6 +597,26 @@ class GPEtaskSpinor(GPEtask):
     def get_energy(self, phi=None):
         """GPEtaskSpinor.m:98-110."""
         return self.observables(phi if phi is not None else self.current_state)["energy"]
+
+
+def detect_core(task, refine=0, z_index=0, component=0, cap=4096):
+    """detect_core(phi, rx, ry, refine) (lib/util/detect_core.m:1-67) of the
+    task's current device state, on the device (gpe_detect_core): (resp,
+    resm), k x 2 arrays of the positive and negative cores' [x, y] in MATLAB's
+    find() order.  3D grids: the slice z_index; spinor tasks: `component`."""
+    if task._state_on_device != "current":
+        st = task._current_state if task._current_state is not None else task.init_state
+        task._upload_state(st)
+    while True:
+        pos = np.zeros((cap, 2))
+        neg = np.zeros((cap, 2))
+        npos, nneg = C.c_int(), C.c_int()
+        L.check(task._ctx, L.lib.gpe_detect_core(task._ctx, int(component), int(z_index), int(refine),
+                                                 L.dptr(pos), cap, C.byref(npos), L.dptr(neg), cap,
+                                                 C.byref(nneg)))
+        if npos.value <= cap and nneg.value <= cap:
+            return pos[:npos.value].copy(), neg[:nneg.value].copy()
+        cap = max(npos.value, nneg.value)
 
 
 def noise_variates(seed, step, n):

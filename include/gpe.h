@@ -289,6 +289,25 @@ GPE_API gpe_status gpe_solve_sgpe(gpe_ctx *ctx, const gpe_split_params *prm, con
 /* applyham / get_energy pieces for the current state at the current V. */
 GPE_API gpe_status gpe_observables(gpe_ctx *ctx, gpe_obs *obs);
 
+/* ---- observables on the device ------------------------------------------ */
+/* lib/util/detect_core.m:1-67 on the 2D slice z_index (0 in 2D) of the
+ * current state (component 0 or 1 of a spinor context): cores where the
+ * phase winds around a plaquette and |del2(|psi|^2)| exceeds 1% of its
+ * maximum.  pos/neg receive up to cap_pos/cap_neg (x, y) pairs in MATLAB's
+ * find() order: [x - dx/2, y - dy/2] for positive and [x - dx/2, y - dx/2]
+ * for negative cores as the reference writes them, or with refine != 0 the
+ * sub-cell positions of refine_core (the first qualifying real root in
+ * ascending order; no real root in (0,1): [0, 0]).  n_pos/n_neg receive the
+ * counts, which may exceed the caps. */
+GPE_API gpe_status gpe_detect_core(gpe_ctx *ctx, int component, int z_index, int refine,
+                                   double *pos, int cap_pos, int *n_pos,
+                                   double *neg, int cap_neg, int *n_neg);
+/* lib/@GPEtask/groundstate_tf.m:1-37 against the potential last set: bisect
+ * mu until (mur-mul)/mu <= eps (bounds = {mul, mur}, or NULL for min/max of
+ * V), set the state to sqrt(vvv/g) with vvv of the last evaluated mu, and
+ * return mu.  g must be positive. */
+GPE_API gpe_status gpe_groundstate_tf(gpe_ctx *ctx, double eps, double N, const double *bounds, double *mu);
+
 /* ---- profiling and timing (CUDA events on the context stream) ---------- */
 GPE_API gpe_status gpe_synchronize(gpe_ctx *ctx);
 GPE_API gpe_status gpe_timer_start(gpe_ctx *ctx);

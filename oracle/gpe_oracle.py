@@ -670,6 +670,89 @@ class GPEtaskSpinor(GPEtask):
 
 
 # ---------------------------------------------------------------------------
+# Vortex-core detection: lib/util/detect_core.m:1-67.  Arrays here are
+# indexed [ix, iy] (the transpose of MATLAB's row = y, column = x matrix), so
+# MATLAB's column-major find() order is this C order.
+# ---------------------------------------------------------------------------
+def _second_diff(U, h, axis):
+    """One dimension of MATLAB's del2: central second differences inside,
+    linear extrapolation to the two edge points (n > 3)."""
+    n = U.shape[axis]
+    g = np.zeros_like(U)
+
+    def s(a, b):
+        return tuple(slice(a, b) if k == axis else slice(None) for k in range(U.ndim))
+
+    g[s(1, n - 1)] = (U[s(2, n)] - 2.0 * U[s(1, n - 1)] + U[s(0, n - 2)]) / h ** 2
+    g[s(0, 1)] = 2.0 * g[s(1, 2)] - g[s(2, 3)]
+    g[s(n - 1, n)] = 2.0 * g[s(n - 2, n - 1)] - g[s(n - 3, n - 2)]
+    return g
+
+
+def del2(U, hx, hy):
+    """del2(U, hx, hy) of a 2D field: (d2/dx2 + d2/dy2)/4 (x along axis 0)."""
+    return (_second_diff(U, hx, 0) + _second_diff(U, hy, 1)) / 4.0
+
+
+def core_charges(phi, rx, ry):
+    """res1 of detect_core.m:14-27: the winding of the phase around each
+    plaquette (corners (i,j), (i-1,j), (i-1,j-1), (i,j-1) in MATLAB's row/column
+    indices, circular), kept where |del2(|phi|^2)| > 1% of its maximum."""
+    n_x, n_y = phi.shape
+    dx = rx[n_x // 2, 0] - rx[n_x // 2 - 1, 0]                # :13
+    dy = ry[0, n_y // 2] - ry[0, n_y // 2 - 1]                # :14
+    an = np.angle(phi)
+    ddphi = np.abs(del2(np.abs(phi) ** 2, dx, dy))            # :18
+    a = [an, np.roll(an, 1, axis=1), np.roll(np.roll(an, 1, axis=1), 1, axis=0), np.roll(an, 1, axis=0)]
+    dif = [a[k] - a[k - 1] for k in range(4)]                 # :24 (k = 0 wraps to the 4th corner)
+    cnt = sum((d > math.pi).astype(int) for d in dif) - sum((d < -math.pi).astype(int) for d in dif)
+    return cnt * (ddphi > 0.01 * np.max(ddphi)), dx, dy       # :25
+
+
+def _refine_core(phi, rx, ry, dx, dy, jx, iy):
+    """refine_core of detect_core.m:51-66 at MATLAB (row, column) = (iy, jx),
+    1-based and already clamped to >= 2 (C.L. Phillips et al., Phys. Rev. E 91,
+    023311 (2015))."""
+    import scipy.linalg
+
+    rep, imp = np.real(phi), np.imag(phi)
+
+    def at(f, r, c):  # MATLAB f(r, c), 1-based
+        return f[c - 1, r - 1]
+
+    r, c = iy, jx
+    A = -np.array([[at(rep, r - 1, c) - at(rep, r, c), at(rep, r, c)],
+                   [at(imp, r - 1, c) - at(imp, r, c), at(imp, r, c)]])
+    B = np.array([[at(rep, r, c) - at(rep, r - 1, c) - at(rep, r, c - 1) + at(rep, r - 1, c - 1),
+                   at(rep, r, c - 1) - at(rep, r, c)],
+                  [at(imp, r, c) - at(imp, r - 1, c) - at(imp, r, c - 1) + at(imp, r - 1, c - 1),
+                   at(imp, r, c - 1) - at(imp, r, c)]])
+    d, v = scipy.linalg.eig(A, B)
+    v = v[0, :] / v[1, :]
+    for i in range(2):
+        if np.real(d[i]) > 0 and np.real(d[i]) < 1 and np.real(v[i]) > 0 and np.real(v[i]) < 1:
+            return [at(rx, r, c) - dy * np.real(d[i]), at(ry, r, c) - dx * np.real(v[i])]
+    return [0.0, 0.0]
+
+
+def detect_core(phi, rx, ry, refine=0):
+    """detect_core.m:1-49: (resp, resm), k x 2 arrays of [x, y] of the positive
+    and negative cores in MATLAB's find() order."""
+    res1, dx, dy = core_charges(phi, rx, ry)
+    out = []
+    for sign in (1, -1):
+        res = res1 * sign > 0
+        if refine > 0:
+            jx, iy = np.nonzero(res)  # C order of [ix, iy] = MATLAB's column-major order
+            pts = [_refine_core(phi, rx, ry, dx, dy, max(j + 1, 2), max(i + 1, 2)) for j, i in zip(jx, iy)]
+            out.append(np.array(pts, dtype=np.float64).reshape(-1, 2))
+        else:
+            ydel = dy if sign > 0 else dx  # :45 subtracts dx from y for the negative cores
+            out.append(np.stack([rx[res] - dx / 2, ry[res] - ydel / 2], axis=1))
+    return out[0], out[1]
+
+
+# ---------------------------------------------------------------------------
 # Vortex imprint: examples/example1_vortex.m:26-30 (also README.md:93-97)
 # ---------------------------------------------------------------------------
 def imprint_vortex(grid: Grid, phi, g, x0, y0=0.0):

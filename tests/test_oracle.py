@@ -285,6 +285,52 @@ def test_spinor_conserves_norm_and_matches_single_component_when_decoupled():
     assert np.max(np.abs(d.current_state[1])) == 0
 
 
+def vortex_field(g, cores, width=2.5):
+    """A Gaussian with a core z/sqrt(1 + |z|^2), z = (x - x_k) + i s_k (y - y_k),
+    at each (x_k, y_k, s_k)."""
+    X, Y = g.mesh["x"], g.mesh["y"]
+    phi = np.exp(-(X ** 2 + Y ** 2) / (2 * width ** 2)).astype(complex)
+    for xk, yk, sk in cores:
+        z = (X - xk) + 1j * sk * (Y - yk)
+        phi = phi * z / np.sqrt(1.0 + np.abs(z) ** 2)
+    return phi
+
+
+def test_detect_core_finds_charges_and_refines_positions():
+    """lib/util/detect_core.m: charges and positions of imprinted cores (the
+    centre (x_j - dx/2, y_i - dy/2) of the plaquette holding the core);
+    refine = 1 (Phillips et al.) recovers the zeros to a few % of a cell."""
+    g = O.Grid(8, 64, 8, 64)
+    cores = [(-2.03, 1.51, 1), (1.27, -0.88, -1), (2.55, 2.14, 1)]
+    phi = vortex_field(g, cores)
+    rx, ry = g.mesh["x"], g.mesh["y"]
+    resp, resm = O.detect_core(phi, rx, ry)
+    assert resp.shape == (2, 2) and resm.shape == (1, 2)
+    for pts, sgn in ((resp, 1), (resm, -1)):
+        for x, y in pts:
+            near = [c for c in cores if c[2] == sgn and abs(c[0] - x) <= g.dx / 2 and abs(c[1] - y) <= g.dy / 2]
+            assert len(near) == 1
+    # MATLAB find() order: column-major over (row = y, column = x) -> ascending x first
+    assert resp[0, 0] < resp[1, 0]
+    rp, rm = O.detect_core(phi, rx, ry, refine=1)
+    truth_p = sorted([c[:2] for c in cores if c[2] == 1])
+    np.testing.assert_allclose(sorted(map(tuple, rp)), truth_p, atol=0.05 * g.dx)
+    np.testing.assert_allclose(rm, [cores[1][:2]], atol=0.05 * g.dx)
+    # no cores: empty k x 2 arrays
+    e1, e2 = O.detect_core(vortex_field(g, []), rx, ry)
+    assert e1.shape == (0, 2) and e2.shape == (0, 2)
+
+
+def test_del2_matches_matlab_edge_extrapolation():
+    """del2 of a quadratic is exact everywhere (edges included): for
+    U = a x^2 + b y^2 it is (2a + 2b)/4."""
+    g = O.Grid(3, 16, 2, 12)
+    U = 0.7 * g.mesh["x"] ** 2 + 1.9 * g.mesh["y"] ** 2
+    np.testing.assert_allclose(O.del2(U, g.dx, g.dy), (2 * 0.7 + 2 * 1.9) / 4, rtol=1e-10)
+    U3 = g.mesh["x"] ** 3  # cubic: second difference 6x exact inside, linear extrapolation exact too
+    np.testing.assert_allclose(O.del2(U3, g.dx, g.dy), 6 * g.mesh["x"] / 4, atol=1e-9)
+
+
 def test_golden_fixtures_reproduce():
     from tests.golden import make_golden as MG
 
