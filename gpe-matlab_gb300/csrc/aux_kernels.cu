@@ -156,7 +156,7 @@ __global__ void k_finalize_block(const BlockFinalArgs a, DevScalars* sc) {
   if (threadIdx.x != 0) return;
   const double w = a.weight;
   const double ncur = n * w;  // solve_split.m:67
-  double muc, scale = 1.0;
+  double muc, scale = 1.0, energy = 0.0;
   if (a.feedback) {  // solve_split.m:68-75
     double NNN = sc->NNN;
     if (a.tau > 0) NNN = sc->NN0 * exp(-a.time2 / a.tau);
@@ -164,12 +164,15 @@ __global__ void k_finalize_block(const BlockFinalArgs a, DevScalars* sc) {
     scale = sqrt(NNN / ncur);
     const double s2 = scale * scale;
     muc = (s2 * (kin + vn) * w + s2 * s2 * a.g * n2 * w) / NNN;
+    energy = s2 * (kin + vn) * w + 0.5 * s2 * s2 * a.g * n2 * w;  // of the renormalised state
     sc->mu = muc;
   } else if (a.fixed_mu) {  // SGPEtask solve_split.m:52,78
     muc = sc->mu;
   } else {  // solve_split.m:76-77
     muc = (kin + vn + a.g * n2) * w / ncur;
+    energy = (kin + vn + 0.5 * a.g * n2) * w;
   }
+  sc->energy = energy;
   sc->scale = scale;
   sc->ncur = ncur;
   sc->muc = muc;
@@ -181,6 +184,7 @@ __global__ void k_finalize_block(const BlockFinalArgs a, DevScalars* sc) {
     *a.hist_mu = muc;
     *a.hist_n = ncur;
     if (a.hist_ok) *a.hist_ok = 1;
+    if (a.hist_e) *a.hist_e = a.fixed_mu ? NAN : energy;
   }
 }
 

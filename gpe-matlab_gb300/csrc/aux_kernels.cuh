@@ -21,6 +21,7 @@ struct BlockFinalArgs {
   double* hist_n;
   int* hist_ok;
   int fixed_mu = 0;      // report sc->mu (the stochastic GPE's mu_init) instead of <psi|H psi>/N
+  double* hist_e = nullptr;  // get_energy of the block-end state (GPEtask.m:97-107), or nullptr
 };
 
 struct ItpFinalArgs {
@@ -81,7 +82,7 @@ struct SpinorFinalArgs {
   double Ntotal;                // mode 0
   int renorm;                   // mode 1: gamma > 0
   double tau, time2;
-  double* hist;                 // mode 1: (mu, ncur) or nullptr
+  double* hist;                 // mode 1: (mu, ncur, energy) or nullptr
   double* obs;                  // mode 2: norm, ekin, epot, eint, ecpl
 };
 template <typename R>

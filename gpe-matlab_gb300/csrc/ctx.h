@@ -71,7 +71,7 @@ struct gpe_ctx {
   int prec = GPE_FP64;
   gpe_params prm{};
   gpe_current cur{};
-  std::vector<double> hist_mu, hist_n;
+  std::vector<double> hist_mu, hist_n, hist_e;
 
   gpe::Field main, polish;  // polish: FP64 field of an FP32 context
   double* V64 = nullptr;    // FP64 copy of V (upload staging; polish potential)

@@ -1112,6 +1112,7 @@ gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool las
   a.hist_mu = hist;
   a.hist_n = hist ? hist + 1 : nullptr;
   a.hist_ok = nullptr;
+  a.hist_e = hist ? hist + 2 : nullptr;
   a.fixed_mu = run.sgpe;  // SGPE reports mu = mu_init (solve_split.m:78)
   Launch L(c, PC_FINALIZE, 0);
   launch_finalize_block(a, c->sc, c->stream);
@@ -1133,10 +1134,12 @@ gpe_status split_finish(gpe_ctx* c, const SplitRun& run, int last_j, double last
     if ((int)c->hist_mu.size() < last_j) {
       c->hist_mu.resize(last_j, 0.0);
       c->hist_n.resize(last_j, 0.0);
+      c->hist_e.resize(last_j, 0.0);
     }
     for (int j = start + 1; j <= last_j; ++j) {
       c->hist_mu[j - 1] = dh[3 * (size_t)(j - start - 1)];
       c->hist_n[j - 1] = dh[3 * (size_t)(j - start - 1) + 1];
+      c->hist_e[j - 1] = dh[3 * (size_t)(j - start - 1) + 2];
     }
     c->cur.current_iter = last_j;
     c->cur.current_time = last_time2;
@@ -1181,9 +1184,11 @@ gpe_status split_impl(gpe_ctx* c, const gpe_split_params* prm, const gpe_sgpe_pa
       if ((int)c->hist_mu.size() < j) {
         c->hist_mu.resize(j, 0.0);
         c->hist_n.resize(j, 0.0);
+        c->hist_e.resize(j, 0.0);
       }
       c->hist_mu[j - 1] = h.muc;
       c->hist_n[j - 1] = h.ncur;
+      c->hist_e[j - 1] = run.sgpe ? NAN : h.energy;
       if (prm->on_step(prm->step_user, j, time2, h.muc, h.ncur) != 0) stop_req = true;
     }
   }
@@ -1459,10 +1464,10 @@ gpe_status batch_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm) {
   for (int j = r0.start + 1; j <= r0.nout && e == cudaSuccess; ++j) {
     for (int jj = 1; jj < r0.nb && e == cudaSuccess; ++jj) e = cudaGraphLaunch(g_plain.x, master);
     if (e == cudaSuccess) e = cudaGraphLaunch(g_last.x, master);
-    // the last block left (muc, ncur) in each context's slot 0: file it
+    // the last block left (muc, ncur, energy) in each context's slot 0: file it
     const size_t hj = (size_t)(j - r0.start - 1);
     for (size_t i = 0; i < n && e == cudaSuccess; ++i)
-      e = cudaMemcpyAsync(cs[i]->d_hist + 3 + 3 * hj, cs[i]->d_hist, 2 * sizeof(double), cudaMemcpyDeviceToDevice,
+      e = cudaMemcpyAsync(cs[i]->d_hist + 3 + 3 * hj, cs[i]->d_hist, 3 * sizeof(double), cudaMemcpyDeviceToDevice,
                           master);
     for (size_t i = 0; i < n; ++i) cs[i]->launches += (long long)(r0.nb - 1) * k_plain[i] + k_last[i];
     last_j = j;
@@ -1861,10 +1866,20 @@ gpe_status gpe_get_history(const gpe_ctx* c, double* mu, double* n, int cap, int
   return GPE_OK;
 }
 
+gpe_status gpe_get_history_energy(const gpe_ctx* c, double* E, int cap, int* len) {
+  if (!c) return GPE_ERR_INVALID;
+  const int L = (int)c->hist_mu.size();
+  if (len) *len = L;
+  for (int k = 0; k < std::min(L, cap); ++k)
+    if (E) E[k] = k < (int)c->hist_e.size() ? c->hist_e[k] : NAN;
+  return GPE_OK;
+}
+
 gpe_status gpe_clear_history(gpe_ctx* c) {
   CHECK(check_ctx(c));
   c->hist_mu.clear();
   c->hist_n.clear();
+  c->hist_e.clear();
   return GPE_OK;
 }
 

@@ -128,7 +128,7 @@ gpe_status spinor_split_impl(gpe_ctx* c, const gpe_split_params* prm) {
   std::vector<AxisPass> half = full;
   for (auto& ap : half) ap.half = 1;
   const int nsteps_out = std::max(0, nout - start);
-  const size_t hlen = 2 * (size_t)std::max(1, nsteps_out);
+  const size_t hlen = 3 * (size_t)std::max(1, nsteps_out);  // (mu, ncur, energy) per outer step
   if (c->d_hist_len < hlen) {
     cudaFree(c->d_hist);
     c->d_hist = nullptr;
@@ -155,7 +155,7 @@ gpe_status spinor_split_impl(gpe_ctx* c, const gpe_split_params* prm) {
         for (const auto& ap : (i == n_rec ? half : full))
           CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dre, dim, nullptr));
       }
-      double* hist = (jj == nb) ? c->d_hist + 2 * (size_t)(j - start - 1) : nullptr;
+      double* hist = (jj == nb) ? c->d_hist + 3 * (size_t)(j - start - 1) : nullptr;
       CHECK(spinor_finalize<R>(c, f, vtd ? spinor_vmu_ptr<R>(c) : (const R*)f.V, 1, time2, hist, gam > 0,
                                nullptr));
     }
@@ -172,9 +172,11 @@ gpe_status spinor_split_impl(gpe_ctx* c, const gpe_split_params* prm) {
       if ((int)c->hist_mu.size() < j) {
         c->hist_mu.resize(j, 0.0);
         c->hist_n.resize(j, 0.0);
+        c->hist_e.resize(j, 0.0);
       }
       c->hist_mu[j - 1] = h.muc;
       c->hist_n[j - 1] = h.ncur;
+      c->hist_e[j - 1] = h.energy;
       if (prm->on_step && prm->on_step(prm->step_user, j, time2, h.muc, h.ncur) != 0) stopped = true;
       if (vtd && !stopped && j < nout) CHECK(spinor_vmu<R>(c, prm, time2));
     }
@@ -183,15 +185,17 @@ gpe_status spinor_split_impl(gpe_ctx* c, const gpe_split_params* prm) {
   CHECK(read_scalars(c, &h));
   if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
   if (last_j > start) {
-    std::vector<double> dh(2 * (size_t)(last_j - start));
+    std::vector<double> dh(3 * (size_t)(last_j - start));
     CU(cudaMemcpy(dh.data(), c->d_hist, dh.size() * sizeof(double), cudaMemcpyDeviceToHost));
     if ((int)c->hist_mu.size() < last_j) {
       c->hist_mu.resize(last_j, 0.0);
       c->hist_n.resize(last_j, 0.0);
+      c->hist_e.resize(last_j, 0.0);
     }
     for (int j = start + 1; j <= last_j; ++j) {
-      c->hist_mu[j - 1] = dh[2 * (size_t)(j - start - 1)];
-      c->hist_n[j - 1] = dh[2 * (size_t)(j - start - 1) + 1];
+      c->hist_mu[j - 1] = dh[3 * (size_t)(j - start - 1)];
+      c->hist_n[j - 1] = dh[3 * (size_t)(j - start - 1) + 1];
+      c->hist_e[j - 1] = dh[3 * (size_t)(j - start - 1) + 2];
     }
     c->cur.current_iter = last_j;
     c->cur.current_time = time2;

@@ -177,6 +177,8 @@ __global__ void k_finalize_spinor(const SpinorFinalArgs a, DevScalars* sc) {
   }
   const double s2 = scale * scale;
   const double mu = (s2 * quad + s2 * s2 * eint) / NNN;
+  const double energy = s2 * quad + 0.5 * s2 * s2 * eint;  // get_energy halves g (GPEtaskSpinor.m:98-110)
+  sc->energy = energy;
   sc->scale = scale;
   sc->mu = mu;
   sc->muc = mu;
@@ -189,6 +191,7 @@ __global__ void k_finalize_spinor(const SpinorFinalArgs a, DevScalars* sc) {
   if (a.hist) {
     a.hist[0] = mu;
     a.hist[1] = ncur;
+    a.hist[2] = energy;
   }
 }
 

@@ -101,6 +101,7 @@ PROTOTYPES = {
     "gpe_get_current": (C.c_int, [_P, C.POINTER(gpe_current)]),
     "gpe_set_current": (C.c_int, [_P, C.POINTER(gpe_current)]),
     "gpe_get_history": (C.c_int, [_P, _D, _D, C.c_int, C.POINTER(C.c_int)]),
+    "gpe_get_history_energy": (C.c_int, [_P, _D, C.c_int, C.POINTER(C.c_int)]),
     "gpe_clear_history": (C.c_int, [_P]),
     "gpe_set_potential": (C.c_int, [_P, _D]),
     "gpe_set_potential_f32": (C.c_int, [_P, _F]),

@@ -319,8 +319,11 @@ class GPEtask:
         L.check(self._ctx, L.lib.gpe_get_history(self._ctx, None, None, 0, C.byref(n)))
         mu = np.zeros(n.value)
         nn = np.zeros(n.value)
+        ee = np.zeros(n.value)
         L.check(self._ctx, L.lib.gpe_get_history(self._ctx, L.dptr(mu), L.dptr(nn), n.value, C.byref(n)))
-        self.history["mu"], self.history["n"] = mu, nn
+        L.check(self._ctx, L.lib.gpe_get_history_energy(self._ctx, L.dptr(ee), n.value, C.byref(n)))
+        # "energy" is an addition (get_energy at every outer step, on the device)
+        self.history["mu"], self.history["n"], self.history["energy"] = mu, nn, ee
 
     def _ext_callback(self, step, time, mu, n):
         """GPEtask.m:115-142 (plot and console line omitted)."""

@@ -216,6 +216,11 @@ GPE_API gpe_status gpe_get_current(const gpe_ctx *ctx, gpe_current *cur);
 GPE_API gpe_status gpe_set_current(gpe_ctx *ctx, const gpe_current *cur);
 /* history.mu / history.n (GPEtask.m:123-126): up to cap entries, *len = count */
 GPE_API gpe_status gpe_get_history(const gpe_ctx *ctx, double *mu, double *n, int cap, int *len);
+/* get_energy(psi) (GPEtask.m:97-107, GPEtaskSpinor.m:98-110) of the state
+ * at the end of every outer step, from the block-end sums on the device (an
+ * addition: the reference's history keeps mu and n only); NaN for SGPE runs,
+ * whose blocks evaluate no energy. */
+GPE_API gpe_status gpe_get_history_energy(const gpe_ctx *ctx, double *E, int cap, int *len);
 GPE_API gpe_status gpe_clear_history(gpe_ctx *ctx);
 
 /* ---- data ------------------------------------------------------------- */
