@@ -29,9 +29,13 @@
 //   gpe_mex('set_spinor_params', h, g, coupling, nlincpl)
 //       spinor contexts take [phi1(:); phi2(:)] and [V1(:); V2(:)] in set_state /
 //       set_potential / getVtotal, and get_state returns them stacked the same way
+//   [resp, resm] = gpe_mex('detect_core', h, z_index, refine, component)   % detect_core.m on the device
+//   mu = gpe_mex('groundstate_tf', h, eps, N[, mul, mur])                 % groundstate_tf.m on the device
 #include <string.h>
 
+#include <algorithm>
 #include <string>
+#include <vector>
 
 #include "gpe.h"
 #include "mex.h"
@@ -276,6 +280,38 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     r[4] = o.mu_integral;
     r[5] = o.energy;
     r[6] = o.ecpl;
+  } else if (cmd == "detect_core") {
+    // [resp, resm] = gpe_mex('detect_core', h, z_index, refine, component): detect_core.m
+    // of the current device state (slice z_index, 1-based as in MATLAB; 1 in 2D)
+    if (nrhs != 5) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('detect_core', h, z_index, refine, component)");
+    const int z = (int)scalar(prhs[2]) - 1, refine = (int)scalar(prhs[3]), comp = (int)scalar(prhs[4]) - 1;
+    int np = 0, nm = 0;
+    check(c, gpe_detect_core(c, comp, z, refine, nullptr, 0, &np, nullptr, 0, &nm));
+    std::vector<double> p(2 * (size_t)std::max(np, 1)), m(2 * (size_t)std::max(nm, 1));
+    check(c, gpe_detect_core(c, comp, z, refine, p.data(), np, &np, m.data(), nm, &nm));
+    // k x 2 column-major results from (x, y) pairs
+    plhs[0] = mxCreateDoubleMatrix(np, 2, mxREAL);
+    for (int k = 0; k < np; ++k) {
+      mxGetDoubles(plhs[0])[k] = p[2 * k];
+      mxGetDoubles(plhs[0])[np + k] = p[2 * k + 1];
+    }
+    if (nlhs > 1) {
+      plhs[1] = mxCreateDoubleMatrix(nm, 2, mxREAL);
+      for (int k = 0; k < nm; ++k) {
+        mxGetDoubles(plhs[1])[k] = m[2 * k];
+        mxGetDoubles(plhs[1])[nm + k] = m[2 * k + 1];
+      }
+    }
+  } else if (cmd == "groundstate_tf") {
+    // mu = gpe_mex('groundstate_tf', h, eps, N[, mul, mur]): the state becomes the TF profile
+    if (nrhs != 4 && nrhs != 6) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('groundstate_tf', h, eps, N[, mul, mur])");
+    double b[2] = {0.0, 0.0}, mu = 0.0;
+    if (nrhs == 6) {
+      b[0] = scalar(prhs[4]);
+      b[1] = scalar(prhs[5]);
+    }
+    check(c, gpe_groundstate_tf(c, scalar(prhs[2]), scalar(prhs[3]), nrhs == 6 ? b : nullptr, &mu));
+    plhs[0] = mxCreateDoubleScalar(mu);
   } else if (cmd == "adjoint") {
     // [loss, dLdV] = gpe_mex('adjoint', h, target, ddt, nsteps, K, budget, precision)
     // precision: 0 = the context's, 2 = FP64 sweep.  dLdV has the grid's shape.
