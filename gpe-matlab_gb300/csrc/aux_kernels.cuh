@@ -93,6 +93,22 @@ int launch_spinor_sums(const cx<R>* psi, const R* V, long long P, const DevScala
                        cudaStream_t s);
 void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream_t s);
 
+// Array-omega angular momentum, lz_kernels.cu.
+struct LzGeom {
+  int nx, ny;       // slice size (z slices are independent)
+  double h;         // derivative spacing (grid1d deriv1 with obj.dx for both axes)
+  double x0, y0;    // coordinates of ix = 0, iy = 0
+  double hxg, hyg;  // grid spacings of the coordinates
+};
+// out = phi + (cre + i cim) * omega * lz(src); out may be phi, never src.
+template <typename R>
+void launch_lz_cn(cx<R>* out, const cx<R>* phi, const cx<R>* src, const R* om, long long n, const LzGeom& g,
+                  double cre, double cim, cudaStream_t st);
+// Per-CTA sums of real(conj(psi) (-omega lz psi)) (times scale^2 if use_scale); returns CTAs.
+template <typename R>
+int launch_lz_energy(const cx<R>* psi, const R* om, long long n, const LzGeom& g, const DevScalars* sc,
+                     int use_scale, double* out, cudaStream_t st);
+
 // On-device observables, observables.cu.
 struct CoreGeom {
   double x0, y0;    // coordinates of column 0 and row 0 of the slice

@@ -32,7 +32,8 @@ struct Field {
   void* rotw[2] = {nullptr, nullptr};            // per transverse index: -omega*y (x) / +omega*x (y)
   double rotw_omega = 0.0;                       // omega the rotw arrays hold
   void* kks[3] = {nullptr, nullptr, nullptr};    // per axis: permuted k^2/2, N real (energy cut-off)
-  void* php2[3] = {nullptr, nullptr, nullptr};   // spinor: the kinetic factors of half a step
+  void* php2[3] = {nullptr, nullptr, nullptr};   // spinor, array omega: the kinetic factors of half a step
+  void* cn[2] = {nullptr, nullptr};              // array omega: Crank-Nicolson iterates (P complex each)
 };
 
 struct ProfRec {
@@ -66,6 +67,12 @@ struct gpe_ctx {
   void* VmuR = nullptr;   // the same in the context precision
   double* spin_part = nullptr;  // spinor sums: [SP_NSUMS][grid] partials, then 8 observables
   void* obs_buf = nullptr;      // scratch of the on-device observables (vortex-core detection)
+  // Array omega (ssft_kin_step.m:3-11): omega per grid point, FP64 and the
+  // context precision, and the Crank-Nicolson iteration count n_crank.
+  bool omega_field = false;
+  double* omf64 = nullptr;
+  void* omfR = nullptr;
+  int n_crank = 3;
   size_t obs_len = 0;
   double weight = 1.0;
   int prec = GPE_FP64;

@@ -182,6 +182,21 @@ std::vector<AxisPass> axis_passes(const gpe_ctx* c, double ecut = 0.0) {
   return v;
 }
 
+// The passes of one kinetic step.  Array omega (ssft_kin_step.m:3-11): the
+// half-step passes, the Crank-Nicolson Lz update (an entry with axis = -1),
+// the half-step passes again; otherwise axis_passes.
+std::vector<AxisPass> step_passes(const gpe_ctx* c, double ecut = 0.0) {
+  if (!c->omega_field) return axis_passes(c, ecut);
+  std::vector<AxisPass> h = axis_passes(c);
+  for (auto& ap : h) ap.half = 1;
+  std::vector<AxisPass> v = h;
+  AxisPass cn = h[0];
+  cn.axis = -1;
+  v.push_back(cn);
+  v.insert(v.end(), h.begin(), h.end());
+  return v;
+}
+
 // One pass per axis (energy sums): the axis passes without the second x half.
 std::vector<AxisPass> energy_axes(const gpe_ctx* c) {
   std::vector<AxisPass> v = axis_passes(c);
@@ -510,8 +525,9 @@ gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
             std::complex<double>(mag * std::cos(kk * dim * h), -mag * std::sin(kk * dim * h));
       }
     CHECK(upload_cx<R>(c, f.php[ax], ph));
-    if (c->ncomp == 2) {
+    if (c->ncomp == 2 || c->omega_field) {
       // GPEtaskSpinor/solve_split.m:44-45: ekkp = exp(-kk dt/2) at block starts;
+      // set_kinop.m:3-4 for array omega: kinop = exp(-kk dt/2)
       // the last step's ekk times ekkm = exp(+kk dt/2) is exp(-kk dt/2) too
       for (int t = 0; t < pi.T; ++t)
         for (int m = 0; m < pi.E; ++m) {
@@ -581,6 +597,7 @@ void free_field(Field& f, const double* V64) {
     cudaFree(f.kks[i]);
     cudaFree(f.php2[i]);
   }
+  for (int i = 0; i < 2; ++i) cudaFree(f.cn[i]);
   for (int i = 0; i < 2; ++i) {
     cudaFree(f.rot[i]);
     cudaFree(f.rotw[i]);
@@ -694,6 +711,59 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
 
 // Kinetic-energy passes (one forward FFT per axis); with `pot`, the y pass
 // also sums n, Vn, n^2 and every pass applies the pending scale.
+// ---- array omega: the Crank-Nicolson Lz update and its energy ----------------
+LzGeom lz_geom(const gpe_ctx* c) {
+  LzGeom g;
+  g.nx = c->n[0];
+  g.ny = c->n[1];
+  g.h = c->dx[0];  // derivy.m passes obj.dx as well
+  g.x0 = coord(c, 0, 0);
+  g.y0 = coord(c, 1, 0);
+  g.hxg = c->dx[0];
+  g.hyg = c->dx[1];
+  return g;
+}
+
+template <typename R>
+const R* omega_field_ptr(const gpe_ctx* c) {
+  return sizeof(R) == 8 ? (const R*)c->omf64 : (const R*)c->omfR;
+}
+
+template <typename R>
+gpe_status ensure_cn_buffers(gpe_ctx* c, Field& f) {
+  for (int k = 0; k < 2; ++k)
+    if (!f.cn[k]) CU(cudaMalloc(&f.cn[k], (size_t)c->P * 2 * sizeof(R)));
+  return GPE_OK;
+}
+
+// ssft_kin_step.m:5-10 between the two half kinetic steps, dt = dre + i dim:
+//   lphi = phi; n_crank times: lphi = phi + dt/2 omega lz(lphi); phi += dt omega lz(lphi)
+template <typename R>
+gpe_status cn_step(gpe_ctx* c, Field& f, double dre, double dim) {
+  CHECK(ensure_cn_buffers<R>(c, f));
+  const LzGeom g = lz_geom(c);
+  const R* om = omega_field_ptr<R>(c);
+  cx<R>* phi = (cx<R>*)f.psi;
+  const cx<R>* src = phi;
+  int k = 0;
+  for (int it = 0; it < c->n_crank; ++it) {
+    cx<R>* out = (cx<R>*)f.cn[k];
+    Launch L(c, PC_ELEMENTWISE, (double)c->P * 6 * sizeof(R));
+    launch_lz_cn<R>(out, phi, src, om, c->P, g, 0.5 * dre, 0.5 * dim, c->stream);
+    src = out;
+    k ^= 1;
+  }
+  Launch L(c, PC_ELEMENTWISE, (double)c->P * 6 * sizeof(R));
+  if (c->n_crank > 0) {
+    launch_lz_cn<R>(phi, phi, src, om, c->P, g, dre, dim, c->stream);  // reads src's neighbours only
+  } else {
+    launch_lz_cn<R>((cx<R>*)f.cn[0], phi, phi, om, c->P, g, dre, dim, c->stream);
+    CU(cudaMemcpyAsync(phi, f.cn[0], (size_t)c->P * 2 * sizeof(R), cudaMemcpyDeviceToDevice, c->stream));
+  }
+  CU(cudaGetLastError());
+  return GPE_OK;
+}
+
 template <typename R>
 gpe_status energy_passes(gpe_ctx* c, Field& f, bool pot, int nblk_kin[3], int* nblk_pot) {
   CHECK(ensure_rot_weights<R>(c, f));
@@ -705,6 +775,15 @@ gpe_status energy_passes(gpe_ctx* c, Field& f, bool pot, int nblk_kin[3], int* n
     CHECK(run_pass<R>(c, f, ap, KIND_ENERGY, pot ? PRO_SCALE : PRO_NONE, EPI_NONE, ep ? 1 : 0, 0.0, 0.0, &nb));
     nblk_kin[ap.axis] = nb;
     if (ep && nblk_pot) *nblk_pot = nb;
+  }
+  if (c->omega_field) {
+    // the -omega Lz term of applyh0 (GPEtask.m:92-94), appended to the x
+    // pass's kinetic partials so every finalizer adds it to the kinetic sum
+    Launch L(c, PC_NORM, (double)c->P * (2 * sizeof(R) + sizeof(R)));
+    const int nb = launch_lz_energy<R>((const cx<R>*)f.psi, omega_field_ptr<R>(c), c->P, lz_geom(c), c->sc, pot,
+                                       c->partials + (size_t)S_KX * c->cap + nblk_kin[0], c->stream);
+    CU(cudaGetLastError());
+    nblk_kin[0] += nb;
   }
   return GPE_OK;
 }
@@ -748,10 +827,14 @@ struct ItpState {
 
 template <typename R>
 gpe_status itp_iteration(gpe_ctx* c, Field& f, double dt, int i) {
-  auto passes = axis_passes(c);
+  auto passes = step_passes(c);
   int nb = 0;
   for (size_t k = 0; k < passes.size(); ++k) {
     const bool first = k == 0, last = k + 1 == passes.size();
+    if (passes[k].axis < 0) {  // array omega: Crank-Nicolson Lz with the real ITP dt
+      CHECK(cn_step<R>(c, f, dt, 0.0));
+      continue;
+    }
     CHECK(run_pass<R>(c, f, passes[k], KIND_STEP, first ? PRO_ITP : PRO_NONE, last ? EPI_ITP : EPI_NONE, 0,
                       dt, 0.0, last ? &nb : nullptr));
   }
@@ -1056,7 +1139,8 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
   run.dt_outer = ddt * prm->niter_inner;
   run.nb = prm->niter_inner / n_rec;
   // the cut-off mask applies only with noise (SGPEtask/solve_split.m:40)
-  run.passes = axis_passes(c, (sg && sg->T > 0 && sg->ecut > 0) ? sg->ecut : 0.0);
+  run.passes = step_passes(c, (sg && sg->T > 0 && sg->ecut > 0) ? sg->ecut : 0.0);
+  if (c->omega_field) CHECK(ensure_cn_buffers<R>(c, f));  // before any graph capture
   run.hist_off = hist_extra;
   const int nsteps_out = std::max(0, nout - start);
   const size_t hlen = hist_extra + 3 * (size_t)std::max(1, nsteps_out);
@@ -1088,6 +1172,10 @@ gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool las
     }
     for (size_t k = 0; k < run.passes.size(); ++k) {
       const bool first = k == 0, last = k + 1 == run.passes.size();
+      if (run.passes[k].axis < 0) {  // array omega: Crank-Nicolson Lz (ssft_kin_step.m:5-10)
+        CHECK(cn_step<R>(c, f, run.dre, run.dim));
+        continue;
+      }
       const int pro = (first && !run.sgpe) ? (i == 1 ? PRO_RT_HALF : PRO_RT_FULL) : PRO_NONE;
       const int epi = (last && i == run.n_rec) ? EPI_RT_END : EPI_NONE;
       CHECK(run_pass<R>(c, f, run.passes[k], KIND_STEP, pro, epi, 0, run.dre, run.dim,
@@ -1718,13 +1806,13 @@ static gpe_status create_impl(const gpe_grid_desc* d, gpe_ctx** out, int ncomp) 
   }
   // partial-sum capacity: the largest grid of any pass in either precision
   // and any plan variant
-  long long cap = 8LL * 1024;
+  long long cap = 8LL * 1024;  // (+ room for the Lz energy partials after the x pass's, array omega)
   for (auto& ap : axis_passes(c)) {
     cap = std::max(cap, pass_blocks<float>(ap, 0));
     if (has_alt_plan(ap.N)) cap = std::max(cap, pass_blocks<float>(ap, 1));
     cap = std::max(cap, pass_blocks<double>(ap, 0));
   }
-  c->cap = (int)cap;
+  c->cap = (int)cap + 8 * c->sms;
   gpe_status st = GPE_OK;
   if (cudaMalloc(&c->partials, (size_t)(NSLOTS + 1) * c->cap * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&c->sc, sizeof(DevScalars)) != cudaSuccess ||
@@ -1781,6 +1869,35 @@ gpe_status gpe_set_spinor_params(gpe_ctx* c, const gpe_spinor_params* p) {
   return GPE_OK;
 }
 
+gpe_status gpe_set_omega_field(gpe_ctx* c, const double* omega, int n_crank) {
+  CHECK(check_ctx(c));
+  if (n_crank < 0) return fail(c, GPE_ERR_INVALID, "set_omega_field: n_crank must be >= 0");
+  if (!omega) {
+    if (c->omega_field) {
+      c->main.phase_valid = false;  // the half-step tables follow the mode
+      c->polish.phase_valid = false;
+    }
+    c->omega_field = false;
+    return GPE_OK;
+  }
+  if (c->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "set_omega_field: not available on a spinor context");
+  c->main.phase_valid = false;
+  c->polish.phase_valid = false;
+  for (long long i = 0; i < c->P; ++i)
+    if (!std::isfinite(omega[i])) return fail(c, GPE_ERR_INVALID, "set_omega_field: omega must be finite");
+  if (!c->omf64) CU(cudaMalloc(&c->omf64, (size_t)c->P * sizeof(double)));
+  CU(cudaMemcpy(c->omf64, omega, (size_t)c->P * sizeof(double), cudaMemcpyHostToDevice));
+  if (c->prec == GPE_FP32) {
+    if (!c->omfR) CU(cudaMalloc(&c->omfR, (size_t)c->P * sizeof(float)));
+    launch_convert_re<double, float>(c->omf64, (float*)c->omfR, c->P, c->stream);
+    CU(cudaGetLastError());
+    CU(cudaStreamSynchronize(c->stream));
+  }
+  c->omega_field = true;
+  c->n_crank = n_crank;
+  return GPE_OK;
+}
+
 gpe_status gpe_get_spinor_params(const gpe_ctx* c, gpe_spinor_params* p) {
   if (!c || !p) return fail(nullptr, GPE_ERR_INVALID, "null argument");
   if (c->ncomp != 2) return GPE_ERR_STATE;
@@ -1799,6 +1916,8 @@ void gpe_destroy(gpe_ctx* c) {
   cudaFree(c->VmuR);
   cudaFree(c->spin_part);
   cudaFree(c->obs_buf);
+  cudaFree(c->omf64);
+  cudaFree(c->omfR);
   cudaFree(c->partials);
   cudaFree(c->sc);
   cudaFree(c->d_hist);
@@ -1979,6 +2098,8 @@ gpe_status gpe_groundstate_itp(gpe_ctx* c, const gpe_itp_params* prm, double* MU
   if (!prm || !(prm->dt > 0) || !std::isfinite(prm->dt) || !(prm->eps > 0))
     return fail(c, GPE_ERR_INVALID, "groundstate_itp: dt and eps must be positive");
   if (cap < 0) return fail(c, GPE_ERR_INVALID, "negative cap");
+  if (c->omega_field && c->prm.omega != 0.0)
+    return fail(c, GPE_ERR_INVALID, "omega is either a scalar (gpe_params.omega) or an array (gpe_set_omega_field)");
   c->err.clear();
   CHECK(maybe_autotune(c));
   if (c->prec == GPE_FP32) return itp_impl<float>(c, prm, MU, MU2, EE, cap, res);
@@ -1991,6 +2112,8 @@ gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
   if (!prm || !(prm->ddt > 0) || !std::isfinite(prm->ddt))
     return fail(c, GPE_ERR_INVALID, "solve_split: ddt must be positive");
   if (!prm->vtd) CHECK(need_V(c));
+  if (c->omega_field && c->prm.omega != 0.0)
+    return fail(c, GPE_ERR_INVALID, "omega is either a scalar (gpe_params.omega) or an array (gpe_set_omega_field)");
   c->err.clear();
   if (c->ncomp == 2) {
     if (c->prm.omega != 0.0)
@@ -2022,7 +2145,8 @@ gpe_status gpe_adjoint_grad(gpe_ctx* c, const gpe_adjoint_params* prm, const dou
   if (c->prm.gamma != 0.0 || c->prm.decay_rate > 0)
     return fail(c, GPE_ERR_UNSUPPORTED,
                 "adjoint: only gamma = 0 and decay_rate = 0 (conservative dynamics) are differentiated");
-  if (c->prm.omega != 0.0) return fail(c, GPE_ERR_UNSUPPORTED, "adjoint: the rotating frame is not differentiated");
+  if (c->prm.omega != 0.0 || c->omega_field)
+    return fail(c, GPE_ERR_UNSUPPORTED, "adjoint: the rotating frame is not differentiated");
   const int prec = prm->precision ? prm->precision : c->prec;
   if (prec != GPE_FP32 && prec != GPE_FP64) return fail(c, GPE_ERR_INVALID, "adjoint: precision must be 0, GPE_FP32 or GPE_FP64");
   if (prec == GPE_FP32 && c->prec == GPE_FP64)
@@ -2245,7 +2369,7 @@ gpe_status gpe_solve_sgpe(gpe_ctx* c, const gpe_split_params* prm, const gpe_sgp
     return fail(c, GPE_ERR_INVALID, "solve_sgpe: ddt must be positive");
   if (!(sg->T >= 0) || !std::isfinite(sg->T) || !(sg->ecut >= 0))
     return fail(c, GPE_ERR_INVALID, "solve_sgpe: T and ecut must be >= 0");
-  if (c->prm.omega != 0.0)
+  if (c->prm.omega != 0.0 || c->omega_field)
     return fail(c, GPE_ERR_UNSUPPORTED, "solve_sgpe: omega != 0 (the reference's Lz Crank-Nicolson branch)");
   if (!prm->vtd) CHECK(need_V(c));
   c->err.clear();

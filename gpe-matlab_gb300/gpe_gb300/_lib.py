@@ -89,6 +89,7 @@ _F = C.POINTER(C.c_float)
 PROTOTYPES = {
     "gpe_create": (C.c_int, [C.POINTER(gpe_grid_desc), C.POINTER(_P)]),
     "gpe_create_spinor": (C.c_int, [C.POINTER(gpe_grid_desc), C.POINTER(_P)]),
+    "gpe_set_omega_field": (C.c_int, [_P, _D, C.c_int]),
     "gpe_set_spinor_params": (C.c_int, [_P, C.POINTER(gpe_spinor_params)]),
     "gpe_get_spinor_params": (C.c_int, [_P, C.POINTER(gpe_spinor_params)]),
     "gpe_destroy": (None, [_P]),

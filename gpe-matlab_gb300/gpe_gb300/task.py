@@ -8,8 +8,9 @@ GPU; this class only packs properties, uploads arrays, evaluates host-side
 callbacks (time-dependent potential, user callback) and exposes the results.
 
 Differences from the reference, all deliberate:
-* ``omega``: a scalar rotating frame runs on the GPU (set_kinop.m:5-7,
-  ssft_kin_step.m:12-15); the array-omega Lz Crank-Nicolson branch raises.
+* ``omega``: a scalar rotating frame (set_kinop.m:5-7, ssft_kin_step.m:12-15)
+  and an omega array (the Lz Crank-Nicolson branch, ssft_kin_step.m:3-11)
+  both run on the GPU.
 * ``'rand'`` initial states use a seeded numpy generator (the reference calls
   an unseeded ``rand``, GPEtask.m:49-52).
 * ``show_image`` and the console status line are not implemented (UI).
@@ -36,6 +37,7 @@ class GPEtask:
         # public properties with the reference defaults (GPEtask.m:4-34)
         self.g = 0.0
         self.omega = 0.0
+        self.n_crank = 3
         self.n_recalc = 10
         self.gamma = 0.0
         self.decay_rate = 0.0
@@ -98,10 +100,15 @@ class GPEtask:
         self._state_on_device = None
 
     def _push_params(self):
-        if np.size(self.omega) != 1:
-            raise NotImplementedError("array omega (Lz Crank-Nicolson, ssft_kin_step.m:3-11) is not supported")
         p = L.gpe_params()
-        p.omega = float(self.omega)
+        if np.size(self.omega) != 1:
+            # array omega: the Lz Crank-Nicolson branch (ssft_kin_step.m:3-11)
+            om = np.ascontiguousarray(np.broadcast_to(np.asarray(self.omega, dtype=np.float64), self.grid.shape))
+            L.check(self._ctx, L.lib.gpe_set_omega_field(self._ctx, L.dptr(om), int(self.n_crank)))
+            p.omega = 0.0
+        else:
+            L.check(self._ctx, L.lib.gpe_set_omega_field(self._ctx, None, int(self.n_crank)))
+            p.omega = float(np.asarray(self.omega).ravel()[0])
         p.g = self._g_scalar()
         p.gamma = float(self.gamma)
         p.decay_rate = float(self.decay_rate)
@@ -460,6 +467,7 @@ class GPEtaskSpinor(GPEtask):
         self.nlincpl = 0.0
         self.ncomp = 2
         self.omega = 0.0
+        self.n_crank = 3
         self.n_recalc = 10
         self.gamma = 0.0
         self.decay_rate = 0.0

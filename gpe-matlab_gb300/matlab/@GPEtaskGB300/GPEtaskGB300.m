@@ -133,12 +133,17 @@ classdef GPEtaskGB300 < GPEtask
 
     methods (Access = protected)
         function gb300_push(task)
+            om = 0;
             if ~isscalar(task.omega)
-                error('gpe:omega', 'array omega (Lz Crank-Nicolson) is not supported by libgpe');
+                % array omega: the Lz Crank-Nicolson branch (ssft_kin_step.m:3-11)
+                gpe_mex('set_omega_field', task.gb300_handle, double(gather(task.omega)), task.n_crank);
+            else
+                gpe_mex('set_omega_field', task.gb300_handle, [], task.n_crank);
+                om = double(task.omega);
             end
             gpe_mex('set_params', task.gb300_handle, task.g, task.gamma, task.decay_rate, ...
                 task.Ntotal, task.mu_init, task.n_recalc, task.itp_max_iter, task.itp_min_iter, ...
-                double(task.itp_adjust_stepsize), double(task.omega));
+                double(task.itp_adjust_stepsize), om);
             n = task.current_n;
             if isempty(n)
                 n = 0;

@@ -163,6 +163,12 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     check(c, gpe_get_history(c, mxGetDoubles(plhs[0]), mxGetDoubles(nn), len, &len));
     if (nlhs > 1) plhs[1] = nn;
     else mxDestroyArray(nn);
+  } else if (cmd == "set_omega_field") {
+    // gpe_mex('set_omega_field', h, omega, n_crank): array omega (omega = [] returns to scalar)
+    if (nrhs != 4) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('set_omega_field', h, omega, n_crank)");
+    const bool none = mxGetNumberOfElements(prhs[2]) == 0;
+    if (!none && (!mxIsDouble(prhs[2]) || mxIsComplex(prhs[2]))) mexErrMsgIdAndTxt("gpe:arg", "omega must be real double");
+    check(c, gpe_set_omega_field(c, none ? nullptr : mxGetDoubles(prhs[2]), (int)scalar(prhs[3])));
   } else if (cmd == "set_spinor_params") {
     // gpe_mex('set_spinor_params', h, g (2x2), coupling (complex scalar), nlincpl)
     if (nrhs != 5) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('set_spinor_params', h, g, coupling, nlincpl)");

@@ -198,6 +198,15 @@ GPE_API gpe_status gpe_create(const gpe_grid_desc *desc, gpe_ctx **out);
  * applyham/get_energy.  ITP, the adjoint, SGPE, batching and the autotuner
  * return GPE_ERR_UNSUPPORTED on it. */
 GPE_API gpe_status gpe_create_spinor(const gpe_grid_desc *desc, gpe_ctx **out);
+/* Array omega (GPEtask.omega as an array, ssft_kin_step.m:3-11,
+ * set_kinop.m:3-4, GPEtask.m:92-94): omega per grid point (nx*ny*nz doubles,
+ * MATLAB order) and the Crank-Nicolson iteration count n_crank [3].  The
+ * kinetic step becomes exp(-kk dt/2), n_crank iterations of
+ * lphi = phi + dt/2 omega lz(lphi), phi += dt omega lz(lphi), exp(-kk dt/2);
+ * energies and mu add <psi|-omega lz psi> (reported inside ekin).  lz uses
+ * grid1d's 4th-order derivatives with zero outside the grid.  NULL returns
+ * to scalar omega (gpe_params.omega, which must be 0 while an array is set). */
+GPE_API gpe_status gpe_set_omega_field(gpe_ctx *ctx, const double *omega, int n_crank);
 GPE_API gpe_status gpe_set_spinor_params(gpe_ctx *ctx, const gpe_spinor_params *p);
 GPE_API gpe_status gpe_get_spinor_params(const gpe_ctx *ctx, gpe_spinor_params *p);
 GPE_API void gpe_destroy(gpe_ctx *ctx);

@@ -148,6 +148,32 @@ class Grid:
     def ifft1(self, f, ax):
         return sfft.ifft(f, axis=self.axis[ax], workers=_WORKERS)
 
+    # lib/@grid1d/grid1d.m:52-57 (deriv1, stencil1 = [-1, 8, 0, -8, 1]/12):
+    # convn(A, stencil/h, 'same') along one axis, zero outside the grid, i.e.
+    # (-f(i+2) + 8 f(i+1) - 8 f(i-1) + f(i-2)) / (12 h)
+    def deriv1(self, f, ax, h):
+        a = self.axis[ax]
+        n = f.shape[a]
+        pad = [(0, 0)] * f.ndim
+        pad[a] = (2, 2)
+        g = np.pad(f, pad)
+
+        def sh(k):  # f(i + k) for i = 0..n-1
+            return np.take(g, np.arange(2 + k, 2 + k + n), axis=a)
+
+        return (-sh(2) + 8 * sh(1) - 8 * sh(-1) + sh(-2)) / (12 * h)
+
+    # lib/@grid2d/derivx.m:2, derivy.m:2 (both take the spacing obj.dx)
+    def derivx(self, f):
+        return self.deriv1(f, "x", self.dx)
+
+    def derivy(self, f):
+        return self.deriv1(f, "y", self.dx)
+
+    # lib/@grid2d/lz.m:4-8
+    def lz(self, phi, r0=(0.0, 0.0)):
+        return -1j * ((self.mesh["x"] - r0[0]) * self.derivy(phi) - (self.mesh["y"] - r0[1]) * self.derivx(phi))
+
     # lib/@grid2d/lap.m:5-10, lib/@grid3d/lap.m:5-11
     def lap(self, phi, omega=0.0):
         if omega == 0:
@@ -164,14 +190,15 @@ class Grid:
 # Solver: lib/@GPEtask
 # ---------------------------------------------------------------------------
 class GPEtask:
-    """lib/@GPEtask/GPEtask.m:1-167: omega == 0 and scalar omega (rotating
-    frame); the array-omega (Lz Crank-Nicolson) branches are not restated."""
+    """lib/@GPEtask/GPEtask.m:1-167: omega == 0, scalar omega (rotating
+    frame) and array omega (the Lz Crank-Nicolson branches)."""
 
     def __init__(self, grid: Grid, trappot):
         # GPEtask.m:41-60 (rng('shuffle') and the FFTW planner are not numerics)
         self.grid = grid
         self.g = 0.0
         self.omega = 0.0
+        self.n_crank = 3
         self.n_recalc = 10
         self.gamma = 0.0
         self.decay_rate = 0.0
@@ -212,11 +239,21 @@ class GPEtask:
             time = self.current_time
         return self.applyh0(phi, time) + self.g * np.abs(phi) ** 2 * phi
 
-    # GPEtask.m:80-95 (scalar omega; the array-omega Lz term :92-94 is not restated)
+    def _omega_array(self):
+        return np.size(self.omega) > 1  # ~isscalar(omega)
+
+    # GPEtask.m:80-95
     def applyh0(self, phi, time=None):
         if time is None:
             time = self.current_time
-        return self.getVtotal(time) * phi + self.grid.lap(phi, self.omega)
+        res = self.getVtotal(time) * phi
+        if not self._omega_array() and self.omega != 0:
+            res = res + self.grid.lap(phi, self.omega)
+        else:
+            res = res + self.grid.lap(phi)
+        if self._omega_array():
+            res = res - self.omega * self.grid.lz(phi)
+        return res
 
     # GPEtask.m:97-107
     def get_energy(self, phi=None, time=None):
@@ -279,18 +316,28 @@ class GPEtask:
             mu = (mul + mur) / 2
         return np.sqrt(vvv / self.g), mu
 
-    # lib/@GPEtask/set_kinop.m:1-11 (scalar omega: :5-7, omega == 0: :9)
+    # lib/@GPEtask/set_kinop.m:1-11 (array omega: :3-4, scalar omega: :5-7, omega == 0: :9)
     def set_kinop(self, dt):
         grid = self.grid
-        if self.omega != 0:
+        if self._omega_array():
+            self.kinop = np.exp(-grid.kk * dt / 2)
+        elif self.omega != 0:
             self.kinop = np.exp(-(grid.KX ** 2 / 2 - grid.KX * grid.mesh["y"] * self.omega) * dt / 2)
             self.kinop2 = np.exp(-(grid.KY ** 2 / 2 + grid.KZ ** 2 / 2 + grid.KY * grid.mesh["x"] * self.omega) * dt)
         else:
             self.kinop = np.exp(-grid.kk * dt)
 
-    # lib/@GPEtask/ssft_kin_step.m:12-17
+    # lib/@GPEtask/ssft_kin_step.m:1-17
     def ssft_kin_step(self, phi, dt):
         grid = self.grid
+        if self._omega_array():                                                      # :3-11
+            phi = grid.ifft(self.kinop * grid.fft(phi))
+            lphi = phi
+            for _ in range(self.n_crank):
+                lphi = phi + dt * self.omega * grid.lz(lphi)
+                lphi = 0.5 * (phi + lphi)
+            phi = phi + dt * self.omega * grid.lz(lphi)
+            return grid.ifft(self.kinop * grid.fft(phi))
         if self.omega != 0:
             phi = grid.ifft1(self.kinop * grid.fft1(phi, "x"), "x")                 # :13
             if grid.ndims == 3:                                                      # :14

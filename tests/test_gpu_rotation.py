@@ -99,3 +99,76 @@ def test_rotating_frame_large_grid_and_adjoint_rejected(gpe):
     with pytest.raises(gpe.GPEError) as e:
         task.adjoint_grad(psi0, 0.002, 3, phi0=psi0)
     assert e.value.status == L.GPE_ERR_UNSUPPORTED
+
+
+# ---- array omega: the Lz Crank-Nicolson branch (ssft_kin_step.m:3-11) ----
+def omega_field(og):
+    return 0.35 + 0.05 * og.mesh["x"] - 0.03 * og.mesh["y"]
+
+
+@pytest.mark.parametrize("precision", ["double", "single"])
+def test_array_omega_itp_2d(gpe, precision):
+    task, og, ot = pair(gpe, (4.0, 48, 3.5, 32), precision, trap2, Ntotal=20.0, g=1.0, itp_max_iter=300)
+    task.omega = ot.omega = omega_field(og)
+    X, Y = og.mesh["x"], og.mesh["y"]
+    phi0 = (np.exp(-(X ** 2 + Y ** 2) / 2) * (1 + 0.3 * (X + 1j * Y))).astype(complex)
+    phi, MU, MU2, EE = task.groundstate_itp(0.01, 1e-8, phi0, nargout=4)
+    ophi, oMU, oMU2, oEE = ot.groundstate_itp(0.01, 1e-8, phi0, nargout=4)
+    if precision == "double":
+        assert len(MU) == len(oMU)
+        np.testing.assert_allclose(MU, oMU, rtol=1e-11)
+        chk = oMU2 != 0
+        np.testing.assert_allclose(MU2[chk], oMU2[chk], rtol=1e-11)
+        np.testing.assert_allclose(EE[chk], oEE[chk], rtol=1e-11)
+        assert rel_l2(phi, ophi) < 1e-11
+    else:
+        # the energy is variational (second order in the state's distance from
+        # the fixed point); MU(i) of the norm ratio is first order, and the
+        # FP32-then-FP64 path stops at a different point of the convergence
+        assert EE[-1] == pytest.approx(oEE[-1], rel=1e-6)
+        assert MU[-1] == pytest.approx(oMU[-1], rel=5e-6)
+
+
+@pytest.mark.parametrize("axes", [(4.0, 48, 3.5, 32), (4.0, 32, 3.5, 24, 2.5, 16)], ids=["2d", "3d"])
+@pytest.mark.parametrize("precision", ["double", "single"])
+@pytest.mark.parametrize("n_crank", [3, 0])
+def test_array_omega_dynamics(gpe, axes, precision, n_crank):
+    """Damped dynamics: mu is fed back every block, so the -omega Lz energy
+    enters the step too."""
+    V = trap2 if len(axes) == 4 else trap3
+    task, og, ot = pair(gpe, axes, precision, V, Ntotal=15.0, g=1.0, gamma=0.03, n_crank=n_crank)
+    task.omega = ot.omega = omega_field(og)
+    X, Y = og.mesh["x"], og.mesh["y"]
+    psi0 = (np.exp(-((X - 0.4) ** 2 + Y ** 2) / 2) * np.exp(0.4j * Y)).astype(complex)
+    task.init_state = psi0
+    ot.init_state = psi0
+    task.solve_split(0.004, 10, 3)
+    ot.solve_split(0.004, 10, 3)
+    tol = 1e-11 if precision == "double" else 2e-5
+    assert rel_l2(task.current_state, ot.current_state) < tol
+    np.testing.assert_allclose(task.history["mu"], ot.history["mu"], rtol=10 * tol)
+    np.testing.assert_allclose(task.history["n"], ot.history["n"], rtol=tol)
+
+
+def test_array_omega_energy_and_errors(gpe):
+    import ctypes as C
+
+    from gpe_gb300 import _lib as L
+
+    task, og, ot = pair(gpe, (4.0, 48, 3.5, 32), "double", trap2, g=1.3)
+    task.omega = ot.omega = omega_field(og)
+    X, Y = og.mesh["x"], og.mesh["y"]
+    phi = ((X + 1j * Y) * np.exp(-(X ** 2 + Y ** 2) / 2)).astype(complex)
+    assert task.get_energy(phi) == pytest.approx(ot.get_energy(phi), rel=1e-12)
+    # a scalar omega next to an array is refused (GPEtask keeps one of the two)
+    p = L.gpe_params()
+    L.check(task._ctx, L.lib.gpe_get_params(task._ctx, C.byref(p)))
+    p.omega = 0.2
+    L.check(task._ctx, L.lib.gpe_set_params(task._ctx, C.byref(p)))
+    prm = L.gpe_split_params()
+    prm.ddt, prm.niter_inner, prm.niter_outer = 0.004, 10, 1
+    assert L.lib.gpe_solve_split(task._ctx, C.byref(prm)) == L.GPE_ERR_INVALID
+    # back to scalar omega
+    task.omega = 0.0
+    ot.omega = 0.0
+    assert task.get_energy(phi) == pytest.approx(ot.get_energy(phi), rel=1e-12)

@@ -331,6 +331,42 @@ def test_del2_matches_matlab_edge_extrapolation():
     np.testing.assert_allclose(O.del2(U3, g.dx, g.dy), 6 * g.mesh["x"] / 4, atol=1e-9)
 
 
+def test_lz_of_an_angular_momentum_eigenstate():
+    """grid2d/lz.m with the 4th-order stencil of grid1d.m:52-57: (x + i y) f(r)
+    has Lz = +1 and (x - i y) f(r) Lz = -1, to the stencil's O(h^4) error;
+    deriv1 is exact on cubics away from the zero-padded edges."""
+    g = O.Grid(6, 96, 6, 96)
+    X, Y = g.mesh["x"], g.mesh["y"]
+    f = np.exp(-(X ** 2 + Y ** 2) / 2)
+    for s in (1, -1):
+        phi = (X + 1j * s * Y) * f
+        assert np.max(np.abs(g.lz(phi) - s * phi)) < 3e-4 * np.max(np.abs(phi))  # h = 0.126
+    cub = X ** 3 - 2 * X
+    d = g.derivx(cub)
+    np.testing.assert_allclose(d[2:-2], (3 * X ** 2 - 2)[2:-2], rtol=0, atol=1e-9)
+
+
+def test_array_omega_keeps_the_isotropic_ground_state():
+    """Array omega (the Crank-Nicolson Lz branch, ssft_kin_step.m:3-11): a
+    nodeless ground state of an isotropic trap has Lz psi ~ 0, so a uniform
+    omega array leaves the ITP fixed point as it is without rotation, and the
+    -omega Lz energy (GPEtask.m:92-94) of an Lz = 1 state is -omega N."""
+    g = O.Grid(6, 48, 6, 48)
+    X, Y = g.mesh["x"], g.mesh["y"]
+    out = []
+    for om in (0.0, np.full(g.shape, 0.3)):
+        t = O.GPEtask(g, lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2))
+        t.Ntotal, t.g, t.omega = 10.0, 1.0, om
+        out.append(t.groundstate_itp(0.01, 1e-9, np.exp(-(X ** 2 + Y ** 2) / 2).astype(complex), nargout=1)[0])
+    # the stencil's O(h^4) error on the radial profile (h = 0.26) is the difference
+    assert np.linalg.norm(out[1] - out[0]) / np.linalg.norm(out[0]) < 1e-4
+    t = O.GPEtask(g, lambda X, Y, Z: 0 * X)
+    t.omega = np.full(g.shape, 0.3)
+    phi = (X + 1j * Y) * np.exp(-(X ** 2 + Y ** 2) / 2)
+    lz_energy = np.real(g.inner(phi, t.applyh0(phi) - g.lap(phi)))
+    assert lz_energy == pytest.approx(-0.3 * g.integrate(np.abs(phi) ** 2), rel=2e-3)  # stencil error, h = 0.26
+
+
 def test_golden_fixtures_reproduce():
     from tests.golden import make_golden as MG
 
