@@ -171,6 +171,54 @@ void launch_sgpe_nl_noise(cx<R>* psi, const R* V, long long n, DevScalars* sc, d
                                                                       (R)sigma, seed, step);
 }
 
+// The block end of solve_split.m:60-65 as one elementwise pass: the last
+// step's full factor exp((mu - V - g|p|^2) dt), the inverse half step
+// exp((V - mu + g|p|^2) dt/2), and per CTA the sums n, V n, n^2 into the
+// partial slots S_N, S_VN, S_N2 (what the pass epilogue EPI_RT_END does).
+template <typename R>
+__global__ void __launch_bounds__(ADJ_THREADS) k_rt_block_end(cx<R>* __restrict__ psi, const R* __restrict__ V,
+                                                             long long n, const DevScalars* sc, R g, R dre, R dim,
+                                                             double* partials, int cap) {
+  if (sc->stop) return;
+  const R mu = (R)sc->mu;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (long long i = (long long)blockIdx.x * ADJ_THREADS + threadIdx.x; i < n;
+       i += (long long)gridDim.x * ADJ_THREADS) {
+    cx<R> p = psi[i];
+    const R VV = V[i] - mu;
+    p = cmul(cexp_real_times(-VV - g * norm2(p), dre, dim), p);
+    p = cmul(cexp_real_times((VV + g * norm2(p)) * R(0.5), dre, dim), p);
+    psi[i] = p;
+    const double nn = (double)norm2(p);
+    a0 += nn;
+    a1 += (double)V[i] * nn;
+    a2 += nn * nn;
+  }
+  __shared__ double sh[3][ADJ_THREADS];
+  sh[0][threadIdx.x] = a0;
+  sh[1][threadIdx.x] = a1;
+  sh[2][threadIdx.x] = a2;
+  __syncthreads();
+  for (int o = ADJ_THREADS / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int k = 0; k < 3; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partials[(size_t)S_N * cap + blockIdx.x] = sh[0][0];
+    partials[(size_t)S_VN * cap + blockIdx.x] = sh[1][0];
+    partials[(size_t)S_N2 * cap + blockIdx.x] = sh[2][0];
+  }
+}
+
+template <typename R>
+int launch_rt_block_end(cx<R>* psi, const R* V, long long n, const DevScalars* sc, double g, double dre, double dim,
+                        double* partials, int cap, cudaStream_t s) {
+  const int nb = elem_grid(n, ADJ_THREADS);
+  k_rt_block_end<R><<<nb, ADJ_THREADS, 0, s>>>(psi, V, n, sc, (R)g, (R)dre, (R)dim, partials, cap);
+  return nb;
+}
+
 __global__ void k_selftest_noise(float* out, long long n, unsigned long long seed, unsigned long long step) {
   for (long long i = (long long)blockIdx.x * ADJ_THREADS + threadIdx.x; i < n;
        i += (long long)gridDim.x * ADJ_THREADS) {
@@ -192,7 +240,9 @@ cudaError_t launch_selftest_noise(float* out, long long n, unsigned long long se
   template int launch_inner<R>(const cx<R>*, const cx<R>*, long long, double*, cudaStream_t);          \
   template void launch_cscale<R>(cx<R>*, const cx<R>*, long long, double, double, cudaStream_t);        \
   template void launch_sgpe_nl_noise<R>(cx<R>*, const R*, long long, DevScalars*, double, double, double, int, \
-                                        double, unsigned long long, unsigned long long, cudaStream_t);
+                                        double, unsigned long long, unsigned long long, cudaStream_t);     \
+  template int launch_rt_block_end<R>(cx<R>*, const R*, long long, const DevScalars*, double, double, double,  \
+                                      double*, int, cudaStream_t);
 INST_ADJ(float)
 INST_ADJ(double)
 

@@ -100,10 +100,18 @@ struct LzGeom {
   double x0, y0;    // coordinates of ix = 0, iy = 0
   double hxg, hyg;  // grid spacings of the coordinates
 };
-// out = phi + (cre + i cim) * omega * lz(src); out may be phi, never src.
+// out = phi + (cre + i cim) * omega * lz(src), omega = om[i] or the scalar
+// oms when om is null; out may be phi, never src.
 template <typename R>
-void launch_lz_cn(cx<R>* out, const cx<R>* phi, const cx<R>* src, const R* om, long long n, const LzGeom& g,
-                  double cre, double cim, cudaStream_t st);
+void launch_lz_cn(cx<R>* out, const cx<R>* phi, const cx<R>* src, const R* om, double oms, long long n,
+                  const LzGeom& g, double cre, double cim, cudaStream_t st);
+// The block end of solve_split as an elementwise pass (the last step's full
+// nonlinear factor, the inverse half step, sums n, Vn, n^2 per CTA into the
+// partial slots): the pass epilogue EPI_RT_END for runs whose last kinetic
+// pass cannot carry it.  Returns CTAs.
+template <typename R>
+int launch_rt_block_end(cx<R>* psi, const R* V, long long n, const DevScalars* sc, double g, double dre, double dim,
+                        double* partials, int cap, cudaStream_t s);
 // Per-CTA sums of real(conj(psi) (-omega lz psi)) (times scale^2 if use_scale); returns CTAs.
 template <typename R>
 int launch_lz_energy(const cx<R>* psi, const R* om, long long n, const LzGeom& g, const DevScalars* sc,

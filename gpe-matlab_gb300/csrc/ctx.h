@@ -70,6 +70,7 @@ struct gpe_ctx {
   // Array omega (ssft_kin_step.m:3-11): omega per grid point, FP64 and the
   // context precision, and the Crank-Nicolson iteration count n_crank.
   bool omega_field = false;
+  bool adi_off = false;   // rotating SGPE run: scalar omega drives only its Lz step, not the ADI kinetic factors
   double* omf64 = nullptr;
   void* omfR = nullptr;
   int n_crank = 3;

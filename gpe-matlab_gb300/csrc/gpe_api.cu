@@ -119,6 +119,11 @@ PassGeom dispatch_geom(int N, int var, bool strided) {
   return PassGeom{0, 1, 0};
 }
 
+// The scalar omega of the rotating-frame kinetic factors (set_kinop.m:5-7,
+// ssft_kin_step.m:12-15, lap.m:8-10); 0 while a rotating SGPE runs, whose
+// omega enters only through its Lz Crank-Nicolson update.
+double adi_omega(const gpe_ctx* c) { return c->adi_off ? 0.0 : c->prm.omega; }
+
 enum { SPLIT_FULL = 0, SPLIT_FWD = 1, SPLIT_INV = 2, SPLIT_MASKED = 3 };
 
 struct AxisPass {
@@ -166,7 +171,7 @@ std::vector<AxisPass> axis_passes(const gpe_ctx* c, double ecut = 0.0) {
     }
     return v;
   }
-  if (c->prm.omega != 0.0) {
+  if (adi_omega(c) != 0.0) {
     AxisPass rx = px, ry = py;
     rx.rot = 1;
     ry.rot = 2;
@@ -200,7 +205,7 @@ std::vector<AxisPass> step_passes(const gpe_ctx* c, double ecut = 0.0) {
 // One pass per axis (energy sums): the axis passes without the second x half.
 std::vector<AxisPass> energy_axes(const gpe_ctx* c) {
   std::vector<AxisPass> v = axis_passes(c);
-  if (c->prm.omega != 0.0) v.pop_back();
+  if (adi_omega(c) != 0.0) v.pop_back();
   return v;
 }
 
@@ -478,7 +483,7 @@ double coord(const gpe_ctx* c, int ax, int i) { return -0.5 * c->span[ax] + i * 
 // coordinate: rotw[0][iy] = -omega*y(iy), rotw[1][ix] = +omega*x(ix).
 template <typename R>
 gpe_status ensure_rot_weights(gpe_ctx* c, Field& f) {
-  const double om = c->prm.omega;
+  const double om = adi_omega(c);
   if (om == 0.0 || (f.rotw[0] && f.rotw_omega == om)) return GPE_OK;
   for (int r = 0; r < 2; ++r) {
     const int tax = r == 0 ? 1 : 0;  // transverse axis: y for x pencils, x for y pencils
@@ -510,7 +515,7 @@ gpe_status build_static_tables(gpe_ctx* c, Field& f) {
 template <typename R>
 gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
   if (f.phase_valid && f.phase_dt[0] == dre && f.phase_dt[1] == dim) return GPE_OK;
-  const double om = c->prm.omega;
+  const double om = adi_omega(c);
   for (int ax = 0; ax < c->ndims; ++ax) {
     const int N = c->n[ax];
     const PlanInfo pi = dispatch_plan(N, f.plan_var[ax]);
@@ -738,26 +743,29 @@ gpe_status ensure_cn_buffers(gpe_ctx* c, Field& f) {
 
 // ssft_kin_step.m:5-10 between the two half kinetic steps, dt = dre + i dim:
 //   lphi = phi; n_crank times: lphi = phi + dt/2 omega lz(lphi); phi += dt omega lz(lphi)
+// with the omega array, or (the rotating SGPE, @SGPEtask/solve_split.m:58-64)
+// the scalar omega when no array is set.
 template <typename R>
 gpe_status cn_step(gpe_ctx* c, Field& f, double dre, double dim) {
   CHECK(ensure_cn_buffers<R>(c, f));
   const LzGeom g = lz_geom(c);
-  const R* om = omega_field_ptr<R>(c);
+  const R* om = c->omega_field ? omega_field_ptr<R>(c) : nullptr;
+  const double oms = c->prm.omega;
   cx<R>* phi = (cx<R>*)f.psi;
   const cx<R>* src = phi;
   int k = 0;
   for (int it = 0; it < c->n_crank; ++it) {
     cx<R>* out = (cx<R>*)f.cn[k];
     Launch L(c, PC_ELEMENTWISE, (double)c->P * 6 * sizeof(R));
-    launch_lz_cn<R>(out, phi, src, om, c->P, g, 0.5 * dre, 0.5 * dim, c->stream);
+    launch_lz_cn<R>(out, phi, src, om, oms, c->P, g, 0.5 * dre, 0.5 * dim, c->stream);
     src = out;
     k ^= 1;
   }
   Launch L(c, PC_ELEMENTWISE, (double)c->P * 6 * sizeof(R));
   if (c->n_crank > 0) {
-    launch_lz_cn<R>(phi, phi, src, om, c->P, g, dre, dim, c->stream);  // reads src's neighbours only
+    launch_lz_cn<R>(phi, phi, src, om, oms, c->P, g, dre, dim, c->stream);  // reads src's neighbours only
   } else {
-    launch_lz_cn<R>((cx<R>*)f.cn[0], phi, phi, om, c->P, g, dre, dim, c->stream);
+    launch_lz_cn<R>((cx<R>*)f.cn[0], phi, phi, om, oms, c->P, g, dre, dim, c->stream);
     CU(cudaMemcpyAsync(phi, f.cn[0], (size_t)c->P * 2 * sizeof(R), cudaMemcpyDeviceToDevice, c->stream));
   }
   CU(cudaGetLastError());
@@ -1073,6 +1081,7 @@ struct SplitRun {
   // Stochastic GPE (SGPEtask.solve_split): mu fixed at mu_init, no
   // renormalisation, noise sigma * (n1 + i n2) before every kinetic step.
   bool sgpe = false;
+  bool sgpe_cn = false;        // rotating SGPE: Lz Crank-Nicolson after each kinetic step (solve_split.m:58-64)
   double sigma = 0.0;          // sqrt(T gamma ddt / weight), solve_split.m:49
   unsigned long long seed = 0;
   int niter_inner = 1;         // for the global step index of the noise counter
@@ -1133,6 +1142,8 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
   run.niter_inner = prm->niter_inner;
   if (sg) {
     run.sgpe = true;
+    run.sgpe_cn = c->prm.omega != 0.0;
+    if (run.sgpe_cn) CHECK(ensure_cn_buffers<R>(c, f));
     run.sigma = std::sqrt(sg->T * gam * ddt / c->weight);
     run.seed = sg->seed;
   }
@@ -1177,9 +1188,20 @@ gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool las
         continue;
       }
       const int pro = (first && !run.sgpe) ? (i == 1 ? PRO_RT_HALF : PRO_RT_FULL) : PRO_NONE;
-      const int epi = (last && i == run.n_rec) ? EPI_RT_END : EPI_NONE;
-      CHECK(run_pass<R>(c, f, run.passes[k], KIND_STEP, pro, epi, 0, run.dre, run.dim,
-                        (last && i == run.n_rec) ? &nb_epi : nullptr));
+      const bool end = last && i == run.n_rec && !run.sgpe_cn;
+      CHECK(run_pass<R>(c, f, run.passes[k], KIND_STEP, pro, end ? EPI_RT_END : EPI_NONE, 0, run.dre, run.dim,
+                        end ? &nb_epi : nullptr));
+    }
+    if (run.sgpe_cn) {
+      // rotating SGPE: the Lz update follows the kinetic step, the nonlinear
+      // factor follows it (the next step's first kernel, or the block end)
+      CHECK(cn_step<R>(c, f, run.dre, run.dim));
+      if (i == run.n_rec) {
+        Launch L(c, PC_NL_PHASE, (double)c->P * (4 * sizeof(R) + sizeof(R)));
+        nb_epi = launch_rt_block_end<R>((cx<R>*)f.psi, (const R*)f.V, c->P, c->sc, c->prm.g, run.dre, run.dim,
+                                        c->partials, c->cap, c->stream);
+        CU(cudaGetLastError());
+      }
     }
   }
   const bool need_mu = (run.feedback || last_block) && !run.sgpe;
@@ -1872,6 +1894,7 @@ gpe_status gpe_set_spinor_params(gpe_ctx* c, const gpe_spinor_params* p) {
 gpe_status gpe_set_omega_field(gpe_ctx* c, const double* omega, int n_crank) {
   CHECK(check_ctx(c));
   if (n_crank < 0) return fail(c, GPE_ERR_INVALID, "set_omega_field: n_crank must be >= 0");
+  c->n_crank = n_crank;  // also the rotating SGPE's Crank-Nicolson count
   if (!omega) {
     if (c->omega_field) {
       c->main.phase_valid = false;  // the half-step tables follow the mode
@@ -2369,11 +2392,30 @@ gpe_status gpe_solve_sgpe(gpe_ctx* c, const gpe_split_params* prm, const gpe_sgp
     return fail(c, GPE_ERR_INVALID, "solve_sgpe: ddt must be positive");
   if (!(sg->T >= 0) || !std::isfinite(sg->T) || !(sg->ecut >= 0))
     return fail(c, GPE_ERR_INVALID, "solve_sgpe: T and ecut must be >= 0");
-  if (c->prm.omega != 0.0 || c->omega_field)
-    return fail(c, GPE_ERR_UNSUPPORTED, "solve_sgpe: omega != 0 (the reference's Lz Crank-Nicolson branch)");
+  if (c->omega_field)
+    return fail(c, GPE_ERR_UNSUPPORTED, "solve_sgpe: an omega array (the reference's SGPE takes a scalar omega)");
   if (!prm->vtd) CHECK(need_V(c));
   c->err.clear();
   CHECK(maybe_autotune(c));
+  // The SGPE's kinetic factor is exp(-kk dt) whatever omega is (solve_split.m:
+  // 40-45); a scalar omega acts through the Lz step only.  The kinetic tables
+  // are rebuilt on entry and exit when the rotating-frame ones differ.
+  struct AdiOff {
+    gpe_ctx* c;
+    bool on;
+    AdiOff(gpe_ctx* cc) : c(cc), on(cc->prm.omega != 0.0) {
+      if (on) {
+        c->adi_off = true;
+        c->main.phase_valid = false;
+      }
+    }
+    ~AdiOff() {
+      if (on) {
+        c->adi_off = false;
+        c->main.phase_valid = false;
+      }
+    }
+  } guard(c);
   if (c->prec == GPE_FP32) return split_impl<float>(c, prm, sg);
   return split_impl<double>(c, prm, sg);
 }

@@ -33,17 +33,19 @@ __device__ __forceinline__ cx<R> lz_w(const cx<R>* __restrict__ s, long long i, 
   return mk<R>(X * dy.x - Y * dx.x, X * dy.y - Y * dx.y);
 }
 
-// out = phi + c * omega * lz(src), c complex (lz = -i w).
+// out = phi + c * omega * lz(src), c complex (lz = -i w); omega from the
+// array om, or the scalar oms where om is null.
 template <typename R>
 __global__ void __launch_bounds__(LZ_T) k_lz_cn(cx<R>* out, const cx<R>* phi, const cx<R>* __restrict__ src,
-                                               const R* __restrict__ om, long long n, LzGeom g, R cre, R cim) {
+                                               const R* __restrict__ om, R oms, long long n, LzGeom g, R cre,
+                                               R cim) {
   const long long nxy = (long long)g.nx * g.ny;
   for (long long i = (long long)blockIdx.x * LZ_T + threadIdx.x; i < n; i += (long long)gridDim.x * LZ_T) {
     const long long r = i % nxy;
     const int ix = (int)(r / g.ny), iy = (int)(r % g.ny);
     const cx<R> w = lz_w<R>(src, i, ix, iy, g);
     const cx<R> lz = mk<R>(w.y, -w.x);  // -i w
-    const R o = om[i];
+    const R o = om ? om[i] : oms;
     const cx<R> t = mk<R>(o * (cre * lz.x - cim * lz.y), o * (cre * lz.y + cim * lz.x));
     const cx<R> p = phi[i];
     out[i] = mk<R>(p.x + t.x, p.y + t.y);
@@ -79,9 +81,9 @@ __global__ void __launch_bounds__(LZ_T) k_lz_energy(const cx<R>* __restrict__ ps
 }
 
 template <typename R>
-void launch_lz_cn(cx<R>* out, const cx<R>* phi, const cx<R>* src, const R* om, long long n, const LzGeom& g,
-                  double cre, double cim, cudaStream_t st) {
-  k_lz_cn<R><<<elem_grid(n, LZ_T), LZ_T, 0, st>>>(out, phi, src, om, n, g, (R)cre, (R)cim);
+void launch_lz_cn(cx<R>* out, const cx<R>* phi, const cx<R>* src, const R* om, double oms, long long n,
+                  const LzGeom& g, double cre, double cim, cudaStream_t st) {
+  k_lz_cn<R><<<elem_grid(n, LZ_T), LZ_T, 0, st>>>(out, phi, src, om, (R)oms, n, g, (R)cre, (R)cim);
 }
 
 template <typename R>
@@ -93,8 +95,8 @@ int launch_lz_energy(const cx<R>* psi, const R* om, long long n, const LzGeom& g
 }
 
 #define INST_LZ(R)                                                                                     \
-  template void launch_lz_cn<R>(cx<R>*, const cx<R>*, const cx<R>*, const R*, long long, const LzGeom&,  \
-                                double, double, cudaStream_t);                                         \
+  template void launch_lz_cn<R>(cx<R>*, const cx<R>*, const cx<R>*, const R*, double, long long,         \
+                                const LzGeom&, double, double, cudaStream_t);                          \
   template int launch_lz_energy<R>(const cx<R>*, const R*, long long, const LzGeom&, const DevScalars*, int, \
                                    double*, cudaStream_t);
 INST_LZ(float)

@@ -581,6 +581,12 @@ class SGPEtask(GPEtask):
                 for _ in range(n_rec):                                   # :59-70
                     phi = phi + variance * noise(phi.shape)
                     phi = grid.ifft(ekk * grid.fft(phi))
+                    if self.omega != 0:                                  # :61-67
+                        lphi = phi
+                        for _ in range(self.n_crank):
+                            lphi = phi + dt * self.omega * grid.lz(lphi)
+                            lphi = 0.5 * (phi + lphi)
+                        phi = phi + dt * self.omega * grid.lz(lphi)
                     phi = np.exp((mu - VV - g * phi * np.conj(phi)) * dt) * phi
                 phi = np.exp((VV - mu + g * phi * np.conj(phi)) * dt / 2) * phi  # :73
                 tmp2 = np.real(phi * np.conj(phi))

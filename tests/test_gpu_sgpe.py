@@ -8,6 +8,9 @@
 * T > 0: the oracle fed the device's own noise variates: FP32 <= 2e-5.
 * The noise amplitude of one step from a zero state: within 5% of
   sqrt(T gamma ddt / weight) propagated through the kinetic factor.
+* Rotating SGPE (scalar omega: the Lz Crank-Nicolson update after each
+  kinetic step, solve_split.m:61-67): T = 0 FP64 and T > 0 FP32 with the
+  device noise, against the oracle.
 * Energy cut-off (ecut > 0 with T > 0, solve_split.m:40-42): the oracle fed
   the device's noise (a numpy restatement of the generator in FP64), 2D and
   3D, FP64 <= 1e-11 and FP32 <= 2e-5; one step of pure noise leaves no mode
@@ -155,7 +158,8 @@ def test_sgpe_noise_amplitude(gpe):
 def test_sgpe_unsupported_options(gpe):
     from gpe_gb300 import _lib as L
 
-    task, og, ot = make_pair(gpe, (4.0, 32, 3.5, 32), "single", g=1.0, gamma=0.1, T=1.0, omega=0.5)
+    task, og, ot = make_pair(gpe, (4.0, 32, 3.5, 32), "single", g=1.0, gamma=0.1, T=1.0)
+    task.omega = 0.5 + 0.0 * og.mesh["x"]  # an omega array: the reference's SGPE takes a scalar
     task.init_state = np.ones(og.shape, complex)
     with pytest.raises(gpe.GPEError) as e:
         task.solve_split(0.004, 10, 1)
@@ -235,3 +239,25 @@ def test_sgpe_block_count_follows_sgpe_solve_split(gpe):
     with pytest.raises(gpe.GPEError) as e:
         task.solve_split(0.004, 5, 1)
     assert e.value.status == L.GPE_ERR_INVALID
+
+
+@pytest.mark.parametrize("precision,T", [("double", 0.0), ("single", 0.4)])
+def test_rotating_sgpe_matches_oracle(gpe, precision, T):
+    task, og, ot = make_pair(gpe, (4.0, 48, 3.5, 32), precision, g=0.8, gamma=0.05, mu_init=2.0, T=T,
+                             omega=0.45, n_crank=3, n_recalc=5)
+    task.seed = 31
+    steps = iter(range(10 ** 6))
+
+    def noise(shape):
+        return gauss2_np(task.seed, next(steps), int(np.prod(shape))).reshape(shape)
+
+    ot.noise = noise
+    X, Y = og.mesh["x"], og.mesh["y"]
+    psi0 = (np.exp(-((X - 0.5) ** 2 + Y ** 2) / 2) * (1 + 0.2 * (X + 1j * Y))).astype(complex)
+    task.init_state = psi0
+    ot.init_state = psi0
+    task.solve_split(0.004, 10, 2)
+    ot.solve_split(0.004, 10, 2)
+    tol = 1e-11 if precision == "double" else 2e-5
+    assert rel_l2(task.current_state, ot.current_state) < tol
+    np.testing.assert_allclose(task.history["n"], ot.history["n"], rtol=tol)
