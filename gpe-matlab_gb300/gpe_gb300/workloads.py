@@ -145,13 +145,20 @@ class BatchWorkload:
     def npoints(self) -> int:
         return int(sum(r["n"] ** 2 for r in self.realisations()))
 
-    def make_tasks(self, precision: str = "single", device: int = 0):
-        """Tasks holding their ground state with the vortices imprinted."""
+    def shard(self, rank: int = 0, world: int = 1):
+        """Realisation indices of one rank: the independent realisations are
+        dealt round-robin over the ranks (no exchange between them)."""
+        return list(range(rank, self.count, world))
+
+    def make_tasks(self, precision: str = "single", device: int = 0, rank: int = 0, world: int = 1):
+        """Tasks of this rank's realisations, holding their ground state with
+        the vortices imprinted."""
         from .imprint import imprint_vortex
         from .task import GPEtask
 
         tasks = []
-        for r in self.realisations():
+        rs = self.realisations()
+        for r in (rs[i] for i in self.shard(rank, world)):
             grid = grid2d(self.box, r["n"], self.box, r["n"], precision=precision)
             lam = r["lam"]
             task = GPEtask(grid, lambda X, Y, Z, lam=lam: 0.5 * (X ** 2 + (lam * Y) ** 2), device=device)
