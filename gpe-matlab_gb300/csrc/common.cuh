@@ -287,6 +287,7 @@ struct PassArgs {
   R gr, drer, dimr;        // g, dre, dim rounded to R by the host (no FP64 work per thread)
   int prefetch = 0;        // direct pass: 1 = prefetch the tile one wave ahead into L2
   int pf_ahead = 0;        // set by the launcher: resident CTAs of the launch (one wave)
+  int pdl = 0;             // launch with programmatic stream serialisation (host side)
   // Rotating frame (x and y passes; null/0 otherwise).  Pencil b has the
   // transverse grid index b % rot_period (y for x pencils, x for y pencils).
   const cx<R>* rot = nullptr;  // step: [transverse index][slot] cross-term factors

@@ -98,6 +98,7 @@ struct gpe_ctx {
 
   int sms = 152;          // SM count of the device
   int pass_variant = 0;   // 0: direct passes + L2 prefetch, 1: TMA-staged where they apply, 2: direct
+  int pdl = 1;            // direct passes: programmatic dependent launch (GPE_PDL=0 turns it off)
   int tune_mode = 2;      // FFT plan autotuner: 0 off, 1 explicit only, 2 on the first hot-path call
   bool tuned = false;     // the autotuner has set main.plan_var
   bool prof = false;

@@ -665,6 +665,7 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.drer = (R)dre;
   a.dimr = (R)dim;
   a.prefetch = c->pass_variant == 0;
+  a.pdl = c->pdl;
   if (ap.rot != 0) {
     const int r = ap.rot - 1;  // 0: x pencils (transverse y), 1: y pencils (transverse x)
     a.rot_period = c->n[r == 0 ? 1 : 0];
@@ -1821,6 +1822,8 @@ static gpe_status create_impl(const gpe_grid_desc* d, gpe_ctx** out, int ncomp) 
   }
   cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
   if (c->sms <= 0) c->sms = 152;
+  // GPE_PDL=0|1: launch the direct passes with programmatic dependent launch.
+  if (const char* e = getenv("GPE_PDL")) c->pdl = atoi(e) != 0;
   // GPE_AUTOTUNE=0|1|2 sets the initial autotuner mode (gpe_autotune) of new contexts.
   if (const char* e = getenv("GPE_AUTOTUNE")) {
     const int m = atoi(e);

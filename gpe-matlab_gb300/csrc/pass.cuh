@@ -348,6 +348,18 @@ template <typename R, class P, class L, int KIND>
 __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_kernel(const PassArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);
+  // Programmatic dependent launch: the next kernel in the stream may be
+  // scheduled as soon as every CTA of this one has started.  A CTA of the
+  // first wave, started early that way, hints its own tile into L2 while the
+  // previous kernel drains (L2 is the point of coherence, so the hint cannot
+  // hold stale data), then waits for that kernel's completion and memory
+  // before it reads anything.  Without the launch attribute both are no-ops.
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if (a.pf_ahead > 0 && (long long)blockIdx.x < a.pf_ahead) {
+    const long long b0 = (long long)blockIdx.x * L::FFTS;
+    if (b0 < a.n_batch) L::prefetch(a, b0, a.n_batch - b0 < L::FFTS ? a.n_batch - b0 : (long long)L::FFTS);
+  }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   // The pending scale and mu, converted to R once per CTA (the FP64 pipe of
   // this GPU is narrow: per-thread conversions showed up in the pass time).
   __shared__ R scal[2];

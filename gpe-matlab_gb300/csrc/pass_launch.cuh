@@ -57,8 +57,21 @@ static cudaError_t launch_layout(const PassArgs<R>& a, cudaStream_t s) {
     const int wave = resident_ctas((const void*)kern, L::THREADS, smem) * device_sm_count();
     if (wave > 0 && blocks > wave) b.pf_ahead = wave;
   }
-  kern<<<(unsigned)blocks, L::THREADS, smem, s>>>(b);
-  return cudaGetLastError();
+  if (!a.pdl) {
+    kern<<<(unsigned)blocks, L::THREADS, smem, s>>>(b);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(L::THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, b);
 }
 
 template <typename R, int N, int V>
