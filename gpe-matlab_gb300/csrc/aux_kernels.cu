@@ -113,6 +113,10 @@ constexpr int FIN_GRID = 32;
 constexpr int FIN_CHUNK = 256;
 
 __global__ void k_finalize_block(const BlockFinalArgs a, DevScalars* sc) {
+  // programmatic dependent launch (see the pass kernel): let the next pass be
+  // scheduled now, read nothing before the previous kernel has completed
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   if (sc->stop) return;  // set only by earlier kernels: the same for every CTA
   const int cap = a.cap;
   const double* p[6] = {a.partials + S_N * cap,        a.partials + S_VN * cap,       a.partials + S_N2 * cap,
@@ -318,7 +322,20 @@ void launch_finalize_block(const BlockFinalArgs& a, DevScalars* sc, cudaStream_t
   for (int ax = 0; ax < 3; ++ax) longest = a.nblk_kin[ax] > longest ? a.nblk_kin[ax] : longest;
   int grid = (longest + FIN_CHUNK - 1) / FIN_CHUNK;
   grid = grid < 1 ? 1 : grid > FIN_GRID ? FIN_GRID : grid;
-  k_finalize_block<<<grid, FIN_THREADS, 0, s>>>(a, sc);
+  if (!a.pdl) {
+    k_finalize_block<<<grid, FIN_THREADS, 0, s>>>(a, sc);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(FIN_THREADS);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_finalize_block, a, sc);
 }
 void launch_finalize_itp(const ItpFinalArgs& a, DevScalars* sc, cudaStream_t s) {
   k_finalize_itp<<<1, FIN_THREADS, 0, s>>>(a, sc);

@@ -22,6 +22,7 @@ struct BlockFinalArgs {
   int* hist_ok;
   int fixed_mu = 0;      // report sc->mu (the stochastic GPE's mu_init) instead of <psi|H psi>/N
   double* hist_e = nullptr;  // get_energy of the block-end state (GPEtask.m:97-107), or nullptr
+  int pdl = 0;               // launch with programmatic stream serialisation
 };
 
 struct ItpFinalArgs {
