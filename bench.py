@@ -11,8 +11,9 @@ steps (10 blocks of n_recalc = 10, mu feedback every block).
 Prints one JSON line.  `value` is complex-FP32 throughput with the state
 resident in HBM; `fp64` is the same kernels in FP64 on the same start state;
 `error` states the FP32 result against the FP64 one after 100 steps; `e2e`
-runs each step through the public host API with pinned host buffers (state
-upload, 100 steps, state download).  `--impl reference` times the FP64 CPU
+runs each step through the C ABI (the drop-in boundary) with pinned host
+buffers: gpe_set_state from the host, one outer step of gpe_solve_split,
+gpe_get_state to the host.  `--impl reference` times the FP64 CPU
 restatement of the reference's solve_split (the reference is MATLAB, which
 this machine does not have) on the same workload, all host cores.
 """
@@ -228,6 +229,39 @@ def imprint(gpe, W, grid, task, phi):
     return phi
 
 
+def e2e_abi(task, host_in, host_out, ddt, inner, steps):
+    """`steps` outer steps, each through the C ABI with host buffers: the
+    state uploaded from host_in, one outer step of `inner` split steps from
+    current_iter 0 (gpe_solve_split), the state downloaded into host_out.
+    Returns the wall seconds."""
+    import ctypes as C
+
+    from gpe_gb300 import _lib as L
+
+    task._push_params()
+    ctx = task._ctx
+    prm = L.gpe_split_params()
+    prm.ddt, prm.niter_inner, prm.niter_outer = float(ddt), int(inner), 1
+    cur = L.gpe_current()
+    fin = host_in.view(np.float32) if host_in.dtype == np.complex64 else host_in.view(np.float64)
+    fout = host_out.view(np.float32) if host_out.dtype == np.complex64 else host_out.view(np.float64)
+    set_state = L.lib.gpe_set_state_f32 if host_in.dtype == np.complex64 else L.lib.gpe_set_state
+    get_state = L.lib.gpe_get_state_f32 if host_out.dtype == np.complex64 else L.lib.gpe_get_state
+    ptr = L.fptr if host_in.dtype == np.complex64 else L.dptr
+
+    def one():
+        L.check(ctx, L.lib.gpe_set_current(ctx, C.byref(cur)))   # current_iter = 0
+        L.check(ctx, set_state(ctx, ptr(fin)))
+        L.check(ctx, L.lib.gpe_solve_split(ctx, C.byref(prm)))
+        L.check(ctx, get_state(ctx, ptr(fout)))
+
+    one()  # warm
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    return time.perf_counter() - t0
+
+
 def run_gpu(args, dist):
     global INNER
     import gpe_gb300 as gpe
@@ -311,17 +345,7 @@ def run_gpu(args, dist):
     host_out = np.empty_like(host_in)
     e2e_steps = max(1, min(args.steps, 5))
     with gpe.pinned(host_in), gpe.pinned(host_out):
-        task.init_state = host_in
-        task.current_iter = 0
-        task.solve_split(W.dt, INNER, 1)
-        task._download(host_out)
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            task.init_state = host_in
-            task.current_iter = 0
-            task.solve_split(W.dt, INNER, 1)
-            task._download(host_out)
-        e2e_t = time.perf_counter() - t0
+        e2e_t = e2e_abi(task, host_in, host_out, W.dt, INNER, e2e_steps)
     e2e_t = dist.reduce(e2e_t, "max")
     e2e_val = dist.reduce(float(P) * INNER * e2e_steps, "sum") / e2e_t
     # ---- CPU baseline (rank 0, N = 1 only): bounded sample ---------------------
@@ -600,17 +624,7 @@ def run_spinor(args, dist):
     host_out = np.empty_like(host_in)
     e2e_steps = max(1, min(args.steps, 3))
     with gpe.pinned(host_in), gpe.pinned(host_out):
-        task.init_state = host_in
-        task.current_iter = 0
-        task.solve_split(S.dt, inner, 1)
-        task._download(host_out)
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            task.init_state = host_in
-            task.current_iter = 0
-            task.solve_split(S.dt, inner, 1)
-            task._download(host_out)
-        e2e_t = time.perf_counter() - t0
+        e2e_t = e2e_abi(task, host_in, host_out, S.dt, inner, e2e_steps)
     e2e_t = dist.reduce(e2e_t, "max")
     e2e_val = dist.reduce(float(P) * inner * e2e_steps, "sum") / e2e_t
     cpu = None

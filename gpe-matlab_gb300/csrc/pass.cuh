@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
   // hold stale data), then waits for that kernel's completion and memory
   // before it reads anything.  Without the launch attribute both are no-ops.
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  if (a.pf_ahead > 0 && (long long)blockIdx.x < a.pf_ahead) {
+  if (a.pdl && a.pf_ahead > 0 && (long long)blockIdx.x < a.pf_ahead) {
     const long long b0 = (long long)blockIdx.x * L::FFTS;
     if (b0 < a.n_batch) L::prefetch(a, b0, a.n_batch - b0 < L::FFTS ? a.n_batch - b0 : (long long)L::FFTS);
   }
