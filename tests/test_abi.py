@@ -108,3 +108,16 @@ def test_no_gpu_reports_no_device():
     d.precision = L.GPE_FP32
     assert L.lib.gpe_create(C.byref(d), C.byref(ctx)) == L.GPE_ERR_NO_DEVICE
     assert not ctx.value
+
+
+def test_mex_gateway_compiles_against_the_documented_api():
+    """matlab/gpe_mex.cpp cannot be built without MATLAB; this compiles it
+    (syntax and types) against declarations of the documented MEX C API and
+    include/gpe.h, so a call that no longer matches the C ABI fails here."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    src = ROOT / "gpe-matlab_gb300" / "matlab" / "gpe_mex.cpp"
+    r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(ROOT / "tests" / "mex_stub"),
+                        "-I", str(ROOT / "include"), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
