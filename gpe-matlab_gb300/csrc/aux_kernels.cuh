@@ -79,7 +79,7 @@ struct SpinorFinalArgs {
   double weight;
   double g[4];
   double cre, cim;
-  int mode;                     // 0: run start, 1: block end, 2: observables
+  int mode;                     // 0: run start, 1: block end, 2: observables, 3: ITP (MU2 -> hist, EE -> obs)
   double Ntotal;                // mode 0
   int renorm;                   // mode 1: gamma > 0
   double tau, time2;
@@ -93,6 +93,14 @@ template <typename R>
 int launch_spinor_sums(const cx<R>* psi, const R* V, long long P, const DevScalars* sc, double* out,
                        cudaStream_t s);
 void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream_t s);
+// Spinor ITP: the factors exp(-(V_j + sum_k g(j,k) |psi_k|^2) dt) into f (2P)
+// and, after the kinetic half step, the coupling rotation times them.
+template <typename R>
+void launch_spinor_itp_factors(const cx<R>* psi, const R* V, long long P, const DevScalars* sc, const SpinorNL<R>& q,
+                               R* f, cudaStream_t s);
+template <typename R>
+void launch_spinor_itp_couple(cx<R>* psi, const R* f, long long P, const DevScalars* sc, const SpinorNL<R>& q,
+                              cudaStream_t s);
 
 // Array-omega angular momentum, lz_kernels.cu.
 struct LzGeom {

@@ -2129,12 +2129,17 @@ gpe_status gpe_get_state_device(gpe_ctx* c, void* d, int precision) {
 gpe_status gpe_groundstate_itp(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* MU2, double* EE,
                                int cap, gpe_itp_result* res) {
   CHECK(check_ctx(c));
-  if (c->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "groundstate_itp: not available on a spinor context");
   CHECK(need_state(c));
   CHECK(need_V(c));
   if (!prm || !(prm->dt > 0) || !std::isfinite(prm->dt) || !(prm->eps > 0))
     return fail(c, GPE_ERR_INVALID, "groundstate_itp: dt and eps must be positive");
   if (cap < 0) return fail(c, GPE_ERR_INVALID, "negative cap");
+  if (c->ncomp == 2) {
+    if (c->prm.omega != 0.0) return fail(c, GPE_ERR_UNSUPPORTED, "groundstate_itp (spinor): omega != 0");
+    c->err.clear();
+    if (c->prec == GPE_FP32) return spinor_itp_impl<float>(c, prm, MU, MU2, EE, cap, res);
+    return spinor_itp_impl<double>(c, prm, MU, MU2, EE, cap, res);
+  }
   if (c->omega_field && c->prm.omega != 0.0)
     return fail(c, GPE_ERR_INVALID, "omega is either a scalar (gpe_params.omega) or an array (gpe_set_omega_field)");
   c->err.clear();

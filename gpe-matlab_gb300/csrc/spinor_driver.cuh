@@ -224,3 +224,122 @@ gpe_status spinor_observables(gpe_ctx* c, gpe_obs* o) {
   o->energy = v[1] + v[2] + 0.5 * v[3] + v[4];  // get_energy halves g (GPEtaskSpinor.m:98-110)
   return GPE_OK;
 }
+
+// GPEtaskSpinor.groundstate_itp (lib/@GPEtaskSpinor/groundstate_itp.m:1-145,
+// omega = 0) from the current state.  Per iteration: the nonlinear factors of
+// the state before the kinetic half step, the half step, the coupling rotation
+// times the factors, the half step, normalisation to Ntotal (MU = log(m)/dt),
+// and with want_mu2 / want_energy MU2 and EE of every iteration (otherwise
+// MU2 = MU and EE = MU2, as with fewer outputs there).  Every 10 iterations
+// after iswitch + 10 the host tests delta = (|EE(i)-EE(i-9)|/9 +
+// |EE(i)-EE(i-1)|)/dt < eps: then it stops if dt < eps or dt < 5e-6, or
+// divides dt by 1.5.  The arrays returned drop the last iteration (:132-141).
+template <typename R>
+gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* MU2, double* EE, int cap,
+                           gpe_itp_result* res) {
+  Field& f = c->main;
+  const long long P = c->P;
+  const int maxit = std::max(1, c->prm.itp_max_iter);
+  const bool want_mu2 = prm->want_mu2 != 0, want_e = prm->want_energy != 0;
+  double dt = prm->dt;
+  const double eps = prm->eps;
+  if (!(c->prm.Ntotal > 0)) return fail(c, GPE_ERR_INVALID, "groundstate_itp (spinor): Ntotal must be positive");
+  // f_j buffer (2P) and the per-iteration MU, MU2, EE arrays on the device
+  if (!f.aux) CU(cudaMalloc(&f.aux, (size_t)c->PS * sizeof(R)));
+  const size_t hlen = 3 * (size_t)maxit;
+  if (c->d_hist_len < hlen) {
+    cudaFree(c->d_hist);
+    c->d_hist = nullptr;
+    CU(cudaMalloc(&c->d_hist, hlen * sizeof(double)));
+    c->d_hist_len = hlen;
+  }
+  double* dMU = c->d_hist;
+  double* dMU2 = c->d_hist + maxit;
+  double* dEE = c->d_hist + 2 * (size_t)maxit;
+  CHECK(materialize<R>(c));
+  launch_reset_scalars(c->sc, c->stream);
+  CHECK(set_kinop<R>(c, f, dt, 0.0));
+  SpinorNL<R> q = spinor_nl_consts<R>(c, dt, 0.0);  // cosh / sinh(dt |c|) with the coupling phase (:45-48)
+  std::vector<AxisPass> half = axis_passes(c);
+  for (auto& ap : half) ap.half = 1;
+  auto ee_of = [&](int i, std::vector<double>& host, int lo) { return host[i - lo]; };
+  int i = 1, iswitch = 20;
+  bool converged = false;
+  std::vector<double> win;
+  for (;; ++i) {
+    {
+      Launch L(c, PC_NL_PHASE, (double)c->PS * (2 * sizeof(R) + 2 * sizeof(R)));
+      launch_spinor_itp_factors<R>((const cx<R>*)f.psi, (const R*)f.V, P, c->sc, q, (R*)f.aux, c->stream);
+    }
+    for (const auto& ap : half) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
+    {
+      Launch L(c, PC_NL_PHASE, (double)c->PS * (4 * sizeof(R) + sizeof(R)));
+      launch_spinor_itp_couple<R>((cx<R>*)f.psi, (const R*)f.aux, P, c->sc, q, c->stream);
+      launch_set_scale_one(c->sc, c->stream);
+    }
+    for (const auto& ap : half) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
+    int nb;
+    {
+      Launch L(c, PC_NORM, (double)c->PS * 2 * sizeof(R));
+      nb = launch_norm<R>((const cx<R>*)f.psi, c->PS, c->sc, c->partials, c->cap, c->stream);
+    }
+    ItpFinalArgs a{c->partials, c->cap, nb, c->weight, dt, c->prm.Ntotal, 0.0, i, dMU};
+    {
+      Launch L(c, PC_FINALIZE, 0);
+      launch_finalize_itp(a, c->sc, c->stream);  // scale = m = sqrt(Ntotal/ntot), MU(i) = log(m)/dt
+    }
+    if (want_mu2 || want_e)
+      CHECK(spinor_finalize<R>(c, f, (const R*)f.V, 3, 0.0, want_mu2 ? dMU2 + (i - 1) : nullptr, false,
+                               want_e ? dEE + (i - 1) : nullptr));
+    CU(cudaGetLastError());
+    if ((i - iswitch) > 10 && i % 10 == 0) {
+      // EE(i-9 .. i): EE = MU2 without want_energy, MU2 = MU without want_mu2
+      const double* src = want_e ? dEE : (want_mu2 ? dMU2 : dMU);
+      win.resize(10);
+      CU(cudaMemcpyAsync(win.data(), src + (i - 10), 10 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      DevScalars h;
+      CHECK(read_scalars(c, &h));  // synchronises
+      if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "groundstate_itp (spinor): non-finite norm");
+      const double e_i = ee_of(i, win, i - 9), e_i1 = ee_of(i - 1, win, i - 9), e_i9 = ee_of(i - 9, win, i - 9);
+      const double delta = (std::abs(e_i - e_i9) / 9 + std::abs(e_i - e_i1)) / dt;
+      if (delta < eps) {
+        if (dt < eps || dt < 5e-6) {
+          converged = true;
+          break;
+        }
+        dt = dt / 1.5;
+        CHECK(set_kinop<R>(c, f, dt, 0.0));
+        q = spinor_nl_consts<R>(c, dt, 0.0);
+        iswitch = i;
+      }
+    }
+    if (i >= maxit) break;  // the reference warns (:123-126)
+  }
+  DevScalars h;
+  CHECK(read_scalars(c, &h));
+  if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "groundstate_itp (spinor): non-finite norm");
+  CHECK(materialize<R>(c));  // the state times its normalisation factor
+  const int n_out = i - 1;   // MU(1:i-1) (:132-141)
+  const int k = std::min(n_out, cap);
+  std::vector<double> hm(std::max(k, 1));
+  if (k > 0) {
+    CU(cudaMemcpy(hm.data(), dMU, k * sizeof(double), cudaMemcpyDeviceToHost));
+    if (MU) std::copy(hm.begin(), hm.begin() + k, MU);
+    std::vector<double> h2(k), he(k);
+    if (want_mu2) CU(cudaMemcpy(h2.data(), dMU2, k * sizeof(double), cudaMemcpyDeviceToHost));
+    else h2 = std::vector<double>(hm.begin(), hm.begin() + k);
+    if (want_e) CU(cudaMemcpy(he.data(), dEE, k * sizeof(double), cudaMemcpyDeviceToHost));
+    else he = h2;
+    if (MU2) std::copy(h2.begin(), h2.end(), MU2);
+    if (EE) std::copy(he.begin(), he.end(), EE);
+  }
+  if (res) {
+    res->iters = n_out;
+    res->converged = converged;
+    res->fp32_iters = 0;
+    res->final_dt = dt;
+    res->last_delta = 0.0;
+  }
+  if (!converged) c->err = "groundstate_itp: Convergence not reached";
+  return GPE_OK;
+}

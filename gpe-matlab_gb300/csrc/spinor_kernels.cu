@@ -61,6 +61,42 @@ __global__ void __launch_bounds__(SP_THREADS) k_spinor_nl(cx<R>* __restrict__ ps
   }
 }
 
+// Imaginary-time step of GPEtaskSpinor.groundstate_itp (groundstate_itp.m:
+// 63-81), real dt.  First, from the state before the kinetic half step, the
+// factors f_j = exp(-(V_j + sum_k g(j,k) |s psi_k|^2) dt) (s: pending factor).
+template <typename R>
+__global__ void __launch_bounds__(SP_THREADS) k_spinor_itp_factors(const cx<R>* __restrict__ psi,
+                                                                  const R* __restrict__ V, long long P,
+                                                                  const DevScalars* sc, SpinorNL<R> q,
+                                                                  R* __restrict__ f) {
+  __shared__ R s0;
+  if (threadIdx.x == 0) s0 = (R)sc->scale;
+  if (__syncthreads_or(sc->stop != 0)) return;
+  const R s = s0, dt = q.dre;
+  for (long long i = (long long)blockIdx.x * SP_THREADS + threadIdx.x; i < P; i += (long long)gridDim.x * SP_THREADS) {
+    const R n1 = norm2(psi[i]) * s * s, n2 = norm2(psi[i + P]) * s * s;
+    f[i] = rexp(-(V[i] + q.g11 * n1 + q.g12 * n2) * dt);
+    f[i + P] = rexp(-(V[i + P] + q.g21 * n1 + q.g22 * n2) * dt);
+  }
+}
+
+// Then, after the kinetic half step, psi1 <- f1 (cosom s psi1 - sinomp s psi2),
+// psi2 <- f2 (cosom s psi2 - sinomm s psi1) (:72-73); the caller resets the
+// pending factor.
+template <typename R>
+__global__ void __launch_bounds__(SP_THREADS) k_spinor_itp_couple(cx<R>* __restrict__ psi, const R* __restrict__ f,
+                                                                 long long P, const DevScalars* sc, SpinorNL<R> q) {
+  __shared__ R s0;
+  if (threadIdx.x == 0) s0 = (R)sc->scale;
+  if (__syncthreads_or(sc->stop != 0)) return;
+  const R s = s0;
+  for (long long i = (long long)blockIdx.x * SP_THREADS + threadIdx.x; i < P; i += (long long)gridDim.x * SP_THREADS) {
+    const cx<R> p1 = rmul(psi[i], s), p2 = rmul(psi[i + P], s);
+    psi[i] = rmul(cmul(q.cosom, p1) - cmul(q.sinomp, p2), f[i]);
+    psi[i + P] = rmul(cmul(q.cosom, p2) - cmul(q.sinomm, p1), f[i + P]);
+  }
+}
+
 // Compensated per-thread sum in the context precision.
 template <typename R>
 struct KSum {
@@ -148,6 +184,14 @@ __global__ void k_finalize_spinor(const SpinorFinalArgs a, DevScalars* sc) {
   // <psi1|c psi2> + <psi2|conj(c) psi1> = 2 Re(c * sum conj(psi1) psi2)
   const double ecpl = 2.0 * (a.cre * s[7] - a.cim * s[8]) * w;
   const double quad = kin * w + ev + ecpl;
+  if (a.mode == 3) {
+    // ITP (groundstate_itp.m:90-99): MU2 = <psi|H psi>/Ntotal and EE =
+    // get_energy/Ntotal of the state times the pending factor
+    const double s = sc->scale, s2 = s * s;
+    if (a.hist) *a.hist = (s2 * quad + s2 * s2 * eint) / a.Ntotal;
+    if (a.obs) *a.obs = (s2 * quad + 0.5 * s2 * s2 * eint) / a.Ntotal;
+    return;
+  }
   if (a.mode == 2) {
     a.obs[0] = ncur;
     a.obs[1] = kin * w;
@@ -209,6 +253,17 @@ int launch_spinor_sums(const cx<R>* psi, const R* V, long long P, const DevScala
   return grid;
 }
 
+template <typename R>
+void launch_spinor_itp_factors(const cx<R>* psi, const R* V, long long P, const DevScalars* sc, const SpinorNL<R>& q,
+                               R* f, cudaStream_t s) {
+  k_spinor_itp_factors<R><<<elem_grid(P, SP_THREADS), SP_THREADS, 0, s>>>(psi, V, P, sc, q, f);
+}
+template <typename R>
+void launch_spinor_itp_couple(cx<R>* psi, const R* f, long long P, const DevScalars* sc, const SpinorNL<R>& q,
+                              cudaStream_t s) {
+  k_spinor_itp_couple<R><<<elem_grid(P, SP_THREADS), SP_THREADS, 0, s>>>(psi, f, P, sc, q);
+}
+
 void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream_t s) {
   k_finalize_spinor<<<1, FIN_T, 0, s>>>(a, sc);
 }
@@ -216,7 +271,11 @@ void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream
 #define INST_SPINOR(R)                                                                                     \
   template void launch_spinor_nl<R>(cx<R>*, const R*, long long, const DevScalars*, int, const SpinorNL<R>&, \
                                     cudaStream_t);                                                         \
-  template int launch_spinor_sums<R>(const cx<R>*, const R*, long long, const DevScalars*, double*, cudaStream_t);
+  template int launch_spinor_sums<R>(const cx<R>*, const R*, long long, const DevScalars*, double*, cudaStream_t); \
+  template void launch_spinor_itp_factors<R>(const cx<R>*, const R*, long long, const DevScalars*,                \
+                                             const SpinorNL<R>&, R*, cudaStream_t);                               \
+  template void launch_spinor_itp_couple<R>(cx<R>*, const R*, long long, const DevScalars*, const SpinorNL<R>&,   \
+                                            cudaStream_t);
 INST_SPINOR(float)
 INST_SPINOR(double)
 

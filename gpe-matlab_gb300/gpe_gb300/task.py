@@ -455,8 +455,8 @@ class GPEtaskSpinor(GPEtask):
     coupling, ``nlincpl`` its density-dependent part.  States are pairs
     [phi1, phi2].  solve_split runs GPEtaskSpinor.solve_split on the GPU
     (one context holding both components); ``Vtd`` is a callable added to
-    both potentials or a pair of callables (GPEtaskSpinor.m:23-42).  The
-    spinor's groundstate_itp is not built; omega must be 0."""
+    both potentials or a pair of callables (GPEtaskSpinor.m:23-42).
+    groundstate_itp is the spinor's own (groundstate_itp.m); omega must be 0."""
 
     def __init__(self, grid: _GridBase, trappot, device: int = 0):
         self.grid = grid
@@ -476,7 +476,7 @@ class GPEtaskSpinor(GPEtask):
         self.Vtd = None
         self.V0 = 0
         self.user_callback = None
-        self.itp_max_iter = 5000
+        self.itp_max_iter = 500000  # the spinor ITP's own cap (groundstate_itp.m:123)
         self.itp_min_iter = 50
         self.itp_adjust_stepsize = False
         self.last_itp = None
@@ -590,8 +590,39 @@ class GPEtaskSpinor(GPEtask):
         for k in range(2):
             arr[k * P:(k + 1) * P] = np.broadcast_to(np.asarray(V[k], dtype=np.float64), self.grid.shape).ravel()
 
-    def groundstate_itp(self, *args, **kwargs):
-        raise NotImplementedError("GPEtaskSpinor.groundstate_itp is not built (split-step dynamics only)")
+    def groundstate_itp(self, dt, eps, phi0=None, nargout=1, rng=None):
+        """lib/@GPEtaskSpinor/groundstate_itp.m:1-145 on the GPU.  phi0: a pair, or
+        None for the reference's random start (normalised uniform complex noise
+        per component / sqrt(2), seeded here).  Returns phi, or (phi, MU, MU2,
+        EE)[:nargout]; MU2/EE are evaluated when nargout asks for them (the
+        convergence test then uses them, as in the reference)."""
+        self._push_params()
+        self._upload_V(self.getVtotal(0))
+        if phi0 is None:
+            rng = rng or np.random.default_rng()
+            phi0 = [self.grid.normalize(rng.random(self.grid.shape) + 1j * rng.random(self.grid.shape)) / math.sqrt(2)
+                    for _ in range(2)]
+        self._upload_state(phi0)
+        prm = L.gpe_itp_params()
+        prm.dt = float(dt)
+        prm.eps = float(eps)
+        prm.want_mu2 = int(nargout >= 3)
+        prm.want_energy = int(nargout >= 4)
+        cap = int(self.itp_max_iter)
+        MU, MU2, EE = np.zeros(cap), np.zeros(cap), np.zeros(cap)
+        res = L.gpe_itp_result()
+        L.check(self._ctx, L.lib.gpe_groundstate_itp(self._ctx, C.byref(prm), L.dptr(MU), L.dptr(MU2),
+                                                     L.dptr(EE), cap, C.byref(res)))
+        if not res.converged:
+            warnings.warn("Convergence not reached")
+        self.last_itp = res
+        n = res.iters
+        phi = self._download()
+        self.init_state = phi
+        self._current_state = phi
+        self._state_on_device = "current"
+        outs = (phi, MU[:n].copy(), MU2[:n].copy(), EE[:n].copy())
+        return phi if nargout <= 1 else outs[:nargout]
 
     def observables(self, phi=None):
         """<psi|H psi> pieces of the pair (default: the current device state),

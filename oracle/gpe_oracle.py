@@ -659,6 +659,58 @@ class GPEtaskSpinor(GPEtask):
             self.g = tmp
         return res
 
+    # lib/@GPEtaskSpinor/groundstate_itp.m:1-145 (omega == 0)
+    def groundstate_itp(self, dt, eps, phi, nargout=4, max_iter=500000):
+        """Returns (phi, MU, MU2, EE); MU2/EE are filled as the reference does
+        for the given nargout (MU2 = MU when nargout < 3, EE = MU2 when
+        nargout < 4), and the returned arrays drop the last iteration (:132-141)."""
+        grid = self.grid
+        ncomp = self.g.shape[0]                                          # :20
+        VV = self.getVtotal(0)
+        coupl = self.coupling
+        g = self.g
+        phi = [np.asarray(p, dtype=np.complex128) for p in phi]
+        ekk = np.exp(-grid.kk * dt * 0.5)                                # :29
+        MU, MU2, EE = [], [], []
+        i = 1
+        iswitch = 20
+        cang = np.angle(coupl)                                           # :45-48
+        cosom = np.cosh(dt * abs(coupl))
+        sinomm = np.sinh(dt * abs(coupl)) * np.exp(-1j * cang)
+        sinomp = np.sinh(dt * abs(coupl)) * np.exp(1j * cang)
+        while True:
+            tmp2 = [VV[j] + sum(g[j, k] * np.abs(phi[k]) ** 2 for k in range(ncomp)) for j in range(ncomp)]
+            phi = [grid.ifft(ekk * grid.fft(p)) for p in phi]            # :69-70
+            t0 = np.exp(-tmp2[0] * dt) * (cosom * phi[0] - sinomp * phi[1])  # :72-73
+            t1 = np.exp(-tmp2[1] * dt) * (cosom * phi[1] - sinomm * phi[0])
+            phi = [grid.ifft(ekk * grid.fft(t)) for t in (t0, t1)]      # :80-81
+            ntot = np.real(grid.integrate(phi[0] * np.conj(phi[0]) + phi[1] * np.conj(phi[1])))
+            mu = math.sqrt(self.Ntotal / ntot)                           # :84-88
+            MU.append(math.log(mu) / dt)
+            phi = [p * mu for p in phi]
+            self.current_state = phi
+            MU2.append(np.real(self.inner(phi, self.applyham(phi))) / self.Ntotal if nargout >= 3 else MU[-1])
+            EE.append(self.get_energy(phi) / self.Ntotal if nargout >= 4 else MU2[-1])
+            if (i - iswitch) > 10 and i % 10 == 0:                       # :101-122
+                delta = (abs(EE[i - 1] - EE[i - 10]) / 9 + abs(EE[i - 1] - EE[i - 2])) / dt
+                if delta < eps:
+                    if dt < eps or dt < 5e-6:
+                        break
+                    dt = dt / 1.5
+                    ekk = np.exp(-grid.kk * dt * 0.5)
+                    cosom = np.cosh(dt * abs(coupl))
+                    sinomm = np.sinh(dt * abs(coupl)) * np.exp(-1j * cang)
+                    sinomp = np.sinh(dt * abs(coupl)) * np.exp(1j * cang)
+                    iswitch = i
+            if i >= max_iter:                                            # :123-126
+                warnings.warn("Convergence not reached")
+                break
+            i += 1
+        self.init_state = phi                                            # :143-144
+        self.current_state = phi
+        self.final_dt = dt
+        return phi, np.array(MU[:i - 1]), np.array(MU2[:i - 1]), np.array(EE[:i - 1])
+
     # lib/@GPEtaskSpinor/solve_split.m:1-119
     def solve_split(self, ddt, niter_inner, niter_outer):
         grid = self.grid

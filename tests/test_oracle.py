@@ -375,3 +375,29 @@ def test_golden_fixtures_reproduce():
         out = fn()
         for k in ref.files:
             np.testing.assert_allclose(out[k], ref[k], rtol=1e-12, atol=1e-12, err_msg=f"{name}:{k}")
+
+
+def test_spinor_itp_decoupled_matches_single_component_ground_state():
+    """GPEtaskSpinor.groundstate_itp (lib/@GPEtaskSpinor/groundstate_itp.m)
+    with coupling = 0, g = diag(g0, g0), identical traps and identical halves
+    converges to the one-component ground state of N/2 per component: the
+    harmonic g = 0 case has mu = E/N = 1 (2D, omega = 1)."""
+    g = O.Grid(6, 48, 6, 48)
+    V = lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2)
+    t = O.GPEtaskSpinor(g, [V, V])
+    t.g = np.zeros((2, 2))
+    t.Ntotal = 2.0
+    X, Y = g.mesh["x"], g.mesh["y"]
+    p0 = np.exp(-((X - 0.3) ** 2 + Y ** 2) / 3).astype(complex)
+    phi, MU, MU2, EE = t.groundstate_itp(0.01, 1e-7, [p0, p0])
+    assert EE[-1] == pytest.approx(1.0, abs=1e-6)
+    assert MU2[-1] == pytest.approx(1.0, abs=1e-6)
+    assert len(MU) == len(EE) and len(MU) > 30
+    np.testing.assert_allclose(g.integrate(np.abs(phi[0]) ** 2), 1.0, rtol=1e-12)
+    # the coupling term 2 Re(c <phi1|phi2>) of the symmetric state is c N, so
+    # E/N = 1 + c: c = -0.25 makes it the ground state (0.75), c = +0.25 the
+    # excited one (1.25), which ITP keeps from a symmetric start
+    for c in (-0.25, 0.25):
+        t.coupling = c
+        phi, MU, MU2, EE = t.groundstate_itp(0.01, 1e-7, [p0, p0])
+        assert EE[-1] == pytest.approx(1.0 + c, abs=1e-5)
