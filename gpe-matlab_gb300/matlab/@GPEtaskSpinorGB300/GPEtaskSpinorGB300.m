@@ -5,7 +5,8 @@ classdef GPEtaskSpinorGB300 < GPEtaskSpinor
     % Drop-in for GPEtaskSpinor: construct it exactly like
     % GPEtaskSpinor(grid, {V1, V2}); g (2x2), coupling, nlincpl, gamma,
     % decay_rate, Ntotal, n_recalc, Vtd, init_state/current_state ({phi1,
-    % phi2}), history and user_callback keep their meaning.  omega must be 0.
+    % phi2}), history and user_callback keep their meaning; solve_split,
+    % groundstate_itp and get_energy run on the GPU.  omega must be 0.
     % Single-precision grid axes run the step in complex FP32.
     %
     % UNVERIFIED: no MATLAB was available where this file was written; the
@@ -64,6 +65,26 @@ classdef GPEtaskSpinorGB300 < GPEtaskSpinor
             phi = task.current_state;
         end
 
+        function [phi, varargout] = groundstate_itp(task, dt, eps, phi)
+            % @GPEtaskSpinor/groundstate_itp.m semantics, executed by libgpe.
+            if nargin <= 3
+                V = task.getVtotal(0);
+                phi = cellfun(@(x) task.grid.normalize(rand(size(V{1}), 'like', V{1}) + ...
+                    1i * rand(size(V{1}), 'like', V{1})) ./ sqrt(2), cell(1, 2), 'UniformOutput', false);
+            end
+            task.gb300_push();
+            v = task.getVtotal(0);
+            gpe_mex('set_potential', task.gb300_handle, double(gather([v{1}(:); v{2}(:)])));
+            gpe_mex('set_state', task.gb300_handle, complex(gather([phi{1}(:); phi{2}(:)])));
+            [MU, MU2, EE] = gpe_mex('itp', task.gb300_handle, dt, eps, nargout >= 3, nargout >= 4);
+            phi = task.gb300_state();
+            if nargout >= 2, varargout{1} = MU; end
+            if nargout >= 3, varargout{2} = MU2; end
+            if nargout >= 4, varargout{3} = EE; end
+            task.init_state = phi;
+            task.current_state = phi;
+        end
+
         function V = gb300_vtotal(task, time)
             % getVtotal(time) of both components, stacked (called once per block).
             v = task.getVtotal(time);
@@ -97,8 +118,9 @@ classdef GPEtaskSpinorGB300 < GPEtaskSpinor
             if ~isscalar(task.omega) || task.omega ~= 0
                 error('gpe:omega', 'libgpe runs GPEtaskSpinor with omega = 0 only');
             end
+            % the spinor ITP's own iteration cap (groundstate_itp.m:123) in place of itp_max_iter
             gpe_mex('set_params', task.gb300_handle, 0, task.gamma, task.decay_rate, ...
-                task.Ntotal, task.mu_init, task.n_recalc, task.itp_max_iter, task.itp_min_iter, ...
+                task.Ntotal, task.mu_init, task.n_recalc, 500000, task.itp_min_iter, ...
                 double(task.itp_adjust_stepsize), 0);
             gpe_mex('set_spinor_params', task.gb300_handle, double(task.g), task.coupling, task.nlincpl);
             n = task.current_n;
