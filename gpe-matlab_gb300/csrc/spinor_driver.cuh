@@ -265,6 +265,7 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
   auto ee_of = [&](int i, std::vector<double>& host, int lo) { return host[i - lo]; };
   int i = 1, iswitch = 20;
   bool converged = false;
+  double last_delta = NAN;
   std::vector<double> win;
   for (;; ++i) {
     {
@@ -302,6 +303,7 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
       if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "groundstate_itp (spinor): non-finite norm");
       const double e_i = ee_of(i, win, i - 9), e_i1 = ee_of(i - 1, win, i - 9), e_i9 = ee_of(i - 9, win, i - 9);
       const double delta = (std::abs(e_i - e_i9) / 9 + std::abs(e_i - e_i1)) / dt;
+      last_delta = delta;
       if (delta < eps) {
         if (dt < eps || dt < 5e-6) {
           converged = true;
@@ -338,7 +340,7 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
     res->converged = converged;
     res->fp32_iters = 0;
     res->final_dt = dt;
-    res->last_delta = 0.0;
+    res->last_delta = last_delta;  // the last convergence test's delta (NaN: none ran)
   }
   if (!converged) c->err = "groundstate_itp: Convergence not reached";
   return GPE_OK;
