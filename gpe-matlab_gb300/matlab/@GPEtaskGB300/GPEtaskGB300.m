@@ -52,7 +52,7 @@ classdef GPEtaskGB300 < GPEtask
             task.gb300_push();
             gpe_mex('set_potential', task.gb300_handle, double(gather(task.getVtotal(0))));
             phi = task.process_init_state(phi0);
-            gpe_mex('set_state', task.gb300_handle, complex(gather(phi)));
+            task.gb300_put_state(phi);
             [MU, MU2, EE] = gpe_mex('itp', task.gb300_handle, dt, eps, nargout >= 3, nargout >= 4);
             phi = task.gb300_state();
             if nargout >= 2
@@ -87,7 +87,7 @@ classdef GPEtaskGB300 < GPEtask
             else
                 phi = task.init_state;
             end
-            gpe_mex('set_state', task.gb300_handle, complex(gather(phi)));
+            task.gb300_put_state(phi);
             timedep = isa(task.Vtd, 'function_handle') || numel(task.V0) > 1;
             if ~timedep
                 gpe_mex('set_potential', task.gb300_handle, double(gather(task.Vtrap)));
@@ -116,7 +116,7 @@ classdef GPEtaskGB300 < GPEtask
             if nargin < 8, fp64 = false; end
             task.gb300_push();
             gpe_mex('set_potential', task.gb300_handle, double(gather(task.Vtrap)));
-            gpe_mex('set_state', task.gb300_handle, complex(gather(phi0)));
+            task.gb300_put_state(phi0);
             [loss, dLdV] = gpe_mex('adjoint', task.gb300_handle, complex(double(gather(target))), ...
                 ddt, nsteps, K, budget, 2 * double(fp64));
         end
@@ -124,7 +124,7 @@ classdef GPEtaskGB300 < GPEtask
         function E = get_energy(task, phi, time)
             % GPEtask.m:97-107 on the GPU (current V).
             if nargin >= 2
-                gpe_mex('set_state', task.gb300_handle, complex(gather(phi)));
+                task.gb300_put_state(phi);
             end
             o = gpe_mex('observables', task.gb300_handle);
             E = o(6);
@@ -153,9 +153,20 @@ classdef GPEtaskGB300 < GPEtask
         end
 
         function phi = gb300_state(task)
-            phi = gpe_mex('get_state', task.gb300_handle, task.gb300_class, size(task.grid.mesh.x));
+            % gpuArray grids get a gpuArray straight from the device state
             if isa(task.grid.x, 'gpuArray')
-                phi = gpuArray(phi);
+                phi = gpe_mex('get_state_gpu', task.gb300_handle, task.gb300_class, size(task.grid.mesh.x));
+            else
+                phi = gpe_mex('get_state', task.gb300_handle, task.gb300_class, size(task.grid.mesh.x));
+            end
+        end
+
+        function gb300_put_state(task, phi)
+            % a gpuArray state is copied device to device (mxGPUArray), a host one uploaded
+            if isa(phi, 'gpuArray')
+                gpe_mex('set_state_gpu', task.gb300_handle, complex(phi));
+            else
+                gpe_mex('set_state', task.gb300_handle, complex(phi));
             end
         end
     end

@@ -29,6 +29,8 @@
 //   gpe_mex('set_spinor_params', h, g, coupling, nlincpl)
 //       spinor contexts take [phi1(:); phi2(:)] and [V1(:); V2(:)] in set_state /
 //       set_potential / getVtotal, and get_state returns them stacked the same way
+//   gpe_mex('set_state_gpu', h, psi_gpuArray)                            % device to device
+//   psi = gpe_mex('get_state_gpu', h, 'double'|'single', size)           % a new gpuArray
 //   [resp, resm] = gpe_mex('detect_core', h, z_index, refine, component)   % detect_core.m on the device
 //   mu = gpe_mex('groundstate_tf', h, eps, N[, mul, mur])                 % groundstate_tf.m on the device
 #include <string.h>
@@ -38,6 +40,7 @@
 #include <vector>
 
 #include "gpe.h"
+#include "gpu/mxGPUArray.h"
 #include "mex.h"
 
 namespace {
@@ -197,6 +200,36 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     if (!mxIsComplex(psi)) mexErrMsgIdAndTxt("gpe:arg", "psi must be complex (use complex(psi))");
     if (mxIsSingle(psi)) check(c, gpe_set_state_f32(c, reinterpret_cast<const float*>(mxGetComplexSingles(psi))));
     else check(c, gpe_set_state(c, reinterpret_cast<const double*>(mxGetComplexDoubles(psi))));
+  } else if (cmd == "set_state_gpu") {
+    // gpe_mex('set_state_gpu', h, psi): psi a complex gpuArray (single or
+    // double, interleaved on the device); copied device to device
+    mxInitGPU();
+    const mxGPUArray* g = mxGPUCreateFromMxArray(prhs[2]);
+    if (mxGPUGetComplexity(g) != mxCOMPLEX) {
+      mxGPUDestroyGPUArray(g);
+      mexErrMsgIdAndTxt("gpe:arg", "psi must be complex (use complex(psi))");
+    }
+    const int prec = mxGPUGetClassID(g) == mxSINGLE_CLASS ? GPE_FP32 : GPE_FP64;
+    const gpe_status st = gpe_set_state_device(c, mxGPUGetDataReadOnly(g), prec);
+    mxGPUDestroyGPUArray(g);
+    check(c, st);
+  } else if (cmd == "get_state_gpu") {
+    // psi = gpe_mex('get_state_gpu', h, cls, dims): the state as a new complex gpuArray
+    if (nrhs < 4) mexErrMsgIdAndTxt("gpe:usage", "get_state_gpu needs the class and the size");
+    mxInitGPU();
+    const std::string cls = str(prhs[2]);
+    const double* sz = mxGetDoubles(prhs[3]);
+    const mwSize nd = mxGetNumberOfElements(prhs[3]) > 2 ? 3 : 2;
+    mwSize dims[3] = {(mwSize)sz[0], (mwSize)sz[1], nd > 2 ? (mwSize)sz[2] : 1};
+    mxGPUArray* g = mxGPUCreateGPUArray(nd, dims, cls == "single" ? mxSINGLE_CLASS : mxDOUBLE_CLASS, mxCOMPLEX,
+                                        MX_GPU_DO_NOT_INITIALIZE);
+    const gpe_status st = gpe_get_state_device(c, mxGPUGetData(g), cls == "single" ? GPE_FP32 : GPE_FP64);
+    if (st != GPE_OK) {
+      mxGPUDestroyGPUArray(g);
+      check(c, st);
+    }
+    plhs[0] = mxGPUCreateMxArrayOnGPU(g);
+    mxGPUDestroyGPUArray(g);
   } else if (cmd == "get_state") {
     // dims come from the caller's grid: psi = gpe_mex('get_state', h, cls, size(grid.mesh.x))
     const std::string cls = nrhs > 2 ? str(prhs[2]) : "double";
