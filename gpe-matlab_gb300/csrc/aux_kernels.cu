@@ -315,7 +315,10 @@ __global__ void k_reset_scalars(DevScalars* sc) {
   sc->best_delta = INFINITY;
 }
 
-__global__ void k_set_scale_one(DevScalars* sc) { sc->scale = 1.0; }
+__global__ void k_set_scale_one(DevScalars* sc) {
+  sc->scale = 1.0;
+  sc->scale2 = 1.0;
+}
 
 void launch_finalize_block(const BlockFinalArgs& a, DevScalars* sc, cudaStream_t s) {
   int longest = a.nblk_epi;

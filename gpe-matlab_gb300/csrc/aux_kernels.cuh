@@ -95,12 +95,26 @@ int launch_spinor_sums(const cx<R>* psi, const R* V, long long P, const DevScala
 void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream_t s);
 // Spinor ITP: the factors exp(-(V_j + sum_k g(j,k) |psi_k|^2) dt) into f (2P)
 // and, after the kinetic half step, the coupling rotation times them.
+// `split`: component 2 carries its own pending factor scale2 (two-component ITP).
 template <typename R>
 void launch_spinor_itp_factors(const cx<R>* psi, const R* V, long long P, const DevScalars* sc, const SpinorNL<R>& q,
-                               R* f, cudaStream_t s);
+                               R* f, int split, cudaStream_t s);
 template <typename R>
 void launch_spinor_itp_couple(cx<R>* psi, const R* f, long long P, const DevScalars* sc, const SpinorNL<R>& q,
-                              cudaStream_t s);
+                              int split, cudaStream_t s);
+// Incoherent two-component ITP (GPEtask2comp): per-component norms and factors.
+struct MixFinalArgs {
+  const double* part1;          // per-CTA sums of |psi_1|^2
+  const double* part2;          // per-CTA sums of |psi_2|^2
+  int nblk1, nblk2;
+  double weight, dt, N1, N2;
+  int iter;                     // 1-based iteration index
+  double* MU1;
+  double* MU2;
+};
+template <typename R>
+void launch_mix_apply_scales(cx<R>* psi, long long P, const DevScalars* sc, cudaStream_t s);
+void launch_finalize_mix(const MixFinalArgs& a, DevScalars* sc, cudaStream_t s);
 
 // Array-omega angular momentum, lz_kernels.cu.
 struct LzGeom {

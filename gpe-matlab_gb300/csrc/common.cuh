@@ -215,6 +215,7 @@ struct DevScalars {
   double dtmin;       // groundstate_itp.m:35,63-65
   double sums[8];     // last finalized sums (see Slot), weighted by the cell volume
   double energy;      // get_energy of the state at the last block end (solve_split)
+  double scale2;      // two-component ITP: pending factor of component 2 (scale: component 1)
   int stop;           // nonzero: pass kernels and finalizers do nothing
   int iter;           // ITP iterations completed
   int stall;          // ITP checks in a row without a 10% residual drop

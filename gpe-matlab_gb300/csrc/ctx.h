@@ -33,6 +33,7 @@ struct Field {
   double rotw_omega = 0.0;                       // omega the rotw arrays hold
   void* kks[3] = {nullptr, nullptr, nullptr};    // per axis: permuted k^2/2, N real (energy cut-off)
   void* php2[3] = {nullptr, nullptr, nullptr};   // spinor, array omega: the kinetic factors of half a step
+  void* php2b[3] = {nullptr, nullptr, nullptr};  // two-component ITP with M2 != M1: component 2's half-step factors
   void* cn[2] = {nullptr, nullptr};              // array omega: Crank-Nicolson iterates (P complex each)
 };
 

@@ -134,7 +134,8 @@ struct AxisPass {
   int rot = 0;  // rotating frame: 1 = x pass with exp(+kx y omega dt/2), 2 = y pass with exp(-ky x omega dt)
   int split = SPLIT_FULL;  // energy cut-off chain: forward half only, inverse half only, or the masked pass
   double ecut = 0.0;
-  int half = 0;  // spinor contexts: the half-step kinetic factors exp(-k^2/2 dt/2)
+  int half = 0;  // spinor contexts: the half-step kinetic factors exp(-k^2/2 dt/2); 2: component 2's (php2b)
+  int one_comp = 0;  // the pencils of one component only (psi_buf points at it)
 };
 
 // Pass order: y (contiguous, carries the prologue), x, then z (3D).  The
@@ -149,8 +150,8 @@ struct AxisPass {
 // Spinor contexts: the components lie one after the other, so the pencils of
 // every component are one batch (pencil index b = pencil + component * count;
 // for z pencils outer = P steps to the next component).
-std::vector<AxisPass> axis_passes(const gpe_ctx* c, double ecut = 0.0) {
-  const long long nx = c->n[0], ny = c->n[1], nz = c->ndims == 3 ? c->n[2] : 1, nc = c->ncomp;
+std::vector<AxisPass> axis_passes(const gpe_ctx* c, double ecut = 0.0, bool one_comp = false) {
+  const long long nx = c->n[0], ny = c->n[1], nz = c->ndims == 3 ? c->n[2] : 1, nc = one_comp ? 1 : c->ncomp;
   const AxisPass py{1, (int)ny, false, nx * nz * nc, 1, 1, 0};
   const AxisPass px{0, (int)nx, true, ny * nz * nc, ny, ny, nx * ny};
   const AxisPass pz{2, (int)nz, true, nx * ny * nc, nx * ny, nx * ny, c->P};
@@ -184,6 +185,7 @@ std::vector<AxisPass> axis_passes(const gpe_ctx* c, double ecut = 0.0) {
   v.push_back(py);
   v.push_back(px);
   if (c->ndims == 3) v.push_back(pz);
+  for (auto& ap : v) ap.one_comp = one_comp;
   return v;
 }
 
@@ -512,6 +514,24 @@ gpe_status build_static_tables(gpe_ctx* c, Field& f) {
 // k^2 part stays in the per-axis table; the cross term, which depends on the
 // pencil's transverse coordinate, is a second table rot[ax][i][slot] =
 // exp(+kx y(i) omega dt/2) (x) or exp(-ky x(i) omega dt) (y).
+// exp(-k^2/4 dt)/N of axis ax in slot order (the per-axis factor of
+// exp(-kk dt/2)), dt = dre + i dim, into dst (allocated on first use).
+template <typename R>
+gpe_status half_table(gpe_ctx* c, const Field& f, int ax, double dre, double dim, void*& dst) {
+  const int N = c->n[ax];
+  const PlanInfo pi = dispatch_plan(N, f.plan_var[ax]);
+  std::vector<std::complex<double>> ph(N);
+  for (int t = 0; t < pi.T; ++t)
+    for (int m = 0; m < pi.E; ++m) {
+      const double k = kval(c, ax, plan_spec_pos(pi, t, m));
+      const double kk = k * k / 4.0;
+      const double mag = std::exp(-kk * dre) / N;
+      ph[slot_index<R>(pi.T, t, m)] = std::complex<double>(mag * std::cos(kk * dim), -mag * std::sin(kk * dim));
+    }
+  if (!dst) CU(cudaMalloc(&dst, N * 2 * sizeof(R)));
+  return upload_cx<R>(c, dst, ph);
+}
+
 template <typename R>
 gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
   if (f.phase_valid && f.phase_dt[0] == dre && f.phase_dt[1] == dim) return GPE_OK;
@@ -530,20 +550,10 @@ gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
             std::complex<double>(mag * std::cos(kk * dim * h), -mag * std::sin(kk * dim * h));
       }
     CHECK(upload_cx<R>(c, f.php[ax], ph));
-    if (c->ncomp == 2 || c->omega_field) {
-      // GPEtaskSpinor/solve_split.m:44-45: ekkp = exp(-kk dt/2) at block starts;
-      // set_kinop.m:3-4 for array omega: kinop = exp(-kk dt/2)
-      // the last step's ekk times ekkm = exp(+kk dt/2) is exp(-kk dt/2) too
-      for (int t = 0; t < pi.T; ++t)
-        for (int m = 0; m < pi.E; ++m) {
-          const double k = kval(c, ax, plan_spec_pos(pi, t, m));
-          const double kk = k * k / 4.0;
-          const double mag = std::exp(-kk * dre) / N;
-          ph[slot_index<R>(pi.T, t, m)] = std::complex<double>(mag * std::cos(kk * dim), -mag * std::sin(kk * dim));
-        }
-      if (!f.php2[ax]) CU(cudaMalloc(&f.php2[ax], N * 2 * sizeof(R)));
-      CHECK(upload_cx<R>(c, f.php2[ax], ph));
-    }
+    // GPEtaskSpinor/solve_split.m:44-45: ekkp = exp(-kk dt/2) at block starts;
+    // set_kinop.m:3-4 for array omega: kinop = exp(-kk dt/2)
+    // the last step's ekk times ekkm = exp(+kk dt/2) is exp(-kk dt/2) too
+    if (c->ncomp == 2 || c->omega_field) CHECK(half_table<R>(c, f, ax, dre, dim, f.php2[ax]));
     if (om != 0.0 && ax < 2) {
       const int tax = ax == 0 ? 1 : 0;  // transverse axis of the pencils
       const int nt = c->n[tax];
@@ -601,6 +611,7 @@ void free_field(Field& f, const double* V64) {
     cudaFree(f.kp[i]);
     cudaFree(f.kks[i]);
     cudaFree(f.php2[i]);
+    cudaFree(f.php2b[i]);
   }
   for (int i = 0; i < 2; ++i) cudaFree(f.cn[i]);
   for (int i = 0; i < 2; ++i) {
@@ -641,7 +652,7 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.psi = (cx<R>*)(psi_buf ? psi_buf : f.psi);  // psi_buf: another array of the grid's shape
   a.V = (const R*)f.V;
   a.aux = (R*)f.aux;
-  a.php = (const cx<R>*)(ap.half ? f.php2[ap.axis] : f.php[ap.axis]);
+  a.php = (const cx<R>*)(ap.half == 2 ? f.php2b[ap.axis] : ap.half ? f.php2[ap.axis] : f.php[ap.axis]);
   if (!a.php) return fail(c, GPE_ERR_STATE, "kinetic factors not set");
   a.tws = (const cx<R>*)f.tws[ap.axis];
   a.k2p = (const R*)f.k2p[ap.axis];
@@ -688,7 +699,7 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
     a.mask_pa = c->n[1];
     a.ecut = (R)ap.ecut;
   }
-  const double P = (double)c->PS;  // points of every component the pass covers
+  const double P = (double)(ap.one_comp ? c->P : c->PS);  // points the pass covers
   double bytes = (kind == KIND_ENERGY ? 1.0 : 2.0) * P * 2 * sizeof(R);
   const bool useV = pro == PRO_RT_HALF || pro == PRO_RT_FULL || pro == PRO_ITP || epi == EPI_RT_END ||
                     (kind == KIND_ENERGY && energy_pot);
@@ -1861,6 +1872,7 @@ static gpe_status create_impl(const gpe_grid_desc* d, gpe_ctx** out, int ncomp) 
   DevScalars z;
   memset(&z, 0, sizeof(z));
   z.scale = 1.0;
+  z.scale2 = 1.0;
   z.best_delta = INFINITY;
   cudaMemcpy(c->sc, &z, sizeof(z), cudaMemcpyHostToDevice);
   if (c->prec == GPE_FP32) st = alloc_field<float>(c, c->main, GPE_FP32, false);
@@ -2146,6 +2158,22 @@ gpe_status gpe_groundstate_itp(gpe_ctx* c, const gpe_itp_params* prm, double* MU
   CHECK(maybe_autotune(c));
   if (c->prec == GPE_FP32) return itp_impl<float>(c, prm, MU, MU2, EE, cap, res);
   return itp_impl<double>(c, prm, MU, MU2, EE, cap, res);
+}
+
+gpe_status gpe_groundstate_itp_2comp(gpe_ctx* c, const gpe_itp_params* prm, double N1, double N2, double M1,
+                                     double M2, double* MU1, double* MU2, double* EE, int cap,
+                                     gpe_itp_result* res) {
+  CHECK(check_ctx(c));
+  if (c->ncomp != 2) return fail(c, GPE_ERR_UNSUPPORTED, "groundstate_itp (2comp): needs a two-component context");
+  CHECK(need_state(c));
+  CHECK(need_V(c));
+  if (!prm || !(prm->dt > 0) || !std::isfinite(prm->dt) || !(prm->eps > 0))
+    return fail(c, GPE_ERR_INVALID, "groundstate_itp: dt and eps must be positive");
+  if (cap < 0) return fail(c, GPE_ERR_INVALID, "negative cap");
+  if (c->prm.omega != 0.0) return fail(c, GPE_ERR_UNSUPPORTED, "groundstate_itp (2comp): omega != 0");
+  c->err.clear();
+  if (c->prec == GPE_FP32) return mix_itp_impl<float>(c, prm, N1, N2, M1, M2, MU1, MU2, EE, cap, res);
+  return mix_itp_impl<double>(c, prm, N1, N2, M1, M2, MU1, MU2, EE, cap, res);
 }
 
 gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {

@@ -270,12 +270,12 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
   for (;; ++i) {
     {
       Launch L(c, PC_NL_PHASE, (double)c->PS * (2 * sizeof(R) + 2 * sizeof(R)));
-      launch_spinor_itp_factors<R>((const cx<R>*)f.psi, (const R*)f.V, P, c->sc, q, (R*)f.aux, c->stream);
+      launch_spinor_itp_factors<R>((const cx<R>*)f.psi, (const R*)f.V, P, c->sc, q, (R*)f.aux, 0, c->stream);
     }
     for (const auto& ap : half) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
     {
       Launch L(c, PC_NL_PHASE, (double)c->PS * (4 * sizeof(R) + sizeof(R)));
-      launch_spinor_itp_couple<R>((cx<R>*)f.psi, (const R*)f.aux, P, c->sc, q, c->stream);
+      launch_spinor_itp_couple<R>((cx<R>*)f.psi, (const R*)f.aux, P, c->sc, q, 0, c->stream);
       launch_set_scale_one(c->sc, c->stream);
     }
     for (const auto& ap : half) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
@@ -341,6 +341,166 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
     res->fp32_iters = 0;
     res->final_dt = dt;
     res->last_delta = last_delta;  // the last convergence test's delta (NaN: none ran)
+  }
+  if (!converged) c->err = "groundstate_itp: Convergence not reached";
+  return GPE_OK;
+}
+
+// GPEtask2comp.groundstate_itp (lib/@GPEtask2comp/groundstate_itp.m:1-157,
+// omega = 0) from the current state of a spinor context, coupling = 0.  Per
+// iteration: the factors exp(-(V_j + sum_k g(j,k)|psi_k|^2) dt) from the state
+// before the step (:58-59), the kinetic half step with each component's own
+// exp(-kk dt/2/M_j) (:67-68; one launch over both components when M1 == M2),
+// the factors, the kinetic half step again (:78-79), the two norms and the
+// finalizer (m_j = sqrt(N_j/n_j) kept pending per component, MU1(i), MU2(i),
+// :82-90).  With want_energy the factors are applied at once and EE(i) =
+// get_energy/Ntotal (:98-99); the convergence test of :113-135 runs on EE
+// (MU2 without want_energy, :101).
+template <typename R>
+gpe_status mix_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double N1, double N2, double M1, double M2,
+                        double* MU1, double* MU2, double* EE, int cap, gpe_itp_result* res) {
+  Field& f = c->main;
+  const long long P = c->P;
+  const int maxit = std::max(1, c->prm.itp_max_iter);
+  const bool want_e = prm->want_energy != 0;
+  double dt = prm->dt;
+  const double eps = prm->eps;
+  if (!(N1 > 0) || !(N2 > 0)) return fail(c, GPE_ERR_INVALID, "groundstate_itp (2comp): N1 and N2 must be positive");
+  if (!(M1 > 0) || !(M2 > 0)) return fail(c, GPE_ERR_INVALID, "groundstate_itp (2comp): M1 and M2 must be positive");
+  if (want_e && !(c->prm.Ntotal > 0))
+    return fail(c, GPE_ERR_INVALID, "groundstate_itp (2comp): EE divides by Ntotal, which must be positive");
+  if (c->spin.coupling_re != 0.0 || c->spin.coupling_im != 0.0 || c->spin.nlincpl != 0.0)
+    return fail(c, GPE_ERR_INVALID, "groundstate_itp (2comp): an incoherent mixture has coupling = nlincpl = 0");
+  if (!f.aux) CU(cudaMalloc(&f.aux, (size_t)c->PS * sizeof(R)));
+  const size_t hlen = 3 * (size_t)maxit;
+  if (c->d_hist_len < hlen) {
+    cudaFree(c->d_hist);
+    c->d_hist = nullptr;
+    CU(cudaMalloc(&c->d_hist, hlen * sizeof(double)));
+    c->d_hist_len = hlen;
+  }
+  double* dMU1 = c->d_hist;
+  double* dMU2 = c->d_hist + maxit;
+  double* dEE = c->d_hist + 2 * (size_t)maxit;
+  CHECK(materialize<R>(c));  // also resets scale2
+  launch_reset_scalars(c->sc, c->stream);
+  const bool same_mass = M1 == M2;
+  auto set_tables = [&](double h) -> gpe_status {
+    CHECK(set_kinop<R>(c, f, h / M1, 0.0));  // php2 = exp(-kk h/2/M1)
+    if (!same_mass)
+      for (int ax = 0; ax < c->ndims; ++ax) CHECK(half_table<R>(c, f, ax, h / M2, 0.0, f.php2b[ax]));
+    return GPE_OK;
+  };
+  CHECK(set_tables(dt));
+  SpinorNL<R> q = spinor_nl_consts<R>(c, dt, 0.0);  // coupling 0: cosom = 1, sinomm = sinomp = 0
+  std::vector<AxisPass> both = axis_passes(c), one = axis_passes(c, 0.0, true), two = one;
+  for (auto& ap : both) ap.half = 1;
+  for (auto& ap : one) ap.half = 1;
+  for (auto& ap : two) ap.half = 2;
+  cx<R>* psi2 = (cx<R>*)f.psi + P;
+  auto kinetic = [&]() -> gpe_status {
+    if (same_mass) {
+      for (const auto& ap : both) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
+      return GPE_OK;
+    }
+    for (const auto& ap : one) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr, f.psi));
+    for (const auto& ap : two) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr, psi2));
+    return GPE_OK;
+  };
+  int i = 1, iswitch = 20;
+  bool converged = false, pending = false;
+  double last_delta = NAN;
+  std::vector<double> win(10);
+  for (;; ++i) {
+    {
+      Launch L(c, PC_NL_PHASE, (double)c->PS * (2 * sizeof(R) + 2 * sizeof(R)));
+      launch_spinor_itp_factors<R>((const cx<R>*)f.psi, (const R*)f.V, P, c->sc, q, (R*)f.aux, 1, c->stream);
+    }
+    CHECK(kinetic());
+    {
+      Launch L(c, PC_NL_PHASE, (double)c->PS * (4 * sizeof(R) + sizeof(R)));
+      launch_spinor_itp_couple<R>((cx<R>*)f.psi, (const R*)f.aux, P, c->sc, q, 1, c->stream);
+      launch_set_scale_one(c->sc, c->stream);
+    }
+    CHECK(kinetic());
+    MixFinalArgs a{};
+    {
+      Launch L(c, PC_NORM, (double)c->PS * 2 * sizeof(R));
+      a.nblk1 = launch_norm<R>((const cx<R>*)f.psi, P, c->sc, c->partials, c->cap, c->stream);
+      a.nblk2 = launch_norm<R>(psi2, P, c->sc, c->partials + c->cap, c->cap, c->stream);
+    }
+    a.part1 = c->partials + (size_t)S_N * c->cap;
+    a.part2 = c->partials + (size_t)(S_N + 1) * c->cap;
+    a.weight = c->weight;
+    a.dt = dt;
+    a.N1 = N1;
+    a.N2 = N2;
+    a.iter = i;
+    a.MU1 = dMU1;
+    a.MU2 = dMU2;
+    {
+      Launch L(c, PC_FINALIZE, 0);
+      launch_finalize_mix(a, c->sc, c->stream);
+    }
+    pending = true;
+    if (want_e) {
+      {
+        Launch L(c, PC_ELEMENTWISE, (double)c->PS * 4 * sizeof(R));
+        launch_mix_apply_scales<R>((cx<R>*)f.psi, P, c->sc, c->stream);
+        launch_set_scale_one(c->sc, c->stream);
+      }
+      pending = false;
+      CHECK(spinor_finalize<R>(c, f, (const R*)f.V, 3, 0.0, nullptr, false, dEE + (i - 1)));
+    }
+    CU(cudaGetLastError());
+    if ((i - iswitch) > 10 && i % 10 == 0) {
+      const double* src = want_e ? dEE : dMU2;
+      CU(cudaMemcpyAsync(win.data(), src + (i - 10), 10 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      DevScalars h;
+      CHECK(read_scalars(c, &h));  // synchronises
+      if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "groundstate_itp (2comp): non-finite norm");
+      // win[k] = EE(i-9+k): EE(i) = win[9], EE(i-1) = win[8], EE(i-9) = win[0]
+      const double delta = (std::abs(win[9] - win[0]) / 9 + std::abs(win[9] - win[8])) / dt;
+      last_delta = delta;
+      if (delta < eps) {
+        if (dt < eps || dt < 5e-6) {
+          converged = true;
+          break;
+        }
+        dt = dt / 1.5;
+        CHECK(set_tables(dt));
+        q = spinor_nl_consts<R>(c, dt, 0.0);
+        iswitch = i;
+      }
+    }
+    if (i >= maxit) break;  // the reference warns (:136-139)
+  }
+  if (pending) {
+    Launch L(c, PC_ELEMENTWISE, (double)c->PS * 4 * sizeof(R));
+    launch_mix_apply_scales<R>((cx<R>*)f.psi, P, c->sc, c->stream);
+    launch_set_scale_one(c->sc, c->stream);
+  }
+  DevScalars h;
+  CHECK(read_scalars(c, &h));
+  if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "groundstate_itp (2comp): non-finite norm");
+  const int n_out = i - 1;  // MU1(1:i-1) (:143-154)
+  const int k = std::min(n_out, cap);
+  if (k > 0) {
+    std::vector<double> h1(k), h2(k), he(k);
+    CU(cudaMemcpy(h1.data(), dMU1, k * sizeof(double), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(h2.data(), dMU2, k * sizeof(double), cudaMemcpyDeviceToHost));
+    if (want_e) CU(cudaMemcpy(he.data(), dEE, k * sizeof(double), cudaMemcpyDeviceToHost));
+    else he = h2;
+    if (MU1) std::copy(h1.begin(), h1.end(), MU1);
+    if (MU2) std::copy(h2.begin(), h2.end(), MU2);
+    if (EE) std::copy(he.begin(), he.end(), EE);
+  }
+  if (res) {
+    res->iters = n_out;
+    res->converged = converged;
+    res->fp32_iters = 0;
+    res->final_dt = dt;
+    res->last_delta = last_delta;
   }
   if (!converged) c->err = "groundstate_itp: Convergence not reached";
   return GPE_OK;

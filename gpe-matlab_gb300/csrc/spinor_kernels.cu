@@ -63,18 +63,23 @@ __global__ void __launch_bounds__(SP_THREADS) k_spinor_nl(cx<R>* __restrict__ ps
 
 // Imaginary-time step of GPEtaskSpinor.groundstate_itp (groundstate_itp.m:
 // 63-81), real dt.  First, from the state before the kinetic half step, the
-// factors f_j = exp(-(V_j + sum_k g(j,k) |s psi_k|^2) dt) (s: pending factor).
+// factors f_j = exp(-(V_j + sum_k g(j,k) |s_k psi_k|^2) dt) (s_k: pending
+// factors; `split`: the two-component ITP keeps one per component, scale and
+// scale2, GPEtask2comp/groundstate_itp.m:58-59, otherwise both are scale).
 template <typename R>
 __global__ void __launch_bounds__(SP_THREADS) k_spinor_itp_factors(const cx<R>* __restrict__ psi,
                                                                   const R* __restrict__ V, long long P,
                                                                   const DevScalars* sc, SpinorNL<R> q,
-                                                                  R* __restrict__ f) {
-  __shared__ R s0;
-  if (threadIdx.x == 0) s0 = (R)sc->scale;
+                                                                  R* __restrict__ f, int split) {
+  __shared__ R s0[2];
+  if (threadIdx.x == 0) {
+    s0[0] = (R)sc->scale;
+    s0[1] = (R)(split ? sc->scale2 : sc->scale);
+  }
   if (__syncthreads_or(sc->stop != 0)) return;
-  const R s = s0, dt = q.dre;
+  const R sa = s0[0], sb = s0[1], dt = q.dre;
   for (long long i = (long long)blockIdx.x * SP_THREADS + threadIdx.x; i < P; i += (long long)gridDim.x * SP_THREADS) {
-    const R n1 = norm2(psi[i]) * s * s, n2 = norm2(psi[i + P]) * s * s;
+    const R n1 = norm2(psi[i]) * sa * sa, n2 = norm2(psi[i + P]) * sb * sb;
     f[i] = rexp(-(V[i] + q.g11 * n1 + q.g12 * n2) * dt);
     f[i + P] = rexp(-(V[i + P] + q.g21 * n1 + q.g22 * n2) * dt);
   }
@@ -85,15 +90,37 @@ __global__ void __launch_bounds__(SP_THREADS) k_spinor_itp_factors(const cx<R>* 
 // pending factor.
 template <typename R>
 __global__ void __launch_bounds__(SP_THREADS) k_spinor_itp_couple(cx<R>* __restrict__ psi, const R* __restrict__ f,
-                                                                 long long P, const DevScalars* sc, SpinorNL<R> q) {
-  __shared__ R s0;
-  if (threadIdx.x == 0) s0 = (R)sc->scale;
+                                                                 long long P, const DevScalars* sc, SpinorNL<R> q,
+                                                                 int split) {
+  __shared__ R s0[2];
+  if (threadIdx.x == 0) {
+    s0[0] = (R)sc->scale;
+    s0[1] = (R)(split ? sc->scale2 : sc->scale);
+  }
   if (__syncthreads_or(sc->stop != 0)) return;
-  const R s = s0;
+  const R sa = s0[0], sb = s0[1];
   for (long long i = (long long)blockIdx.x * SP_THREADS + threadIdx.x; i < P; i += (long long)gridDim.x * SP_THREADS) {
-    const cx<R> p1 = rmul(psi[i], s), p2 = rmul(psi[i + P], s);
+    const cx<R> p1 = rmul(psi[i], sa), p2 = rmul(psi[i + P], sb);
     psi[i] = rmul(cmul(q.cosom, p1) - cmul(q.sinomp, p2), f[i]);
     psi[i + P] = rmul(cmul(q.cosom, p2) - cmul(q.sinomm, p1), f[i + P]);
+  }
+}
+
+// The pending factors of the two-component ITP applied to the stored state
+// (component 1 times scale, component 2 times scale2); the caller resets them.
+template <typename R>
+__global__ void __launch_bounds__(SP_THREADS) k_mix_apply_scales(cx<R>* __restrict__ psi, long long P,
+                                                                const DevScalars* sc) {
+  __shared__ R s0[2];
+  if (threadIdx.x == 0) {
+    s0[0] = (R)sc->scale;
+    s0[1] = (R)sc->scale2;
+  }
+  __syncthreads();
+  const R sa = s0[0], sb = s0[1];
+  for (long long i = (long long)blockIdx.x * SP_THREADS + threadIdx.x; i < P; i += (long long)gridDim.x * SP_THREADS) {
+    psi[i] = rmul(psi[i], sa);
+    psi[i + P] = rmul(psi[i + P], sb);
   }
 }
 
@@ -239,6 +266,30 @@ __global__ void k_finalize_spinor(const SpinorFinalArgs a, DevScalars* sc) {
   }
 }
 
+// GPEtask2comp/groundstate_itp.m:82-90: n_j = integrate(|psi_j|^2) from the
+// per-CTA partials of each component, m_j = sqrt(N_j/n_j) kept pending as
+// scale / scale2, MU1(i) = log(m1)/dt, MU2(i) = log(m2)/dt.
+__global__ void k_finalize_mix(const MixFinalArgs a, DevScalars* sc) {
+  if (sc->stop) return;
+  __shared__ double sh[FIN_T];
+  const double n1 = cta_sum_fixed(a.part1, a.nblk1, sh) * a.weight;
+  const double n2 = cta_sum_fixed(a.part2, a.nblk2, sh) * a.weight;
+  if (threadIdx.x != 0) return;
+  const double m1 = sqrt(a.N1 / n1), m2 = sqrt(a.N2 / n2);
+  sc->scale = m1;
+  sc->scale2 = m2;
+  sc->ncur = n1 + n2;
+  sc->iter = a.iter;
+  sc->mu_itp = log(m1) / a.dt;
+  a.MU1[a.iter - 1] = log(m1) / a.dt;
+  a.MU2[a.iter - 1] = log(m2) / a.dt;
+  if (!isfinite(n1) || !isfinite(n2) || !isfinite(m1) || !isfinite(m2) || !(n1 > 0.0) || !(n2 > 0.0)) {
+    sc->nonfinite = 1;
+    sc->status = NONFINITE;
+    sc->stop = 1;
+  }
+}
+
 template <typename R>
 void launch_spinor_nl(cx<R>* psi, const R* V, long long P, const DevScalars* sc, int first, const SpinorNL<R>& q,
                       cudaStream_t s) {
@@ -255,13 +306,20 @@ int launch_spinor_sums(const cx<R>* psi, const R* V, long long P, const DevScala
 
 template <typename R>
 void launch_spinor_itp_factors(const cx<R>* psi, const R* V, long long P, const DevScalars* sc, const SpinorNL<R>& q,
-                               R* f, cudaStream_t s) {
-  k_spinor_itp_factors<R><<<elem_grid(P, SP_THREADS), SP_THREADS, 0, s>>>(psi, V, P, sc, q, f);
+                               R* f, int split, cudaStream_t s) {
+  k_spinor_itp_factors<R><<<elem_grid(P, SP_THREADS), SP_THREADS, 0, s>>>(psi, V, P, sc, q, f, split);
 }
 template <typename R>
 void launch_spinor_itp_couple(cx<R>* psi, const R* f, long long P, const DevScalars* sc, const SpinorNL<R>& q,
-                              cudaStream_t s) {
-  k_spinor_itp_couple<R><<<elem_grid(P, SP_THREADS), SP_THREADS, 0, s>>>(psi, f, P, sc, q);
+                              int split, cudaStream_t s) {
+  k_spinor_itp_couple<R><<<elem_grid(P, SP_THREADS), SP_THREADS, 0, s>>>(psi, f, P, sc, q, split);
+}
+template <typename R>
+void launch_mix_apply_scales(cx<R>* psi, long long P, const DevScalars* sc, cudaStream_t s) {
+  k_mix_apply_scales<R><<<elem_grid(P, SP_THREADS), SP_THREADS, 0, s>>>(psi, P, sc);
+}
+void launch_finalize_mix(const MixFinalArgs& a, DevScalars* sc, cudaStream_t s) {
+  k_finalize_mix<<<1, FIN_T, 0, s>>>(a, sc);
 }
 
 void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream_t s) {
@@ -273,9 +331,10 @@ void launch_finalize_spinor(const SpinorFinalArgs& a, DevScalars* sc, cudaStream
                                     cudaStream_t);                                                         \
   template int launch_spinor_sums<R>(const cx<R>*, const R*, long long, const DevScalars*, double*, cudaStream_t); \
   template void launch_spinor_itp_factors<R>(const cx<R>*, const R*, long long, const DevScalars*,                \
-                                             const SpinorNL<R>&, R*, cudaStream_t);                               \
+                                             const SpinorNL<R>&, R*, int, cudaStream_t);                          \
   template void launch_spinor_itp_couple<R>(cx<R>*, const R*, long long, const DevScalars*, const SpinorNL<R>&,   \
-                                            cudaStream_t);
+                                            int, cudaStream_t);                                                   \
+  template void launch_mix_apply_scales<R>(cx<R>*, long long, const DevScalars*, cudaStream_t);
 INST_SPINOR(float)
 INST_SPINOR(double)
 

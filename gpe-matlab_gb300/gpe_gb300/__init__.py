@@ -13,7 +13,7 @@ Host mirror of the reference's MATLAB class API over libgpe.so:
 from ._lib import GPEError, lib  # noqa: F401  (loads libgpe.so or raises)
 from .grid import grid2d, grid3d  # noqa: F401
 from .imprint import imprint_vortex, imprint_vortex_ring  # noqa: F401
-from .task import GPEtask, GPEtaskSpinor, SGPEtask, detect_core, noise_variates, solve_split_batch  # noqa: F401
+from .task import GPEtask, GPEtask2comp, GPEtaskSpinor, SGPEtask, detect_core, noise_variates, solve_split_batch  # noqa: F401
 
 
 def device_available() -> bool:

@@ -114,6 +114,8 @@ PROTOTYPES = {
     "gpe_get_state_device": (C.c_int, [_P, _P, C.c_int]),
     "gpe_groundstate_itp": (C.c_int, [_P, C.POINTER(gpe_itp_params), _D, _D, _D, C.c_int,
                                       C.POINTER(gpe_itp_result)]),
+    "gpe_groundstate_itp_2comp": (C.c_int, [_P, C.POINTER(gpe_itp_params), C.c_double, C.c_double, C.c_double,
+                                            C.c_double, _D, _D, _D, C.c_int, C.POINTER(gpe_itp_result)]),
     "gpe_solve_split": (C.c_int, [_P, C.POINTER(gpe_split_params)]),
     "gpe_solve_split_batch": (C.c_int, [C.POINTER(_P), C.c_int, C.POINTER(gpe_split_params)]),
     "gpe_adjoint_grad": (C.c_int, [_P, C.POINTER(gpe_adjoint_params), _D, _D, _D]),

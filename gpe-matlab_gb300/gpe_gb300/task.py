@@ -641,6 +641,60 @@ class GPEtaskSpinor(GPEtask):
         return self.observables(phi if phi is not None else self.current_state)["energy"]
 
 
+class GPEtask2comp(GPEtaskSpinor):
+    """GPEtask2comp(grid, {V1, V2}) (lib/@GPEtask2comp/GPEtask2comp.m:1-150): an
+    incoherent two-component mixture.  ``g`` is a 2x2 matrix, ``N1``/``N2`` the
+    particle numbers and ``M1``/``M2`` the masses of the components.
+    groundstate_itp is the class's own (groundstate_itp.m: each component with
+    its own kinetic factor exp(-kk dt/2/M_j) and its own normalisation N_j);
+    solve_split, get_energy and observables are GPEtaskSpinor's with coupling =
+    nlincpl = 0, which is what @GPEtask2comp/solve_split.m and
+    GPEtask2comp.m:41-118 compute (that class declares no coupling)."""
+
+    def __init__(self, grid: _GridBase, trappot, device: int = 0):
+        super().__init__(grid, trappot, device)
+        self.N1 = 0.0
+        self.N2 = 0.0
+        self.M1 = 1.0
+        self.M2 = 1.0
+
+    def groundstate_itp(self, dt, eps, phi0=None, nargout=1, rng=None):
+        """lib/@GPEtask2comp/groundstate_itp.m:1-157 on the GPU (omega = 0).
+        phi0: a pair, or None for the reference's random start.  Returns phi,
+        or (phi, MU1, MU2, EE)[:nargout]: MU_j(i) = log(sqrt(N_j/n_j))/dt of
+        each component; EE = get_energy/Ntotal when nargout >= 4 (else MU2,
+        which the convergence test then uses, :98-102)."""
+        if self.coupling != 0 or self.nlincpl != 0:
+            raise ValueError("GPEtask2comp: an incoherent mixture has coupling = nlincpl = 0")
+        self._push_params()
+        self._upload_V(self.getVtotal(0))
+        if phi0 is None:
+            rng = rng or np.random.default_rng()
+            phi0 = [self.grid.normalize(rng.random(self.grid.shape) + 1j * rng.random(self.grid.shape)) / math.sqrt(2)
+                    for _ in range(2)]
+        self._upload_state(phi0)
+        prm = L.gpe_itp_params()
+        prm.dt = float(dt)
+        prm.eps = float(eps)
+        prm.want_energy = int(nargout >= 4)
+        cap = int(self.itp_max_iter)
+        MU1, MU2, EE = np.zeros(cap), np.zeros(cap), np.zeros(cap)
+        res = L.gpe_itp_result()
+        L.check(self._ctx, L.lib.gpe_groundstate_itp_2comp(
+            self._ctx, C.byref(prm), float(self.N1), float(self.N2), float(self.M1), float(self.M2),
+            L.dptr(MU1), L.dptr(MU2), L.dptr(EE), cap, C.byref(res)))
+        if not res.converged:
+            warnings.warn("Convergence not reached")
+        self.last_itp = res
+        n = res.iters
+        phi = self._download()
+        self.init_state = phi
+        self._current_state = phi
+        self._state_on_device = "current"
+        outs = (phi, MU1[:n].copy(), MU2[:n].copy(), EE[:n].copy())
+        return phi if nargout <= 1 else outs[:nargout]
+
+
 def detect_core(task, refine=0, z_index=0, component=0, cap=4096):
     """detect_core(phi, rx, ry, refine) (lib/util/detect_core.m:1-67) of the
     task's current device state, on the device (gpe_detect_core): (resp,

@@ -27,6 +27,7 @@
 //   gpe_mex('sgpe', h, ddt, nin, nout, task, timedep, T, ecut, seed)   % SGPEtask.solve_split
 //   h = gpe_mex('create_spinor', ndims, n, dx, span, precision)      % GPEtaskSpinor context
 //   gpe_mex('set_spinor_params', h, g, coupling, nlincpl)
+//   [MU1, MU2, EE] = gpe_mex('itp_2comp', h, dt, eps, want_energy, [N1 N2], [M1 M2])   % GPEtask2comp ITP
 //       spinor contexts take [phi1(:); phi2(:)] and [V1(:); V2(:)] in set_state /
 //       set_potential / getVtotal, and get_state returns them stacked the same way
 //   gpe_mex('set_state_gpu', h, psi_gpuArray)                            % device to device
@@ -270,6 +271,37 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     else mxDestroyArray(EE);
     if (nlhs > 3) plhs[3] = mxCreateDoubleScalar(res.iters);
     if (nlhs > 4) plhs[4] = mxCreateDoubleScalar(res.converged);
+    if (!res.converged) mexWarnMsgIdAndTxt("gpe:itp", "Convergence not reached");
+  } else if (cmd == "itp_2comp") {
+    // [MU1, MU2, EE] = gpe_mex('itp_2comp', h, dt, eps, want_energy, [N1 N2], [M1 M2])
+    if (nrhs != 7) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('itp_2comp', h, dt, eps, want_energy, [N1 N2], [M1 M2])");
+    gpe_itp_params p;
+    memset(&p, 0, sizeof(p));
+    p.dt = scalar(prhs[2]);
+    p.eps = scalar(prhs[3]);
+    p.want_energy = (int)scalar(prhs[4]);
+    if (mxGetNumberOfElements(prhs[5]) != 2 || mxGetNumberOfElements(prhs[6]) != 2 || !mxIsDouble(prhs[5]) ||
+        !mxIsDouble(prhs[6]))
+      mexErrMsgIdAndTxt("gpe:usage", "itp_2comp: [N1 N2] and [M1 M2] are two doubles each");
+    const double* Nj = mxGetDoubles(prhs[5]);
+    const double* Mj = mxGetDoubles(prhs[6]);
+    gpe_params prm;
+    check(c, gpe_get_params(c, &prm));
+    const int cap = prm.itp_max_iter;
+    mxArray* MU1 = mxCreateDoubleMatrix(cap, 1, mxREAL);
+    mxArray* MU2 = mxCreateDoubleMatrix(cap, 1, mxREAL);
+    mxArray* EE = mxCreateDoubleMatrix(cap, 1, mxREAL);
+    gpe_itp_result res;
+    check(c, gpe_groundstate_itp_2comp(c, &p, Nj[0], Nj[1], Mj[0], Mj[1], mxGetDoubles(MU1), mxGetDoubles(MU2),
+                                       mxGetDoubles(EE), cap, &res));
+    mxSetM(MU1, res.iters);
+    mxSetM(MU2, res.iters);
+    mxSetM(EE, res.iters);
+    plhs[0] = MU1;
+    if (nlhs > 1) plhs[1] = MU2;
+    else mxDestroyArray(MU2);
+    if (nlhs > 2) plhs[2] = EE;
+    else mxDestroyArray(EE);
     if (!res.converged) mexWarnMsgIdAndTxt("gpe:itp", "Convergence not reached");
   } else if (cmd == "split") {
     if (nrhs != 7) mexErrMsgIdAndTxt("gpe:usage", "gpe_mex('split', h, ddt, nin, nout, task, timedep)");

@@ -209,6 +209,21 @@ GPE_API gpe_status gpe_create_spinor(const gpe_grid_desc *desc, gpe_ctx **out);
 GPE_API gpe_status gpe_set_omega_field(gpe_ctx *ctx, const double *omega, int n_crank);
 GPE_API gpe_status gpe_set_spinor_params(gpe_ctx *ctx, const gpe_spinor_params *p);
 GPE_API gpe_status gpe_get_spinor_params(const gpe_ctx *ctx, gpe_spinor_params *p);
+/* Incoherent two-component mixture (GPEtask2comp), imaginary time:
+ * lib/@GPEtask2comp/groundstate_itp.m:1-157 on a spinor context from its
+ * current state, with the spinor's g (coupling and nlincpl must be 0) and
+ * omega = 0.  Each component j relaxes with its own kinetic factor
+ * exp(-kk dt/2/M_j) (:29-30) and is renormalised to its own N_j (:82-90);
+ * MU1(i) = log(sqrt(N1/n1))/dt, MU2(i) likewise for component 2 (not the
+ * <psi|H psi> of gpe_groundstate_itp).  EE(i) = get_energy/Ntotal
+ * (GPEtask2comp.m:107-118, Ntotal from gpe_set_params) when want_energy, else
+ * MU2(i) (:98-102); the convergence test of :113-135 runs on EE.  MU1, MU2,
+ * EE (each may be NULL) receive up to cap entries; the iteration cap is
+ * 500000 (:136).  prm->want_mu2, fp64_polish and switch_delta are not used. */
+GPE_API gpe_status gpe_groundstate_itp_2comp(gpe_ctx *ctx, const gpe_itp_params *prm,
+                               double N1, double N2, double M1, double M2,
+                               double *MU1, double *MU2, double *EE, int cap,
+                               gpe_itp_result *res);
 GPE_API void gpe_destroy(gpe_ctx *ctx);
 /* Message of the last failed call on ctx (ctx may be NULL: last failure of
  * gpe_create on this thread). Never NULL. */

@@ -774,6 +774,73 @@ class GPEtaskSpinor(GPEtask):
         return phi
 
 
+class GPEtask2comp(GPEtaskSpinor):
+    """GPEtask2comp (lib/@GPEtask2comp/GPEtask2comp.m:1-150): an incoherent
+    mixture, components normalised separately to N1 and N2, masses M1, M2 in
+    the imaginary-time kinetic factors; applyham/get_energy are the spinor's
+    without coupling (GPEtask2comp.m:45-63, 94-106)."""
+
+    def __init__(self, grid, trappot):
+        super().__init__(grid, trappot)
+        self.N1 = self.N2 = 0.0
+        self.M1 = self.M2 = 1.0
+
+    # GPEtask2comp.m:45-63 (the spinor's with coupling = 0)
+    def applyham1c(self, phi, j, time=None):
+        if time is None:
+            time = self.current_time
+        res = self.getVtotal(time)[j]
+        for k in range(self.ncomp):
+            res = res + self.g[j, k] * np.abs(phi[k]) ** 2
+        return res * phi[j] + self.grid.lap(phi[j])
+
+    # lib/@GPEtask2comp/groundstate_itp.m:1-129 (omega == 0)
+    def groundstate_itp(self, dt, eps, phi, nargout=4, max_iter=500000):
+        """Returns (phi, MU1, MU2, EE); EE = get_energy/Ntotal when nargout >= 4,
+        else MU2 (:71-75); the returned arrays drop the last iteration."""
+        grid = self.grid
+        VV = self.getVtotal(0)
+        g = self.g
+        phi = [np.asarray(p, dtype=np.complex128) for p in phi]
+        ekk1 = np.exp(-grid.kk * dt * 0.5 / self.M1)                    # :11-12
+        ekk2 = np.exp(-grid.kk * dt * 0.5 / self.M2)
+        MU1, MU2, EE = [], [], []
+        i = 1
+        iswitch = 20
+        while True:
+            t1 = VV[0] + g[0, 0] * np.abs(phi[0]) ** 2 + g[0, 1] * np.abs(phi[1]) ** 2   # :30-31
+            t2 = VV[1] + g[1, 0] * np.abs(phi[0]) ** 2 + g[1, 1] * np.abs(phi[1]) ** 2
+            phi = [grid.ifft(ekk1 * grid.fft(phi[0])), grid.ifft(ekk2 * grid.fft(phi[1]))]  # :39-40
+            phi = [np.exp(-t1 * dt) * phi[0], np.exp(-t2 * dt) * phi[1]]                # :42-43
+            phi = [grid.ifft(ekk1 * grid.fft(phi[0])), grid.ifft(ekk2 * grid.fft(phi[1]))]  # :51-52
+            n1c = np.real(grid.integrate(phi[0] * np.conj(phi[0])))                      # :55-58
+            n2c = np.real(grid.integrate(phi[1] * np.conj(phi[1])))
+            mu1 = math.sqrt(self.N1 / n1c)
+            mu2 = math.sqrt(self.N2 / n2c)
+            MU1.append(math.log(mu1) / dt)
+            MU2.append(math.log(mu2) / dt)
+            phi = [phi[0] * mu1, phi[1] * mu2]
+            self.current_state = phi
+            EE.append(self.get_energy(phi) / self.Ntotal if nargout >= 4 else MU2[-1])  # :67-71
+            if (i - iswitch) > 10 and i % 10 == 0:                                      # :72-92
+                delta = (abs(EE[i - 1] - EE[i - 10]) / 9 + abs(EE[i - 1] - EE[i - 2])) / dt
+                if delta < eps:
+                    if dt < eps or dt < 5e-6:
+                        break
+                    dt = dt / 1.5
+                    ekk1 = np.exp(-grid.kk * dt * 0.5 / self.M1)
+                    ekk2 = np.exp(-grid.kk * dt * 0.5 / self.M2)
+                    iswitch = i
+            if i >= max_iter:
+                warnings.warn("Convergence not reached")
+                break
+            i += 1
+        self.init_state = phi
+        self.current_state = phi
+        self.final_dt = dt
+        return phi, np.array(MU1[:i - 1]), np.array(MU2[:i - 1]), np.array(EE[:i - 1])
+
+
 # ---------------------------------------------------------------------------
 # Vortex-core detection: lib/util/detect_core.m:1-67.  Arrays here are
 # indexed [ix, iy] (the transpose of MATLAB's row = y, column = x matrix), so

@@ -145,3 +145,25 @@ def test_energy_history_and_itp_outputs_are_sliced_to_the_reported_lengths(fake)
     assert (prm.want_mu2, prm.want_energy) == (1, 1)
     assert len(MU) == len(MU2) == len(EE) == 0  # the fake reports zero iterations
     assert isinstance(phi, list) and len(phi) == 2
+
+
+def test_two_component_itp_passes_particle_numbers_and_masses(fake):
+    import gpe_gb300 as gpe
+
+    grid = gpe.grid2d(4.0, 16, 3.0, 8)
+    t = gpe.GPEtask2comp(grid, [lambda X, Y, Z: 0 * X, lambda X, Y, Z: 0 * X + 1.0])
+    t.g = np.array([[1.0, 0.5], [0.5, 2.0]])
+    t.N1, t.N2, t.M1, t.M2, t.Ntotal = 2.0, 3.0, 1.0, 4.0, 5.0
+    phi, MU1 = t.groundstate_itp(0.01, 1e-6, [np.ones(grid.shape, complex)] * 2, nargout=2)
+    args = fake.last("gpe_groundstate_itp_2comp")
+    assert args[2:6] == (2.0, 3.0, 1.0, 4.0)
+    assert args[1]._obj.want_energy == 0  # EE is MU2 unless nargout >= 4
+    assert "gpe_groundstate_itp" not in fake.names()
+    # the coupling of the spinor parameters stays zero
+    sp = fake.last("gpe_set_spinor_params")[1]._obj
+    assert (sp.coupling_re, sp.coupling_im, sp.nlincpl) == (0.0, 0.0, 0.0)
+    t.groundstate_itp(0.01, 1e-6, [np.ones(grid.shape, complex)] * 2, nargout=4)
+    assert fake.last("gpe_groundstate_itp_2comp")[1]._obj.want_energy == 1
+    t.coupling = 0.1
+    with pytest.raises(ValueError):
+        t.groundstate_itp(0.01, 1e-6, [np.ones(grid.shape, complex)] * 2)

@@ -401,3 +401,27 @@ def test_spinor_itp_decoupled_matches_single_component_ground_state():
         t.coupling = c
         phi, MU, MU2, EE = t.groundstate_itp(0.01, 1e-7, [p0, p0])
         assert EE[-1] == pytest.approx(1.0 + c, abs=1e-5)
+
+
+def test_two_component_itp_known_answers():
+    """GPEtask2comp.groundstate_itp (lib/@GPEtask2comp/groundstate_itp.m):
+    without interactions each component relaxes to the harmonic ground state
+    of its own mass, mu_j = omega_j = 1/sqrt(M_j) in 2D for V = r^2/2 (each
+    normalised to its own N_j); EE = get_energy/Ntotal then equals
+    (N1 mu1 + N2 mu2)/Ntotal."""
+    g = O.Grid(6, 48, 6, 48)
+    V = lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2)
+    t = O.GPEtask2comp(g, [V, V])
+    t.g = np.zeros((2, 2))
+    t.N1, t.N2, t.Ntotal = 1.0, 3.0, 4.0
+    t.M1, t.M2 = 1.0, 4.0
+    X, Y = g.mesh["x"], g.mesh["y"]
+    p0 = np.exp(-((X - 0.2) ** 2 + Y ** 2) / 3).astype(complex)
+    phi, MU1, MU2, EE = t.groundstate_itp(0.01, 1e-7, [p0, p0])
+    assert MU1[-1] == pytest.approx(1.0, abs=1e-4)
+    assert MU2[-1] == pytest.approx(0.5, abs=1e-4)  # 1/sqrt(4)
+    np.testing.assert_allclose([g.integrate(np.abs(p) ** 2) for p in phi], [1.0, 3.0], rtol=1e-12)
+    # get_energy uses lap without the mass (GPEtask2comp.m:45-63): E_j = N_j (w/4 + 1/(4w) ...)
+    # for a Gaussian of width set by M_j; compare against the direct sum
+    E = sum(np.real(g.inner(p, g.lap(p) + V(X, Y, 0) * p)) for p in phi) / 4.0
+    assert EE[-1] == pytest.approx(E, rel=1e-10)
