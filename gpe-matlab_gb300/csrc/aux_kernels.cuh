@@ -135,9 +135,10 @@ void launch_lz_cn(cx<R>* out, const cx<R>* phi, const cx<R>* src, const R* om, d
 template <typename R>
 int launch_rt_block_end(cx<R>* psi, const R* V, long long n, const DevScalars* sc, double g, double dre, double dim,
                         double* partials, int cap, cudaStream_t s);
-// Per-CTA sums of real(conj(psi) (-omega lz psi)) (times scale^2 if use_scale); returns CTAs.
+// Per-CTA sums of real(conj(psi) (-omega lz psi)) (times scale^2 if use_scale),
+// omega per point (om) or the scalar oms (om null); returns CTAs.
 template <typename R>
-int launch_lz_energy(const cx<R>* psi, const R* om, long long n, const LzGeom& g, const DevScalars* sc,
+int launch_lz_energy(const cx<R>* psi, const R* om, double oms, long long n, const LzGeom& g, const DevScalars* sc,
                      int use_scale, double* out, cudaStream_t st);
 
 // On-device observables, observables.cu.

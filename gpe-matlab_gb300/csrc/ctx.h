@@ -34,6 +34,9 @@ struct Field {
   void* kks[3] = {nullptr, nullptr, nullptr};    // per axis: permuted k^2/2, N real (energy cut-off)
   void* php2[3] = {nullptr, nullptr, nullptr};   // spinor, array omega: the kinetic factors of half a step
   void* php2b[3] = {nullptr, nullptr, nullptr};  // two-component ITP with M2 != M1: component 2's half-step factors
+  // Rotating two-component ITPs: per table set (component mass) the x and y
+  // half-step factors and their rotation tables (x: [y][slot], y: [x][slot]).
+  void* rth[2][4] = {{nullptr, nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr, nullptr}};
   void* cn[2] = {nullptr, nullptr};              // array omega: Crank-Nicolson iterates (P complex each)
 };
 
@@ -72,6 +75,7 @@ struct gpe_ctx {
   // context precision, and the Crank-Nicolson iteration count n_crank.
   bool omega_field = false;
   bool adi_off = false;   // rotating SGPE run: scalar omega drives only its Lz step, not the ADI kinetic factors
+  bool lz_scalar = false; // rotating spinor ITP: energies add -omega <psi|lz psi> with grid1d's stencil lz
   double* omf64 = nullptr;
   void* omfR = nullptr;
   int n_crank = 3;

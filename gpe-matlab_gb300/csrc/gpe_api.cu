@@ -532,6 +532,57 @@ gpe_status half_table(gpe_ctx* c, const Field& f, int ax, double dre, double dim
   return upload_cx<R>(c, dst, ph);
 }
 
+// Rotating two-component ITPs (GPEtaskSpinor/groundstate_itp.m:30-33,
+// GPEtask2comp/groundstate_itp.m:31-36, 2D): the x factor
+// exp(-(kx^2/2 - kx y omega) tau) and the y factor exp(-(ky^2/2 + ky x omega) tau),
+// tau = dt/(2M), each as the per-axis table exp(-k^2/2 tau)/N (set[0], set[1])
+// and the rotation table over the pencil's transverse coordinate c,
+// exp(+kx y omega tau) / exp(-ky x omega tau) (set[2], set[3]).
+template <typename R>
+gpe_status rot_half_tables(gpe_ctx* c, const Field& f, double tau, void* set[4]) {
+  const double om = c->prm.omega;
+  for (int ax = 0; ax < 2; ++ax) {
+    CHECK(half_table<R>(c, f, ax, 2.0 * tau, 0.0, set[ax]));
+    const int N = c->n[ax];
+    const PlanInfo pi = dispatch_plan(N, f.plan_var[ax]);
+    const int tax = ax == 0 ? 1 : 0;
+    const int nt = c->n[tax];
+    const double s = (ax == 0 ? om : -om) * tau;
+    std::vector<std::complex<double>> rt((size_t)nt * N);
+    for (int i = 0; i < nt; ++i) {
+      const double xc = coord(c, tax, i);
+      for (int t = 0; t < pi.T; ++t)
+        for (int m = 0; m < pi.E; ++m)
+          rt[(size_t)i * N + slot_index<R>(pi.T, t, m)] = std::exp(s * kval(c, ax, plan_spec_pos(pi, t, m)) * xc);
+    }
+    if (!set[2 + ax]) CU(cudaMalloc(&set[2 + ax], rt.size() * 2 * sizeof(R)));
+    CHECK(upload_cx<R>(c, set[2 + ax], rt));
+  }
+  return GPE_OK;
+}
+
+// The x (rot = 1) and y (rot = 2) passes of a rotating half step on a 2D
+// grid, over every component or (one_comp) one.
+std::vector<AxisPass> rot_xy_passes(const gpe_ctx* c, bool one_comp) {
+  const long long nx = c->n[0], ny = c->n[1], nc = one_comp ? 1 : c->ncomp;
+  AxisPass px{0, (int)nx, true, ny * nc, ny, ny, nx * ny};
+  AxisPass py{1, (int)ny, false, nx * nc, 1, 1, 0};
+  px.rot = 1;
+  py.rot = 2;
+  px.one_comp = py.one_comp = one_comp;
+  return {px, py};
+}
+
+// A view of f whose x/y kinetic and rotation tables are one rot_half_tables set.
+Field rot_view(const Field& f, void* const set[4]) {
+  Field r = f;
+  r.php[0] = set[0];
+  r.php[1] = set[1];
+  r.rot[0] = set[2];
+  r.rot[1] = set[3];
+  return r;
+}
+
 template <typename R>
 gpe_status set_kinop(gpe_ctx* c, Field& f, double dre, double dim) {
   if (f.phase_valid && f.phase_dt[0] == dre && f.phase_dt[1] == dim) return GPE_OK;
@@ -613,6 +664,8 @@ void free_field(Field& f, const double* V64) {
     cudaFree(f.php2[i]);
     cudaFree(f.php2b[i]);
   }
+  for (auto& set : f.rth)
+    for (void* p : set) cudaFree(p);
   for (int i = 0; i < 2; ++i) cudaFree(f.cn[i]);
   for (int i = 0; i < 2; ++i) {
     cudaFree(f.rot[i]);
@@ -796,11 +849,13 @@ gpe_status energy_passes(gpe_ctx* c, Field& f, bool pot, int nblk_kin[3], int* n
     nblk_kin[ap.axis] = nb;
     if (ep && nblk_pot) *nblk_pot = nb;
   }
-  if (c->omega_field) {
-    // the -omega Lz term of applyh0 (GPEtask.m:92-94), appended to the x
-    // pass's kinetic partials so every finalizer adds it to the kinetic sum
-    Launch L(c, PC_NORM, (double)c->P * (2 * sizeof(R) + sizeof(R)));
-    const int nb = launch_lz_energy<R>((const cx<R>*)f.psi, omega_field_ptr<R>(c), c->P, lz_geom(c), c->sc, pot,
+  if (c->omega_field || c->lz_scalar) {
+    // the -omega Lz term of applyh0 (GPEtask.m:92-94; GPEtaskSpinor.m:72-74
+    // per component with scalar omega), appended to the x pass's kinetic
+    // partials so every finalizer adds it to the kinetic sum
+    Launch L(c, PC_NORM, (double)c->PS * (2 * sizeof(R) + sizeof(R)));
+    const R* om = c->omega_field ? omega_field_ptr<R>(c) : nullptr;
+    const int nb = launch_lz_energy<R>((const cx<R>*)f.psi, om, c->prm.omega, c->PS, lz_geom(c), c->sc, pot,
                                        c->partials + (size_t)S_KX * c->cap + nblk_kin[0], c->stream);
     CU(cudaGetLastError());
     nblk_kin[0] += nb;
@@ -2147,7 +2202,9 @@ gpe_status gpe_groundstate_itp(gpe_ctx* c, const gpe_itp_params* prm, double* MU
     return fail(c, GPE_ERR_INVALID, "groundstate_itp: dt and eps must be positive");
   if (cap < 0) return fail(c, GPE_ERR_INVALID, "negative cap");
   if (c->ncomp == 2) {
-    if (c->prm.omega != 0.0) return fail(c, GPE_ERR_UNSUPPORTED, "groundstate_itp (spinor): omega != 0");
+    if (c->prm.omega != 0.0 && c->ndims != 2)
+      return fail(c, GPE_ERR_UNSUPPORTED,
+                  "groundstate_itp (spinor): omega != 0 in 3D (the reference's rotating branch has no z kinetic factor)");
     c->err.clear();
     if (c->prec == GPE_FP32) return spinor_itp_impl<float>(c, prm, MU, MU2, EE, cap, res);
     return spinor_itp_impl<double>(c, prm, MU, MU2, EE, cap, res);
@@ -2170,7 +2227,9 @@ gpe_status gpe_groundstate_itp_2comp(gpe_ctx* c, const gpe_itp_params* prm, doub
   if (!prm || !(prm->dt > 0) || !std::isfinite(prm->dt) || !(prm->eps > 0))
     return fail(c, GPE_ERR_INVALID, "groundstate_itp: dt and eps must be positive");
   if (cap < 0) return fail(c, GPE_ERR_INVALID, "negative cap");
-  if (c->prm.omega != 0.0) return fail(c, GPE_ERR_UNSUPPORTED, "groundstate_itp (2comp): omega != 0");
+  if (c->prm.omega != 0.0 && c->ndims != 2)
+    return fail(c, GPE_ERR_UNSUPPORTED,
+                "groundstate_itp (2comp): omega != 0 in 3D (the reference's rotating branch has no z kinetic factor)");
   c->err.clear();
   if (c->prec == GPE_FP32) return mix_itp_impl<float>(c, prm, N1, N2, M1, M2, MU1, MU2, EE, cap, res);
   return mix_itp_impl<double>(c, prm, N1, N2, M1, M2, MU1, MU2, EE, cap, res);

@@ -53,11 +53,12 @@ __global__ void __launch_bounds__(LZ_T) k_lz_cn(cx<R>* out, const cx<R>* phi, co
 }
 
 // Per CTA: sum of real(conj(psi) * (-omega lz(psi))) = -omega Im(conj(psi) w),
-// times scale^2 when the state carries a pending factor.
+// times scale^2 when the state carries a pending factor; omega per point (om)
+// or the scalar oms when om is null.
 template <typename R>
 __global__ void __launch_bounds__(LZ_T) k_lz_energy(const cx<R>* __restrict__ psi, const R* __restrict__ om,
-                                                   long long n, LzGeom g, const DevScalars* sc, int use_scale,
-                                                   double* out) {
+                                                   double oms, long long n, LzGeom g, const DevScalars* sc,
+                                                   int use_scale, double* out) {
   if (sc->stop) return;
   double acc = 0.0;
   for (long long i = (long long)blockIdx.x * LZ_T + threadIdx.x; i < n; i += (long long)gridDim.x * LZ_T) {
@@ -65,7 +66,8 @@ __global__ void __launch_bounds__(LZ_T) k_lz_energy(const cx<R>* __restrict__ ps
     const int ix = (int)(r / g.ny), iy = (int)(r % g.ny);
     const cx<R> w = lz_w<R>(psi, i, ix, iy, g);
     const cx<R> p = psi[i];
-    acc += -(double)om[i] * ((double)p.x * w.y - (double)p.y * w.x);
+    const double o = om ? (double)om[i] : oms;
+    acc += -o * ((double)p.x * w.y - (double)p.y * w.x);
   }
   __shared__ double sh[LZ_T];
   sh[threadIdx.x] = acc;
@@ -87,17 +89,17 @@ void launch_lz_cn(cx<R>* out, const cx<R>* phi, const cx<R>* src, const R* om, d
 }
 
 template <typename R>
-int launch_lz_energy(const cx<R>* psi, const R* om, long long n, const LzGeom& g, const DevScalars* sc,
+int launch_lz_energy(const cx<R>* psi, const R* om, double oms, long long n, const LzGeom& g, const DevScalars* sc,
                      int use_scale, double* out, cudaStream_t st) {
   const int nb = elem_grid(n, LZ_T);
-  k_lz_energy<R><<<nb, LZ_T, 0, st>>>(psi, om, n, g, sc, use_scale, out);
+  k_lz_energy<R><<<nb, LZ_T, 0, st>>>(psi, om, oms, n, g, sc, use_scale, out);
   return nb;
 }
 
 #define INST_LZ(R)                                                                                     \
   template void launch_lz_cn<R>(cx<R>*, const cx<R>*, const cx<R>*, const R*, double, long long,         \
                                 const LzGeom&, double, double, cudaStream_t);                          \
-  template int launch_lz_energy<R>(const cx<R>*, const R*, long long, const LzGeom&, const DevScalars*, int, \
+  template int launch_lz_energy<R>(const cx<R>*, const R*, double, long long, const LzGeom&, const DevScalars*, int, \
                                    double*, cudaStream_t);
 INST_LZ(float)
 INST_LZ(double)

@@ -225,8 +225,8 @@ gpe_status spinor_observables(gpe_ctx* c, gpe_obs* o) {
   return GPE_OK;
 }
 
-// GPEtaskSpinor.groundstate_itp (lib/@GPEtaskSpinor/groundstate_itp.m:1-145,
-// omega = 0) from the current state.  Per iteration: the nonlinear factors of
+// GPEtaskSpinor.groundstate_itp (lib/@GPEtaskSpinor/groundstate_itp.m:1-145;
+// omega != 0 on 2D grids) from the current state.  Per iteration: the nonlinear factors of
 // the state before the kinetic half step, the half step, the coupling rotation
 // times the factors, the half step, normalisation to Ntotal (MU = log(m)/dt),
 // and with want_mu2 / want_energy MU2 and EE of every iteration (otherwise
@@ -258,10 +258,36 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
   double* dEE = c->d_hist + 2 * (size_t)maxit;
   CHECK(materialize<R>(c));
   launch_reset_scalars(c->sc, c->stream);
-  CHECK(set_kinop<R>(c, f, dt, 0.0));
+  // Rotating frame (2D, :30-33, 61-80): the kinetic half step is the x factor
+  // then the y factor, on both sides of the nonlinear factor; energies use
+  // lap without omega plus -omega lz with grid1d's stencil (GPEtaskSpinor.m:72-74).
+  const bool rot = c->prm.omega != 0.0;
+  struct Flags {
+    gpe_ctx* c;
+    bool adi_off, lz_scalar;
+    ~Flags() {
+      c->adi_off = adi_off;
+      c->lz_scalar = lz_scalar;
+    }
+  } flags{c, c->adi_off, c->lz_scalar};
+  if (rot) {
+    c->adi_off = true;
+    c->lz_scalar = true;
+  }
+  auto set_tables = [&](double h) -> gpe_status {
+    if (rot) return rot_half_tables<R>(c, f, 0.5 * h, f.rth[0]);
+    return set_kinop<R>(c, f, h, 0.0);
+  };
+  CHECK(set_tables(dt));
   SpinorNL<R> q = spinor_nl_consts<R>(c, dt, 0.0);  // cosh / sinh(dt |c|) with the coupling phase (:45-48)
-  std::vector<AxisPass> half = axis_passes(c);
-  for (auto& ap : half) ap.half = 1;
+  std::vector<AxisPass> half = rot ? rot_xy_passes(c, false) : axis_passes(c);
+  if (!rot)
+    for (auto& ap : half) ap.half = 1;
+  auto kinetic = [&]() -> gpe_status {
+    Field fr = rot ? rot_view(f, f.rth[0]) : f;
+    for (const auto& ap : half) CHECK(run_pass<R>(c, fr, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
+    return GPE_OK;
+  };
   auto ee_of = [&](int i, std::vector<double>& host, int lo) { return host[i - lo]; };
   int i = 1, iswitch = 20;
   bool converged = false;
@@ -272,13 +298,13 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
       Launch L(c, PC_NL_PHASE, (double)c->PS * (2 * sizeof(R) + 2 * sizeof(R)));
       launch_spinor_itp_factors<R>((const cx<R>*)f.psi, (const R*)f.V, P, c->sc, q, (R*)f.aux, 0, c->stream);
     }
-    for (const auto& ap : half) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
+    CHECK(kinetic());
     {
       Launch L(c, PC_NL_PHASE, (double)c->PS * (4 * sizeof(R) + sizeof(R)));
       launch_spinor_itp_couple<R>((cx<R>*)f.psi, (const R*)f.aux, P, c->sc, q, 0, c->stream);
       launch_set_scale_one(c->sc, c->stream);
     }
-    for (const auto& ap : half) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
+    CHECK(kinetic());
     int nb;
     {
       Launch L(c, PC_NORM, (double)c->PS * 2 * sizeof(R));
@@ -310,7 +336,7 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
           break;
         }
         dt = dt / 1.5;
-        CHECK(set_kinop<R>(c, f, dt, 0.0));
+        CHECK(set_tables(dt));
         q = spinor_nl_consts<R>(c, dt, 0.0);
         iswitch = i;
       }
@@ -346,8 +372,8 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
   return GPE_OK;
 }
 
-// GPEtask2comp.groundstate_itp (lib/@GPEtask2comp/groundstate_itp.m:1-157,
-// omega = 0) from the current state of a spinor context, coupling = 0.  Per
+// GPEtask2comp.groundstate_itp (lib/@GPEtask2comp/groundstate_itp.m:1-157;
+// omega != 0 on 2D grids) from the current state of a spinor context, coupling = 0.  Per
 // iteration: the factors exp(-(V_j + sum_k g(j,k)|psi_k|^2) dt) from the state
 // before the step (:58-59), the kinetic half step with each component's own
 // exp(-kk dt/2/M_j) (:67-68; one launch over both components when M1 == M2),
@@ -385,7 +411,16 @@ gpe_status mix_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double N1, double
   CHECK(materialize<R>(c));  // also resets scale2
   launch_reset_scalars(c->sc, c->stream);
   const bool same_mass = M1 == M2;
+  // Rotating frame (2D, :31-36, 61-80): x then y half steps before the
+  // nonlinear factor, y then x after it, each with exp(-(k^2/2 -+ k c omega)
+  // dt/2/M_j); energies use lap(phi, omega) (GPEtask2comp.m:60).
+  const bool rot = c->prm.omega != 0.0;
   auto set_tables = [&](double h) -> gpe_status {
+    if (rot) {
+      CHECK(rot_half_tables<R>(c, f, 0.5 * h / M1, f.rth[0]));
+      if (!same_mass) CHECK(rot_half_tables<R>(c, f, 0.5 * h / M2, f.rth[1]));
+      return GPE_OK;
+    }
     CHECK(set_kinop<R>(c, f, h / M1, 0.0));  // php2 = exp(-kk h/2/M1)
     if (!same_mass)
       for (int ax = 0; ax < c->ndims; ++ax) CHECK(half_table<R>(c, f, ax, h / M2, 0.0, f.php2b[ax]));
@@ -398,7 +433,25 @@ gpe_status mix_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double N1, double
   for (auto& ap : one) ap.half = 1;
   for (auto& ap : two) ap.half = 2;
   cx<R>* psi2 = (cx<R>*)f.psi + P;
+  const std::vector<AxisPass> rboth = rot ? rot_xy_passes(c, false) : std::vector<AxisPass>();
+  const std::vector<AxisPass> rone = rot ? rot_xy_passes(c, true) : std::vector<AxisPass>();
+  bool second = false;  // the half step after the nonlinear factor (y first)
   auto kinetic = [&]() -> gpe_status {
+    if (rot) {
+      const int o0 = second ? 1 : 0, o1 = 1 - o0;
+      if (same_mass) {
+        Field fr = rot_view(f, f.rth[0]);
+        for (int k : {o0, o1}) CHECK(run_pass<R>(c, fr, rboth[k], KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
+      } else {
+        for (int j = 0; j < 2; ++j) {
+          Field fr = rot_view(f, f.rth[j]);
+          void* pj = j == 0 ? f.psi : (void*)psi2;
+          for (int k : {o0, o1})
+            CHECK(run_pass<R>(c, fr, rone[k], KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr, pj));
+        }
+      }
+      return GPE_OK;
+    }
     if (same_mass) {
       for (const auto& ap : both) CHECK(run_pass<R>(c, f, ap, KIND_STEP, PRO_NONE, EPI_NONE, 0, dt, 0.0, nullptr));
       return GPE_OK;
@@ -416,12 +469,14 @@ gpe_status mix_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double N1, double
       Launch L(c, PC_NL_PHASE, (double)c->PS * (2 * sizeof(R) + 2 * sizeof(R)));
       launch_spinor_itp_factors<R>((const cx<R>*)f.psi, (const R*)f.V, P, c->sc, q, (R*)f.aux, 1, c->stream);
     }
+    second = false;
     CHECK(kinetic());
     {
       Launch L(c, PC_NL_PHASE, (double)c->PS * (4 * sizeof(R) + sizeof(R)));
       launch_spinor_itp_couple<R>((cx<R>*)f.psi, (const R*)f.aux, P, c->sc, q, 1, c->stream);
       launch_set_scale_one(c->sc, c->stream);
     }
+    second = true;
     CHECK(kinetic());
     MixFinalArgs a{};
     {

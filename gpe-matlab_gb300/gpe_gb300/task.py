@@ -456,7 +456,8 @@ class GPEtaskSpinor(GPEtask):
     [phi1, phi2].  solve_split runs GPEtaskSpinor.solve_split on the GPU
     (one context holding both components); ``Vtd`` is a callable added to
     both potentials or a pair of callables (GPEtaskSpinor.m:23-42).
-    groundstate_itp is the spinor's own (groundstate_itp.m); omega must be 0."""
+    groundstate_itp is the spinor's own (groundstate_itp.m, with its rotating
+    branch for a scalar omega on 2D grids); elsewhere omega must be 0."""
 
     def __init__(self, grid: _GridBase, trappot, device: int = 0):
         self.grid = grid
@@ -659,7 +660,8 @@ class GPEtask2comp(GPEtaskSpinor):
         self.M2 = 1.0
 
     def groundstate_itp(self, dt, eps, phi0=None, nargout=1, rng=None):
-        """lib/@GPEtask2comp/groundstate_itp.m:1-157 on the GPU (omega = 0).
+        """lib/@GPEtask2comp/groundstate_itp.m:1-157 on the GPU (a scalar
+        omega on 2D grids takes the reference's rotating branch).
         phi0: a pair, or None for the reference's random start.  Returns phi,
         or (phi, MU1, MU2, EE)[:nargout]: MU_j(i) = log(sqrt(N_j/n_j))/dt of
         each component; EE = get_energy/Ntotal when nargout >= 4 (else MU2,

@@ -5,8 +5,9 @@ classdef GPEtask2compGB300 < GPEtask2comp
     % Drop-in for GPEtask2comp: construct it exactly like
     % GPEtask2comp(grid, {V1, V2}); g (2x2), N1, N2, M1, M2 and Ntotal keep
     % their meaning, and groundstate_itp (lib/@GPEtask2comp/groundstate_itp.m)
-    % returns phi ({phi1, phi2}), MU1, MU2 and EE as the reference does.
-    % omega must be 0.  Single-precision grid axes run in complex FP32.
+    % returns phi ({phi1, phi2}), MU1, MU2 and EE as the reference does,
+    % with a scalar omega on 2D grids (its rotating branch).  Single-precision
+    % grid axes run in complex FP32.
     %
     % UNVERIFIED: no MATLAB was available where this file was written; the
     % library calls it makes are covered by the Python tests of the same ABI.
@@ -46,8 +47,8 @@ classdef GPEtask2compGB300 < GPEtask2comp
 
         function [phi, varargout] = groundstate_itp(task, dt, eps, phi)
             % @GPEtask2comp/groundstate_itp.m semantics, executed by libgpe.
-            if ~isscalar(task.omega) || task.omega ~= 0
-                error('gpe:omega', 'libgpe runs GPEtask2comp.groundstate_itp with omega = 0 only');
+            if ~isscalar(task.omega)
+                error('gpe:omega', 'libgpe runs GPEtask2comp.groundstate_itp with a scalar omega');
             end
             V = task.getVtotal(0);
             if nargin <= 3
@@ -59,7 +60,7 @@ classdef GPEtask2compGB300 < GPEtask2comp
                 ntot = 0;
             end
             % the reference's iteration cap (groundstate_itp.m:136) as itp_max_iter
-            gpe_mex('set_params', task.gb300_handle, 0, 0, 0, ntot, 0, 10, 500000, 50, 0, 0);
+            gpe_mex('set_params', task.gb300_handle, 0, 0, 0, ntot, 0, 10, 500000, 50, 0, double(task.omega));
             gpe_mex('set_spinor_params', task.gb300_handle, double(task.g), 0, 0);
             gpe_mex('set_potential', task.gb300_handle, double(gather([V{1}(:); V{2}(:)])));
             gpe_mex('set_state', task.gb300_handle, complex(gather([phi{1}(:); phi{2}(:)])));

@@ -6,7 +6,8 @@ classdef GPEtaskSpinorGB300 < GPEtaskSpinor
     % GPEtaskSpinor(grid, {V1, V2}); g (2x2), coupling, nlincpl, gamma,
     % decay_rate, Ntotal, n_recalc, Vtd, init_state/current_state ({phi1,
     % phi2}), history and user_callback keep their meaning; solve_split,
-    % groundstate_itp and get_energy run on the GPU.  omega must be 0.
+    % groundstate_itp and get_energy run on the GPU.  omega must be 0 except
+    % in groundstate_itp on 2D grids (its rotating branch).
     % Single-precision grid axes run the step in complex FP32.
     %
     % UNVERIFIED: no MATLAB was available where this file was written; the
@@ -72,7 +73,7 @@ classdef GPEtaskSpinorGB300 < GPEtaskSpinor
                 phi = cellfun(@(x) task.grid.normalize(rand(size(V{1}), 'like', V{1}) + ...
                     1i * rand(size(V{1}), 'like', V{1})) ./ sqrt(2), cell(1, 2), 'UniformOutput', false);
             end
-            task.gb300_push();
+            task.gb300_push(true);
             v = task.getVtotal(0);
             gpe_mex('set_potential', task.gb300_handle, double(gather([v{1}(:); v{2}(:)])));
             gpe_mex('set_state', task.gb300_handle, complex(gather([phi{1}(:); phi{2}(:)])));
@@ -114,14 +115,18 @@ classdef GPEtaskSpinorGB300 < GPEtaskSpinor
     end
 
     methods (Access = protected)
-        function gb300_push(task)
-            if ~isscalar(task.omega) || task.omega ~= 0
-                error('gpe:omega', 'libgpe runs GPEtaskSpinor with omega = 0 only');
+        function gb300_push(task, itp)
+            % itp: groundstate_itp, whose rotating branch takes a scalar omega
+            if nargin < 2
+                itp = false;
+            end
+            if ~isscalar(task.omega) || (task.omega ~= 0 && ~itp)
+                error('gpe:omega', 'libgpe runs GPEtaskSpinor with omega = 0 outside groundstate_itp');
             end
             % the spinor ITP's own iteration cap (groundstate_itp.m:123) in place of itp_max_iter
             gpe_mex('set_params', task.gb300_handle, 0, task.gamma, task.decay_rate, ...
                 task.Ntotal, task.mu_init, task.n_recalc, 500000, task.itp_min_iter, ...
-                double(task.itp_adjust_stepsize), 0);
+                double(task.itp_adjust_stepsize), double(task.omega));
             gpe_mex('set_spinor_params', task.gb300_handle, double(task.g), task.coupling, task.nlincpl);
             n = task.current_n;
             if isempty(n)

@@ -171,8 +171,9 @@ typedef struct {
 
 /* Coherently coupled two-component condensate, lib/@GPEtaskSpinor
  * (GPEtaskSpinor.m:4-8; solve_split.m:61-91).  The other properties
- * (gamma, decay_rate, Ntotal, n_recalc; omega must be 0) come from
- * gpe_set_params, whose g is not used by a spinor context. */
+ * (gamma, decay_rate, Ntotal, n_recalc; omega, which only the imaginary-time
+ * solvers on 2D grids take) come from gpe_set_params, whose g is not used by
+ * a spinor context. */
 typedef struct {
     double g[4];            /* interaction matrix g(j,k) at g[2*(j-1)+(k-1)]     */
     double coupling_re;     /* coupling (Rabi frequency), complex      [0]       */
@@ -211,15 +212,19 @@ GPE_API gpe_status gpe_set_spinor_params(gpe_ctx *ctx, const gpe_spinor_params *
 GPE_API gpe_status gpe_get_spinor_params(const gpe_ctx *ctx, gpe_spinor_params *p);
 /* Incoherent two-component mixture (GPEtask2comp), imaginary time:
  * lib/@GPEtask2comp/groundstate_itp.m:1-157 on a spinor context from its
- * current state, with the spinor's g (coupling and nlincpl must be 0) and
- * omega = 0.  Each component j relaxes with its own kinetic factor
+ * current state, with the spinor's g (coupling and nlincpl must be 0).
+ * Each component j relaxes with its own kinetic factor
  * exp(-kk dt/2/M_j) (:29-30) and is renormalised to its own N_j (:82-90);
  * MU1(i) = log(sqrt(N1/n1))/dt, MU2(i) likewise for component 2 (not the
  * <psi|H psi> of gpe_groundstate_itp).  EE(i) = get_energy/Ntotal
  * (GPEtask2comp.m:107-118, Ntotal from gpe_set_params) when want_energy, else
  * MU2(i) (:98-102); the convergence test of :113-135 runs on EE.  MU1, MU2,
  * EE (each may be NULL) receive up to cap entries; the iteration cap is
- * 500000 (:136).  prm->want_mu2, fp64_polish and switch_delta are not used. */
+ * gpe_params.itp_max_iter (the reference's is 500000, :136).  Scalar omega
+ * (2D grids; :31-36, 61-80): the half step is exp(-(kx^2/2 - kx y omega)
+ * dt/2/M_j) then exp(-(ky^2/2 + ky x omega) dt/2/M_j) before the nonlinear
+ * factor and the same in reverse order after it; EE then uses
+ * lap(phi, omega).  prm->want_mu2, fp64_polish and switch_delta are not used. */
 GPE_API gpe_status gpe_groundstate_itp_2comp(gpe_ctx *ctx, const gpe_itp_params *prm,
                                double N1, double N2, double M1, double M2,
                                double *MU1, double *MU2, double *EE, int cap,
@@ -271,7 +276,13 @@ GPE_API gpe_status gpe_host_unregister(void *ptr);
  * array phi0 is applied: psi <- sqrt(Ntotal)*normalize(psi) when Ntotal > 0).
  * MU, MU2, EE (each may be NULL) receive up to cap entries, already divided
  * by Ntotal as the reference returns them.  On return the state holds the
- * ground state (init_state = phi, groundstate_itp.m:111). */
+ * ground state (init_state = phi, groundstate_itp.m:111).
+ * Spinor context: lib/@GPEtaskSpinor/groundstate_itp.m:1-145 (MU from the
+ * total norm, MU2 = <psi|H psi>/Ntotal, EE = get_energy/Ntotal).  Scalar
+ * omega (2D grids, :30-33, 61-80): each kinetic half step is
+ * exp(-(kx^2/2 - kx y omega) dt/2) then exp(-(ky^2/2 + ky x omega) dt/2), and
+ * MU2/EE add -omega <psi|lz psi> with grid1d's 4th-order lz
+ * (GPEtaskSpinor.m:72-74). */
 GPE_API gpe_status gpe_groundstate_itp(gpe_ctx *ctx, const gpe_itp_params *prm,
                                double *MU, double *MU2, double *EE, int cap,
                                gpe_itp_result *res);

@@ -625,7 +625,7 @@ class GPEtaskSpinor(GPEtask):
             return [V + f(self, time) for V, f in zip(self.Vtrap, self.Vtd)]
         return self.Vtrap
 
-    # GPEtaskSpinor.m:53-72 (omega == 0)
+    # GPEtaskSpinor.m:55-76 (scalar omega: -omega lz with grid1d's stencil, :72-74)
     def applyham1c(self, phi, j, time=None):
         if time is None:
             time = self.current_time
@@ -637,7 +637,26 @@ class GPEtaskSpinor(GPEtask):
             res = res + self.coupling * phi[1]
         else:
             res = res + np.conj(self.coupling) * phi[0]
+        if self.omega != 0:
+            res = res - self.omega * self.grid.lz(phi[j])
         return res
+
+    # the rotating half step of groundstate_itp.m:61-65 (spinor: x then y on
+    # both sides) and of GPEtask2comp/groundstate_itp.m:61-80 (y then x after
+    # the nonlinear factor); ekx/eky of :31-32, tau = dt/(2M)
+    def _rot_factors(self, dt, M=1.0):
+        grid = self.grid
+        om = self.omega
+        ekx = np.exp(-(grid.KX ** 2 - 2 * grid.KX * grid.mesh["y"] * om) / 4 * dt / M)
+        eky = np.exp(-(grid.KY ** 2 + 2 * grid.KY * grid.mesh["x"] * om) / 4 * dt / M)
+        return ekx, eky
+
+    def _rot_half(self, p, ek, order):
+        grid = self.grid
+        for ax in order:
+            f = ek[0] if ax == "x" else ek[1]
+            p = grid.ifft1(f * grid.fft1(p, ax), ax)
+        return p
 
     # GPEtaskSpinor.m:74-82
     def applyham(self, phi, time=None):
@@ -659,7 +678,8 @@ class GPEtaskSpinor(GPEtask):
             self.g = tmp
         return res
 
-    # lib/@GPEtaskSpinor/groundstate_itp.m:1-145 (omega == 0)
+    # lib/@GPEtaskSpinor/groundstate_itp.m:1-145 (scalar omega: the x and y
+    # half steps of :30-33, 61-80 in place of ekk)
     def groundstate_itp(self, dt, eps, phi, nargout=4, max_iter=500000):
         """Returns (phi, MU, MU2, EE); MU2/EE are filled as the reference does
         for the given nargout (MU2 = MU when nargout < 3, EE = MU2 when
@@ -671,6 +691,8 @@ class GPEtaskSpinor(GPEtask):
         g = self.g
         phi = [np.asarray(p, dtype=np.complex128) for p in phi]
         ekk = np.exp(-grid.kk * dt * 0.5)                                # :29
+        rot = self.omega != 0
+        ek = self._rot_factors(dt) if rot else None                      # :30-33
         MU, MU2, EE = [], [], []
         i = 1
         iswitch = 20
@@ -680,10 +702,16 @@ class GPEtaskSpinor(GPEtask):
         sinomp = np.sinh(dt * abs(coupl)) * np.exp(1j * cang)
         while True:
             tmp2 = [VV[j] + sum(g[j, k] * np.abs(phi[k]) ** 2 for k in range(ncomp)) for j in range(ncomp)]
-            phi = [grid.ifft(ekk * grid.fft(p)) for p in phi]            # :69-70
+            if rot:                                                      # :61-65
+                phi = [self._rot_half(p, ek, "xy") for p in phi]
+            else:
+                phi = [grid.ifft(ekk * grid.fft(p)) for p in phi]        # :69-70
             t0 = np.exp(-tmp2[0] * dt) * (cosom * phi[0] - sinomp * phi[1])  # :72-73
             t1 = np.exp(-tmp2[1] * dt) * (cosom * phi[1] - sinomm * phi[0])
-            phi = [grid.ifft(ekk * grid.fft(t)) for t in (t0, t1)]      # :80-81
+            if rot:                                                      # :74-78
+                phi = [self._rot_half(t, ek, "xy") for t in (t0, t1)]
+            else:
+                phi = [grid.ifft(ekk * grid.fft(t)) for t in (t0, t1)]  # :80-81
             ntot = np.real(grid.integrate(phi[0] * np.conj(phi[0]) + phi[1] * np.conj(phi[1])))
             mu = math.sqrt(self.Ntotal / ntot)                           # :84-88
             MU.append(math.log(mu) / dt)
@@ -698,6 +726,7 @@ class GPEtaskSpinor(GPEtask):
                         break
                     dt = dt / 1.5
                     ekk = np.exp(-grid.kk * dt * 0.5)
+                    ek = self._rot_factors(dt) if rot else None
                     cosom = np.cosh(dt * abs(coupl))
                     sinomm = np.sinh(dt * abs(coupl)) * np.exp(-1j * cang)
                     sinomp = np.sinh(dt * abs(coupl)) * np.exp(1j * cang)
@@ -778,42 +807,53 @@ class GPEtask2comp(GPEtaskSpinor):
     """GPEtask2comp (lib/@GPEtask2comp/GPEtask2comp.m:1-150): an incoherent
     mixture, components normalised separately to N1 and N2, masses M1, M2 in
     the imaginary-time kinetic factors; applyham/get_energy are the spinor's
-    without coupling (GPEtask2comp.m:45-63, 94-106)."""
+    without coupling (GPEtask2comp.m:51-74, 107-118), the rotating frame
+    through lap(phi, omega)."""
 
     def __init__(self, grid, trappot):
         super().__init__(grid, trappot)
         self.N1 = self.N2 = 0.0
         self.M1 = self.M2 = 1.0
 
-    # GPEtask2comp.m:45-63 (the spinor's with coupling = 0)
+    # GPEtask2comp.m:51-64: no coupling; the rotating frame enters through
+    # lap(phi, omega) (:60), not through lz
     def applyham1c(self, phi, j, time=None):
         if time is None:
             time = self.current_time
         res = self.getVtotal(time)[j]
         for k in range(self.ncomp):
             res = res + self.g[j, k] * np.abs(phi[k]) ** 2
-        return res * phi[j] + self.grid.lap(phi[j])
+        return res * phi[j] + self.grid.lap(phi[j], self.omega)
 
-    # lib/@GPEtask2comp/groundstate_itp.m:1-129 (omega == 0)
+    # lib/@GPEtask2comp/groundstate_itp.m:1-157 (scalar omega: the x/y half
+    # steps of :31-36, 61-80 with each component's mass)
     def groundstate_itp(self, dt, eps, phi, nargout=4, max_iter=500000):
         """Returns (phi, MU1, MU2, EE); EE = get_energy/Ntotal when nargout >= 4,
-        else MU2 (:71-75); the returned arrays drop the last iteration."""
+        else MU2 (:98-102); the returned arrays drop the last iteration (:143-154)."""
         grid = self.grid
         VV = self.getVtotal(0)
         g = self.g
         phi = [np.asarray(p, dtype=np.complex128) for p in phi]
-        ekk1 = np.exp(-grid.kk * dt * 0.5 / self.M1)                    # :11-12
+        ekk1 = np.exp(-grid.kk * dt * 0.5 / self.M1)                    # :29-30
         ekk2 = np.exp(-grid.kk * dt * 0.5 / self.M2)
+        rot = self.omega != 0
+        ek = (self._rot_factors(dt, self.M1), self._rot_factors(dt, self.M2)) if rot else None
         MU1, MU2, EE = [], [], []
         i = 1
         iswitch = 20
         while True:
-            t1 = VV[0] + g[0, 0] * np.abs(phi[0]) ** 2 + g[0, 1] * np.abs(phi[1]) ** 2   # :30-31
+            t1 = VV[0] + g[0, 0] * np.abs(phi[0]) ** 2 + g[0, 1] * np.abs(phi[1]) ** 2   # :58-59
             t2 = VV[1] + g[1, 0] * np.abs(phi[0]) ** 2 + g[1, 1] * np.abs(phi[1]) ** 2
-            phi = [grid.ifft(ekk1 * grid.fft(phi[0])), grid.ifft(ekk2 * grid.fft(phi[1]))]  # :39-40
-            phi = [np.exp(-t1 * dt) * phi[0], np.exp(-t2 * dt) * phi[1]]                # :42-43
-            phi = [grid.ifft(ekk1 * grid.fft(phi[0])), grid.ifft(ekk2 * grid.fft(phi[1]))]  # :51-52
-            n1c = np.real(grid.integrate(phi[0] * np.conj(phi[0])))                      # :55-58
+            if rot:                                                                     # :61-65
+                phi = [self._rot_half(phi[0], ek[0], "xy"), self._rot_half(phi[1], ek[1], "xy")]
+            else:                                                                       # :67-68
+                phi = [grid.ifft(ekk1 * grid.fft(phi[0])), grid.ifft(ekk2 * grid.fft(phi[1]))]
+            phi = [np.exp(-t1 * dt) * phi[0], np.exp(-t2 * dt) * phi[1]]                # :70-71
+            if rot:                                                                     # :72-76
+                phi = [self._rot_half(phi[0], ek[0], "yx"), self._rot_half(phi[1], ek[1], "yx")]
+            else:                                                                       # :78-79
+                phi = [grid.ifft(ekk1 * grid.fft(phi[0])), grid.ifft(ekk2 * grid.fft(phi[1]))]
+            n1c = np.real(grid.integrate(phi[0] * np.conj(phi[0])))                      # :82-90
             n2c = np.real(grid.integrate(phi[1] * np.conj(phi[1])))
             mu1 = math.sqrt(self.N1 / n1c)
             mu2 = math.sqrt(self.N2 / n2c)
@@ -821,8 +861,8 @@ class GPEtask2comp(GPEtaskSpinor):
             MU2.append(math.log(mu2) / dt)
             phi = [phi[0] * mu1, phi[1] * mu2]
             self.current_state = phi
-            EE.append(self.get_energy(phi) / self.Ntotal if nargout >= 4 else MU2[-1])  # :67-71
-            if (i - iswitch) > 10 and i % 10 == 0:                                      # :72-92
+            EE.append(self.get_energy(phi) / self.Ntotal if nargout >= 4 else MU2[-1])  # :98-102
+            if (i - iswitch) > 10 and i % 10 == 0:                                      # :113-135
                 delta = (abs(EE[i - 1] - EE[i - 10]) / 9 + abs(EE[i - 1] - EE[i - 2])) / dt
                 if delta < eps:
                     if dt < eps or dt < 5e-6:
@@ -830,6 +870,8 @@ class GPEtask2comp(GPEtaskSpinor):
                     dt = dt / 1.5
                     ekk1 = np.exp(-grid.kk * dt * 0.5 / self.M1)
                     ekk2 = np.exp(-grid.kk * dt * 0.5 / self.M2)
+                    if rot:
+                        ek = (self._rot_factors(dt, self.M1), self._rot_factors(dt, self.M2))
                     iswitch = i
             if i >= max_iter:
                 warnings.warn("Convergence not reached")

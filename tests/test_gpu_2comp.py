@@ -9,7 +9,8 @@ lib/@GPEtask2comp/groundstate_itp.m:1-157) through the C ABI
   (one launch per component with its own exp(-kk dt/2/M_j) tables);
 * nargout = 2, where the convergence test runs on MU2 instead of EE;
 * FP32 reaches the FP64 ground-state energy;
-* the error statuses (coupling set, omega set, a one-component context).
+* the rotating branch (scalar omega, 2D) with equal and unequal masses;
+* the error statuses (coupling set, omega in 3D, a one-component context).
 """
 import ctypes as C
 
@@ -93,10 +94,6 @@ def test_2comp_error_statuses(gpe):
     with pytest.raises(ValueError):
         task.groundstate_itp(0.02, 1e-5, p0)
     task.coupling = 0.0
-    task.omega = 0.3
-    with pytest.raises(gpe.GPEError) as e:
-        task.groundstate_itp(0.02, 1e-5, p0)
-    assert e.value.status == L.GPE_ERR_UNSUPPORTED
     one = gpe.GPEtask(gpe.grid2d(4.0, 32, 3.5, 24), lambda X, Y, Z: 0 * X)
     one.init_state = np.ones(one.grid.shape, complex)
     one._push_params()
@@ -108,3 +105,30 @@ def test_2comp_error_statuses(gpe):
     st = L.lib.gpe_groundstate_itp_2comp(one._ctx, C.byref(prm), 1.0, 1.0, 1.0, 1.0, None, None, None, 0,
                                          C.byref(res))
     assert st == L.GPE_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("masses", [(1.0, 1.0), (1.0, 2.5)], ids=["equal_mass", "unequal_mass"])
+def test_2comp_rotating_itp_matches_oracle(gpe, masses):
+    """The rotating branch of GPEtask2comp.groundstate_itp (groundstate_itp.m:
+    31-36, 61-80, 2D): x then y half steps before the nonlinear factor, y then
+    x after it, each with its component's mass; EE from lap(phi, omega)
+    (GPEtask2comp.m:60).  FP64 against the oracle, iteration for iteration."""
+    task, og, ot, p0 = make_pair(gpe, (4.0, 32, 3.5, 24), "double", M1=masses[0], M2=masses[1], omega=0.3)
+    X = og.mesh["x"]
+    p0 = [p0[0] * np.exp(0.25j * X), p0[1]]
+    phi, MU1, MU2, EE = task.groundstate_itp(0.02, 1e-5, p0, nargout=4)
+    ophi, oMU1, oMU2, oEE = ot.groundstate_itp(0.02, 1e-5, p0, nargout=4)
+    assert len(MU1) == len(oMU1) > 20
+    np.testing.assert_allclose(MU1, oMU1, rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(MU2, oMU2, rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(EE, oEE, rtol=1e-10)
+    assert rel_l2(phi, ophi) < 1e-10
+
+
+def test_2comp_rotating_itp_3d_is_refused(gpe):
+    from gpe_gb300 import _lib as L
+
+    task, og, ot, p0 = make_pair(gpe, (4.0, 24, 3.5, 16, 3.0, 16), "double", omega=0.3)
+    with pytest.raises(gpe.GPEError) as e:
+        task.groundstate_itp(0.02, 1e-5, p0)
+    assert e.value.status == L.GPE_ERR_UNSUPPORTED

@@ -165,3 +165,34 @@ def test_spinor_itp_fp32_reaches_the_fp64_energy(gpe):
     # the two runs may stop at different dt levels (FP32 noise in the test on
     # EE); the ground-state energy agrees to the splitting error there
     assert EE[-1] == pytest.approx(oEE[-1], rel=1e-5)
+
+
+@pytest.mark.parametrize("nargout", [4, 3])
+def test_spinor_rotating_itp_matches_oracle(gpe, nargout):
+    """The rotating branch of GPEtaskSpinor.groundstate_itp (groundstate_itp.m:
+    30-33, 61-80, 2D): x then y half-step factors with the kx*y*omega and
+    ky*x*omega terms on both sides of the nonlinear + coupling factor; MU2 and
+    EE add -omega <psi|lz psi> with grid1d's stencil (GPEtaskSpinor.m:72-74).
+    FP64 against the oracle, iteration for iteration."""
+    task, og, ot = make_pair(gpe, (4.0, 32, 3.5, 24), "double", g=G, coupling=-0.3 + 0.1j, Ntotal=3.0,
+                             omega=0.35)
+    X, Y = og.mesh["x"], og.mesh["y"]
+    p0 = [(np.exp(-(X ** 2 + Y ** 2) / 2) * np.exp(0.3j * X)).astype(complex),
+          (0.7 * np.exp(-((X - 0.3) ** 2 + Y ** 2) / 2) * np.exp(-0.2j * Y)).astype(complex)]
+    out = task.groundstate_itp(0.02, 1e-5, p0, nargout=nargout)
+    ref = ot.groundstate_itp(0.02, 1e-5, p0, nargout=nargout)
+    assert len(out[1]) == len(ref[1]) > 20
+    np.testing.assert_allclose(out[1], ref[1], rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(out[2], ref[2], rtol=1e-10)
+    if nargout == 4:
+        np.testing.assert_allclose(out[3], ref[3], rtol=1e-10)
+    assert rel_l2(out[0], ref[0]) < 1e-10
+
+
+def test_spinor_rotating_itp_3d_is_refused(gpe):
+    from gpe_gb300 import _lib as L
+
+    task, og, ot = make_pair(gpe, AXES[1], "double", g=G, Ntotal=1.0, omega=0.3)
+    with pytest.raises(gpe.GPEError) as e:
+        task.groundstate_itp(0.02, 1e-5, task.init_state)
+    assert e.value.status == L.GPE_ERR_UNSUPPORTED

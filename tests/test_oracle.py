@@ -425,3 +425,50 @@ def test_two_component_itp_known_answers():
     # for a Gaussian of width set by M_j; compare against the direct sum
     E = sum(np.real(g.inner(p, g.lap(p) + V(X, Y, 0) * p)) for p in phi) / 4.0
     assert EE[-1] == pytest.approx(E, rel=1e-10)
+
+
+@pytest.mark.parametrize("cls", ["spinor", "2comp"])
+def test_rotating_two_component_itp_reduces_to_the_plain_one(cls):
+    """The rotating branches of the two-component ITPs
+    (GPEtaskSpinor/groundstate_itp.m:30-33, GPEtask2comp/groundstate_itp.m:31-36)
+    with a vanishing omega: the x and y half-step factors then multiply to
+    exp(-kk dt/2/M) exactly (the 1D transforms along x and y commute), so the
+    run matches the omega = 0 branch iteration for iteration."""
+    g = O.Grid(4.0, 32, 3.5, 24)
+    V = [lambda X, Y, Z: 0.5 * (X ** 2 + 1.3 * Y ** 2)] * 2
+    X, Y = g.mesh["x"], g.mesh["y"]
+    p0 = [np.exp(-((X - 0.3) ** 2 + Y ** 2) / 2).astype(complex), 0.6 * np.exp(-(X ** 2 + Y ** 2) / 3).astype(complex)]
+    out = []
+    for om in (0.0, 1e-300):
+        t = O.GPEtaskSpinor(g, V) if cls == "spinor" else O.GPEtask2comp(g, V)
+        t.g = np.array([[1.0, 0.5], [0.5, 0.8]])
+        t.Ntotal = 3.0
+        if cls == "spinor":
+            t.coupling = 0.2
+        else:
+            t.N1, t.N2, t.M1, t.M2 = 2.0, 1.0, 1.0, 1.7
+        t.omega = om
+        out.append(t.groundstate_itp(0.02, 1e-4, p0, nargout=4))
+    (a, *ha), (b, *hb) = out
+    assert len(ha[0]) == len(hb[0])
+    for x, y in zip(ha, hb):
+        np.testing.assert_allclose(x, y, rtol=1e-10, atol=1e-12)
+    for x, y in zip(a, b):
+        np.testing.assert_allclose(x, y, rtol=1e-10, atol=1e-12)
+
+
+def test_rotating_2comp_energy_is_the_rotating_frame_laplacian():
+    """GPEtask2comp.get_energy with omega (GPEtask2comp.m:60, grid2d/lap.m:8-10):
+    for a state that is a function of r only (Lz psi = 0), the rotating terms
+    cancel in <psi|lap(psi, omega)>, and the energy equals the omega = 0 one."""
+    g = O.Grid(6.0, 48, 6.0, 48)
+    X, Y = g.mesh["x"], g.mesh["y"]
+    p = [np.exp(-(X ** 2 + Y ** 2) / 3).astype(complex), 0.5 * np.exp(-(X ** 2 + Y ** 2) / 2).astype(complex)]
+    V = [lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2)] * 2
+    e = []
+    for om in (0.0, 0.4):
+        t = O.GPEtask2comp(g, V)
+        t.g = np.array([[1.0, 0.5], [0.5, 0.8]])
+        t.omega = om
+        e.append(t.get_energy(p))
+    assert e[1] == pytest.approx(e[0], rel=1e-10)
