@@ -2245,8 +2245,6 @@ gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
     return fail(c, GPE_ERR_INVALID, "omega is either a scalar (gpe_params.omega) or an array (gpe_set_omega_field)");
   c->err.clear();
   if (c->ncomp == 2) {
-    if (c->prm.omega != 0.0)
-      return fail(c, GPE_ERR_UNSUPPORTED, "solve_split (spinor): omega != 0 is not supported");
     if (c->prec == GPE_FP32) return spinor_split_impl<float>(c, prm);
     return spinor_split_impl<double>(c, prm);
   }
@@ -2362,7 +2360,6 @@ gpe_status gpe_observables(gpe_ctx* c, gpe_obs* o) {
   if (!o) return fail(c, GPE_ERR_INVALID, "null output");
   o->ecpl = 0.0;
   if (c->ncomp == 2) {
-    if (c->prm.omega != 0.0) return fail(c, GPE_ERR_UNSUPPORTED, "observables (spinor): omega != 0");
     if (c->prec == GPE_FP32) return spinor_observables<float>(c, o);
     return spinor_observables<double>(c, o);
   }

@@ -39,6 +39,26 @@ SpinorNL<R> spinor_nl_consts(const gpe_ctx* c, double dre, double dim) {
   return q;
 }
 
+// GPEtaskSpinor's rotating frame outside the ITP's kinetic factors: its
+// solve_split steps with the plain kinetic factor (solve_split.m:42-44 have no
+// omega) and its applyham adds -omega lz with grid1d's stencil
+// (GPEtaskSpinor.m:72-74).  While one is alive the kinetic tables and the
+// energy passes of a context with scalar omega follow those rules.
+struct SpinorOmegaScope {
+  gpe_ctx* c;
+  bool adi_off, lz_scalar;
+  explicit SpinorOmegaScope(gpe_ctx* ctx) : c(ctx), adi_off(ctx->adi_off), lz_scalar(ctx->lz_scalar) {
+    if (c->prm.omega != 0.0) {
+      c->adi_off = true;
+      c->lz_scalar = true;
+    }
+  }
+  ~SpinorOmegaScope() {
+    c->adi_off = adi_off;
+    c->lz_scalar = lz_scalar;
+  }
+};
+
 // Kinetic sums over both components, the spinor sums against Vsum and the
 // finalizer in `mode` (0 run start, 1 block end, 2 observables).
 template <typename R>
@@ -116,6 +136,7 @@ gpe_status spinor_split_impl(gpe_ctx* c, const gpe_split_params* prm) {
   const int start = c->cur.current_iter, nout = prm->niter_outer;
   const std::complex<double> dtc = ddt * std::complex<double>(0.0, 1.0) / std::complex<double>(1.0, gam);  // :41
   const double dre = dtc.real(), dim = dtc.imag();
+  SpinorOmegaScope scope(c);  // omega: plain kinetic factors, mu with -omega lz
   CHECK(set_kinop<R>(c, f, dre, dim));
   CHECK(materialize<R>(c));
   launch_reset_scalars(c->sc, c->stream);
@@ -208,6 +229,7 @@ gpe_status spinor_split_impl(gpe_ctx* c, const gpe_split_params* prm) {
 // applyham / get_energy pieces of both components at the current V.
 template <typename R>
 gpe_status spinor_observables(gpe_ctx* c, gpe_obs* o) {
+  SpinorOmegaScope scope(c);  // -omega lz inside ekin
   CHECK(materialize<R>(c));
   launch_reset_scalars(c->sc, c->stream);
   double* obs = c->spin_part + (size_t)SP_NSUMS * 8 * c->sms;
@@ -262,18 +284,7 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
   // then the y factor, on both sides of the nonlinear factor; energies use
   // lap without omega plus -omega lz with grid1d's stencil (GPEtaskSpinor.m:72-74).
   const bool rot = c->prm.omega != 0.0;
-  struct Flags {
-    gpe_ctx* c;
-    bool adi_off, lz_scalar;
-    ~Flags() {
-      c->adi_off = adi_off;
-      c->lz_scalar = lz_scalar;
-    }
-  } flags{c, c->adi_off, c->lz_scalar};
-  if (rot) {
-    c->adi_off = true;
-    c->lz_scalar = true;
-  }
+  SpinorOmegaScope scope(c);
   auto set_tables = [&](double h) -> gpe_status {
     if (rot) return rot_half_tables<R>(c, f, 0.5 * h, f.rth[0]);
     return set_kinop<R>(c, f, h, 0.0);

@@ -457,7 +457,9 @@ class GPEtaskSpinor(GPEtask):
     (one context holding both components); ``Vtd`` is a callable added to
     both potentials or a pair of callables (GPEtaskSpinor.m:23-42).
     groundstate_itp is the spinor's own (groundstate_itp.m, with its rotating
-    branch for a scalar omega on 2D grids); elsewhere omega must be 0."""
+    branch for a scalar omega on 2D grids); solve_split and the observables
+    take a scalar omega as GPEtaskSpinor does (plain kinetic step, -omega lz
+    in mu and the energies)."""
 
     def __init__(self, grid: _GridBase, trappot, device: int = 0):
         self.grid = grid
@@ -658,6 +660,20 @@ class GPEtask2comp(GPEtaskSpinor):
         self.N2 = 0.0
         self.M1 = 1.0
         self.M2 = 1.0
+
+    def _plain_frame_only(self, what):
+        if np.size(self.omega) != 1 or float(np.asarray(self.omega).ravel()[0]) != 0.0:
+            raise NotImplementedError(
+                f"GPEtask2comp.{what} with omega != 0: its applyham takes lap(phi, omega) (GPEtask2comp.m:60), "
+                "which the library evaluates only inside groundstate_itp")
+
+    def solve_split(self, ddt, niter_inner, niter_outer):
+        self._plain_frame_only("solve_split")
+        return super().solve_split(ddt, niter_inner, niter_outer)
+
+    def observables(self, phi=None):
+        self._plain_frame_only("observables")
+        return super().observables(phi)
 
     def groundstate_itp(self, dt, eps, phi0=None, nargout=1, rng=None):
         """lib/@GPEtask2comp/groundstate_itp.m:1-157 on the GPU (a scalar

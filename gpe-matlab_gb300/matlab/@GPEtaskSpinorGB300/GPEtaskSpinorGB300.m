@@ -6,8 +6,8 @@ classdef GPEtaskSpinorGB300 < GPEtaskSpinor
     % GPEtaskSpinor(grid, {V1, V2}); g (2x2), coupling, nlincpl, gamma,
     % decay_rate, Ntotal, n_recalc, Vtd, init_state/current_state ({phi1,
     % phi2}), history and user_callback keep their meaning; solve_split,
-    % groundstate_itp and get_energy run on the GPU.  omega must be 0 except
-    % in groundstate_itp on 2D grids (its rotating branch).
+    % groundstate_itp and get_energy run on the GPU, with a scalar omega
+    % (groundstate_itp: its rotating branch, 2D grids).
     % Single-precision grid axes run the step in complex FP32.
     %
     % UNVERIFIED: no MATLAB was available where this file was written; the
@@ -115,13 +115,9 @@ classdef GPEtaskSpinorGB300 < GPEtaskSpinor
     end
 
     methods (Access = protected)
-        function gb300_push(task, itp)
-            % itp: groundstate_itp, whose rotating branch takes a scalar omega
-            if nargin < 2
-                itp = false;
-            end
-            if ~isscalar(task.omega) || (task.omega ~= 0 && ~itp)
-                error('gpe:omega', 'libgpe runs GPEtaskSpinor with omega = 0 outside groundstate_itp');
+        function gb300_push(task, ~)
+            if ~isscalar(task.omega)
+                error('gpe:omega', 'libgpe runs GPEtaskSpinor with a scalar omega');
             end
             % the spinor ITP's own iteration cap (groundstate_itp.m:123) in place of itp_max_iter
             gpe_mex('set_params', task.gb300_handle, 0, task.gamma, task.decay_rate, ...

@@ -171,9 +171,8 @@ typedef struct {
 
 /* Coherently coupled two-component condensate, lib/@GPEtaskSpinor
  * (GPEtaskSpinor.m:4-8; solve_split.m:61-91).  The other properties
- * (gamma, decay_rate, Ntotal, n_recalc; omega, which only the imaginary-time
- * solvers on 2D grids take) come from gpe_set_params, whose g is not used by
- * a spinor context. */
+ * (gamma, decay_rate, Ntotal, n_recalc, scalar omega) come from
+ * gpe_set_params, whose g is not used by a spinor context. */
 typedef struct {
     double g[4];            /* interaction matrix g(j,k) at g[2*(j-1)+(k-1)]     */
     double coupling_re;     /* coupling (Rabi frequency), complex      [0]       */
@@ -196,8 +195,13 @@ GPE_API gpe_status gpe_create(const gpe_grid_desc *desc, gpe_ctx **out);
  * potential and Vtd buffers hold both components, component 1 then 2
  * (2*nx*ny*nz points: MATLAB's {phi1, phi2} / {V1, V2} concatenated);
  * gpe_solve_split runs GPEtaskSpinor.solve_split and gpe_observables its
- * applyham/get_energy.  ITP, the adjoint, SGPE, batching and the autotuner
- * return GPE_ERR_UNSUPPORTED on it. */
+ * applyham/get_energy, gpe_groundstate_itp its groundstate_itp and
+ * gpe_groundstate_itp_2comp GPEtask2comp's.  Scalar omega follows
+ * GPEtaskSpinor: solve_split keeps the plain kinetic factor (its
+ * solve_split.m has no omega) and mu / the observables add -omega <psi|lz psi>
+ * with grid1d's stencil (GPEtaskSpinor.m:72-74).  The adjoint, SGPE,
+ * batching, the autotuner, gpe_set_omega_field and gpe_groundstate_tf return
+ * GPE_ERR_UNSUPPORTED on it. */
 GPE_API gpe_status gpe_create_spinor(const gpe_grid_desc *desc, gpe_ctx **out);
 /* Array omega (GPEtask.omega as an array, ssft_kin_step.m:3-11,
  * set_kinop.m:3-4, GPEtask.m:92-94): omega per grid point (nx*ny*nz doubles,

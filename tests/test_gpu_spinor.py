@@ -125,10 +125,6 @@ def test_spinor_error_statuses(gpe):
     with pytest.raises(gpe.GPEError) as e:
         task.solve_split(0.004, 5, 1)        # floor(5/10) = 0 blocks (solve_split.m:66)
     assert e.value.status == L.GPE_ERR_INVALID
-    task.omega = 0.4
-    with pytest.raises(gpe.GPEError) as e:
-        task.solve_split(0.004, 10, 1)
-    assert e.value.status == L.GPE_ERR_UNSUPPORTED
     ch = (C.c_int * 3)()
     assert L.lib.gpe_autotune(task._ctx, 1, ch) == L.GPE_ERR_UNSUPPORTED
 
@@ -196,3 +192,36 @@ def test_spinor_rotating_itp_3d_is_refused(gpe):
     with pytest.raises(gpe.GPEError) as e:
         task.groundstate_itp(0.02, 1e-5, task.init_state)
     assert e.value.status == L.GPE_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("axes", AXES, ids=["2d", "3d"])
+@pytest.mark.parametrize("precision", ["double", "single"])
+def test_spinor_split_with_omega_matches_oracle(gpe, axes, precision):
+    """GPEtaskSpinor.solve_split with a scalar omega: the step keeps the plain
+    kinetic factor (solve_split.m has no omega) while mu = <psi|H psi>/N adds
+    -omega <psi|lz psi> with grid1d's stencil (GPEtaskSpinor.m:72-74), which
+    feeds back into the step through mu when gamma > 0."""
+    task, og, ot = make_pair(gpe, axes, precision, g=G, coupling=0.4, gamma=0.02, Ntotal=2.0, n_recalc=5,
+                             omega=0.3)
+    task.solve_split(0.004, 10, 2)
+    ot.solve_split(0.004, 10, 2)
+    tol = 1e-11 if precision == "double" else 2e-5
+    assert rel_l2(task.current_state, ot.current_state) < tol
+    np.testing.assert_allclose(task.history["mu"], np.real(ot.history["mu"]), rtol=10 * tol)
+    # the Lz term is visible in mu: the same run without it differs
+    phi = ot.current_state
+    mu_lz = np.real(ot.inner(phi, ot.applyham(phi))) / 2.0
+    ot.omega = 0.0
+    mu_plain = np.real(ot.inner(phi, ot.applyham(phi))) / 2.0
+    assert abs(mu_lz - mu_plain) > 1e-3 * abs(mu_lz)
+
+
+@pytest.mark.parametrize("precision", ["double", "single"])
+def test_spinor_energy_with_omega_matches_oracle(gpe, precision):
+    task, og, ot = make_pair(gpe, AXES[0], precision, g=G, coupling=0.5 + 0.3j, omega=0.45)
+    X = og.mesh["x"]
+    phi = [ot.init_state[0] * np.exp(0.4j * og.mesh["y"]), ot.init_state[1] * np.exp(-0.3j * X)]
+    obs = task.observables(phi)
+    tol = 1e-11 if precision == "double" else 2e-6
+    assert obs["energy"] == pytest.approx(ot.get_energy(phi), rel=tol)
+    assert obs["mu_integral"] == pytest.approx(np.real(ot.inner(phi, ot.applyham(phi))), rel=tol)

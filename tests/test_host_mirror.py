@@ -167,3 +167,16 @@ def test_two_component_itp_passes_particle_numbers_and_masses(fake):
     t.coupling = 0.1
     with pytest.raises(ValueError):
         t.groundstate_itp(0.01, 1e-6, [np.ones(grid.shape, complex)] * 2)
+
+
+def test_two_component_observables_and_split_refuse_a_rotating_frame(fake):
+    import gpe_gb300 as gpe
+
+    grid = gpe.grid2d(4.0, 16, 3.0, 8)
+    t = gpe.GPEtask2comp(grid, [lambda X, Y, Z: 0 * X, lambda X, Y, Z: 0 * X])
+    t.omega = 0.2
+    with pytest.raises(NotImplementedError):
+        t.observables([np.ones(grid.shape, complex)] * 2)
+    with pytest.raises(NotImplementedError):
+        t.solve_split(0.01, 10, 1)
+    assert "gpe_observables" not in fake.names() and "gpe_solve_split" not in fake.names()
