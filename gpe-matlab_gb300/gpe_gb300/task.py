@@ -293,8 +293,7 @@ class GPEtask:
 
         def _step(user, step, time, mu, n):
             try:
-                self._ext_callback(step, time, mu, n)
-                return 0
+                return 1 if self._ext_callback(step, time, mu, n) else 0  # nonzero: end the run here
             except BaseException as e:
                 errors.append(e)
                 return 1
@@ -333,7 +332,9 @@ class GPEtask:
         self.history["mu"], self.history["n"], self.history["energy"] = mu, nn, ee
 
     def _ext_callback(self, step, time, mu, n):
-        """GPEtask.m:115-142 (plot and console line omitted)."""
+        """GPEtask.m:115-142 (plot and console line omitted).  Returns True to
+        end the run after this outer step; GPEtask.solve_split ignores the
+        callback's result (solve_split.m:80)."""
         self.current_time = time
         self.current_iter = step
         self.current_mu = mu
@@ -343,6 +344,7 @@ class GPEtask:
         self._sync_history()
         if callable(self.user_callback):
             self.user_callback(self)
+        return False
 
     def observables(self, phi=None):
         """<psi|H psi> pieces of psi (default: the current device state)."""
@@ -438,6 +440,19 @@ class SGPEtask(GPEtask):
         self.T = 0.0
         self.ecut = 0.0
         self.seed = 0
+
+    def _ext_callback(self, step, time, mu, n):
+        """SGPEtask.m:20-44: as GPEtask's, and a user_callback that returns
+        'TERM' ends the run after this outer step (solve_split.m:77-80)."""
+        self.current_time = time
+        self.current_iter = step
+        self.current_mu = mu
+        self.current_n = n
+        self._current_state = None
+        self._state_on_device = "current"
+        self._sync_history()
+        res = self.user_callback(self) if callable(self.user_callback) else None
+        return isinstance(res, str) and res == "TERM"
 
     def solve_split(self, ddt, niter_inner, niter_outer):
         """lib/@SGPEtask/solve_split.m:1-81."""

@@ -101,10 +101,12 @@ classdef GPEtaskGB300 < GPEtask
             V = double(gather(task.getVtotal(time)));
         end
 
-        function gb300_step(task, step, time, mu, n)
-            % Called by the gateway after each outer step (solve_split.m:80).
+        function stop = gb300_step(task, step, time, mu, n)
+            % Called by the gateway after each outer step (solve_split.m:80);
+            % GPEtask ignores the callback's return, so the run never stops here.
             phi = task.gb300_state();
             task.ext_callback(phi, step, time, mu, n);
+            stop = 0;
         end
 
         function [loss, dLdV] = adjoint_grad(task, target, ddt, nsteps, phi0, K, budget, fp64)

@@ -92,9 +92,10 @@ classdef GPEtaskSpinorGB300 < GPEtaskSpinor
             V = double(gather([v{1}(:); v{2}(:)]));
         end
 
-        function gb300_step(task, step, time, mu, n)
-            % Called by the gateway after each outer step (solve_split.m:115).
+        function stop = gb300_step(task, step, time, mu, n)
+            % Called by the gateway after each outer step (solve_split.m:115); never stops the run.
             task.ext_callback(task.gb300_state(), step, time, mu, n);
+            stop = 0;
         end
 
         function E = get_energy(task, phi, time)

@@ -85,13 +85,20 @@ int vtd_cb(void* user, double time, double* V_out) {
   return rc;
 }
 
-// ext_callback bookkeeping in MATLAB (GPEtask.m:115-142).
+// ext_callback bookkeeping in MATLAB (GPEtask.m:115-142).  task.gb300_step
+// returns nonzero to end the run after this outer step (SGPEtask: the user
+// callback returned 'TERM', @SGPEtask/solve_split.m:77-80).
 int step_cb(void* user, int step, double time, double mu, double n) {
   SplitCtx* s = static_cast<SplitCtx*>(user);
   mxArray* in[5] = {const_cast<mxArray*>(s->task), mxCreateDoubleScalar(step), mxCreateDoubleScalar(time),
                     mxCreateDoubleScalar(mu), mxCreateDoubleScalar(n)};
-  const int rc = mexCallMATLAB(0, nullptr, 5, in, "gb300_step");
+  mxArray* out[1] = {nullptr};
+  int rc = mexCallMATLAB(1, out, 5, in, "gb300_step");
   for (int i = 1; i < 5; ++i) mxDestroyArray(in[i]);
+  if (rc == 0 && out[0]) {
+    if (mxGetNumberOfElements(out[0]) == 1 && mxGetScalar(out[0]) != 0.0) rc = 1;
+    mxDestroyArray(out[0]);
+  }
   return rc;
 }
 

@@ -276,8 +276,8 @@ class GPEtask:
         _set_hist(self.history["mu"], step, mu)
         self.current_n = n
         _set_hist(self.history["n"], step, n)
-        if callable(self.user_callback):
-            self.user_callback(self)
+        res = self.user_callback(self) if callable(self.user_callback) else ""
+        return res  # SGPEtask.m:33-43 returns the callback's text; GPEtask's callers ignore it
 
     # GPEtask.m:144-164
     def process_init_state(self, phi0, rng=None):
@@ -591,7 +591,9 @@ class SGPEtask(GPEtask):
                 phi = np.exp((VV - mu + g * phi * np.conj(phi)) * dt / 2) * phi  # :73
                 tmp2 = np.real(phi * np.conj(phi))
                 ncur = grid.integrate(tmp2)                              # :76
-            self.ext_callback(phi, j, time2, mu, ncur)                   # :78
+            err = self.ext_callback(phi, j, time2, mu, ncur)             # :77
+            if isinstance(err, str) and err == "TERM":                   # :78-80
+                break
         return phi
 
 

@@ -261,3 +261,26 @@ def test_rotating_sgpe_matches_oracle(gpe, precision, T):
     tol = 1e-11 if precision == "double" else 2e-5
     assert rel_l2(task.current_state, ot.current_state) < tol
     np.testing.assert_allclose(task.history["n"], ot.history["n"], rtol=tol)
+
+
+def test_sgpe_user_callback_term_ends_the_run(gpe):
+    """@SGPEtask/solve_split.m:77-80: a user_callback that returns 'TERM'
+    ends the run after that outer step (the library's on_step stop); the
+    state and history are those of the oracle stopped at the same step."""
+    task, og, ot = make_pair(gpe, (4.0, 48, 3.5, 32), "double", g=1.0, gamma=0.05, mu_init=1.7, T=0.0)
+    X, Y = og.mesh["x"], og.mesh["y"]
+    psi0 = (np.exp(-((X - 0.5) ** 2 + Y ** 2) / 2) * np.exp(0.3j * Y)).astype(complex)
+    cb = lambda t: "TERM" if t.current_iter == 2 else ""  # noqa: E731
+    for t in (task, ot):
+        t.init_state = psi0
+        t.user_callback = cb
+        t.solve_split(0.004, 10, 5)
+    assert task.current_iter == ot.current_iter == 2
+    assert len(task.history["n"]) == 2
+    assert rel_l2(task.current_state, ot.current_state) < 1e-11
+    # GPEtask ignores the callback's result (@GPEtask/solve_split.m:80)
+    plain = gpe.GPEtask(task.grid, lambda X, Y, Z: 0.5 * (X ** 2 + 1.2 * Y ** 2))
+    plain.init_state = psi0
+    plain.user_callback = cb
+    plain.solve_split(0.004, 10, 3)
+    assert plain.current_iter == 3

@@ -29,7 +29,7 @@ class FakeLib:
                     assert prm.vtd(None, 0.25, buf) == 0
                     self.vtd_values = np.ctypeslib.as_array(buf).copy()
                 if prm.on_step:
-                    prm.on_step(None, 1, 0.5, 1.5, 2.5)
+                    self.step_rc = prm.on_step(None, 1, 0.5, 1.5, 2.5)
             if name in ("gpe_get_history", "gpe_get_history_energy"):
                 args[-1]._obj.value = 0
             if name == "gpe_detect_core":
@@ -180,3 +180,18 @@ def test_two_component_observables_and_split_refuse_a_rotating_frame(fake):
     with pytest.raises(NotImplementedError):
         t.solve_split(0.01, 10, 1)
     assert "gpe_observables" not in fake.names() and "gpe_solve_split" not in fake.names()
+
+
+@pytest.mark.parametrize("cls,stops", [("SGPEtask", 1), ("GPEtask", 0)])
+def test_term_from_the_user_callback_stops_only_the_sgpe(fake, cls, stops):
+    """SGPEtask.solve_split ends the run when ext_callback returns 'TERM'
+    (@SGPEtask/solve_split.m:77-80, SGPEtask.m:33-43); GPEtask ignores the
+    callback's result (@GPEtask/solve_split.m:80)."""
+    import gpe_gb300 as gpe
+
+    grid = gpe.grid2d(4.0, 16, 3.0, 8)
+    t = getattr(gpe, cls)(grid, lambda X, Y, Z: 0 * X)
+    t.init_state = np.ones(grid.shape, complex)
+    t.user_callback = lambda task: "TERM"
+    t.solve_split(0.01, 10, 3)
+    assert fake.step_rc == stops
