@@ -107,6 +107,7 @@ struct gpe_ctx {
   int tune_mode = 2;      // FFT plan autotuner: 0 off, 1 explicit only, 2 on the first hot-path call
   bool tuned = false;     // the autotuner has set main.plan_var
   bool prof = false;
+  bool nvtx = false;      // GPE_NVTX=1: an NVTX range around every kernel launch, named by its class
   std::vector<gpe::ProfRec> prof_pending;
   std::vector<cudaEvent_t> ev_pool;
   std::vector<gpe::ProfClass> prof_classes;

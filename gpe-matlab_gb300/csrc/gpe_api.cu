@@ -20,6 +20,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "ctx.h"
 
 using namespace gpe;
@@ -341,12 +343,14 @@ struct Launch {
   cudaEvent_t a = nullptr;
   Launch(gpe_ctx* c_, int cls_, double bytes_) : c(c_), cls(cls_), bytes(bytes_) {
     c->launches++;
+    if (c->nvtx) nvtxRangePushA(kProfNames[cls]);
     if (c->prof) {
       a = pool_event(c);
       cudaEventRecord(a, c->stream);
     }
   }
   ~Launch() {
+    if (c->nvtx) nvtxRangePop();
     if (c->prof) {
       cudaEvent_t b = pool_event(c);
       cudaEventRecord(b, c->stream);
@@ -1901,6 +1905,8 @@ static gpe_status create_impl(const gpe_grid_desc* d, gpe_ctx** out, int ncomp) 
   if (c->sms <= 0) c->sms = 152;
   // GPE_PDL=0|1: launch the direct passes with programmatic dependent launch.
   if (const char* e = getenv("GPE_PDL")) c->pdl = atoi(e) != 0;
+  // GPE_NVTX=1: a host NVTX range (named by the kernel class) around every launch.
+  if (const char* e = getenv("GPE_NVTX")) c->nvtx = atoi(e) != 0;
   // GPE_AUTOTUNE=0|1|2 sets the initial autotuner mode (gpe_autotune) of new contexts.
   if (const char* e = getenv("GPE_AUTOTUNE")) {
     const int m = atoi(e);
