@@ -154,10 +154,14 @@ typedef struct {
     double current_n;
 } gpe_current;
 
-/* <psi|H psi> pieces, GPEtask.m:73-107 (omega = 0).  Spinor contexts
- * (GPEtaskSpinor.m:53-110): sums over both components, eint =
- * sum_jk g(j,k) integrate(|psi_j|^2 |psi_k|^2), ecpl = the coupling term
- * 2 Re(coupling * inner(psi_1, psi_2)); 0 for one component. */
+/* <psi|H psi> pieces, GPEtask.m:73-107.  With omega the rotating-frame term
+ * is part of ekin: scalar omega real(inner(psi, lap(psi, omega)))
+ * (lap.m:8-10), an omega array <psi|-omega lz psi> added to the kinetic sum
+ * (GPEtask.m:92-94).  Spinor contexts (GPEtaskSpinor.m:53-110): sums over
+ * both components, eint = sum_jk g(j,k) integrate(|psi_j|^2 |psi_k|^2), ecpl =
+ * the coupling term 2 Re(coupling * inner(psi_1, psi_2)) (0 for one
+ * component), and a scalar omega adds -omega <psi_j|lz psi_j> with grid1d's
+ * stencil to ekin (GPEtaskSpinor.m:72-74). */
 typedef struct {
     double norm;            /* integrate(|psi|^2)                                */
     double ekin;            /* real(inner(psi, lap(psi)))                        */
