@@ -93,11 +93,49 @@ def case_itp3d_adjust_16():
     return {"psi0": psi0, "phi": phi, "MU": MU, "MU2": MU2, "EE": EE}
 
 
+def _pair_start(g):
+    X, Y = g.mesh["x"], g.mesh["y"]
+    return [(np.exp(-((X - 0.4) ** 2 + Y ** 2) / 2) * np.exp(0.3j * Y)).astype(complex),
+            (0.6 * np.exp(-(X ** 2 + (Y + 0.3) ** 2) / 2.5) * np.exp(-0.2j * X)).astype(complex)]
+
+
+def case_spinor_split2d_32x24():
+    """GPEtaskSpinor.solve_split at 32x24: asymmetric g, complex coupling,
+    damping with decay, shifted second trap, 3 outer steps of 2 blocks."""
+    g = O.Grid(4.0, 32, 3.5, 24)
+    V1 = lambda X, Y, Z: 0.5 * (X ** 2 + 1.2 * Y ** 2)  # noqa: E731
+    V2 = lambda X, Y, Z: 0.5 * (X ** 2 + 1.2 * Y ** 2) + 0.3 * X  # noqa: E731
+    t = O.GPEtaskSpinor(g, [V1, V2])
+    t.g = np.array([[1.0, 0.7], [0.5, 0.8]])
+    t.coupling = 0.6 * np.exp(0.7j)
+    t.gamma, t.decay_rate, t.Ntotal, t.n_recalc = 0.05, 2.0, 3.0, 5
+    p0 = _pair_start(g)
+    t.init_state = p0
+    t.solve_split(0.004, 10, 3)
+    return {"psi0_1": p0[0], "psi0_2": p0[1], "psi_1": t.current_state[0], "psi_2": t.current_state[1],
+            "hist_mu": np.real(np.array(t.history["mu"])), "hist_n": np.array(t.history["n"])}
+
+
+def case_itp_2comp2d_32x24():
+    """GPEtask2comp.groundstate_itp at 32x24: N1 = 2, N2 = 1, masses 1 and
+    2.5, EE with Ntotal = 3."""
+    g = O.Grid(4.0, 32, 3.5, 24)
+    V = lambda X, Y, Z: 0.5 * (X ** 2 + 1.3 * Y ** 2)  # noqa: E731
+    t = O.GPEtask2comp(g, [V, V])
+    t.g = np.array([[1.0, 0.6], [0.6, 0.8]])
+    t.N1, t.N2, t.M1, t.M2, t.Ntotal = 2.0, 1.0, 1.0, 2.5, 3.0
+    p0 = _pair_start(g)
+    phi, MU1, MU2, EE = t.groundstate_itp(0.02, 1e-3, p0, nargout=4)
+    return {"psi0_1": p0[0], "psi0_2": p0[1], "phi_1": phi[0], "phi_2": phi[1], "MU1": MU1, "MU2": MU2, "EE": EE}
+
+
 CASES = {
     "itp_vortex2d_64": case_itp_vortex2d_64,
     "split_damped2d_48": case_split_damped2d_48,
     "split3d_24x32x16": case_split3d_24x32x16,
     "itp3d_adjust_16": case_itp3d_adjust_16,
+    "spinor_split2d_32x24": case_spinor_split2d_32x24,
+    "itp_2comp2d_32x24": case_itp_2comp2d_32x24,
 }
 
 

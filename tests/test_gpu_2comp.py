@@ -132,3 +132,22 @@ def test_2comp_rotating_itp_3d_is_refused(gpe):
     with pytest.raises(gpe.GPEError) as e:
         task.groundstate_itp(0.02, 1e-5, p0)
     assert e.value.status == L.GPE_ERR_UNSUPPORTED
+
+
+def test_2comp_itp_matches_the_golden_fixture(gpe):
+    """The committed fixture tests/golden/itp_2comp2d_32x24.npz (the FP64
+    oracle's GPEtask2comp.groundstate_itp on fixed inputs), FP64."""
+    from tests.golden import make_golden as MG
+
+    ref = np.load(MG.path("itp_2comp2d_32x24"))
+    grid = gpe.grid2d(4.0, 32, 3.5, 24, precision="double")
+    V = lambda X, Y, Z: 0.5 * (X ** 2 + 1.3 * Y ** 2)  # noqa: E731
+    task = gpe.GPEtask2comp(grid, [V, V])
+    task.g = np.array([[1.0, 0.6], [0.6, 0.8]])
+    task.N1, task.N2, task.M1, task.M2, task.Ntotal = 2.0, 1.0, 1.0, 2.5, 3.0
+    phi, MU1, MU2, EE = task.groundstate_itp(0.02, 1e-3, [ref["psi0_1"], ref["psi0_2"]], nargout=4)
+    assert len(MU1) == len(ref["MU1"])
+    np.testing.assert_allclose(MU1, ref["MU1"], rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(MU2, ref["MU2"], rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(EE, ref["EE"], rtol=1e-10)
+    assert rel_l2(phi, [ref["phi_1"], ref["phi_2"]]) < 1e-10

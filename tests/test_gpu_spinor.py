@@ -225,3 +225,22 @@ def test_spinor_energy_with_omega_matches_oracle(gpe, precision):
     tol = 1e-11 if precision == "double" else 2e-6
     assert obs["energy"] == pytest.approx(ot.get_energy(phi), rel=tol)
     assert obs["mu_integral"] == pytest.approx(np.real(ot.inner(phi, ot.applyham(phi))), rel=tol)
+
+
+def test_spinor_split_matches_the_golden_fixture(gpe):
+    """The committed fixture tests/golden/spinor_split2d_32x24.npz (the FP64
+    oracle's GPEtaskSpinor.solve_split on fixed inputs), FP64."""
+    from tests.golden import make_golden as MG
+
+    ref = np.load(MG.path("spinor_split2d_32x24"))
+    grid = gpe.grid2d(4.0, 32, 3.5, 24, precision="double")
+    task = gpe.GPEtaskSpinor(grid, [lambda X, Y, Z: 0.5 * (X ** 2 + 1.2 * Y ** 2),
+                                    lambda X, Y, Z: 0.5 * (X ** 2 + 1.2 * Y ** 2) + 0.3 * X])
+    task.g = np.array([[1.0, 0.7], [0.5, 0.8]])
+    task.coupling = 0.6 * np.exp(0.7j)
+    task.gamma, task.decay_rate, task.Ntotal, task.n_recalc = 0.05, 2.0, 3.0, 5
+    task.init_state = [ref["psi0_1"], ref["psi0_2"]]
+    task.solve_split(0.004, 10, 3)
+    assert rel_l2(task.current_state, [ref["psi_1"], ref["psi_2"]]) < 1e-11
+    np.testing.assert_allclose(task.history["mu"], ref["hist_mu"], rtol=1e-10)
+    np.testing.assert_allclose(task.history["n"], ref["hist_n"], rtol=1e-11)
