@@ -472,3 +472,28 @@ def test_rotating_2comp_energy_is_the_rotating_frame_laplacian():
         t.omega = om
         e.append(t.get_energy(p))
     assert e[1] == pytest.approx(e[0], rel=1e-10)
+
+
+def test_spinor_lz_energy_is_the_one_component_array_omega_term():
+    """GPEtaskSpinor.applyham with a scalar omega subtracts omega*lz(phi_j)
+    with grid1d's stencil (GPEtaskSpinor.m:72-74), the operator that
+    GPEtask.applyh0 applies for an omega array (GPEtask.m:92-94).  With the
+    coupling and g zero, the spinor's energy is therefore the sum of the two
+    one-component energies with a uniform omega array."""
+    g = O.Grid(4.0, 32, 3.5, 24)
+    X, Y = g.mesh["x"], g.mesh["y"]
+    V = [lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2), lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2) + 0.2 * X]
+    phi = [((X + 0.5j * Y) * np.exp(-(X ** 2 + Y ** 2) / 2)).astype(complex),
+           (np.exp(-(X ** 2 + Y ** 2) / 3) * np.exp(0.4j * Y)).astype(complex)]
+    s = O.GPEtaskSpinor(g, V)
+    s.g = np.zeros((2, 2))
+    s.omega = 0.35
+    e_sp = s.get_energy(phi)
+    e_one = 0.0
+    for j in range(2):
+        t = O.GPEtask(g, V[j])
+        t.omega = np.full(g.shape, 0.35)
+        e_one += t.get_energy(phi[j])
+    assert e_sp == pytest.approx(e_one, rel=1e-12)
+    s.omega = 0.0
+    assert abs(s.get_energy(phi) - e_sp) > 1e-3 * abs(e_sp)  # the term is not negligible here
