@@ -41,3 +41,33 @@ def test_vortex_imprint_matches_the_oracle():
     a = gpe.imprint_vortex(g, phi, 0.06, 5.0)
     b = O.imprint_vortex(o, phi, 0.06, 5.0)
     np.testing.assert_allclose(a, b, rtol=1e-14, atol=1e-14)
+
+
+def test_vortex_ring_imprint_winds_once_around_its_core():
+    """imprint_vortex_ring (the 512^3 workload's defect): the phase winds
+    once around the ring core in the (x, z) half plane y = 0, x > 0, the amplitude
+    vanishes on the core circle and is untouched far from it."""
+    import gpe_gb300 as gpe
+
+    g = gpe.grid3d(8.0, 32, 8.0, 32, 8.0, 32)
+    phi = np.ones(g.shape, complex)
+    R, xi = 4.0, 0.5
+    out = gpe.imprint_vortex_ring(g, phi, 1.0, R, xi=xi)
+    # the plaquette phase winding of the imprinted state in the y = 0 plane
+    # (x > 0 half) is +1 at the core and 0 elsewhere
+    iy0 = np.argmin(np.abs(g.y))
+    sl = out[:, :, iy0]  # (z, x)
+    a, b, c, e = sl[:-1, :-1], sl[:-1, 1:], sl[1:, 1:], sl[1:, :-1]
+    w = np.angle(b / a) + np.angle(c / b) + np.angle(e / c) + np.angle(a / e)
+    charges = np.rint(w / (2 * np.pi)).astype(int)
+    xs = g.x[:-1]
+    assert np.sum(np.abs(charges[:, xs > 0])) == 1
+    X, Y, Z = g.mesh["x"], g.mesh["y"], g.mesh["z"]
+    d = np.sqrt((np.sqrt(X ** 2 + Y ** 2) - R) ** 2 + Z ** 2)
+    assert np.all(np.abs(out[d < 0.05 * xi]) < 0.06)
+    far = d > 8 * xi
+    np.testing.assert_allclose(np.abs(out[far]), 1.0, atol=1e-6)
+    # the imprinted phase is atan2(Z, rho - R) (mod 2 pi) wherever the amplitude is not zero
+    ph = np.angle(out[far])
+    ref = np.arctan2(Z[far], np.sqrt(X[far] ** 2 + Y[far] ** 2) - R)
+    np.testing.assert_allclose(np.angle(np.exp(1j * (ph - ref))), 0.0, atol=1e-12)
