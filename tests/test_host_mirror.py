@@ -195,3 +195,17 @@ def test_term_from_the_user_callback_stops_only_the_sgpe(fake, cls, stops):
     t.user_callback = lambda task: "TERM"
     t.solve_split(0.01, 10, 3)
     assert fake.step_rc == stops
+
+
+def test_two_component_itp_pushes_a_scalar_omega(fake):
+    """The rotating branch of GPEtask2comp.groundstate_itp takes the scalar
+    omega through gpe_set_params (no omega array on a two-component context)."""
+    import gpe_gb300 as gpe
+
+    grid = gpe.grid2d(4.0, 16, 3.0, 8)
+    t = gpe.GPEtask2comp(grid, [lambda X, Y, Z: 0 * X, lambda X, Y, Z: 0 * X])
+    t.N1, t.N2, t.omega = 1.0, 1.0, 0.3
+    t.groundstate_itp(0.01, 1e-6, [np.ones(grid.shape, complex)] * 2)
+    assert fake.last("gpe_set_params")[1]._obj.omega == 0.3
+    assert fake.last("gpe_set_omega_field")[1] is None
+    assert fake.names().index("gpe_set_params") < fake.names().index("gpe_groundstate_itp_2comp")
