@@ -152,9 +152,11 @@ def ground_state(gpe, W, precision="single", device=0):
     return grid, task, phi
 
 
-def cpu_reference_steps(W, phi, steps: int, cores: int, max_seconds: float = 25.0):
-    """Times up to `steps` inner split steps (at most ~max_seconds) of the FP64
-    oracle (the restatement of the reference's solve_split)."""
+def oracle_task(W, phi, cores: int):
+    """The FP64 oracle's GPEtask (the restatement of the reference's solve_split)
+    on the workload's grid, potential and parameters, holding phi.  Built from
+    the oracle and the library-free workload tables only: nothing here loads
+    libgpe.so."""
     from oracle import gpe_oracle as O
 
     O.set_workers(cores)
@@ -163,28 +165,61 @@ def cpu_reference_steps(W, phi, steps: int, cores: int, max_seconds: float = 25.
     ot = O.GPEtask(og, W.potential())
     ot.Ntotal, ot.g, ot.gamma = W.Ntotal, W.g, W.gamma
     ot.init_state = np.asarray(phi, dtype=np.complex128)
+    return og, ot
+
+
+def cpu_reference_run(W, phi, cores: int, warm: int, samples: int, per_sample=None, budget_s: float = 150.0):
+    """Times the FP64 oracle's solve_split on the workload: `warm` untimed
+    samples, then `samples` timed samples of `per_sample` split steps each.
+    The clock starts after the warm-up samples, so solve_split's setup (the
+    kinetic table and the applyham of solve_split.m:41) and the first steps
+    are outside it.  per_sample None: chosen from the first split step's time
+    so that the whole run stays near budget_s (1 .. niter_inner steps).
+    Returns (grid-pt-steps/s, timed split steps, timed seconds, per_sample)."""
+    og, ot = oracle_task(W, phi, cores)
     stamps = []
+    plan = {"per": per_sample, "total": None}
 
     class Done(Exception):
         pass
 
-    def on_inner(i):
+    def on_inner(_j):
         stamps.append(time.perf_counter())
-        if len(stamps) > steps or stamps[-1] - t0 > max_seconds:
+        if plan["total"] is None:
+            if plan["per"] is None:
+                t1 = stamps[0] - t0  # one split step plus the setup
+                plan["per"] = int(max(1, min(W.niter_inner, budget_s / max(1, warm + samples) / t1)))
+            plan["total"] = (warm + samples) * plan["per"]
+        if len(stamps) >= plan["total"]:
             raise Done
 
     t0 = time.perf_counter()
     try:
-        ot.solve_split(W.dt, 10, 10 ** 6, inner_callback=on_inner)
+        ot.solve_split(W.dt, W.niter_inner, 10 ** 6, inner_callback=on_inner)
     except Done:
         pass
-    t_steps = stamps[-1] - t0 if stamps else float("nan")
-    n = len(stamps)
-    return W.npoints * n / t_steps, n, t_steps
+    per = plan["per"]
+    i0 = warm * per - 1
+    n = len(stamps) - 1 - i0
+    t = stamps[-1] - stamps[i0]
+    return W.npoints * n / t, n, t, per
+
+
+def workload_config(W):
+    """The workload's description, identical in both arms' JSON lines."""
+    return {"workload": W.name, "grid": list(W.n), "box": W.box[0], "trap_lambda": list(W.trap), "g": W.g,
+            "Ntotal": W.Ntotal, "dt": W.dt, "gamma": W.gamma, "niter_inner": W.niter_inner, "n_recalc": 10,
+            "l2": l2_note(W)}
 
 
 def run_reference(args, dist):
-    from gpe_gb300.workloads import WORKLOADS
+    """--impl reference: the FP64 oracle (the restatement of the reference's
+    solve_split; the reference itself is MATLAB, absent here) on the host
+    cores, on the same workload as the gb300 arm.  One bench step is a
+    bounded sample of split steps.  The grid, potential and start state come
+    from the oracle and the library-free workload tables: this arm never
+    loads libgpe.so."""
+    from gpe_workloads import WORKLOADS
 
     if dist.rank != 0:
         return
@@ -194,18 +229,24 @@ def run_reference(args, dist):
         return
     W = WORKLOADS[args.workload]
     cores = os.cpu_count() or 1
-    # Start state: the seeded Gaussian (the timed work does not depend on it).
-    grid = W.make_grid("double")
-    phi = W.initial_state(grid) * 10.0
-    val, n, t = cpu_reference_steps(W, phi, args.warmup + args.steps, cores, max_seconds=150.0)
+    from oracle import gpe_oracle as O
+
+    gargs = [v for pair in zip(W.box, W.n) for v in pair]
+    # Start state: the seeded Gaussian (the FFT/elementwise work per step does
+    # not depend on the state).
+    phi = W.initial_state(O.Grid(*gargs)) * 10.0
+    val, n, t, per = cpu_reference_run(W, phi, cores, args.warmup, args.steps)
     line = {
         "metric": METRIC, "value": val, "unit": UNIT, "impl": "reference", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t / max(n, 1), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": W.name, "grid": list(W.n), "dt": W.dt, "gamma": W.gamma, "step": "1 split step"},
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian start)",
+        "config": workload_config(W),
+        "step": f"a sample of {per} split steps of solve_split (of the gb300 arm's {W.niter_inner}-step outer "
+                f"step); value = grid points x split steps / s",
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{n} split steps of the {'x'.join(map(str, W.n))} FP64 oracle "
-                                   f"(numpy + scipy.fft, {cores} workers)"},
+                         "sample": f"{args.warmup} warm-up and {args.steps} timed samples of {per} split steps "
+                                   f"({n} timed) of the {'x'.join(map(str, W.n))} FP64 oracle solve_split "
+                                   f"(numpy + scipy.fft, {cores} workers); clock started after the warm-up"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -265,7 +306,7 @@ def e2e_abi(task, host_in, host_out, ddt, inner, steps):
 def run_gpu(args, dist):
     global INNER
     import gpe_gb300 as gpe
-    from gpe_gb300.workloads import WORKLOADS
+    from gpe_workloads import WORKLOADS
 
     W = WORKLOADS[args.workload]
     INNER = W.niter_inner
@@ -352,20 +393,20 @@ def run_gpu(args, dist):
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
         cores = os.cpu_count() or 1
-        cval, n, t = cpu_reference_steps(W, phi, args.cpu_steps, cores)
+        cval, n, t, _ = cpu_reference_run(W, phi, cores, 1, args.cpu_steps, per_sample=1)
         cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{n} split steps of the same {'x'.join(map(str, W.n))} workload in the FP64 "
-                         f"oracle (numpy + scipy.fft with {cores} workers), {t:.1f} s"}
+                         f"oracle (numpy + scipy.fft with {cores} workers), {t:.1f} s, after one untimed "
+                         f"step and the setup"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms.value / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 (FP64 reductions)", "data": "synthetic (seeded Gaussian -> ITP ground state)",
-        "config": {"workload": W.name, "grid": list(W.n), "box": W.box[0], "trap_lambda": list(W.trap), "g": W.g,
-                   "Ntotal": W.Ntotal, "dt": W.dt, "gamma": W.gamma, "step": f"{INNER} split steps (1 outer step)",
-                   "n_recalc": 10, "l2": l2_note(W),
-                   "fft_plans_xyz": {"chosen_by": "autotuner (0 default plan, 1 alternative, -1 single plan)",
-                                     "x": plans[0], "y": plans[1], "z": plans[2]},
-                   "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU"},
+        "config": workload_config(W),
+        "step": f"{INNER} split steps (1 outer step of solve_split)",
+        "fft_plans_xyz": {"chosen_by": "autotuner (0 default plan, 1 alternative, -1 single plan)",
+                          "x": plans[0], "y": plans[1], "z": plans[2]},
+        "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU",
         "fp64": {"value": value64, "unit": UNIT, "steps": INNER * k64, "ratio_fp32_over_fp64": value / dist.world / value64},
         "error": {"fp32_vs_fp64_rel_l2_after_outer_step": err_l2,
                   "mu_rel_after_outer_step": abs(mu32 - mu64) / abs(mu64),
@@ -397,7 +438,7 @@ def run_batch(args, dist):
 
     import gpe_gb300 as gpe
     from gpe_gb300 import _lib as L
-    from gpe_gb300.workloads import BATCH2D as B
+    from gpe_workloads import BATCH2D as B
 
     tasks = B.make_tasks("single", device=dist.local, rank=dist.rank, world=dist.world)  # realisations sharded
     P = sum(t.grid.npoints for t in tasks)
@@ -441,7 +482,7 @@ ADJ_METRIC = "adjoint grid-pt-steps/s (loss + dloss/dV through the window, per s
 def adjoint_case(gpe, name, dev):
     """(task, psi0, target, V, nsteps, checkpoint_every, basis, describe) of an adjoint workload."""
     if name == "adjoint2d_256":
-        from gpe_gb300.workloads import ADJOINT2D as W
+        from gpe_workloads import ADJOINT2D as W
 
         grid = W.make_grid("single")
         task = gpe.GPEtask(grid, lambda X, Y, Z: W.trap(grid), device=dev)
@@ -456,7 +497,7 @@ def adjoint_case(gpe, name, dev):
                "window_steps": W.steps, "checkpoint_every": W.checkpoint_every,
                "potential": "0.5 r^2 + 16 seeded Gaussian bumps", "target": f"vortex imprinted at x0 = {W.vortex_x0}"}
         return task, psi0, tgt, V, W.steps, W.checkpoint_every, basis, cfg
-    from gpe_gb300.workloads import RING3D as W
+    from gpe_workloads import RING3D as W
 
     grid, task, phi = ground_state(gpe, W, "single", device=dev)
     psi0 = np.asarray(imprint(gpe, W, grid, task, np.asarray(phi, dtype=np.complex128)))
@@ -542,9 +583,12 @@ def run_adjoint(args, dist):
 SPIN_METRIC = "spinor split-step grid-pt-steps/s (2 coupled components, complex FP32)"
 
 
-def spinor_cpu_steps(S, pair, cores: int):
-    """One outer step of 10 split steps (n_recalc 10) of the FP64 oracle's
-    GPEtaskSpinor.solve_split on the workload grid: (grid-pt-steps/s, steps, s)."""
+def spinor_cpu_steps(S, pair, cores: int, blocks: int = 1):
+    """`blocks` outer steps of 10 split steps (one n_recalc block each) of the
+    FP64 oracle's GPEtaskSpinor.solve_split on the workload grid, timed after
+    one untimed block (so the setup, kinetic tables and the applyham before
+    the loop, is outside the clock): (grid-pt-steps/s, steps, s).  Built from
+    the oracle and the library-free workload tables only."""
     from oracle import gpe_oracle as O
 
     O.set_workers(cores)
@@ -552,15 +596,36 @@ def spinor_cpu_steps(S, pair, cores: int):
     ot = O.GPEtaskSpinor(og, S.potentials())
     S.configure(ot)
     ot.init_state = [np.asarray(p, dtype=np.complex128) for p in pair]
-    t0 = time.perf_counter()
-    ot.solve_split(S.dt, 10, 1)
-    t = time.perf_counter() - t0
-    return S.npoints * 10 / t, 10, t
+    stamps = []
+
+    class Done(Exception):
+        pass
+
+    def on_outer(_task):
+        stamps.append(time.perf_counter())
+        if len(stamps) > blocks:
+            raise Done
+
+    ot.user_callback = on_outer
+    try:
+        ot.solve_split(S.dt, 10, 10 ** 6)
+    except Done:
+        pass
+    t = stamps[-1] - stamps[0]
+    return S.npoints * 10 * blocks / t, 10 * blocks, t
+
+
+def spinor_config(S):
+    """The spinor workload's description, identical in both arms."""
+    return {"workload": S.name, "grid": list(S.n), "components": 2, "box": S.box, "g": [list(r) for r in S.g],
+            "coupling": str(S.coupling), "Ntotal": S.Ntotal, "gamma": S.gamma, "dt": S.dt, "n_recalc": 10,
+            "l2": f"inputs larger than L2 (2 states + 2 V = {S.npoints * 24 / 1e6:.0f} MB > 129 MB L2)",
+            "points_counted": "grid points (each carries both components)"}
 
 
 def spinor_start(gpe, dev):
     """The damped workload's ITP ground state (untimed), split into the pair."""
-    from gpe_gb300.workloads import DAMPED3D as W, SPINOR3D as S
+    from gpe_workloads import DAMPED3D as W, SPINOR3D as S
 
     _, t1, phi = ground_state(gpe, W, "single", device=dev)
     phi = np.asarray(phi, dtype=np.complex128)
@@ -633,17 +698,13 @@ def run_spinor(args, dist):
         cval, n, t = spinor_cpu_steps(S, pair, cores)
         cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{n} split steps (one block) of the same 256^3 two-component workload in the FP64 "
-                         f"oracle (numpy + scipy.fft with {cores} workers), {t:.1f} s"}
+                         f"oracle (numpy + scipy.fft with {cores} workers), {t:.1f} s, after one untimed block"}
     line = {
         "metric": SPIN_METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms.value / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 (FP64 reductions)",
         "data": "synthetic (ITP ground state of the damped workload split 70/30)",
-        "config": {"workload": S.name, "grid": list(S.n), "components": 2, "box": S.box, "g": [list(r) for r in S.g],
-                   "coupling": str(S.coupling), "Ntotal": S.Ntotal, "gamma": S.gamma, "dt": S.dt,
-                   "step": f"{inner} split steps (1 outer step)", "n_recalc": 10,
-                   "l2": f"inputs larger than L2 (2 states + 2 V = {P * 24 / 1e6:.0f} MB > 129 MB L2)",
-                   "points_counted": "grid points (each carries both components)"},
+        "config": spinor_config(S), "step": f"{inner} split steps (1 outer step)",
         "fp64": {"value": value64, "unit": UNIT, "steps": inner, "ratio_fp32_over_fp64": value / dist.world / value64},
         "error": {"fp32_vs_fp64_rel_l2_after_outer_step": err_l2, "mu_rel_after_outer_step": abs(mu32 - mu64) / abs(mu64)},
         "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -667,25 +728,25 @@ def run_spinor_reference(args, dist):
     """--impl reference for the spinor workload: the FP64 oracle restatement of
     GPEtaskSpinor.solve_split on the host cores (the start state is the
     seeded Gaussian pair; the timed work does not depend on it)."""
-    from gpe_gb300.workloads import DAMPED3D as W, SPINOR3D as S
+    from gpe_workloads import DAMPED3D as W, SPINOR3D as S
 
     if dist.rank != 0:
         return
+    from oracle import gpe_oracle as O
+
     cores = os.cpu_count() or 1
-    grid = W.make_grid("double")
+    grid = O.Grid(W.box[0], W.n[0], W.box[1], W.n[1], W.box[2], W.n[2])
     pair = S.initial_pair(W.initial_state(grid) * 10.0)
-    vals = []
-    for _ in range(max(1, min(args.steps, 2))):
-        v, n, t = spinor_cpu_steps(S, pair, cores)
-        vals.append((v, n, t))
-    v = float(np.median([x[0] for x in vals]))
+    blocks = max(1, min(args.steps, 2))
+    v, n, t = spinor_cpu_steps(S, pair, cores, blocks)
     line = {
-        "metric": SPIN_METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": 1, "steps": len(vals),
-        "warmup": args.warmup, "ms_per_step": 1e3 * vals[-1][2] / vals[-1][1], "higher_is_better": True,
+        "metric": SPIN_METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": 1, "steps": blocks,
+        "warmup": 1, "ms_per_step": 1e3 * t / blocks, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": S.name, "grid": list(S.n), "components": 2, "dt": S.dt, "step": "1 split step"},
+        "config": spinor_config(S), "step": "one block of 10 split steps (n_recalc 10)",
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{len(vals)} x 10 split steps of the 256^3 two-component FP64 oracle"},
+                         "sample": f"{blocks} x 10 split steps of the 256^3 two-component FP64 oracle after one "
+                                   f"untimed block"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -696,7 +757,7 @@ def run_profile_case(precision: str, blocks: int, variant: int = 0, plans: int =
     parameters from the seeded Gaussian (no ITP), `blocks` blocks of 10 steps.
     The FFT plans are fixed (no autotuning under the profiler): `plans` = bit
     mask of the axes (bit 0 = x) that use the alternative plan."""
-    from gpe_gb300.workloads import DAMPED3D as W
+    from gpe_workloads import DAMPED3D as W
 
     grid, task = W.make_task(precision)
     task.autotune(16 + plans)

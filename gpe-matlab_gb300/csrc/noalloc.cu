@@ -18,8 +18,19 @@
 // reads.  Calls that overlap on the GPU (different streams, or threads using
 // the same device concurrently) race on the array and must be serialised by
 // the caller.
+//
+// The value is integrate(|psi|^2), the particle number that solve_split
+// calls ncur (solve_split.m:65-67 of GPE-MATLAB) and gpe_obs.norm reports:
+// the square of MATLAB's grid.norm (norm.m:11).
+//
+// Before any CUDA call the input pointer is checked for the alignment of
+// one complex element, and then asked of the driver: memory the GPU cannot
+// address as device memory of the current device (plain or page-locked host
+// memory, another device's memory) is refused with GPE_ERR_INVALID instead
+// of being handed to a kernel.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -105,14 +116,15 @@ static gpe_status na_fail(gpe_status st, const std::string& msg) {
 
 using namespace gpe;
 
-// The device address of the scratch array for the current device, looked up
-// once per device (the lookup needs that device current, and must not run
-// inside a stream capture; the first call on each device does it).
-static gpe_status na_scratch(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return na_fail(GPE_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+// The device address of the scratch array on device `dev` (the current
+// device), looked up once per device (the lookup needs that device current,
+// and must not run inside a stream capture; the first call on each device
+// does it).  The address stays valid for the life of the CUDA context: a
+// cudaDeviceReset by the host application ends it, and this library (its
+// contexts and this entry point alike) must not be used across one.
+static gpe_status na_scratch(int dev, double** out) {
   if (dev < 0 || dev >= NA_MAX_DEVICES) return na_fail(GPE_ERR_INVALID, "device ordinal beyond 63");
+  cudaError_t e;
   std::lock_guard<std::mutex> lock(g_na_mu);
   if (!g_na_ptr[dev]) {
     void* p = nullptr;
@@ -135,8 +147,33 @@ extern "C" GPE_API gpe_status gpe_norm_noalloc(const void* d_psi, long long npoi
     return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: " + std::to_string(npoints) +
                                         " points exceed the fixed scratch of this entry point (at most " +
                                         std::to_string(NA_MAX_POINTS) + " points, i.e. 512^3)");
+  // One complex element is 8 (FP32) or 16 (FP64) bytes; the kernel loads
+  // whole elements, so a pointer off that boundary is refused here, before
+  // any CUDA call.
+  const uintptr_t align = precision == GPE_FP32 ? sizeof(cx<float>) : sizeof(cx<double>);
+  if (reinterpret_cast<uintptr_t>(d_psi) % align != 0)
+    return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: d_psi is not aligned to one complex element (" +
+                                        std::to_string(align) + " bytes)");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return na_fail(GPE_ERR_CUDA, std::string("gpe_norm_noalloc: cudaGetDevice: ") +
+                                                         cudaGetErrorString(e));
+  // Only memory of the current device (or managed memory) goes to the kernel.
+  cudaPointerAttributes pa{};
+  e = cudaPointerGetAttributes(&pa, d_psi);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();  // the query's error is not sticky; clear it
+    return na_fail(GPE_ERR_INVALID, std::string("gpe_norm_noalloc: d_psi is not a CUDA pointer (") +
+                                        cudaGetErrorString(e) + ")");
+  }
+  if (pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged)
+    return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: d_psi is host memory; pass device memory of the "
+                                    "current device");
+  if (pa.type == cudaMemoryTypeDevice && pa.device != dev)
+    return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: d_psi lives on device " + std::to_string(pa.device) +
+                                        ", not on the current device " + std::to_string(dev));
   double* scratch = nullptr;
-  gpe_status st = na_scratch(&scratch);
+  gpe_status st = na_scratch(dev, &scratch);
   if (st != GPE_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nparts = (int)((npoints + NA_CHUNK - 1) / NA_CHUNK);
@@ -145,7 +182,7 @@ extern "C" GPE_API gpe_status gpe_norm_noalloc(const void* d_psi, long long npoi
   else
     k_na_partials<double><<<nparts, NA_THREADS, 0, s>>>(static_cast<const cx<double>*>(d_psi), npoints, scratch);
   k_na_final<<<1, NA_THREADS, 0, s>>>(scratch, nparts, weight, scratch + NA_MAX_PARTIALS);
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(norm_out, scratch + NA_MAX_PARTIALS, sizeof(double),
                                             cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

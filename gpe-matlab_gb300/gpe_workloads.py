@@ -12,8 +12,11 @@ here and marked ``assumed``:
   same), so 0.01 (256^3, mu ~ 71) and 0.004 (512^3, mu ~ 180) are used,
   with eps = 1e-6.
 
-``scale`` shrinks the grid for fast parity tests while keeping the box, so
-the same physics runs at 32^2 / 64^2 / 32^3.
+The parameter tables, potentials and seeded start states here import
+nothing of the library: the CPU reference timing builds its grids (the
+oracle's), potentials and start states from them without loading libgpe.so.
+Only the factories that build library grids and tasks (``make_grid``,
+``make_task``, ``make_tasks``) import ``gpe_gb300``, when they are called.
 """
 from __future__ import annotations
 
@@ -21,7 +24,11 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .grid import grid2d, grid3d
+
+def _grids():
+    from gpe_gb300.grid import grid2d, grid3d
+
+    return grid2d, grid3d
 
 
 @dataclass
@@ -51,6 +58,7 @@ class Workload:
         return int(np.prod(self.n))
 
     def make_grid(self, precision: str = "double", n=None):
+        grid2d, grid3d = _grids()
         n = tuple(n or self.n)
         if self.ndims == 2:
             return grid2d(self.box[0], n[0], self.box[1], n[1], precision=precision)
@@ -75,7 +83,7 @@ class Workload:
         return phi + self.noise * noise
 
     def make_task(self, precision: str = "double", n=None, device: int = 0):
-        from .task import GPEtask
+        from gpe_gb300.task import GPEtask
 
         grid = self.make_grid(precision, n)
         task = GPEtask(grid, self.potential(), device=device)
@@ -153,9 +161,10 @@ class BatchWorkload:
     def make_tasks(self, precision: str = "single", device: int = 0, rank: int = 0, world: int = 1):
         """Tasks of this rank's realisations, holding their ground state with
         the vortices imprinted."""
-        from .imprint import imprint_vortex
-        from .task import GPEtask
+        from gpe_gb300.imprint import imprint_vortex
+        from gpe_gb300.task import GPEtask
 
+        grid2d, _ = _grids()
         tasks = []
         rs = self.realisations()
         for r in (rs[i] for i in self.shard(rank, world)):
@@ -210,6 +219,7 @@ class AdjointWorkload:
     seed: int = 4
 
     def make_grid(self, precision: str = "single", n=None):
+        grid2d, _ = _grids()
         n = n or self.n
         return grid2d(self.box, n, self.box, n, precision=precision)
 
@@ -279,8 +289,9 @@ class SpinorWorkload:
         return task
 
     def make_task(self, precision: str = "single", device: int = 0):
-        from .task import GPEtaskSpinor
+        from gpe_gb300.task import GPEtaskSpinor
 
+        _, grid3d = _grids()
         b, n = self.box, self.n
         grid = grid3d(b, n[0], b, n[1], b, n[2], precision=precision)
         return grid, self.configure(GPEtaskSpinor(grid, self.potentials(), device=device))

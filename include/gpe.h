@@ -370,16 +370,24 @@ GPE_API gpe_status gpe_set_pass_variant(gpe_ctx *ctx, int variant);
 /* integrate(|psi|^2) = sum |psi_i|^2 * weight of a caller-owned device array
  * d_psi (npoints interleaved complex values of `precision`, on the current
  * device), written to the host double *norm_out, on `stream` (a
- * cudaStream_t; NULL = default stream).  No counterpart in the reference:
- * an addition for callers that cannot allocate device memory at that point
- * (MEX code on gpuArray memory owned by MATLAB's allocator, code inside a
- * solve_split callback, applications that own all device memory).  It
- * allocates nothing: its partial sums live in a fixed 256 KB device array
- * inside the library, so it accepts at most 134,217,728 points (512^3) and
- * rejects larger inputs with GPE_ERR_INVALID.  The first call on each device
- * looks up that array's address and should come before any stream capture.
- * All calls share the array: calls that overlap on the GPU race and must be
- * serialised by the caller.  Errors: gpe_last_error(NULL). */
+ * cudaStream_t; NULL = default stream).  This is the particle number the
+ * reference's solve_split calls ncur (solve_split.m:65-67) and gpe_obs.norm
+ * reports, i.e. the SQUARE of MATLAB's grid.norm (norm.m:11).  No
+ * counterpart in the reference: an addition for callers that cannot allocate
+ * device memory at that point (MEX code on gpuArray memory owned by MATLAB's
+ * allocator, code inside a solve_split callback, applications that own all
+ * device memory).  It allocates nothing: its partial sums live in a fixed
+ * 256 KB device array inside the library, so it accepts at most 134,217,728
+ * points (512^3) and rejects larger inputs with GPE_ERR_INVALID.  Before any
+ * device work, d_psi must be aligned to one complex element (8 bytes FP32,
+ * 16 bytes FP64) and must be device memory of the current device (or managed
+ * memory); host memory and another device's memory are refused with
+ * GPE_ERR_INVALID.  The first call on each device looks up that array's
+ * address and should come before any stream capture; the address lives as
+ * long as the device's CUDA context, so no call may follow a cudaDeviceReset.
+ * Each call waits on the host for its result.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * Errors: gpe_last_error(NULL). */
 GPE_API gpe_status gpe_norm_noalloc(const void *d_psi, long long npoints, int precision, double weight,
                                     void *stream, double *norm_out);
 /* FFT plan autotuner (FP32 contexts).  Axis lengths 128, 192, 256, 384 and

@@ -9,7 +9,7 @@ tests fixed inputs and expected outputs; the oracle is pinned to physics by
 tests/test_oracle.py.
 
 Inputs: psi0 = exp(-r^2/(2 sigma^2)) + 1e-3 (N(0,1) + i N(0,1))/sqrt(2) with
-numpy default_rng(seed), as in gpe_gb300.workloads.
+numpy default_rng(seed), as in gpe_workloads.
 """
 from __future__ import annotations
 

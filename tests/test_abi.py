@@ -121,3 +121,17 @@ def test_mex_gateway_compiles_against_the_documented_api():
     r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-Wall", "-I", str(ROOT / "tests" / "mex_stub"),
                         "-I", str(ROOT / "include"), str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_norm_noalloc_refuses_a_misaligned_pointer_before_any_cuda_call():
+    """The alignment check of gpe_norm_noalloc runs before any CUDA call, so
+    it answers without a GPU: a pointer off the 16-byte boundary of a complex
+    double (or the 8-byte one of a complex float) is GPE_ERR_INVALID."""
+    from gpe_gb300 import _lib as L
+
+    out = C.c_double(-1.0)
+    for addr, prec in ((0x10008, L.GPE_FP64), (0x10004, L.GPE_FP32), (0x10001, L.GPE_FP64)):
+        st = L.lib.gpe_norm_noalloc(C.c_void_p(addr), 1024, prec, 1.0, None, C.byref(out))
+        assert st == L.GPE_ERR_INVALID
+        assert b"aligned" in L.lib.gpe_last_error(None)
+    assert out.value == -1.0

@@ -23,7 +23,7 @@ def _rank_main(rank, world, port, out):
                        "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
     sys.path[:0] = [str(ROOT), str(ROOT / "gpe-matlab_gb300")]
     import bench
-    from gpe_gb300.workloads import BATCH2D
+    from gpe_workloads import BATCH2D
 
     d = bench.Dist()
     d.barrier()

@@ -91,7 +91,7 @@ def test_adjoint2d_256_gradient_of_bump_amplitudes(gpe):
     dloss/da_j from the FP32 context (FP32 and FP64 sweeps) against the FP64
     oracle adjoint and against central differences on 32 random directions."""
     from gpe_gb300.imprint import imprint_vortex
-    from gpe_gb300.workloads import ADJOINT2D as W
+    from gpe_workloads import ADJOINT2D as W
 
     g64 = W.make_grid("double")
     t64 = gpe.GPEtask(g64, lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2))

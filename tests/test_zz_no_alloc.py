@@ -4,7 +4,9 @@ gpuArray memory, or code inside a solve_split callback, that cannot allocate
 at that point).  Checked through the C ABI against the context-based
 entry point (gpe_set_state_device + gpe_observables) on two calls in a row,
 so the second call also shows that the shared fixed scratch array carries no
-state over from the first."""
+state over from the first; a further call leaves the device's free memory and
+torch's allocated bytes unchanged (the property the entry point exists for);
+host memory and misaligned pointers are refused before they reach a kernel."""
 import ctypes as C
 
 import numpy as np
@@ -73,3 +75,47 @@ def test_norm_noalloc_rejects_inputs_beyond_its_scratch(gpe):
     st = L.lib.gpe_norm_noalloc(C.c_void_p(buf.data_ptr()), 512 ** 3 + 1, L.GPE_FP32, 1.0, None, C.byref(out))
     assert st == L.GPE_ERR_INVALID
     assert b"exceed" in L.lib.gpe_last_error(None)
+
+
+def test_norm_noalloc_allocates_no_device_memory(gpe):
+    torch = pytest.importorskip("torch")
+    from gpe_gb300 import _lib as L
+
+    rng = np.random.default_rng(5)
+    psi = (rng.standard_normal(64 * 64 * 32) + 1j * rng.standard_normal(64 * 64 * 32))
+    bufs = {L.GPE_FP32: _device_copy(torch, psi.astype(np.complex64)),
+            L.GPE_FP64: _device_copy(torch, psi.astype(np.complex128))}
+    # warm-up calls: the per-device scratch lookup and the lazy loading of
+    # both kernels' code happen here, once per process
+    for prec, buf in bufs.items():
+        _noalloc_norm(buf, psi.size, prec, 0.5)
+    torch.cuda.synchronize()
+    for prec, buf in bufs.items():
+        free0, _ = torch.cuda.mem_get_info()
+        alloc0 = torch.cuda.memory_allocated()
+        got = _noalloc_norm(buf, psi.size, prec, 0.5)
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0, f"device free bytes changed by {free0 - free1}"
+        assert torch.cuda.memory_allocated() == alloc0
+        tol = 1e-6 if prec == L.GPE_FP32 else 1e-12
+        assert got == pytest.approx(0.5 * float(np.sum(np.abs(psi) ** 2)), rel=tol)
+
+
+def test_norm_noalloc_refuses_host_and_misaligned_pointers(gpe):
+    torch = pytest.importorskip("torch")
+    from gpe_gb300 import _lib as L
+
+    out = C.c_double(-1.0)
+    host = np.zeros(2 * 4096, dtype=np.float64)
+    st = L.lib.gpe_norm_noalloc(C.c_void_p(host.ctypes.data), 4096, L.GPE_FP64, 1.0, None, C.byref(out))
+    assert st == L.GPE_ERR_INVALID and b"host memory" in L.lib.gpe_last_error(None)
+    pinned = torch.zeros(2 * 4096, dtype=torch.float64).pin_memory()
+    st = L.lib.gpe_norm_noalloc(C.c_void_p(pinned.data_ptr()), 4096, L.GPE_FP64, 1.0, None, C.byref(out))
+    assert st == L.GPE_ERR_INVALID and b"host memory" in L.lib.gpe_last_error(None)
+    dev = torch.zeros(2 * 4096 + 2, dtype=torch.float64, device="cuda")
+    st = L.lib.gpe_norm_noalloc(C.c_void_p(dev.data_ptr() + 8), 4096, L.GPE_FP64, 1.0, None, C.byref(out))
+    assert st == L.GPE_ERR_INVALID and b"aligned" in L.lib.gpe_last_error(None)
+    assert out.value == -1.0
+    # the library is still usable afterwards
+    assert _noalloc_norm(dev, 4096, L.GPE_FP64, 1.0) == 0.0
