@@ -205,6 +205,16 @@ def cpu_reference_run(W, phi, cores: int, warm: int, samples: int, per_sample=No
     return W.npoints * n / t, n, t, per
 
 
+def oracle_block(W, phi, cores: int):
+    """One block (10 split steps, n_recalc 10) of the FP64 oracle's solve_split
+    from phi: (state, mu, n, grid-pt-steps/s of steps 2..10, 9, seconds)."""
+    og, ot = oracle_task(W, phi, cores)
+    stamps = []
+    ot.solve_split(W.dt, 10, 1, inner_callback=lambda _j: stamps.append(time.perf_counter()))
+    t = stamps[-1] - stamps[0]
+    return (np.asarray(ot.current_state), ot.history["mu"][0], ot.history["n"][0], W.npoints * 9 / t, 9, t)
+
+
 def workload_config(W):
     """The workload's description, identical in both arms' JSON lines."""
     return {"workload": W.name, "grid": list(W.n), "box": W.box[0], "trap_lambda": list(W.trap), "g": W.g,
@@ -380,6 +390,28 @@ def run_gpu(args, dist):
     L.check(t64._ctx, L.lib.gpe_timer_stop(t64._ctx, C.byref(ms64)))
     value64 = float(P) * INNER * k64 / (ms64.value / 1e3)
     err_l2 = float(np.linalg.norm(psi32_1 - psi64_1) / np.linalg.norm(psi64_1))
+    # ---- error against the FP64 oracle: one block (10 split steps) from the same
+    # start, FP32 and FP64 kernels; the oracle run is also the CPU baseline sample
+    cpu, vs_oracle = None, None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
+        cores = os.cpu_count() or 1
+        ostate, omu, on, cval, csteps, ct = oracle_block(W, phi, cores)
+        blk = {}
+        for name, tk in (("fp32", task), ("fp64", t64)):
+            tk.init_state = phi
+            tk.current_iter = 0
+            tk.solve_split(W.dt, 10, 1)
+            st = np.asarray(tk.current_state, dtype=np.complex128)
+            blk[name] = {"state_rel_l2": float(np.linalg.norm(st - ostate) / np.linalg.norm(ostate)),
+                         "mu_rel": abs(tk.history["mu"][0] - omu) / abs(omu),
+                         "n_rel": abs(tk.history["n"][0] - on) / abs(on)}
+        vs_oracle = {"horizon": "10 split steps (one n_recalc block) from the imprinted ground state", **blk,
+                     "ground_state": "E and mu of the FP32 ITP vs the oracle's converged ITP: tests/test_gpu_configs.py "
+                                     "(1e-13 / 2e-11 relative on this grid)"}
+        cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{csteps} split steps of the same {'x'.join(map(str, W.n))} workload in the FP64 "
+                         f"oracle (numpy + scipy.fft with {cores} workers), {ct:.1f} s, after one untimed step and "
+                         f"the setup, the block-end mu included"}
     t64.close()
     # ---- e2e through the public API with pinned host buffers --------------------
     host_in = np.ascontiguousarray(phi.astype(np.complex64))
@@ -389,15 +421,6 @@ def run_gpu(args, dist):
         e2e_t = e2e_abi(task, host_in, host_out, W.dt, INNER, e2e_steps)
     e2e_t = dist.reduce(e2e_t, "max")
     e2e_val = dist.reduce(float(P) * INNER * e2e_steps, "sum") / e2e_t
-    # ---- CPU baseline (rank 0, N = 1 only): bounded sample ---------------------
-    cpu = None
-    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
-        cores = os.cpu_count() or 1
-        cval, n, t, _ = cpu_reference_run(W, phi, cores, 1, args.cpu_steps, per_sample=1)
-        cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{n} split steps of the same {'x'.join(map(str, W.n))} workload in the FP64 "
-                         f"oracle (numpy + scipy.fft with {cores} workers), {t:.1f} s, after one untimed "
-                         f"step and the setup"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms.value / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -410,7 +433,8 @@ def run_gpu(args, dist):
         "fp64": {"value": value64, "unit": UNIT, "steps": INNER * k64, "ratio_fp32_over_fp64": value / dist.world / value64},
         "error": {"fp32_vs_fp64_rel_l2_after_outer_step": err_l2,
                   "mu_rel_after_outer_step": abs(mu32 - mu64) / abs(mu64),
-                  "itp_iters": itp.iters, "itp_fp32_iters": itp.fp32_iters, "itp_converged": bool(itp.converged)},
+                  "itp_iters": itp.iters, "itp_fp32_iters": itp.fp32_iters, "itp_converged": bool(itp.converged),
+                  "vs_oracle": vs_oracle},
         "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": top["bytes_per_launch"], "avg_launch_ms": avg_ms,
