@@ -776,20 +776,46 @@ def run_spinor_reference(args, dist):
     print(json.dumps(line), flush=True)
 
 
-def run_profile_case(precision: str, blocks: int, variant: int = 0, plans: int = 0):
-    """Small fixed case for ncu captures: the bench workload's grid and
-    parameters from the seeded Gaussian (no ITP), `blocks` blocks of 10 steps.
-    The FFT plans are fixed (no autotuning under the profiler): `plans` = bit
-    mask of the axes (bit 0 = x) that use the alternative plan."""
-    from gpe_workloads import DAMPED3D as W
+def run_profile_case(precision: str, blocks: int, variant: int = 0, plans: int = 0, workload: str = "damped3d_256"):
+    """Small fixed case for ncu captures: a workload's grid and parameters from
+    its seeded Gaussian start (no ITP), `blocks` blocks of 10 steps (3D: one
+    outer step of 10 per block; 2D: outer steps of the workload's niter_inner,
+    the cluster kernel's launch unit).  The FFT plans of 3D grids are fixed
+    (no autotuning under the profiler): `plans` = bit mask of the axes (bit 0
+    = x) that use the alternative plan.  batch2d_64: the batch's grids from
+    their seeded Gaussian starts, `blocks` outer steps of 100."""
+    import gpe_gb300 as gpe
+    from gpe_workloads import BATCH2D, WORKLOADS
 
+    if workload == "batch2d_64":
+        import numpy as np
+
+        tasks = []
+        for r in BATCH2D.realisations():
+            grid = gpe.grid2d(BATCH2D.box, r["n"], BATCH2D.box, r["n"], precision=precision)
+            t = gpe.GPEtask(grid, lambda X, Y, Z, lam=r["lam"]: 0.5 * (X ** 2 + (lam * Y) ** 2))
+            t.Ntotal, t.g = BATCH2D.Ntotal, r["g"]
+            X, Y = grid.mesh["x"], grid.mesh["y"]
+            t.init_state = np.exp(-(X ** 2 + (r["lam"] * Y) ** 2) / 32.0).astype(complex)
+            tasks.append(t)
+        gpe.solve_split_batch(tasks, BATCH2D.dt, BATCH2D.niter_inner, blocks)
+        print(json.dumps({"profile_case": precision, "workload": workload, "outer_steps": blocks,
+                          "launches": sum(t.kernel_launches() for t in tasks)}))
+        for t in tasks:
+            t.close()
+        return
+    W = WORKLOADS[workload]
     grid, task = W.make_task(precision)
-    task.autotune(16 + plans)
+    if W.ndims == 3:
+        task.autotune(16 + plans)
     task.set_pass_variant(variant)
     task.init_state = W.initial_state(grid) * 30.0
-    task.solve_split(W.dt, 10, blocks)
-    print(json.dumps({"profile_case": precision, "blocks": blocks, "launches": task.kernel_launches(),
-                      "mu": task.current_mu, "n": task.current_n}))
+    if W.ndims == 3:
+        task.solve_split(W.dt, 10, blocks)
+    else:
+        task.solve_split(W.dt, W.niter_inner, blocks)
+    print(json.dumps({"profile_case": precision, "workload": workload, "blocks": blocks,
+                      "launches": task.kernel_launches(), "mu": task.current_mu, "n": task.current_n}))
     task.close()
 
 
@@ -798,6 +824,9 @@ def main():
     ap.add_argument("--profile-case", choices=["single", "double"], default=None,
                     help="run the small fixed case used for ncu captures and exit")
     ap.add_argument("--profile-blocks", type=int, default=2)
+    ap.add_argument("--profile-workload", default="damped3d_256",
+                    choices=["damped3d_256", "ring3d_512", "vortex2d_256", "batch2d_64"],
+                    help="profile case: the workload whose grid and parameters it runs")
     ap.add_argument("--profile-plans", type=int, default=0,
                     help="profile case: bit mask of axes (bit 0 = x) on the alternative FFT plan")
     ap.add_argument("--gpus", type=int, default=1)
@@ -817,7 +846,8 @@ def main():
     ap.add_argument("--adjoint-fp64", action="store_true", help="adjoint workloads: FP64 sweep of the FP32 context")
     args = ap.parse_args()
     if args.profile_case:
-        run_profile_case(args.profile_case, args.profile_blocks, args.pass_variant, args.profile_plans)
+        run_profile_case(args.profile_case, args.profile_blocks, args.pass_variant, args.profile_plans,
+                         args.profile_workload)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -1,0 +1,96 @@
+// cluster2d.h - host-visible part of the persistent cluster kernel of small
+// 2D grids (cluster2d.cuh): the launch arguments, the per-CTA shared-memory
+// plan and the launchers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "plans.cuh"
+
+namespace gpe {
+
+constexpr int C2_THREADS = 256;
+constexpr int C2_RED_BYTES = 1024;  // [8] cluster-visible sums + [8][8] warp partials
+
+// Axis lengths the cluster kernel handles (each must have a Plan<N> with the
+// contiguous-axis padding p + p/16 and T <= N/16).
+#define GPE_C2_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384)
+
+__host__ __device__ inline int c2_T(int n) {
+  switch (n) {
+#define X(v) \
+  case v:    \
+    return Plan<v>::T;
+    GPE_C2_SIZES(X)
+#undef X
+  }
+  return 0;
+}
+// Padded stride between pencils of the contiguous layout (ContigLayout::REG).
+__host__ __device__ constexpr int c2_reg(int n) {
+  const int r0 = n + ((n - 1) >> 4);
+  return (r0 % 2 == 0) ? r0 + 1 : r0;
+}
+
+// Shared-memory plan of one CTA for an nx x ny grid on clusters of cs CTAs.
+struct C2Geom {
+  int cols, cols_pad, rows, regy, home, xbuf;  // home/xbuf in complex elements
+  size_t bytes;
+};
+__host__ __device__ inline C2Geom c2_geom(int nx, int ny, int cs, int esz) {
+  C2Geom g;
+  g.cols = nx / cs;
+  g.rows = ny / cs;
+  const int fpi = C2_THREADS / c2_T(ny);
+  g.cols_pad = (g.cols + fpi - 1) / fpi * fpi;
+  g.regy = c2_reg(ny);
+  g.home = g.cols_pad * g.regy;
+  const int gx = C2_THREADS / c2_T(nx);
+  g.xbuf = gx * nx > fpi * g.regy ? gx * nx : fpi * g.regy;
+  g.bytes = (size_t)(g.home + g.xbuf) * (size_t)esz + C2_RED_BYTES;
+  return g;
+}
+
+// One realisation (context) of the batch.
+struct C2Grid {
+  void* psi;                 // cx<R> state, ny x nx, y fastest
+  const void* V;             // R potential
+  const void* tws[2];        // stage twiddle rows of Plan<n>: [0] x axis, [1] y axis
+  const void* php[2];        // kinetic factors exp(-k^2/2 dt)/n in slot order
+  const void* k2p[2];        // k^2/2/n in slot order (energy sums)
+  DevScalars* sc;
+  double* hist;              // record (muc, ncur, energy) of outer step k at hist + 3*k
+  int nx, ny;
+  int feedback;              // gamma > 0 and mu_init == 0: mu and the norm feed back every block
+  int start;                 // current_iter at the start of the run
+  double weight, g, tau;     // cell volume, coupling, decay time (0: none)
+  double dre, dim;           // complex time step dt = i ddt/(1 + i gamma)
+};
+
+struct C2Args {
+  const C2Grid* grids;
+  const int* order;  // grid indices in cluster order
+  const int* offs;   // cluster c runs order[offs[c] .. offs[c+1])
+  int n_rec, nb;     // steps per block, blocks per outer step
+  int nouter;        // outer steps per launch
+  double ddt, dt_outer;
+};
+
+// Launch of k_cluster2d<R> on nclusters clusters of cs CTAs (cluster2d_f32.cu,
+// cluster2d_f64.cu).
+template <typename R>
+cudaError_t launch_cluster2d(const C2Args& a, int nclusters, int cs, size_t smem, cudaStream_t s);
+template <>
+cudaError_t launch_cluster2d<float>(const C2Args& a, int nclusters, int cs, size_t smem, cudaStream_t s);
+template <>
+cudaError_t launch_cluster2d<double>(const C2Args& a, int nclusters, int cs, size_t smem, cudaStream_t s);
+// Clusters of cs CTAs with `smem` bytes each that can be resident at once
+// (0: this cluster shape does not fit the device).
+template <typename R>
+int cluster2d_max_clusters(int cs, size_t smem);
+template <>
+int cluster2d_max_clusters<float>(int cs, size_t smem);
+template <>
+int cluster2d_max_clusters<double>(int cs, size_t smem);
+
+}  // namespace gpe

@@ -223,7 +223,7 @@ struct DevScalars {
   int nonfinite;      // a reduction produced NaN/Inf
   int timeout;        // a bounded device-side wait gave up
   int fin_count;      // CTAs of a multi-CTA finalizer that are done (0 between launches)
-  int pad_;
+  int outer;         // outer steps the cluster kernel has completed in this run (history slot)
 };
 
 enum StopReason { RUNNING = 0, CONVERGED = 1, SWITCH_FP64 = 2, HALVE_DT = 3, NONFINITE = 4 };

@@ -22,6 +22,7 @@
 
 #include <nvtx3/nvToolsExt.h>
 
+#include "cluster2d.h"
 #include "ctx.h"
 
 using namespace gpe;
@@ -319,11 +320,11 @@ size_t rsize() {
 // ---- profiling --------------------------------------------------------------
 enum ProfCls {
   PC_PASS_Y, PC_PASS_X, PC_PASS_Z, PC_ENERGY_Y, PC_ENERGY_X, PC_ENERGY_Z, PC_FINALIZE, PC_ITP_CHECK,
-  PC_NORM, PC_ELEMENTWISE, PC_NL_PHASE, PC_ADJ_NL, PC_COPY, PC_COUNT
+  PC_NORM, PC_ELEMENTWISE, PC_NL_PHASE, PC_ADJ_NL, PC_COPY, PC_CLUSTER, PC_COUNT
 };
 const char* kProfNames[PC_COUNT] = {"pass_y",   "pass_x",    "pass_z",      "energy_y",  "energy_x",
                                     "energy_z", "finalize",  "itp_check",   "norm",      "elementwise",
-                                    "nl_phase", "adjoint_nl", "state_copy"};
+                                    "nl_phase", "adjoint_nl", "state_copy", "cluster_step"};
 
 cudaEvent_t pool_event(gpe_ctx* c) {
   if (!c->ev_pool.empty()) {
@@ -1196,6 +1197,7 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
   s0.stop = 0;
   s0.status = RUNNING;
   s0.nonfinite = 0;
+  s0.outer = 0;
   s0.NN0 = NN0;
   s0.NNN = NN0;
   if (sg) s0.mu = c->prm.mu_init;  // SGPE: mu = mu_init throughout (SGPEtask solve_split.m:52)
@@ -1674,6 +1676,238 @@ gpe_status batch_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm) {
     if (st2 != GPE_OK) return fail(c, st2, "batch: context " + std::to_string(i) + ": " + cs[i]->err);
   }
   return GPE_OK;
+}
+
+// ---- persistent cluster path of small 2D grids (cluster2d.cuh) --------------------
+// One k_cluster2d launch advances every context of a batch (or the single
+// context of solve_split) by one outer step; the launch is captured once
+// into a CUDA graph and replayed per outer step (it reads its outer-step
+// index from each context's device scalars).  Used for 2D one-component
+// grids with both axis lengths in GPE_C2_SIZES whose state fits the
+// cluster's shared memory, with the default pass variant; anything else
+// takes the per-pass paths.
+bool c2_size_ok(int n) {
+  switch (n) {
+#define X(v) case v:
+    GPE_C2_SIZES(X)
+#undef X
+    return true;
+    default:
+      return false;
+  }
+}
+
+bool c2_eligible(const gpe_ctx* c) {
+  return c->ndims == 2 && c->ncomp == 1 && !c->omega_field && c->prm.omega == 0.0 && c->pass_variant == 0 &&
+         c2_size_ok(c->n[0]) && c2_size_ok(c->n[1]);
+}
+
+struct C2Plan {
+  int cs = 0, nclusters = 0;
+  size_t smem = 0;
+};
+
+// GPE_CLUSTER_SIZE=8|16 forces a cluster size (measurement); GPE_CLUSTER=0
+// turns the path off.
+int c2_env(const char* name, int dflt) {
+  const char* e = getenv(name);
+  return e ? atoi(e) : dflt;
+}
+
+// Cluster size and resident clusters: the candidate that keeps the most CTAs
+// busy (clusters in use x size), 16 first so that a tie gives each grid more
+// SMs.  cs = 0: no cluster shape fits.
+template <typename R>
+C2Plan c2_plan(const std::vector<gpe_ctx*>& cs) {
+  C2Plan best;
+  const int forced = c2_env("GPE_CLUSTER_SIZE", 0);
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cs[0]->device);
+  long long best_score = -1;
+  for (int cand : {16, 8}) {
+    if (forced && cand != forced) continue;
+    size_t smem = 0;
+    bool ok = true;
+    for (auto* c : cs) {
+      if (c->n[0] % cand || c->n[1] % cand) ok = false;
+      smem = std::max(smem, c2_geom(c->n[0], c->n[1], cand, (int)sizeof(cx<R>)).bytes);
+    }
+    if (!ok || smem > (size_t)optin) continue;
+    const int maxc = cluster2d_max_clusters<R>(cand, smem);
+    if (maxc <= 0) continue;
+    const int ncl = std::min<int>((int)cs.size(), maxc);
+    const long long score = (long long)ncl * cand;
+    if (score > best_score) {
+      best_score = score;
+      best.cs = cand;
+      best.nclusters = ncl;
+      best.smem = smem;
+    }
+  }
+  return best;
+}
+
+// Axis tables of the default plans (the cluster kernel is built on Plan<N>).
+template <typename R>
+gpe_status default_plans(gpe_ctx* c) {
+  for (int ax = 0; ax < 2; ++ax)
+    if (c->main.plan_var[ax] != 0) {
+      c->main.plan_var[ax] = 0;
+      CHECK(build_axis_tables<R>(c, c->main, ax));
+    }
+  return GPE_OK;
+}
+
+template <typename R>
+gpe_status cluster_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, const C2Plan& pl) {
+  gpe_ctx* c = cs[0];
+  const size_t n = cs.size();
+  std::vector<SplitRun> runs(n);
+  for (size_t i = 0; i < n; ++i) {
+    int vk = 0;
+    gpe_ctx* ci = cs[i];
+    ci->err.clear();
+    gpe_status st = default_plans<R>(ci);
+    if (st == GPE_OK) st = split_setup<R>(ci, prm, runs[i], vk, 3);
+    if (st != GPE_OK) return n > 1 ? fail(c, st, "batch: context " + std::to_string(i) + ": " + ci->err) : st;
+    CU(cudaStreamSynchronize(ci->stream));
+  }
+  const SplitRun& r0 = runs[0];
+  for (size_t i = 1; i < n; ++i)
+    if (runs[i].n_rec != r0.n_rec || runs[i].start != r0.start)
+      return fail(c, GPE_ERR_INVALID, "batch: all contexts need the same n_recalc and current_iter");
+  // work table: one entry per context
+  std::vector<C2Grid> grids(n);
+  double bytes = 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    gpe_ctx* ci = cs[i];
+    Field& f = ci->main;
+    C2Grid& G = grids[i];
+    G.psi = f.psi;
+    G.V = f.V;
+    for (int ax = 0; ax < 2; ++ax) {
+      G.tws[ax] = f.tws[ax];
+      G.php[ax] = f.php[ax];
+      G.k2p[ax] = f.k2p[ax];
+    }
+    G.sc = ci->sc;
+    G.hist = ci->d_hist + runs[i].hist_off;
+    G.nx = ci->n[0];
+    G.ny = ci->n[1];
+    G.feedback = runs[i].feedback ? 1 : 0;
+    G.start = runs[i].start;
+    G.weight = ci->weight;
+    G.g = ci->prm.g;
+    G.tau = ci->prm.decay_rate;
+    G.dre = runs[i].dre;
+    G.dim = runs[i].dim;
+    bytes += (double)ci->P * (4 * sizeof(R) + sizeof(R));  // state in and out, V once
+  }
+  // Longest-processing-time assignment of the grids to the clusters (cost of
+  // a grid: P log2 P, the FFT work of a step).
+  std::vector<int> idx(n);
+  for (size_t i = 0; i < n; ++i) idx[i] = (int)i;
+  auto cost = [&](int i) { return (double)cs[i]->P * std::log2((double)cs[i]->P); };
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost(a) > cost(b); });
+  const int ncl = pl.nclusters;
+  std::vector<std::vector<int>> lists(ncl);
+  std::vector<double> load(ncl, 0.0);
+  for (int i : idx) {
+    const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    lists[k].push_back(i);
+    load[k] += cost(i);
+  }
+  std::vector<int> order, offs{0};
+  for (auto& l : lists) {
+    order.insert(order.end(), l.begin(), l.end());
+    offs.push_back((int)order.size());
+  }
+  const size_t gb = n * sizeof(C2Grid), ob = order.size() * sizeof(int), fb = offs.size() * sizeof(int);
+  char* dbuf = nullptr;
+  CU(cudaMalloc(&dbuf, gb + ob + fb));
+  struct Free {
+    char* p;
+    ~Free() { cudaFree(p); }
+  } free_dbuf{dbuf};
+  CU(cudaMemcpy(dbuf, grids.data(), gb, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(dbuf + gb, order.data(), ob, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(dbuf + gb + ob, offs.data(), fb, cudaMemcpyHostToDevice));
+  C2Args a;
+  a.grids = reinterpret_cast<const C2Grid*>(dbuf);
+  a.order = reinterpret_cast<const int*>(dbuf + gb);
+  a.offs = reinterpret_cast<const int*>(dbuf + gb + ob);
+  a.n_rec = r0.n_rec;
+  a.nb = r0.nb;
+  a.nouter = 1;
+  a.ddt = r0.ddt;
+  a.dt_outer = r0.dt_outer;
+  cudaStream_t master = c->stream;
+  int last_j = r0.start;
+  bool stop_req = false;
+  const bool direct = c->prof || prm->on_step;
+  BatchGraph gr;
+  if (!direct && r0.nout > r0.start) {
+    CU(cudaStreamBeginCapture(master, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t e = launch_cluster2d<R>(a, ncl, pl.cs, pl.smem, master);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(master, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return fail(c, GPE_ERR_CUDA, std::string("cluster graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    gr.g = g;
+    CU(cudaGraphInstantiate(&gr.x, g, 0));
+  }
+  for (int j = r0.start + 1; j <= r0.nout && !stop_req; ++j) {
+    if (direct) {
+      Launch L(c, PC_CLUSTER, bytes);
+      CU(launch_cluster2d<R>(a, ncl, pl.cs, pl.smem, master));
+    } else {
+      c->launches++;
+      CU(cudaGraphLaunch(gr.x, master));
+    }
+    last_j = j;
+    if (prm->on_step) {  // ext_callback (solve_split.m:80); one context only
+      DevScalars h;
+      CHECK(read_scalars(c, &h));
+      if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
+      const double time2 = (j - 1) * r0.dt_outer + (r0.nb - 1) * r0.ddt * r0.n_rec;
+      c->cur.current_iter = j;
+      c->cur.current_time = time2;
+      c->cur.current_mu = h.muc;
+      c->cur.current_n = h.ncur;
+      if ((int)c->hist_mu.size() < j) {
+        c->hist_mu.resize(j, 0.0);
+        c->hist_n.resize(j, 0.0);
+        c->hist_e.resize(j, 0.0);
+      }
+      c->hist_mu[j - 1] = h.muc;
+      c->hist_n[j - 1] = h.ncur;
+      c->hist_e[j - 1] = h.energy;
+      if (prm->on_step(prm->step_user, j, time2, h.muc, h.ncur) != 0) stop_req = true;
+    }
+  }
+  CU(cudaStreamSynchronize(master));
+  for (size_t i = 0; i < n; ++i) {
+    const double time2 = (last_j - 1) * runs[i].dt_outer + (runs[i].nb - 1) * runs[i].ddt * runs[i].n_rec;
+    const gpe_status st2 = split_finish<R>(cs[i], runs[i], last_j, time2);
+    if (st2 != GPE_OK) return n > 1 ? fail(c, st2, "batch: context " + std::to_string(i) + ": " + cs[i]->err) : st2;
+  }
+  return GPE_OK;
+}
+
+// Runs solve_split on cs through the cluster kernel when every context is
+// eligible (same precision, a cluster shape that fits); *used = false leaves
+// the call to the per-pass paths.
+gpe_status cluster_run(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, bool* used) {
+  *used = false;
+  if (c2_env("GPE_CLUSTER", 1) == 0) return GPE_OK;
+  for (auto* ci : cs)
+    if (!c2_eligible(ci) || ci->prec != cs[0]->prec) return GPE_OK;
+  const C2Plan pl = cs[0]->prec == GPE_FP32 ? c2_plan<float>(cs) : c2_plan<double>(cs);
+  if (pl.cs == 0) return GPE_OK;
+  *used = true;
+  return cs[0]->prec == GPE_FP32 ? cluster_impl<float>(cs, prm, pl) : cluster_impl<double>(cs, prm, pl);
 }
 
 template <typename R>
@@ -2255,6 +2489,13 @@ gpe_status gpe_solve_split(gpe_ctx* c, const gpe_split_params* prm) {
     return spinor_split_impl<double>(c, prm);
   }
   CHECK(maybe_autotune(c));
+  // Small 2D grids: the persistent cluster kernel (any callbacks but Vtd).
+  if (!prm->vtd) {
+    std::vector<gpe_ctx*> one{c};
+    bool used = false;
+    const gpe_status st = cluster_run(one, prm, &used);
+    if (used) return st;
+  }
   // Small grids are launch-bound: run their blocks as replayed CUDA graphs
   // (the batched path with one context) when no per-block host work is
   // needed (no Vtd or outer-step callback, no decay target) and no per-launch
@@ -2316,6 +2557,11 @@ gpe_status gpe_solve_split_batch(gpe_ctx** ctxs, int count, const gpe_split_para
     cs.push_back(ci);
   }
   c->err.clear();
+  {
+    bool used = false;
+    const gpe_status st = cluster_run(cs, prm, &used);
+    if (used) return st;
+  }
   // Batched contexts are tuned whatever their size (one timing per distinct
   // grid shape), before any graph is captured.
   for (auto* ci : cs) {
