@@ -40,6 +40,38 @@ __device__ __forceinline__ cx<R> rmul(cx<R> a, R s) { return mk<R>(a.x * s, a.y 
 template <typename R>
 __device__ __forceinline__ R norm2(cx<R> a) { return a.x * a.x + a.y * a.y; }
 
+// Two FP32 lanes processed by one packed instruction (sm_100+ FADD2, FMUL2,
+// FFMA2: two FP32 results per issue slot).  The paired pass kernels hold two
+// pencils per thread in structure-of-arrays form, cx<fx2>{re of both, im of
+// both}, so every complex operation of the FFT is lane-uniform: one packed
+// instruction does the work of two scalar ones.  Broadcast and negated
+// operands cost nothing extra (they are operand modifiers of the packed ops).
+struct fx2 {
+  float2 v;
+  fx2() = default;
+  __host__ __device__ __forceinline__ fx2(float a) : v{a, a} {}
+  __host__ __device__ __forceinline__ fx2(float a, float b) : v{a, b} {}
+  __host__ __device__ __forceinline__ explicit fx2(float2 a) : v(a) {}
+};
+__device__ __forceinline__ fx2 operator+(fx2 a, fx2 b) { return fx2(__fadd2_rn(a.v, b.v)); }
+__device__ __forceinline__ fx2 operator-(fx2 a) { return fx2(-a.v.x, -a.v.y); }
+__device__ __forceinline__ fx2 operator-(fx2 a, fx2 b) { return fx2(__fadd2_rn(a.v, make_float2(-b.v.x, -b.v.y))); }
+__device__ __forceinline__ fx2 operator*(fx2 a, fx2 b) { return fx2(__fmul2_rn(a.v, b.v)); }
+__device__ __forceinline__ fx2 fma2(fx2 a, fx2 b, fx2 c) { return fx2(__ffma2_rn(a.v, b.v, c.v)); }
+
+// Element type of the FFT tables a pass of lane type R reads (the paired
+// kernels read the FP32 tables and broadcast each entry to both lanes).
+template <typename R>
+struct TabOf {
+  using type = R;
+};
+template <>
+struct TabOf<fx2> {
+  using type = float;
+};
+template <typename R>
+using Tab = typename TabOf<R>::type;
+
 // Read-only (non-coherent cache) loads of table entries.
 __device__ __forceinline__ cx<float> ldg(const cx<float>* p) {
   float2 v = __ldg(reinterpret_cast<const float2*>(p));

@@ -71,6 +71,8 @@ struct BK<float> {
   static constexpr float h3 = 0.8660253882408142f;   // 1/4 + h^2 - 1 = -2.7e-8
   static constexpr float h3b = 0.866025447845459f;   // 1/4 + h^2 - 1 = +7.6e-8, one use in four
 };
+template <>
+struct BK<fx2> : BK<float> {};  // paired lanes: the FP32 constants, broadcast
 
 // a * (SC*C + i*SS*S) for constants C, S and signs SC, SS in {+1, -1}.
 template <typename R, int SC, int SS>
@@ -221,6 +223,27 @@ __device__ __forceinline__ void apply_row(cx<float>* u, const cx<float>* __restr
     }
   }
 }
+// Paired lanes: the FP32 rows, each entry broadcast to both pencils.
+template <int Ns, int RAD, int DIR, bool SMT>
+__device__ __forceinline__ void apply_row(cx<fx2>* u, const cx<float>* __restrict__ rows, int k) {
+  if constexpr (RAD % 2 == 0) {
+    const float4* r4 = reinterpret_cast<const float4*>(rows) + k;
+#pragma unroll
+    for (int i = 0; i < RAD / 2; ++i) {
+      const float4 q = ld_tab<SMT>(r4 + i * Ns);
+      const cx<fx2> w0 = mk<fx2>(fx2(q.x), fx2(q.y)), w1 = mk<fx2>(fx2(q.z), fx2(q.w));
+      if (i > 0) u[2 * i] = DIR < 0 ? cmul(u[2 * i], w0) : cmulc(u[2 * i], w0);
+      u[2 * i + 1] = DIR < 0 ? cmul(u[2 * i + 1], w1) : cmulc(u[2 * i + 1], w1);
+    }
+  } else {
+#pragma unroll
+    for (int r = 1; r < RAD; ++r) {
+      const cx<float> q = ld_tab<SMT>(rows + r * Ns + k);
+      const cx<fx2> w = mk<fx2>(fx2(q.x), fx2(q.y));
+      u[r] = DIR < 0 ? cmul(u[r], w) : cmulc(u[r], w);
+    }
+  }
+}
 template <int Ns, int RAD, int DIR, bool SMT>
 __device__ __forceinline__ void apply_row(cx<double>* u, const cx<double>* __restrict__ rows, int k) {
 #pragma unroll
@@ -231,7 +254,7 @@ __device__ __forceinline__ void apply_row(cx<double>* u, const cx<double>* __res
 }
 
 template <typename R, int N, int T, int Ns, int RAD, bool SMT>
-__device__ __forceinline__ void fwd_stage(cx<R>* v, int t, const cx<R>* __restrict__ rows) {
+__device__ __forceinline__ void fwd_stage(cx<R>* v, int t, const cx<Tab<R>>* __restrict__ rows) {
   constexpr int E = N / T;
   constexpr int NB = E / RAD;
 #pragma unroll
@@ -247,7 +270,7 @@ __device__ __forceinline__ void fwd_stage(cx<R>* v, int t, const cx<R>* __restri
 }
 
 template <typename R, int N, int T, int Ns, int RAD, bool SMT>
-__device__ __forceinline__ void inv_stage(cx<R>* v, int t, const cx<R>* __restrict__ rows) {
+__device__ __forceinline__ void inv_stage(cx<R>* v, int t, const cx<Tab<R>>* __restrict__ rows) {
   constexpr int E = N / T;
   constexpr int NB = E / RAD;
 #pragma unroll
@@ -299,7 +322,7 @@ struct Stages {
   // SMT: tws points to shared memory.
   template <bool SMT, class SM>
   static __device__ __forceinline__ void forward(cx<R>* v, cx<R>* sm, const SM& pol, int t,
-                                                 const cx<R>* __restrict__ tws) {
+                                                 const cx<Tab<R>>* __restrict__ tws) {
     fwd_stage<R, N, T, Ns, RAD, SMT>(v, t, tws + OFF);
     if constexpr (sizeof...(REST) > 0) {
       xchg_scatter_to_own<R, N, T, Ns, RAD>(v, sm, pol, t);
@@ -308,7 +331,7 @@ struct Stages {
   }
   template <bool SMT, class SM>
   static __device__ __forceinline__ void inverse(cx<R>* v, cx<R>* sm, const SM& pol, int t,
-                                                 const cx<R>* __restrict__ tws) {
+                                                 const cx<Tab<R>>* __restrict__ tws) {
     if constexpr (sizeof...(REST) > 0) {
       Stages<R, N, T, Ns * RAD, NEXT_OFF, REST...>::template inverse<SMT>(v, sm, pol, t, tws);
       xchg_own_to_scatter<R, N, T, Ns, RAD>(v, sm, pol, t);

@@ -24,6 +24,7 @@
 
 #include "cluster2d.h"
 #include "ctx.h"
+#include "pass_x2.cuh"
 
 using namespace gpe;
 
@@ -73,11 +74,25 @@ bool has_alt_plan(int n) {
   }
 }
 
-// var: plan variant (0 = Plan<N>; 1 = PlanAlt<N>, FP32 and has_alt_plan(N) only).
+// var: plan variant (0 = Plan<N>; 1 = PlanAlt<N>, FP32 and has_alt_plan(N) only;
+// 2 = PlanAlt<N> with the paired step pass (pass_x2.cuh) for the plain step
+// passes it applies to, the scalar PlanAlt<N> kernels for the others).
+bool x2_pass(int var, const PassArgs<float>& a, bool strided) { return var == 2 && x2_applies(a, strided); }
+
 template <typename R>
 cudaError_t dispatch_pass(int N, int var, const PassArgs<R>& a, bool strided, cudaStream_t s) {
   if constexpr (sizeof(R) == 4) {
-    if (var == 1) {
+    if (x2_pass(var, a, strided)) {
+      switch (N) {
+#define X(v) \
+  case v:    \
+    return launch_pass_x2<v>(a, strided, s);
+        GPE_FOR_EACH_ALT(X)
+#undef X
+      }
+      return cudaErrorInvalidValue;
+    }
+    if (var == 1 || var == 2) {
       switch (N) {
 #define X(v) \
   case v:    \
@@ -98,10 +113,21 @@ cudaError_t dispatch_pass(int N, int var, const PassArgs<R>& a, bool strided, cu
   return cudaErrorInvalidValue;
 }
 
+PassGeom dispatch_x2_geom(int N, bool strided) {
+  switch (N) {
+#define X(v) \
+  case v:    \
+    return pass_x2_geom<v>(strided);
+    GPE_FOR_EACH_ALT(X)
+#undef X
+  }
+  return PassGeom{0, 1, 0};
+}
+
 template <typename R>
 PassGeom dispatch_geom(int N, int var, bool strided) {
   if constexpr (sizeof(R) == 4) {
-    if (var == 1) {
+    if (var == 1 || var == 2) {
       switch (N) {
 #define X(v) \
   case v:    \
@@ -285,7 +311,7 @@ bool use_tma(const gpe_ctx* c, const Field& f, const AxisPass& ap) {
 }
 
 PlanInfo dispatch_plan(int N, int var) {
-  if (var == 1) {
+  if (var == 1 || var == 2) {  // the paired pass reads PlanAlt<N>'s tables
     switch (N) {
 #define X(v) \
   case v:    \
@@ -777,7 +803,16 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
     CU(dispatch_tma<R>(ap.N, a, ap.strided, c->stream, c->sms));
   } else {
     const int var = f.plan_var[ap.axis];
-    if (nblk) *nblk = (int)pass_blocks<R>(ap, var);
+    if (nblk) {
+      bool x2 = false;
+      if constexpr (sizeof(R) == 4) x2 = x2_pass(var, a, ap.strided);
+      if (x2) {
+        const PassGeom g = dispatch_x2_geom(ap.N, ap.strided);
+        *nblk = (int)((ap.n_batch + g.ffts - 1) / g.ffts);
+      } else {
+        *nblk = (int)pass_blocks<R>(ap, var);
+      }
+    }
     Launch L(c, cls, bytes);
     CU(dispatch_pass<R>(ap.N, var, a, ap.strided, c->stream));
   }
@@ -2015,14 +2050,17 @@ gpe_status autotune_main(gpe_ctx* c, int chosen[3]) {
           if (e.first == key) var = e.second;
       }
       if (var < 0) {
-        float t[2];
-        for (int v = 0; v < 2; ++v) {
+        // the default plan, the alternative, the paired pass on the
+        // alternative; a non-default one must be 5% faster than the default
+        float t[3];
+        for (int v = 0; v < 3; ++v) {
           f.plan_var[ap.axis] = v;
           CHECK(build_axis_tables<float>(c, f, ap.axis));
           CHECK(set_kinop<float>(c, f, 0.0, 1e-3));  // any unit-modulus factor: timing only
           CHECK(time_axis_pass(c, f, ap, buf, &t[v]));
         }
-        var = t[1] < 0.95f * t[0] ? 1 : 0;
+        const int best = t[2] < t[1] ? 2 : 1;
+        var = t[best] < 0.95f * t[0] ? best : 0;
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tune_cache.push_back({key, var});
       }
@@ -2575,18 +2613,22 @@ gpe_status gpe_solve_split_batch(gpe_ctx** ctxs, int count, const gpe_split_para
 gpe_status gpe_autotune(gpe_ctx* c, int mode, int* chosen) {
   CHECK(check_ctx(c));
   if (c->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "autotune: not available on a spinor context");
-  if (mode < 0 || (mode > 3 && (mode < 16 || mode > 23)))
+  if (mode < 0 || (mode > 4 && (mode < 16 || mode > 23) && (mode < 32 || mode > 39)))
     return fail(c, GPE_ERR_INVALID,
-                "autotune mode must be 0 (off), 1 (now), 2 (auto), 3 (alternative plans) or 16 + axis mask");
+                "autotune mode must be 0 (off), 1 (now), 2 (auto), 3 (alternative plans), 4 (paired passes), "
+                "16 + axis mask or 32 + axis mask");
   int ch[3] = {-1, -1, -1};
-  if (mode == 0 || mode == 3 || mode >= 16) {
-    // fixed plans: the defaults, the alternative wherever one exists (3), or
-    // the alternative on the axes of bit mask mode - 16 (bit 0 = x) (FP32)
-    const int mask = mode == 3 ? 7 : mode >= 16 ? mode - 16 : 0;
+  if (mode == 0 || mode == 3 || mode == 4 || mode >= 16) {
+    // fixed plans: the defaults, the alternative wherever one exists (3),
+    // the paired passes on the alternative wherever one exists (4), or the
+    // alternative (16 + mask) / paired (32 + mask) on the axes of the bit
+    // mask (bit 0 = x) (FP32)
+    const int mask = (mode == 3 || mode == 4) ? 7 : mode >= 32 ? mode - 32 : mode >= 16 ? mode - 16 : 0;
+    const int alt = (mode == 4 || mode >= 32) ? 2 : 1;
     c->tune_mode = mode == 0 ? 0 : 1;
     c->tuned = mode != 0;
     for (int ax = 0; ax < c->ndims; ++ax) {
-      const int v = ((mask >> ax) & 1) && c->prec == GPE_FP32 && has_alt_plan(c->n[ax]) ? 1 : 0;
+      const int v = ((mask >> ax) & 1) && c->prec == GPE_FP32 && has_alt_plan(c->n[ax]) ? alt : 0;
       if (c->main.plan_var[ax] == v) continue;
       c->main.plan_var[ax] = v;
       if (c->prec == GPE_FP32) CHECK(build_axis_tables<float>(c, c->main, ax));
