@@ -311,6 +311,7 @@ __global__ void k_reset_scalars(DevScalars* sc) {
   sc->stop = 0;
   sc->status = RUNNING;
   sc->nonfinite = 0;
+  sc->timeout = 0;
   sc->stall = 0;
   sc->best_delta = INFINITY;
 }

@@ -340,6 +340,9 @@ struct PassArgs {
   const R* mask_c = nullptr;
   long long mask_pa = 1;
   R ecut = R(0);
+  // TMA pass, test of the timeout path only (0 = off): arm the barriers for
+  // copies that are never issued and give up after this many polls.
+  int tma_stall = 0;
 };
 
 }  // namespace gpe

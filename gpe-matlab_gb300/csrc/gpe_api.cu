@@ -797,6 +797,11 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
                ? 1
                : (epi == EPI_ITP ? 2 : 0);
   if (use_tma<R>(c, f, ap)) {
+    // Test knob of the timeout path (off unless GPE_TEST_TMA_STALL is set):
+    // the TMA pass arms its barriers for copies it never issues and polls
+    // them GPE_TEST_TMA_STALL times, so its bounded wait runs out with no
+    // copy in flight.
+    if (const char* e = getenv("GPE_TEST_TMA_STALL")) a.tma_stall = std::max(0, atoi(e));
     const int grid = dispatch_tma_grid<R>(ap.N, a, ap.strided, c->sms);
     if (nblk) *nblk = grid;
     Launch L(c, cls, bytes);
@@ -1073,6 +1078,7 @@ gpe_status itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* M
   s0.stop = 0;
   s0.status = RUNNING;
   s0.nonfinite = 0;
+  s0.timeout = 0;  // a timed-out earlier call does not fail this one
   s0.iter = 0;
   s0.stall = 0;
   s0.best_delta = INFINITY;
@@ -1232,6 +1238,7 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
   s0.stop = 0;
   s0.status = RUNNING;
   s0.nonfinite = 0;
+  s0.timeout = 0;  // a timed-out earlier call does not fail this one
   s0.outer = 0;
   s0.NN0 = NN0;
   s0.NNN = NN0;

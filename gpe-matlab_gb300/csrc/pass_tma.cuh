@@ -108,8 +108,18 @@ __global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value) pass_tm
   }
   __syncthreads();
 
+  // pend[s]: a copy into slot s is in flight (set by every thread alike).
+  // With the test knob a.tma_stall the barrier is armed for bytes that are
+  // never issued, so nothing is ever in flight and the wait runs out.
+  bool pend[2] = {false, false};
+  const int polls = a.tma_stall > 0 ? a.tma_stall : (1 << 22);
   auto issue = [&](long long tile, int slot) {
     const long long b0 = tile * FFTS;
+    if (a.tma_stall > 0) {
+      if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar[slot], 16u);
+      return;
+    }
+    pend[slot] = true;
     if constexpr (L::CONTIG) {
       if (threadIdx.x == 0) {
         const long long np = (a.n_batch - b0 < FFTS) ? a.n_batch - b0 : FFTS;
@@ -138,17 +148,20 @@ __global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value) pass_tm
     const int slot = k & 1;
     const long long next = tile + gridDim.x;
     if (next < ntiles) issue(next, slot ^ 1);
-    const bool ok = mbar_wait(&bar[slot], (uint32_t)((k >> 1) & 1));
+    const bool ok = mbar_wait(&bar[slot], (uint32_t)((k >> 1) & 1), polls);
     if (!__syncthreads_and(ok)) {
-      // A copy did not land in time: flag it, give in-flight copies a bounded
-      // chance to finish so the CTA does not exit under them, and stop.
+      // A copy did not land in time: flag it, give every copy still in
+      // flight (this slot's and the next tile's) a bounded chance to finish
+      // so the CTA does not exit under them, and stop.
       if (threadIdx.x == 0) {
         atomicExch(&a.sc->timeout, 1);
         atomicExch(&a.sc->stop, 1);
       }
-      mbar_wait(&bar[slot ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
+      if (pend[slot]) mbar_wait(&bar[slot], (uint32_t)((k >> 1) & 1));
+      if (pend[slot ^ 1]) mbar_wait(&bar[slot ^ 1], (uint32_t)(((k + 1) >> 1) & 1));
       return;
     }
+    pend[slot] = false;
 
     const long long b = tile * FFTS + f;
     const bool valid = b < a.n_batch;

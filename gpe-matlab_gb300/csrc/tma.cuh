@@ -69,8 +69,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // Bounded wait for phase `parity` of `bar` to complete.  Each try_wait may
 // suspend the thread for a hardware time slice; 1 << 22 polls bound the wait
 // to well under a second on any correct run.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int it = 0; it < (1 << 22); ++it)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int polls = 1 << 22) {
+  for (int it = 0; it < polls; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
