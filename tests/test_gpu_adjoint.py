@@ -138,3 +138,59 @@ def test_adjoint2d_256_gradient_of_bump_amplitudes(gpe):
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - ga64 @ d) < 1e-6 * scale
         assert abs(fd - gam @ d) < 1e-4 * scale
+
+
+def test_adjoint_500_step_window_with_recompute_matches_oracle(gpe):
+    """The checkpoint/recompute path of config 5's window (500 steps of 0.001)
+    on a grid the oracle runs: FP64, 48 x 48 x 32, a memory budget of 60
+    states, which refuses storing every step (K = 1: 505 states) and leaves
+    the sqrt rule (K = 20: 26 checkpoints, 20 segment states and the sweep's
+    arrays, 49 states) and K = 25 (also 49); both match the oracle adjoint
+    and each other bit for bit."""
+    from gpe_gb300 import _lib as L
+
+    axes = (6, 48, 6, 48, 4, 32)
+    task, og, V, psi0, tgt = small_case(gpe, axes, "double")
+    M, ddt = 500, 0.001
+    S = og.mesh["x"].size * 16
+    budget = 60 * S
+    ref_loss, ref = O.adjoint_grad(og, V, task.g, psi0, tgt, ddt, M)
+    with pytest.raises(gpe.GPEError) as e:
+        task.adjoint_grad(tgt, ddt, M, phi0=psi0, checkpoint_every=1, mem_budget=budget)
+    assert e.value.status == L.GPE_ERR_ALLOC
+    loss_a, dV_a = task.adjoint_grad(tgt, ddt, M, phi0=psi0, checkpoint_every=0, mem_budget=budget)
+    loss_b, dV_b = task.adjoint_grad(tgt, ddt, M, phi0=psi0, checkpoint_every=25, mem_budget=budget)
+    assert abs(loss_a - ref_loss) < 1e-12
+    assert rel_l2(dV_a, ref) < 1e-9
+    np.testing.assert_array_equal(dV_a, dV_b)
+    assert loss_a == loss_b
+    task.close()
+
+
+@pytest.mark.slow
+def test_adjoint3d_512_window_within_60GB(gpe):
+    """Config 5's adjoint: 512^3 FP32 (lambda = (1, 1, 2), g = 1), a vortex
+    ring on a Thomas-Fermi-like start, the 500-step window of 0.001 against
+    the ring-free target under the 60 GB budget.  Storing every state (537
+    GB) is refused; the sqrt rule (K = 20, 49 states, 54 GB with the FP64
+    gradient) and K = 25 give the same loss and gradient bit for bit (the
+    recompute is exact), and the gradient is finite and nonzero."""
+    from gpe_gb300 import _lib as L
+    from gpe_workloads import RING3D as W
+
+    grid, task = W.make_task("single")
+    X, Y, Z = grid.mesh["x"], grid.mesh["y"], grid.mesh["z"]
+    r_tf = 18.0
+    n = np.clip(1.0 - (X ** 2 + Y ** 2 + (2.0 * Z) ** 2) / r_tf ** 2, 0.0, None)
+    phi = np.sqrt(n + 1e-4).astype(np.complex128)
+    psi0 = gpe.imprint_vortex_ring(grid, phi, W.g, 0.5 * r_tf)
+    with pytest.raises(gpe.GPEError) as e:
+        task.adjoint_grad(phi, W.dt, 500, phi0=psi0, checkpoint_every=1, mem_budget=60e9)
+    assert e.value.status == L.GPE_ERR_ALLOC
+    loss_a, dV_a = task.adjoint_grad(phi, W.dt, 500, phi0=psi0, checkpoint_every=0, mem_budget=60e9)
+    loss_b, dV_b = task.adjoint_grad(phi, W.dt, 500, phi0=psi0, checkpoint_every=25, mem_budget=60e9)
+    assert np.isfinite(loss_a) and 0.0 < loss_a < 1.0
+    assert np.all(np.isfinite(dV_a)) and np.linalg.norm(dV_a) > 0
+    assert loss_a == loss_b
+    np.testing.assert_array_equal(dV_a, dV_b)
+    task.close()
