@@ -430,7 +430,8 @@ def run_gpu(args, dist):
         "config": workload_config(W),
         "step": f"{INNER} split steps (1 outer step of solve_split)",
         "fft_plans_xyz": {"chosen_by": ("autotuner" if args.plans < 0 else f"fixed (gpe_autotune mode {args.plans})")
-                          + " (0 default plan, 1 alternative, 2 paired passes, -1 single plan)",
+                          + " (0 default plan, 1 alternative, 2 / 3 paired passes on the alternative / default plan,"
+                          " -1 single plan)",
                           "x": plans[0], "y": plans[1], "z": plans[2]},
         "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU",
         "fp64": {"value": value64, "unit": UNIT, "steps": INNER * k64, "ratio_fp32_over_fp64": value / dist.world / value64},
@@ -810,7 +811,7 @@ def run_profile_case(precision: str, blocks: int, variant: int = 0, plans: int =
     W = WORKLOADS[workload]
     grid, task = W.make_task(precision)
     if W.ndims == 3:
-        task.autotune(plans if plans >= 32 else 16 + plans)
+        task.autotune(plans if plans >= 32 else 16 + plans)  # 32 / 48 + mask: paired passes
     task.set_pass_variant(variant)
     task.init_state = W.initial_state(grid) * 30.0
     if W.ndims == 3:
@@ -832,10 +833,10 @@ def main():
                     help="profile case: the workload whose grid and parameters it runs")
     ap.add_argument("--profile-plans", type=int, default=0,
                     help="profile case: bit mask of axes (bit 0 = x) on the alternative FFT plan; "
-                         "32 + mask: the paired passes on those axes")
+                         "32 / 48 + mask: the paired passes on the alternative / default plan on those axes")
     ap.add_argument("--plans", type=int, default=-1,
                     help="FFT plans of the timed context: -1 the autotuner's choice (default), else a gpe_autotune "
-                         "mode (0 default plans, 3 alternative, 4 paired, 16/32 + axis mask)")
+                         "mode (0 default plans, 3 alternative, 4/5 paired on alternative/default, 16/32/48 + axis mask)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)

@@ -74,19 +74,35 @@ bool has_alt_plan(int n) {
   }
 }
 
+// Axis lengths whose default plan has a paired pass (E = 16).
+bool has_x2d_plan(int n) { return n == 128 || n == 256 || n == 512; }
+
 // var: plan variant (0 = Plan<N>; 1 = PlanAlt<N>, FP32 and has_alt_plan(N) only;
 // 2 = PlanAlt<N> with the paired step pass (pass_x2.cuh) for the plain step
-// passes it applies to, the scalar PlanAlt<N> kernels for the others).
-bool x2_pass(int var, const PassArgs<float>& a, bool strided) { return var == 2 && x2_applies(a, strided); }
+// passes it applies to, the scalar PlanAlt<N> kernels for the others;
+// 3 = the same on Plan<N>, has_x2d_plan(N) only).
+bool x2_pass(int var, const PassArgs<float>& a, bool strided) {
+  return (var == 2 || var == 3) && x2_applies(a, strided);
+}
+// The scalar plan variant behind a paired one (its tables and fallback kernels).
+int scalar_var(int var) { return var == 2 ? 1 : var == 3 ? 0 : var; }
 
 template <typename R>
 cudaError_t dispatch_pass(int N, int var, const PassArgs<R>& a, bool strided, cudaStream_t s) {
   if constexpr (sizeof(R) == 4) {
     if (x2_pass(var, a, strided)) {
+      if (var == 3) {
+        switch (N) {
+          case 128: return launch_pass_x2<128, 0>(a, strided, s);
+          case 256: return launch_pass_x2<256, 0>(a, strided, s);
+          case 512: return launch_pass_x2<512, 0>(a, strided, s);
+        }
+        return cudaErrorInvalidValue;
+      }
       switch (N) {
 #define X(v) \
   case v:    \
-    return launch_pass_x2<v>(a, strided, s);
+    return launch_pass_x2<v, 1>(a, strided, s);
         GPE_FOR_EACH_ALT(X)
 #undef X
       }
@@ -113,11 +129,19 @@ cudaError_t dispatch_pass(int N, int var, const PassArgs<R>& a, bool strided, cu
   return cudaErrorInvalidValue;
 }
 
-PassGeom dispatch_x2_geom(int N, bool strided) {
+PassGeom dispatch_x2_geom(int N, int var, bool strided) {
+  if (var == 3) {
+    switch (N) {
+      case 128: return pass_x2_geom<128, 0>(strided);
+      case 256: return pass_x2_geom<256, 0>(strided);
+      case 512: return pass_x2_geom<512, 0>(strided);
+    }
+    return PassGeom{0, 1, 0};
+  }
   switch (N) {
 #define X(v) \
   case v:    \
-    return pass_x2_geom<v>(strided);
+    return pass_x2_geom<v, 1>(strided);
     GPE_FOR_EACH_ALT(X)
 #undef X
   }
@@ -812,7 +836,7 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
       bool x2 = false;
       if constexpr (sizeof(R) == 4) x2 = x2_pass(var, a, ap.strided);
       if (x2) {
-        const PassGeom g = dispatch_x2_geom(ap.N, ap.strided);
+        const PassGeom g = dispatch_x2_geom(ap.N, var, ap.strided);
         *nblk = (int)((ap.n_batch + g.ffts - 1) / g.ffts);
       } else {
         *nblk = (int)pass_blocks<R>(ap, var);
@@ -2057,16 +2081,20 @@ gpe_status autotune_main(gpe_ctx* c, int chosen[3]) {
           if (e.first == key) var = e.second;
       }
       if (var < 0) {
-        // the default plan, the alternative, the paired pass on the
-        // alternative; a non-default one must be 5% faster than the default
-        float t[3];
-        for (int v = 0; v < 3; ++v) {
+        // the default plan, the alternative, the paired passes on the
+        // alternative and on the default plan; a non-default one must be 5%
+        // faster than the default
+        float t[4] = {0.f, 1e30f, 1e30f, 1e30f};
+        const int nv = has_x2d_plan(ap.N) ? 4 : 3;
+        for (int v = 0; v < nv; ++v) {
           f.plan_var[ap.axis] = v;
           CHECK(build_axis_tables<float>(c, f, ap.axis));
           CHECK(set_kinop<float>(c, f, 0.0, 1e-3));  // any unit-modulus factor: timing only
           CHECK(time_axis_pass(c, f, ap, buf, &t[v]));
         }
-        const int best = t[2] < t[1] ? 2 : 1;
+        int best = 1;
+        for (int v = 2; v < nv; ++v)
+          if (t[v] < t[best]) best = v;
         var = t[best] < 0.95f * t[0] ? best : 0;
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tune_cache.push_back({key, var});
@@ -2620,22 +2648,24 @@ gpe_status gpe_solve_split_batch(gpe_ctx** ctxs, int count, const gpe_split_para
 gpe_status gpe_autotune(gpe_ctx* c, int mode, int* chosen) {
   CHECK(check_ctx(c));
   if (c->ncomp != 1) return fail(c, GPE_ERR_UNSUPPORTED, "autotune: not available on a spinor context");
-  if (mode < 0 || (mode > 4 && (mode < 16 || mode > 23) && (mode < 32 || mode > 39)))
+  if (mode < 0 || (mode > 5 && (mode < 16 || mode > 23) && (mode < 32 || mode > 39) && (mode < 48 || mode > 55)))
     return fail(c, GPE_ERR_INVALID,
-                "autotune mode must be 0 (off), 1 (now), 2 (auto), 3 (alternative plans), 4 (paired passes), "
-                "16 + axis mask or 32 + axis mask");
+                "autotune mode must be 0 (off), 1 (now), 2 (auto), 3 (alternative plans), 4 (paired passes on the "
+                "alternative plans), 5 (paired passes on the default plans), or 16 / 32 / 48 + axis mask");
   int ch[3] = {-1, -1, -1};
-  if (mode == 0 || mode == 3 || mode == 4 || mode >= 16) {
+  if (mode == 0 || mode == 3 || mode == 4 || mode == 5 || mode >= 16) {
     // fixed plans: the defaults, the alternative wherever one exists (3),
-    // the paired passes on the alternative wherever one exists (4), or the
-    // alternative (16 + mask) / paired (32 + mask) on the axes of the bit
-    // mask (bit 0 = x) (FP32)
-    const int mask = (mode == 3 || mode == 4) ? 7 : mode >= 32 ? mode - 32 : mode >= 16 ? mode - 16 : 0;
-    const int alt = (mode == 4 || mode >= 32) ? 2 : 1;
+    // the paired passes on the alternative (4) or on the default plan (5)
+    // wherever they exist, or the alternative (16 + mask), paired on the
+    // alternative (32 + mask), paired on the default (48 + mask) on the
+    // axes of the bit mask (bit 0 = x) (FP32)
+    const int mask = (mode >= 3 && mode <= 5) ? 7 : (mode & 15) & 7;
+    const int var = (mode == 5 || mode >= 48) ? 3 : (mode == 4 || mode >= 32) ? 2 : 1;
     c->tune_mode = mode == 0 ? 0 : 1;
     c->tuned = mode != 0;
     for (int ax = 0; ax < c->ndims; ++ax) {
-      const int v = ((mask >> ax) & 1) && c->prec == GPE_FP32 && has_alt_plan(c->n[ax]) ? alt : 0;
+      const bool has = var == 3 ? has_x2d_plan(c->n[ax]) : has_alt_plan(c->n[ax]);
+      const int v = ((mask >> ax) & 1) && c->prec == GPE_FP32 && has ? var : 0;
       if (c->main.plan_var[ax] == v) continue;
       c->main.plan_var[ax] = v;
       if (c->prec == GPE_FP32) CHECK(build_axis_tables<float>(c, c->main, ax));

@@ -328,12 +328,19 @@ __device__ __forceinline__ void apply_phase_x2(cx<fx2>* v, const cx<float>* __re
   }
 }
 
+// Resident threads per SM the paired passes aim at: E <= 12 points per
+// pencil (two pencils: 2E complex values per thread) at 768 (80 registers),
+// E = 16 at 512 (128 registers).
 #ifndef GPE_X2_THREADS_PER_SM
 #define GPE_X2_THREADS_PER_SM 768
 #endif
+#ifndef GPE_X2_THREADS_PER_SM_E16
+#define GPE_X2_THREADS_PER_SM_E16 512
+#endif
 template <class P, class L>
 struct X2MinBlocks {
-  static constexpr int value = L::THREADS <= GPE_X2_THREADS_PER_SM ? GPE_X2_THREADS_PER_SM / L::THREADS : 1;
+  static constexpr int TPS = P::E >= 16 ? GPE_X2_THREADS_PER_SM_E16 : GPE_X2_THREADS_PER_SM;
+  static constexpr int value = L::THREADS <= TPS ? TPS / L::THREADS : 1;
 };
 template <class P>
 struct X2SmemTables {
@@ -423,9 +430,11 @@ inline bool x2_applies(const PassArgs<float>& a, bool strided) {
   return true;
 }
 
-template <int N>
+// V: the plan the paired pass runs on (plans.cuh PlanSel: 0 = Plan<N>,
+// 1 = PlanAlt<N>).
+template <int N, int V>
 PassGeom pass_x2_geom(bool strided);
-template <int N>
+template <int N, int V>
 cudaError_t launch_pass_x2(const PassArgs<float>& a, bool strided, cudaStream_t s);
 
 }  // namespace gpe

@@ -1,7 +1,8 @@
 // pass_x2_launch.cuh - host launchers of the paired FP32 step pass, explicitly
-// instantiated per axis length in pass_x2_*.cu (the lengths with an
-// alternative plan: the paired pass runs on PlanAlt<N>, E <= 12 points per
-// pencil and thread, and reads that plan's tables).
+// instantiated per axis length and plan in pass_x2_*.cu: on PlanAlt<N> for
+// every length with an alternative plan (E = 8 or 12 points per pencil and
+// thread), and on Plan<N> for 128, 256 and 512 (E = 16).  Each reads the
+// tables of its plan.
 #pragma once
 #include "pass_launch.cuh"
 #include "pass_x2.cuh"
@@ -41,22 +42,22 @@ static cudaError_t launch_x2_layout(const PassArgs<float>& a, cudaStream_t s) {
   return cudaLaunchKernelEx(&cfg, kern, b);
 }
 
-template <int N>
+template <int N, int V>
 PassGeom pass_x2_geom(bool strided) {
-  using P = PlanAlt<N>;
+  using P = typename PlanSel<N, V>::type;
   if (strided) return PassGeom{StridedX2<P>::THREADS, StridedX2<P>::PENCILS, x2_smem_bytes<P, StridedX2<P>>()};
   return PassGeom{ContigX2<P>::THREADS, ContigX2<P>::PENCILS, x2_smem_bytes<P, ContigX2<P>>()};
 }
 
-template <int N>
+template <int N, int V>
 cudaError_t launch_pass_x2(const PassArgs<float>& a, bool strided, cudaStream_t s) {
-  using P = PlanAlt<N>;
+  using P = typename PlanSel<N, V>::type;
   if (strided) return launch_x2_layout<P, StridedX2<P>>(a, s);
   return launch_x2_layout<P, ContigX2<P>>(a, s);
 }
 
-#define GPE_INST_PASS_X2(N)                \
-  template PassGeom pass_x2_geom<N>(bool); \
-  template cudaError_t launch_pass_x2<N>(const PassArgs<float>&, bool, cudaStream_t);
+#define GPE_INST_PASS_X2(N, V)                \
+  template PassGeom pass_x2_geom<N, V>(bool); \
+  template cudaError_t launch_pass_x2<N, V>(const PassArgs<float>&, bool, cudaStream_t);
 
 }  // namespace gpe

@@ -417,9 +417,10 @@ class GPEtask:
 
     def autotune(self, mode: int = 1):
         """FFT plan autotuner (gpe_autotune): 0 default plans, 1 tune now,
-        2 automatic (default), 3 alternative plans, 4 paired passes, 16 + m /
-        32 + m alternative / paired on the axes of bit mask m.  Returns the
-        plan variant per axis (x, y, z: 0 default, 1 alternative, 2 paired);
+        2 automatic (default), 3 alternative plans, 4 / 5 paired passes on
+        the alternative / default plans, 16 + m, 32 + m, 48 + m the same on
+        the axes of bit mask m.  Returns the plan variant per axis (x, y, z:
+        0 default, 1 alternative, 2 paired alternative, 3 paired default);
         -1 where an axis has a single plan."""
         ch = (C.c_int * 3)()
         L.check(self._ctx, L.lib.gpe_autotune(self._ctx, int(mode), ch))

@@ -391,22 +391,25 @@ GPE_API gpe_status gpe_set_pass_variant(gpe_ctx *ctx, int variant);
 GPE_API gpe_status gpe_norm_noalloc(const void *d_psi, long long npoints, int precision, double weight,
                                     void *stream, double *norm_out);
 /* FFT plan autotuner (FP32 contexts).  Axis lengths 128, 192, 256, 384 and
- * 512 have two FFT plans (threads per pencil T and radix schedule) and, on
- * the alternative plan, a paired step pass (two pencils per thread on packed
- * FP32x2 arithmetic); the tuner times the three on each axis pass of this
- * grid and keeps the fastest (a non-default one must win by 5%), caching
- * choices per device and grid shape.
+ * 512 have two FFT plans (threads per pencil T and radix schedule) and a
+ * paired step pass (two pencils per thread on packed FP32x2 arithmetic) on
+ * the alternative plan, and 128, 256, 512 also on the default plan; the
+ * tuner times these on each axis pass of this grid and keeps the fastest (a
+ * non-default one must win by 5%), caching choices per device and grid
+ * shape.
  * mode 0: default plans, no tuning; 1: tune now; 2 (default): tune on the
  * first groundstate_itp / solve_split / observables / adjoint call when the
  * grid has >= 2^20 points, and for every context of solve_split_batch;
  * 3: use the alternative plan wherever one exists (testing, measurement);
- * 4: the paired passes wherever an alternative plan exists;
+ * 4: the paired passes on the alternative plan wherever one exists;
+ * 5: the paired passes on the default plan wherever they exist;
  * 16 + m (m = 0..7): the alternative plan on the axes of bit mask m (bit 0 =
  * x, 1 = y, 2 = z), the default elsewhere (reproducing a tuned choice);
- * 32 + m: the paired passes on the axes of bit mask m.
+ * 32 + m / 48 + m: the paired passes on the alternative / default plan on
+ * the axes of bit mask m.
  * chosen (may be NULL) receives the plan variant of axes x, y, z (0 default,
- * 1 alternative, 2 paired, -1 for a length with one plan, FP64 contexts,
- * 2D z). */
+ * 1 alternative, 2 paired on the alternative, 3 paired on the default, -1
+ * for a length with one plan, FP64 contexts, 2D z). */
 GPE_API gpe_status gpe_autotune(gpe_ctx *ctx, int mode, int *chosen);
 /* Diagnostic: the stochastic GPE's noise variates for points 0..n-1 of step
  * `step` (FP32, interleaved n1, n2 per point), on device 0. */
