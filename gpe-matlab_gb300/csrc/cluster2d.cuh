@@ -40,8 +40,11 @@
 
 namespace gpe {
 
-#define X(v)                                                                            \
-  static_assert(Plan<v>::PADSH == 4 && c2_reg(v) == ContigLayout<Plan<v>, float>::REG, \
+#define X(v)                                                                                                 \
+  static_assert(C2Plan<float, v>::PADSH == 4 && c2_reg(v) == ContigLayout<C2Plan<float, v>, float>::REG &&    \
+                    C2Plan<float, v>::T <= 32 && 32 % C2Plan<float, v>::T == 0 &&                            \
+                    C2Plan<double, v>::PADSH == 4 && c2_reg(v) == ContigLayout<C2Plan<double, v>, double>::REG && \
+                    C2Plan<double, v>::T <= 32 && 32 % C2Plan<double, v>::T == 0,                            \
                 "cluster kernel: contiguous layout of N = " #v);
 GPE_C2_SIZES(X)
 #undef X
@@ -110,15 +113,19 @@ template <typename R, class P>
 __device__ __forceinline__ void c2_y_step(cx<R>* home, const C2Geom& g, const C2Grid& G, int col0,
                                           const PassArgs<R>& pa, R s, R mu) {
   constexpr int T = P::T, E = P::E, N = P::N;
-  constexpr int FPI = C2_THREADS / T;
+  constexpr int FPI = C2Threads<R>::value / T;
   using St = typename P::template St<R>;
   const int f = threadIdx.x / T, t = threadIdx.x % T;
   const cx<R>* tws = static_cast<const cx<R>*>(G.tws[1]);
   const cx<R>* php = static_cast<const cx<R>*>(G.php[1]);
   const R* V = static_cast<const R*>(G.V);
-  for (int p0 = 0; p0 < g.cols_pad; p0 += FPI) {
+  for (int p0 = 0; p0 < g.cols; p0 += FPI) {
     const int pc = p0 + f;
-    const bool valid = pc < g.cols;  // pencils past cols are scratch rows of home
+    // A pencil lies within one warp (T <= 32), and home holds whole warps'
+    // pencils: pencils past cols_pad leave their warp idle (warp-uniform),
+    // the ones in [cols, cols_pad) run on scratch space.
+    if (p0 + (int)(threadIdx.x / 32) * (32 / T) >= g.cols_pad) continue;
+    const bool valid = pc < g.cols;
     const typename ContigLayout<P, R>::Pol pol{pc * g.regy};
     cx<R> v[E];
 #pragma unroll
@@ -146,7 +153,7 @@ template <typename R, class P>
 __device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const C2Geom& g, const C2Grid& G, int rank,
                                           const PassArgs<R>& pa, R mu, Kahan<R>* acc) {
   constexpr int T = P::T, E = P::E, N = P::N;
-  constexpr int GX = C2_THREADS / T;
+  constexpr int GX = C2Threads<R>::value / T;
   using St = typename P::template St<R>;
   const int f = threadIdx.x % GX, t = threadIdx.x / GX;
   const cx<R>* tws = static_cast<const cx<R>*>(G.tws[0]);
@@ -154,7 +161,7 @@ __device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const C2Geom
   const R* V = static_cast<const R*>(G.V);
   const uint32_t hb = smem_u32(home);
   const C2XPol<GX> pol{f};
-  const int c0 = t / g.cols, lc0 = t - c0 * g.cols;  // x = t lives in CTA c0, column lc0 (T <= cols)
+  const int c0 = t / g.cols, lc0 = t - c0 * g.cols;  // x = t lives in CTA c0, column lc0
   for (int r0 = 0; r0 < g.rows; r0 += GX) {
     const bool valid = r0 + f < g.rows;
     const int y = rank * g.rows + (valid ? r0 + f : 0);
@@ -167,7 +174,7 @@ __device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const C2Geom
         v[m] = valid ? c2_ld(c2_map(hb + (uint32_t)(lc * g.regy) * (uint32_t)sizeof(cx<R>) + yoff, c), R(0))
                      : mk<R>(R(0), R(0));
         lc += T;
-        if (lc >= g.cols) {
+        while (lc >= g.cols) {  // T may exceed cols: x = t + T*m lives in CTA x / cols
           lc -= g.cols;
           ++c;
         }
@@ -189,7 +196,7 @@ __device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const C2Geom
       for (int m = 0; m < E; ++m) {
         c2_st(c2_map(hb + (uint32_t)(lc * g.regy) * (uint32_t)sizeof(cx<R>) + yoff, c), v[m]);
         lc += T;
-        if (lc >= g.cols) {
+        while (lc >= g.cols) {  // T may exceed cols: x = t + T*m lives in CTA x / cols
           lc -= g.cols;
           ++c;
         }
@@ -204,14 +211,15 @@ template <typename R, class P>
 __device__ __forceinline__ void c2_y_energy(const cx<R>* home, cx<R>* xbuf, const C2Geom& g, const C2Grid& G,
                                             Kahan<R>& kin) {
   constexpr int T = P::T, E = P::E;
-  constexpr int FPI = C2_THREADS / T;
+  constexpr int FPI = C2Threads<R>::value / T;
   using St = typename P::template St<R>;
   const int f = threadIdx.x / T, t = threadIdx.x % T;
   const cx<R>* tws = static_cast<const cx<R>*>(G.tws[1]);
   const R* k2p = static_cast<const R*>(G.k2p[1]);
   const typename ContigLayout<P, R>::Pol pol{f * g.regy};
-  for (int p0 = 0; p0 < g.cols_pad; p0 += FPI) {
+  for (int p0 = 0; p0 < g.cols; p0 += FPI) {
     const int pc = p0 + f;
+    if (p0 + (int)(threadIdx.x / 32) * (32 / T) >= g.cols_pad) continue;  // as in c2_y_step
     const bool valid = pc < g.cols;
     cx<R> v[E];
 #pragma unroll
@@ -230,7 +238,7 @@ template <typename R, class P>
 __device__ __forceinline__ void c2_x_energy(const cx<R>* home, cx<R>* xbuf, const C2Geom& g, const C2Grid& G,
                                             int rank, Kahan<R>& kin) {
   constexpr int T = P::T, E = P::E;
-  constexpr int GX = C2_THREADS / T;
+  constexpr int GX = C2Threads<R>::value / T;
   using St = typename P::template St<R>;
   const int f = threadIdx.x % GX, t = threadIdx.x / GX;
   const cx<R>* tws = static_cast<const cx<R>*>(G.tws[0]);
@@ -249,7 +257,7 @@ __device__ __forceinline__ void c2_x_energy(const cx<R>* home, cx<R>* xbuf, cons
       v[m] = valid ? c2_ld(c2_map(hb + (uint32_t)(lc * g.regy) * (uint32_t)sizeof(cx<R>) + yoff, c), R(0))
                    : mk<R>(R(0), R(0));
       lc += T;
-      if (lc >= g.cols) {
+      while (lc >= g.cols) {
         lc -= g.cols;
         ++c;
       }
@@ -269,7 +277,7 @@ __device__ void c2_y_step_n(int n, cx<R>* home, const C2Geom& g, const C2Grid& G
   switch (n) {
 #define X(v)                                                  \
   case v:                                                     \
-    c2_y_step<R, Plan<v>>(home, g, G, col0, pa, s, mu);       \
+    c2_y_step<R, C2Plan<R, v>>(home, g, G, col0, pa, s, mu);       \
     break;
     GPE_C2_SIZES(X)
 #undef X
@@ -281,7 +289,7 @@ __device__ void c2_x_step_n(int n, cx<R>* home, cx<R>* xbuf, const C2Geom& g, co
   switch (n) {
 #define X(v)                                                      \
   case v:                                                         \
-    c2_x_step<R, Plan<v>>(home, xbuf, g, G, rank, pa, mu, acc);   \
+    c2_x_step<R, C2Plan<R, v>>(home, xbuf, g, G, rank, pa, mu, acc);   \
     break;
     GPE_C2_SIZES(X)
 #undef X
@@ -293,7 +301,7 @@ __device__ void c2_energy_n(const cx<R>* home, cx<R>* xbuf, const C2Geom& g, con
   switch (G.ny) {
 #define X(v)                                            \
   case v:                                               \
-    c2_y_energy<R, Plan<v>>(home, xbuf, g, G, ky);      \
+    c2_y_energy<R, C2Plan<R, v>>(home, xbuf, g, G, ky);      \
     break;
     GPE_C2_SIZES(X)
 #undef X
@@ -302,7 +310,7 @@ __device__ void c2_energy_n(const cx<R>* home, cx<R>* xbuf, const C2Geom& g, con
   switch (G.nx) {
 #define X(v)                                                 \
   case v:                                                    \
-    c2_x_energy<R, Plan<v>>(home, xbuf, g, G, rank, kx);     \
+    c2_x_energy<R, C2Plan<R, v>>(home, xbuf, g, G, rank, kx);     \
     break;
     GPE_C2_SIZES(X)
 #undef X
@@ -336,13 +344,13 @@ __device__ __forceinline__ void c2_cta_reduce(const Kahan<R>* acc, double* red, 
   __syncthreads();
   if (threadIdx.x < NV) {
     double s = 0.0;
-    for (int w = 0; w < C2_THREADS / 32; ++w) s += wpart[w * 8 + threadIdx.x];
+    for (int w = 0; w < C2Threads<R>::value / 32; ++w) s += wpart[w * 8 + threadIdx.x];
     red[threadIdx.x] = s;
   }
 }
 
 template <typename R>
-__global__ void __launch_bounds__(C2_THREADS, 1) k_cluster2d(const C2Args a) {
+__global__ void __launch_bounds__(C2Threads<R>::value, 1) k_cluster2d(const C2Args a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int rank = (int)c2_rank();
   const int cs = (int)c2_nrank();
@@ -371,7 +379,7 @@ __global__ void __launch_bounds__(C2_THREADS, 1) k_cluster2d(const C2Args a) {
     {
       const cx<R>* src = static_cast<const cx<R>*>(G.psi) + (long long)col0 * G.ny;
       const int total = g.cols * G.ny;
-      for (int i = threadIdx.x; i < total; i += C2_THREADS) {
+      for (int i = threadIdx.x; i < total; i += C2Threads<R>::value) {
         const int pc = i / G.ny, y = i - pc * G.ny;
         home[pc * g.regy + padpos<4>(y)] = src[i];
       }
@@ -471,7 +479,7 @@ __global__ void __launch_bounds__(C2_THREADS, 1) k_cluster2d(const C2Args a) {
     {
       cx<R>* dst = static_cast<cx<R>*>(G.psi) + (long long)col0 * G.ny;
       const int total = g.cols * G.ny;
-      for (int i = threadIdx.x; i < total; i += C2_THREADS) {
+      for (int i = threadIdx.x; i < total; i += C2Threads<R>::value) {
         const int pc = i / G.ny, y = i - pc * G.ny;
         dst[i] = home[pc * g.regy + padpos<4>(y)];
       }
@@ -491,7 +499,7 @@ template <typename R>
 cudaLaunchConfig_t c2_config(int nclusters, int cs, size_t smem, cudaStream_t s, cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(nclusters * cs));
-  cfg.blockDim = dim3(C2_THREADS);
+  cfg.blockDim = dim3(C2Threads<R>::value);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   attr[0].id = cudaLaunchAttributeClusterDimension;

@@ -9,18 +9,34 @@
 
 namespace gpe {
 
-constexpr int C2_THREADS = 256;
-constexpr int C2_RED_BYTES = 1024;  // [8] cluster-visible sums + [8][8] warp partials
+// Threads per CTA: 512 for FP32 (16 warps on the few pencils a CTA owns),
+// 256 for FP64, whose E = 16 double plans would spill at 128 registers.
+template <typename R>
+struct C2Threads {
+  static constexpr int value = sizeof(R) == 8 ? 256 : 512;
+};
+__host__ __device__ constexpr int c2_threads(int esz) { return esz == 16 ? 256 : 512; }
+constexpr int C2_RED_BYTES = 2048;  // [8] cluster-visible sums, [8] broadcast, [16][8] warp partials
 
-// Axis lengths the cluster kernel handles (each must have a Plan<N> with the
-// contiguous-axis padding p + p/16 and T <= N/16).
+// Axis lengths the cluster kernel handles, each on its alternative FFT plan
+// where it has one (PlanAlt<N>: twice the threads per pencil and half the
+// points per thread of Plan<N>, so that an FP32 CTA of 512 threads keeps 16
+// warps busy on the few pencils a cluster CTA owns), else on Plan<N>.  Each
+// needs the contiguous-axis padding p + p/16 and T <= 32.
+// FP64 contexts keep Plan<N> (their per-pass kernels exist for Plan<N>
+// only, and the context's tables must match them).
 #define GPE_C2_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384)
+// Plan variant (plans.cuh PlanSel) the cluster kernel of element size esz
+// (bytes of one complex value) uses for length n: the context's tables.
+__host__ __device__ inline int c2_plan_var(int n, int esz) { return (esz == 16 || n == 64 || n == 96) ? 0 : 1; }
+template <typename R, int N>
+using C2Plan = typename PlanSel<N, (sizeof(R) == 8 || N == 64 || N == 96) ? 0 : 1>::type;
 
-__host__ __device__ inline int c2_T(int n) {
+__host__ __device__ inline int c2_T(int n, int esz) {
   switch (n) {
 #define X(v) \
   case v:    \
-    return Plan<v>::T;
+    return esz == 16 ? C2Plan<double, v>::T : C2Plan<float, v>::T;
     GPE_C2_SIZES(X)
 #undef X
   }
@@ -41,11 +57,12 @@ __host__ __device__ inline C2Geom c2_geom(int nx, int ny, int cs, int esz) {
   C2Geom g;
   g.cols = nx / cs;
   g.rows = ny / cs;
-  const int fpi = C2_THREADS / c2_T(ny);
-  g.cols_pad = (g.cols + fpi - 1) / fpi * fpi;
+  const int fpi = c2_threads(esz) / c2_T(ny, esz);
+  const int fpw = 32 / c2_T(ny, esz);  // pencils per warp: home holds whole warps' pencils
+  g.cols_pad = (g.cols + fpw - 1) / fpw * fpw;
   g.regy = c2_reg(ny);
   g.home = g.cols_pad * g.regy;
-  const int gx = C2_THREADS / c2_T(nx);
+  const int gx = c2_threads(esz) / c2_T(nx, esz);
   g.xbuf = gx * nx > fpi * g.regy ? gx * nx : fpi * g.regy;
   g.bytes = (size_t)(g.home + g.xbuf) * (size_t)esz + C2_RED_BYTES;
   return g;
@@ -55,7 +72,7 @@ __host__ __device__ inline C2Geom c2_geom(int nx, int ny, int cs, int esz) {
 struct C2Grid {
   void* psi;                 // cx<R> state, ny x nx, y fastest
   const void* V;             // R potential
-  const void* tws[2];        // stage twiddle rows of Plan<n>: [0] x axis, [1] y axis
+  const void* tws[2];        // stage twiddle rows of C2Plan<n>: [0] x axis, [1] y axis
   const void* php[2];        // kinetic factors exp(-k^2/2 dt)/n in slot order
   const void* k2p[2];        // k^2/2/n in slot order (energy sums)
   DevScalars* sc;

@@ -225,6 +225,98 @@ __device__ __forceinline__ cx<double> cexp_real_times(double a, double dre, doub
   double m = (dre == 0.0) ? 1.0 : exp(a * dre);
   return mk<double>(m * c, m * s);
 }
+// sin and cos of two lanes: the reduction and polynomials of sincos_bounded
+// on packed lanes.  q = rint(x * 2/pi) by adding and removing 1.5 * 2^23
+// (exact round-to-nearest for |x * 2/pi| < 2^22); the low bits of the
+// shifted value are q's quadrant.  In range: |x| <= 65536 in both lanes.
+__device__ __forceinline__ void quadrant(int qi, float s, float c, float& ss, float& cc) {
+  ss = (qi & 1) ? c : s;
+  cc = (qi & 1) ? s : c;
+  if (qi & 2) ss = -ss;
+  if ((qi + 1) & 2) cc = -cc;
+}
+__device__ __forceinline__ void sincos_x2_inrange(fx2 x, fx2& sp, fx2& cp) {
+  const fx2 shifted = fma2(x, fx2(0.636619772f), fx2(12582912.0f));  // 2/pi; 1.5 * 2^23
+  const fx2 q = shifted - fx2(12582912.0f);
+  fx2 r = fma2(q, fx2(-1.57079637e+00f), x);  // pi/2 rounded to float
+  r = fma2(q, fx2(4.37113900e-08f), r);       // minus (pi/2 - float(pi/2))
+  const fx2 r2 = r * r;
+  fx2 s = fma2(r2, fx2(2.75573192e-06f), fx2(-1.98412698e-04f));
+  s = fma2(r2, s, fx2(8.33333333e-03f));
+  s = fma2(r2, s, fx2(-1.66666667e-01f));
+  s = fma2(r2 * r, s, r);
+  fx2 c = fma2(r2, fx2(-2.75573192e-07f), fx2(2.48015873e-05f));
+  c = fma2(r2, c, fx2(-1.38888889e-03f));
+  c = fma2(r2, c, fx2(4.16666667e-02f));
+  c = fma2(r2, c, fx2(-0.5f));
+  c = fma2(r2, c, fx2(1.0f));
+  float s0, c0, s1, c1;
+  quadrant(__float_as_int(shifted.v.x), s.v.x, c.v.x, s0, c0);
+  quadrant(__float_as_int(shifted.v.y), s.v.y, c.v.y, s1, c1);
+  sp = fx2(s0, s1);
+  cp = fx2(c0, c1);
+}
+// Lanes with |x| > 65536 take the scalar function.
+__device__ __forceinline__ void sincos_x2(fx2 x, fx2& sp, fx2& cp) {
+  if (!(fabsf(x.v.x) <= 65536.0f && fabsf(x.v.y) <= 65536.0f)) {
+    float s0, c0, s1, c1;
+    sincos_bounded(x.v.x, &s0, &c0);
+    sincos_bounded(x.v.y, &s1, &c1);
+    sp = fx2(s0, s1);
+    cp = fx2(c0, c1);
+    return;
+  }
+  sincos_x2_inrange(x, sp, cp);
+}
+
+// exp of two lanes with |x| <= 1/4 (the damping factors of a split step):
+// Taylor series to x^7, truncation < 4e-10 relative.
+__device__ __forceinline__ fx2 exp_x2_small(fx2 x) {
+  fx2 p = fma2(x, fx2(1.98412698e-04f), fx2(1.38888889e-03f));  // 1/7!, 1/6!
+  p = fma2(x, p, fx2(8.33333333e-03f));                         // 1/5!
+  p = fma2(x, p, fx2(4.16666667e-02f));                         // 1/4!
+  p = fma2(x, p, fx2(1.66666667e-01f));                         // 1/3!
+  p = fma2(x, p, fx2(0.5f));
+  p = fma2(x, p, fx2(1.0f));
+  return fma2(x, p, fx2(1.0f));
+}
+// Any argument: lanes beyond 1/4 take expf.
+__device__ __forceinline__ fx2 exp_x2(fx2 x) {
+  if (fabsf(x.v.x) <= 0.25f && fabsf(x.v.y) <= 0.25f) return exp_x2_small(x);
+  return fx2(expf(x.v.x), expf(x.v.y));
+}
+
+// The FP32 phase factors exp(ex[m] (dre + i dim)) applied to v[m], m < E
+// (the real-time prologues of the step passes).  One range check per thread
+// (max |ex| against 65536/|dim| and 1/4/|dre|, true for every split step of a
+// physical run) selects the branch-free path that evaluates two factors at a
+// time on packed lanes; otherwise cexp_real_times, one at a time.
+template <int E>
+__device__ __forceinline__ void apply_rt_phase(cx<float>* v, const float* ex, float dre, float dim) {
+  static_assert(E % 2 == 0, "pairs of points");
+  float mx = 0.0f;
+#pragma unroll
+  for (int m = 0; m < E; ++m) mx = fmaxf(mx, fabsf(ex[m]));
+  if (mx * fabsf(dim) <= 65536.0f && mx * fabsf(dre) <= 0.25f) {
+#pragma unroll
+    for (int m = 0; m < E; m += 2) {
+      const fx2 a(ex[m], ex[m + 1]);
+      fx2 s, c;
+      sincos_x2_inrange(a * fx2(dim), s, c);
+      if (dre != 0.0f) {
+        const fx2 mm = exp_x2_small(a * fx2(dre));
+        c = mm * c;
+        s = mm * s;
+      }
+      v[m] = cmul(mk<float>(c.v.x, s.v.x), v[m]);
+      v[m + 1] = cmul(mk<float>(c.v.y, s.v.y), v[m + 1]);
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = cmul(cexp_real_times(ex[m], dre, dim), v[m]);
+  }
+}
+
 __device__ __forceinline__ float rexp(float a) { return expf(a); }
 __device__ __forceinline__ double rexp(double a) { return exp(a); }
 

@@ -1813,14 +1813,17 @@ C2Plan c2_plan(const std::vector<gpe_ctx*>& cs) {
   return best;
 }
 
-// Axis tables of the default plans (the cluster kernel is built on Plan<N>).
+// Axis tables of the plans the cluster kernel is built on (C2Plan: the
+// alternative plan where the length has one), for both axes.
 template <typename R>
-gpe_status default_plans(gpe_ctx* c) {
-  for (int ax = 0; ax < 2; ++ax)
-    if (c->main.plan_var[ax] != 0) {
-      c->main.plan_var[ax] = 0;
+gpe_status cluster_plans(gpe_ctx* c) {
+  for (int ax = 0; ax < 2; ++ax) {
+    const int v = c2_plan_var(c->n[ax], (int)sizeof(cx<R>));
+    if (c->main.plan_var[ax] != v) {
+      c->main.plan_var[ax] = v;
       CHECK(build_axis_tables<R>(c, c->main, ax));
     }
+  }
   return GPE_OK;
 }
 
@@ -1833,7 +1836,7 @@ gpe_status cluster_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, 
     int vk = 0;
     gpe_ctx* ci = cs[i];
     ci->err.clear();
-    gpe_status st = default_plans<R>(ci);
+    gpe_status st = cluster_plans<R>(ci);
     if (st == GPE_OK) st = split_setup<R>(ci, prm, runs[i], vk, 3);
     if (st != GPE_OK) return n > 1 ? fail(c, st, "batch: context " + std::to_string(i) + ": " + ci->err) : st;
     CU(cudaStreamSynchronize(ci->stream));

@@ -285,18 +285,35 @@ __device__ __forceinline__ void prologue(cx<R>* v, const R* sv, const PassArgs<R
       for (int m = 0; m < E; ++m) v[m] = rmul(v[m], s);
       break;
     case PRO_RT_HALF:  // solve_split.m:55-56
+      if constexpr (sizeof(R) == 4) {
+        float ex[E];
 #pragma unroll
-      for (int m = 0; m < E; ++m) {
-        const cx<R> p = rmul(v[m], s);
-        const R ex = (-(sv[m] - mu) - g * norm2(p)) * R(0.5);
-        v[m] = cmul(cexp_real_times(ex, dre, dim), p);
+        for (int m = 0; m < E; ++m) {
+          v[m] = rmul(v[m], s);
+          ex[m] = (-(sv[m] - mu) - g * norm2(v[m])) * 0.5f;
+        }
+        apply_rt_phase<E>(v, ex, dre, dim);
+      } else {
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+          const cx<R> p = rmul(v[m], s);
+          const R ex = (-(sv[m] - mu) - g * norm2(p)) * R(0.5);
+          v[m] = cmul(cexp_real_times(ex, dre, dim), p);
+        }
       }
       break;
     case PRO_RT_FULL:  // solve_split.m:60-61
+      if constexpr (sizeof(R) == 4) {
+        float ex[E];
 #pragma unroll
-      for (int m = 0; m < E; ++m) {
-        const R ex = -(sv[m] - mu) - g * norm2(v[m]);
-        v[m] = cmul(cexp_real_times(ex, dre, dim), v[m]);
+        for (int m = 0; m < E; ++m) ex[m] = -(sv[m] - mu) - g * norm2(v[m]);
+        apply_rt_phase<E>(v, ex, dre, dim);
+      } else {
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+          const R ex = -(sv[m] - mu) - g * norm2(v[m]);
+          v[m] = cmul(cexp_real_times(ex, dre, dim), v[m]);
+        }
       }
       break;
     case PRO_ITP:  // groundstate_itp.m:36/76, :40

@@ -156,62 +156,6 @@ struct StridedX2 {
 
 // ---- packed elementwise math -------------------------------------------------
 
-// sin and cos of both lanes: the reduction and polynomials of sincos_bounded
-// (common.cuh) on packed lanes.  q = rint(x * 2/pi) by adding and removing
-// 1.5 * 2^23 (exact round-to-nearest for |x * 2/pi| < 2^22); the low bits of
-// the shifted value are q's quadrant.  Lanes with |x| > 65536 take the
-// scalar function.
-__device__ __forceinline__ void quadrant(int qi, float s, float c, float& ss, float& cc) {
-  ss = (qi & 1) ? c : s;
-  cc = (qi & 1) ? s : c;
-  if (qi & 2) ss = -ss;
-  if ((qi + 1) & 2) cc = -cc;
-}
-__device__ __forceinline__ void sincos_x2(fx2 x, fx2& sp, fx2& cp) {
-  if (!(fabsf(x.v.x) <= 65536.0f && fabsf(x.v.y) <= 65536.0f)) {
-    float s0, c0, s1, c1;
-    sincos_bounded(x.v.x, &s0, &c0);
-    sincos_bounded(x.v.y, &s1, &c1);
-    sp = fx2(s0, s1);
-    cp = fx2(c0, c1);
-    return;
-  }
-  const fx2 shifted = fma2(x, fx2(0.636619772f), fx2(12582912.0f));  // 2/pi; 1.5 * 2^23
-  const fx2 q = shifted - fx2(12582912.0f);
-  fx2 r = fma2(q, fx2(-1.57079637e+00f), x);  // pi/2 rounded to float
-  r = fma2(q, fx2(4.37113900e-08f), r);       // minus (pi/2 - float(pi/2))
-  const fx2 r2 = r * r;
-  fx2 s = fma2(r2, fx2(2.75573192e-06f), fx2(-1.98412698e-04f));
-  s = fma2(r2, s, fx2(8.33333333e-03f));
-  s = fma2(r2, s, fx2(-1.66666667e-01f));
-  s = fma2(r2 * r, s, r);
-  fx2 c = fma2(r2, fx2(-2.75573192e-07f), fx2(2.48015873e-05f));
-  c = fma2(r2, c, fx2(-1.38888889e-03f));
-  c = fma2(r2, c, fx2(4.16666667e-02f));
-  c = fma2(r2, c, fx2(-0.5f));
-  c = fma2(r2, c, fx2(1.0f));
-  float s0, c0, s1, c1;
-  quadrant(__float_as_int(shifted.v.x), s.v.x, c.v.x, s0, c0);
-  quadrant(__float_as_int(shifted.v.y), s.v.y, c.v.y, s1, c1);
-  sp = fx2(s0, s1);
-  cp = fx2(c0, c1);
-}
-
-// exp of both lanes.  |x| <= 1/4 (the damping factors of a split step):
-// Taylor series to x^7 (truncation < 4e-10 relative); otherwise expf.
-__device__ __forceinline__ fx2 exp_x2(fx2 x) {
-  if (fabsf(x.v.x) <= 0.25f && fabsf(x.v.y) <= 0.25f) {
-    fx2 p = fma2(x, fx2(1.98412698e-04f), fx2(1.38888889e-03f));  // 1/7!, 1/6!
-    p = fma2(x, p, fx2(8.33333333e-03f));                         // 1/5!
-    p = fma2(x, p, fx2(4.16666667e-02f));                         // 1/4!
-    p = fma2(x, p, fx2(1.66666667e-01f));                         // 1/3!
-    p = fma2(x, p, fx2(0.5f));
-    p = fma2(x, p, fx2(1.0f));
-    return fma2(x, p, fx2(1.0f));
-  }
-  return fx2(expf(x.v.x), expf(x.v.y));
-}
-
 // exp(a * (dre + i dim)) of both lanes (cexp_real_times, common.cuh).
 __device__ __forceinline__ cx<fx2> cexp_real_times_x2(fx2 a, float dre, float dim) {
   fx2 s, c;
