@@ -1526,7 +1526,7 @@ gpe_status adjoint_impl(gpe_ctx* c, Field& f, const gpe_adjoint_params* prm, con
     bufs.push_back(*p);
     return true;
   };
-  void *ck = nullptr, *seg = nullptr, *x = nullptr, *lam = nullptr, *tgt = nullptr;
+  void *ck = nullptr, *seg = nullptr, *x = nullptr, *lam = nullptr, *tgt = nullptr, *fwd32 = nullptr;
   double* dV = nullptr;
   if (!alloc(&ck, (size_t)(nck + 1) * S) || !alloc(&seg, (size_t)K * S) || !alloc(&x, S) || !alloc(&lam, S) ||
       !alloc(&tgt, S) || !alloc((void**)&dV, (size_t)P * sizeof(double))) {
@@ -1534,9 +1534,44 @@ gpe_status adjoint_impl(gpe_ctx* c, Field& f, const gpe_adjoint_params* prm, con
     return fail(c, GPE_ERR_ALLOC, "adjoint: device allocation of the checkpoint store failed");
   }
   auto st_at = [&](void* base, int i) { return (cx<R>*)((char*)base + (size_t)i * S); };
+  // Error attribution of the FP64 sweep of an FP32 context (diagnostic,
+  // GPE_ADJ_FORWARD): "fp32" runs every forward step (and recompute) in the
+  // FP32 kernels, so the sweep sees an FP32 trajectory; "round32" keeps FP64
+  // arithmetic and rounds each step's state to FP32, the storage error of an
+  // FP32 trajectory alone.  Unset: the FP64 forward.
+  int fwd_mode = 0;
+  if constexpr (sizeof(R) == 8) {
+    if (const char* e = getenv("GPE_ADJ_FORWARD"))
+      if (c->prec == GPE_FP32 && &f == &c->polish) fwd_mode = strcmp(e, "fp32") == 0 ? 1 : strcmp(e, "round32") == 0 ? 2 : 0;
+    if (fwd_mode != 0 && !alloc(&fwd32, (size_t)P * sizeof(cx<float>))) {
+      cleanup();
+      return fail(c, GPE_ERR_ALLOC, "adjoint: device allocation of the FP32 forward buffer failed");
+    }
+  }
+  auto forward_step = [&](cx<R>* xs) -> gpe_status {
+    if constexpr (sizeof(R) == 8) {
+      if (fwd_mode == 1) {
+        launch_convert_cx<double, float>(xs, (cx<float>*)fwd32, P, nullptr, c->stream);
+        CHECK(strang_step<float>(c, c->main, (cx<float>*)fwd32, prm->ddt));
+        launch_convert_cx<float, double>((const cx<float>*)fwd32, xs, P, nullptr, c->stream);
+        c->launches += 2;
+        return GPE_OK;
+      }
+      CHECK(strang_step<R>(c, f, xs, prm->ddt));
+      if (fwd_mode == 2) {
+        launch_convert_cx<double, float>(xs, (cx<float>*)fwd32, P, nullptr, c->stream);
+        launch_convert_cx<float, double>((const cx<float>*)fwd32, xs, P, nullptr, c->stream);
+        c->launches += 2;
+      }
+      return GPE_OK;
+    } else {
+      return strang_step<R>(c, f, xs, prm->ddt);
+    }
+  };
   gpe_status st = GPE_OK;
   auto run = [&]() -> gpe_status {
     CHECK(set_kinop<R>(c, f, 0.0, prm->ddt));
+    if (fwd_mode == 1) CHECK(set_kinop<float>(c, c->main, 0.0, prm->ddt));
     // target in the field's precision
     if constexpr (sizeof(R) == 8) {
       CU(cudaMemcpyAsync(tgt, target, (size_t)P * 16, cudaMemcpyHostToDevice, c->stream));
@@ -1559,7 +1594,7 @@ gpe_status adjoint_impl(gpe_ctx* c, Field& f, const gpe_adjoint_params* prm, con
         Launch L(c, PC_COPY, 2.0 * S);
         CU(cudaMemcpyAsync(st_at(ck, m / K), x, S, cudaMemcpyDeviceToDevice, c->stream));
       }
-      CHECK(strang_step<R>(c, f, (cx<R>*)x, prm->ddt));
+      CHECK(forward_step((cx<R>*)x));
     }
     {
       Launch L(c, PC_COPY, 2.0 * S);
@@ -1591,7 +1626,7 @@ gpe_status adjoint_impl(gpe_ctx* c, Field& f, const gpe_adjoint_params* prm, con
       // step-start states x_m0 .. x_{m1-1}; x_m1 is checkpoint s+1
       CU(cudaMemcpyAsync(x, st_at(ck, s), S, cudaMemcpyDeviceToDevice, c->stream));
       for (int m = m0 + 1; m < m1; ++m) {
-        CHECK(strang_step<R>(c, f, (cx<R>*)x, prm->ddt));
+        CHECK(forward_step((cx<R>*)x));
         Launch L(c, PC_COPY, 2.0 * S);
         CU(cudaMemcpyAsync(st_at(seg, m - m0), x, S, cudaMemcpyDeviceToDevice, c->stream));
       }

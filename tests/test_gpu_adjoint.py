@@ -194,3 +194,50 @@ def test_adjoint3d_512_window_within_60GB(gpe):
     assert loss_a == loss_b
     np.testing.assert_array_equal(dV_a, dV_b)
     task.close()
+
+
+@pytest.mark.slow
+def test_adjoint2d_256_fp32_error_sources(gpe, monkeypatch):
+    """Where the FP32 context's gradient error on config 4 (256^2, 2000 steps,
+    checkpoints every 50) comes from, against the FP64 oracle adjoint: the
+    FP32 sweep; the FP64 sweep fed an FP32-arithmetic forward trajectory
+    (GPE_ADJ_FORWARD=fp32); the FP64 sweep of an FP64 forward whose states
+    are rounded to FP32 after every step (GPE_ADJ_FORWARD=round32); the FP64
+    sweep of the FP64 forward.  Printed as an ADJOINT-ERRORS line."""
+    import json
+
+    from gpe_gb300.imprint import imprint_vortex
+    from gpe_workloads import ADJOINT2D as W
+
+    g64 = W.make_grid("double")
+    t64 = gpe.GPEtask(g64, lambda X, Y, Z: 0.5 * (X ** 2 + Y ** 2))
+    t64.Ntotal, t64.g = W.Ntotal, W.g
+    X, Y = g64.mesh["x"], g64.mesh["y"]
+    psi0 = np.asarray(t64.groundstate_itp(W.itp_dt, W.itp_eps, np.exp(-(X ** 2 + Y ** 2) / 32).astype(complex)),
+                      dtype=np.complex128)
+    tgt = imprint_vortex(g64, psi0, W.g, W.vortex_x0)
+    a, basis = W.bumps(g64)
+    V0 = W.trap(g64)
+    Va = V0 + sum(aj * b for aj, b in zip(a, basis))
+    og = O.Grid(W.box, W.n, W.box, W.n)
+    _, dVo = O.adjoint_grad(og, Va, W.g, psi0, tgt, W.dt, W.steps)
+    gao = np.array([np.sum(dVo * b) for b in basis])
+
+    t32 = gpe.GPEtask(W.make_grid("single"), lambda X, Y, Z: V0)
+    t32.g = W.g
+    kw = dict(phi0=psi0, V=Va, checkpoint_every=W.checkpoint_every)
+    errs = {}
+    for name, env, prec in (("fp32_sweep", None, None), ("fp64_sweep_fp32_forward", "fp32", "double"),
+                            ("fp64_sweep_fp64_forward_states_rounded_to_fp32", "round32", "double"),
+                            ("fp64_sweep_fp64_forward", None, "double")):
+        if env:
+            monkeypatch.setenv("GPE_ADJ_FORWARD", env)
+        else:
+            monkeypatch.delenv("GPE_ADJ_FORWARD", raising=False)
+        _, dV = t32.adjoint_grad(tgt, W.dt, W.steps, precision=prec, **kw)
+        errs[name] = {"dLdV_rel_l2": rel_l2(dV, dVo), "dLda_rel_l2": rel_l2(t32.project_gradient(dV, basis), gao)}
+    monkeypatch.delenv("GPE_ADJ_FORWARD", raising=False)
+    print("ADJOINT-ERRORS " + json.dumps(errs), flush=True)
+    assert errs["fp64_sweep_fp64_forward"]["dLda_rel_l2"] < 1e-4
+    t32.close()
+    t64.close()
