@@ -6,6 +6,8 @@
 #include <mutex>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "aux_kernels.cuh"
 
 namespace gpe {
@@ -525,6 +527,41 @@ INST_CONV(double, double)
 }  // namespace gpe
 
 namespace gpe {
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on the driver library).
+bool encode_tile_map(CUtensorMap* m, const void* base, int unit, int units, const long long* tdim, int pencils,
+                     int ax, int len) {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool looked = false;
+  static std::mutex mu;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!looked) {
+      looked = true;
+      void* p = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+              cudaSuccess &&
+          q == cudaDriverEntryPointSuccess)
+        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+      else
+        (void)cudaGetLastError();
+    }
+  }
+  if (!fn) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)(units * tdim[0]), (cuuint64_t)tdim[1], (cuuint64_t)tdim[2],
+                              (cuuint64_t)tdim[3]};
+  const cuuint64_t row = (cuuint64_t)(units * unit) * (cuuint64_t)tdim[0];
+  const cuuint64_t strides[3] = {row, row * (cuuint64_t)tdim[1], row * (cuuint64_t)tdim[1] * (cuuint64_t)tdim[2]};
+  const cuuint32_t box[4] = {(cuuint32_t)(units * pencils), (cuuint32_t)(ax == 1 ? len : 1),
+                             (cuuint32_t)(ax == 2 ? len : 1), 1u};
+  const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
+  const CUtensorMapDataType dt = unit == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  return fn(m, dt, 4, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
 // Occupancy cache for the TMA passes (host side).
 int resident_ctas(const void* kern, int threads, size_t smem) {
   struct Key {

@@ -350,7 +350,7 @@ __device__ __forceinline__ void c2_cta_reduce(const Kahan<R>* acc, double* red, 
 }
 
 template <typename R>
-__global__ void __launch_bounds__(C2Threads<R>::value, 1) k_cluster2d(const C2Args a) {
+__global__ void __launch_bounds__(C2Threads<R>::value, C2Threads<R>::min_blocks) k_cluster2d(const C2Args a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int rank = (int)c2_rank();
   const int cs = (int)c2_nrank();

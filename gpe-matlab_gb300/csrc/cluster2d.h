@@ -9,13 +9,19 @@
 
 namespace gpe {
 
-// Threads per CTA: 512 for FP32 (16 warps on the few pencils a CTA owns),
-// 256 for FP64, whose E = 16 double plans would spill at 128 registers.
+// Threads per CTA: 512 for FP32 (16 warps on the few pencils a CTA owns;
+// GPE_C2_THREADS_F32 = 256 gives two CTAs per SM where shared memory
+// allows), 256 for FP64, whose E = 16 double plans would spill at 128
+// registers.
+#ifndef GPE_C2_THREADS_F32
+#define GPE_C2_THREADS_F32 512
+#endif
 template <typename R>
 struct C2Threads {
-  static constexpr int value = sizeof(R) == 8 ? 256 : 512;
+  static constexpr int value = sizeof(R) == 8 ? 256 : GPE_C2_THREADS_F32;
+  static constexpr int min_blocks = sizeof(R) == 8 ? 1 : 512 / GPE_C2_THREADS_F32;
 };
-__host__ __device__ constexpr int c2_threads(int esz) { return esz == 16 ? 256 : 512; }
+__host__ __device__ constexpr int c2_threads(int esz) { return esz == 16 ? 256 : GPE_C2_THREADS_F32; }
 constexpr int C2_RED_BYTES = 2048;  // [8] cluster-visible sums, [8] broadcast, [16][8] warp partials
 
 // Axis lengths the cluster kernel handles, each on its alternative FFT plan

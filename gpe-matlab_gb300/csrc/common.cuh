@@ -435,6 +435,12 @@ struct PassArgs {
   // TMA pass, test of the timeout path only (0 = off): arm the barriers for
   // copies that are never issued and give up after this many polls.
   int tma_stall = 0;
+  // TMA pass, strided axes: the state (and side array) as 4D tensors
+  // (y, x, z, component) of extents tdim, copied one box per tile through
+  // the kernel's tensor-map parameters (tma_tensor = 1); otherwise one bulk
+  // copy per 128-byte row.
+  int tma_tensor = 0;
+  long long tdim[4] = {1, 1, 1, 1};
 };
 
 }  // namespace gpe

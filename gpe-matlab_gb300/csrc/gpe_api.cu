@@ -826,6 +826,13 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
     // them GPE_TEST_TMA_STALL times, so its bounded wait runs out with no
     // copy in flight.
     if (const char* e = getenv("GPE_TEST_TMA_STALL")) a.tma_stall = std::max(0, atoi(e));
+    // strided tiles as tensor boxes (GPE_TMA_TENSOR=0: one bulk copy per row)
+    const char* tt = getenv("GPE_TMA_TENSOR");
+    a.tma_tensor = !(tt && atoi(tt) == 0);
+    a.tdim[0] = c->n[1];
+    a.tdim[1] = c->n[0];
+    a.tdim[2] = c->ndims == 3 ? c->n[2] : 1;
+    a.tdim[3] = ap.one_comp ? 1 : c->ncomp;
     const int grid = dispatch_tma_grid<R>(ap.N, a, ap.strided, c->sms);
     if (nblk) *nblk = grid;
     Launch L(c, cls, bytes);

@@ -2,6 +2,8 @@
 // instantiated per (precision, axis length) in the pass_*.cu files so that
 // the FFT kernels compile in parallel translation units.
 #pragma once
+#include <string.h>
+
 #include "pass_tma.cuh"
 
 namespace gpe {
@@ -83,6 +85,13 @@ cudaError_t launch_pass(const PassArgs<R>& a, bool strided, cudaStream_t s) {
 
 // ---- TMA-staged persistent variant --------------------------------------
 
+// Tensor map of a state (units = 2: complex) or side array (units = 1) of
+// `unit`-byte reals laid out as tdim = (ny, nx, nz, components), with a box of
+// `pencils` y positions by `len` positions along axis `ax` (1 = x, 2 = z).
+// False when the driver offers no tensor maps or refuses the layout.
+bool encode_tile_map(CUtensorMap* m, const void* base, int unit, int units, const long long* tdim, int pencils,
+                     int ax, int len);
+
 template <typename R, class P, class L>
 static cudaError_t launch_tma_layout(const PassArgs<R>& a, cudaStream_t s, int sms) {
   using SMB = TmaSmem<L, R>;
@@ -97,7 +106,21 @@ static cudaError_t launch_tma_layout(const PassArgs<R>& a, cudaStream_t s, int s
   long long grid = (long long)sms * (per_sm > 0 ? per_sm : 1);
   if (grid > ntiles) grid = ntiles;
   if (grid > a.cap) grid = a.cap;
-  kern<<<(unsigned)grid, L::THREADS, smem, s>>>(a);
+  PassArgs<R> b = a;
+  CUtensorMap tm_psi, tm_side;
+  memset(&tm_psi, 0, sizeof(tm_psi));
+  memset(&tm_side, 0, sizeof(tm_side));
+  if constexpr (!L::CONTIG) {
+    const int ax = a.stride == a.tdim[0] ? 1 : 2;
+    const int len = P::N > 256 ? P::N / 2 : P::N;
+    b.tma_tensor = a.tma_tensor && a.tdim[0] % L::FFTS == 0 &&
+                   encode_tile_map(&tm_psi, a.psi, (int)sizeof(R), 2, a.tdim, L::FFTS, ax, len) &&
+                   (a.side == 0 || encode_tile_map(&tm_side, a.side == 2 ? (const void*)a.aux : (const void*)a.V,
+                                                   (int)sizeof(R), 1, a.tdim, L::FFTS, ax, len));
+  } else {
+    b.tma_tensor = 0;
+  }
+  kern<<<(unsigned)grid, L::THREADS, smem, s>>>(b, tm_psi, tm_side);
   return cudaGetLastError();
 }
 

@@ -75,13 +75,27 @@ struct TmaSmem {
   static constexpr size_t bytes(bool side) { return 2 * PSI_BYTES + (side ? 2 * SIDE_BYTES : 0) + 16; }
 };
 
+#ifndef GPE_TMA_THREADS_PER_SM
+#define GPE_TMA_THREADS_PER_SM 512
+#endif
 template <typename R, class L>
 struct TmaMinBlocks {
-  static constexpr int value = (sizeof(R) == 4 && L::THREADS <= 256) ? 512 / L::THREADS : 1;
+  static constexpr int value = (sizeof(R) == 4 && L::THREADS <= 256) ? GPE_TMA_THREADS_PER_SM / L::THREADS : 1;
 };
 
+// Coordinates (y, x, z, component) of element offset e of the state tensor.
+__device__ __forceinline__ void tensor_coords(const long long* d, long long e, int* c) {
+  const long long plane = d[0] * d[1], vol = plane * d[2];
+  c[0] = (int)(e % d[0]);
+  c[1] = (int)((e / d[0]) % d[1]);
+  c[2] = (int)((e / plane) % d[2]);
+  c[3] = (int)(e / vol);
+}
+
 template <typename R, class P, class L, int KIND>
-__global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value) pass_tma_kernel(const PassArgs<R> a) {
+__global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value)
+    pass_tma_kernel(const PassArgs<R> a, const __grid_constant__ CUtensorMap tm_psi,
+                    const __grid_constant__ CUtensorMap tm_side) {
   extern __shared__ __align__(128) unsigned char smem[];
   // Another CTA may set stop on a timeout while this one starts: the
   // block-wide vote keeps the early exit uniform within the CTA.
@@ -128,6 +142,25 @@ __global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value) pass_tm
         mbar_arrive_expect_tx(&bar[slot], pb + sb);
         tma_load_1d(psib[slot], a.psi + b0 * N, pb, &bar[slot]);
         if (side) tma_load_1d(sideb[slot], side_src + b0 * N, sb, &bar[slot]);
+      }
+    } else if (a.tma_tensor) {
+      // one box per tile (two for N = 512: a box spans at most 256
+      // elements per dimension), landing as [position][pencil]
+      if (threadIdx.x == 0) {
+        const long long base = (b0 % a.inner) + (b0 / a.inner) * a.outer;
+        int cc[4];
+        tensor_coords(a.tdim, base, cc);
+        const int ax = a.stride == a.tdim[0] ? 1 : 2;  // x pencils step by ny, z pencils by nx*ny
+        constexpr int NB = N > 256 ? 2 : 1, BOX = N / NB;
+        mbar_arrive_expect_tx(&bar[slot], (uint32_t)(N * FFTS * (sizeof(cx<R>) + (side ? sizeof(R) : 0))));
+#pragma unroll
+        for (int h = 0; h < NB; ++h) {
+          int q[4] = {cc[0], cc[1], cc[2], cc[3]};
+          q[ax] += h * BOX;
+          // the maps count real units: a complex element is two of them
+          tma_load_4d(psib[slot] + h * BOX * FFTS, &tm_psi, 2 * q[0], q[1], q[2], q[3], &bar[slot]);
+          if (side) tma_load_4d(sideb[slot] + h * BOX * FFTS, &tm_side, q[0], q[1], q[2], q[3], &bar[slot]);
+        }
       }
     } else {
       const long long base = (b0 % a.inner) + (b0 / a.inner) * a.outer;

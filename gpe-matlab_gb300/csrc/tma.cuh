@@ -5,6 +5,7 @@
 // and reports failure, so a kernel never spins forever on a copy that does
 // not arrive.
 #pragma once
+#include <cuda.h>  // CUtensorMap
 #include <stdint.h>
 
 namespace gpe {
@@ -51,6 +52,19 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
           smem_u32(dst)),
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Global -> shared copy of one box of a 4D tensor map (tile mode) at
+// element coordinates (c0 .. c3); the box lands row-major in shared memory
+// (dimension 0 fastest) and signals `bar` with its bytes.  `map` is the
+// address of a __grid_constant__ kernel parameter.
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
       : "memory");
 }
 
