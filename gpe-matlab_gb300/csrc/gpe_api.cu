@@ -1545,11 +1545,18 @@ gpe_status adjoint_impl(gpe_ctx* c, Field& f, const gpe_adjoint_params* prm, con
   // GPE_ADJ_FORWARD): "fp32" runs every forward step (and recompute) in the
   // FP32 kernels, so the sweep sees an FP32 trajectory; "round32" keeps FP64
   // arithmetic and rounds each step's state to FP32, the storage error of an
-  // FP32 trajectory alone.  Unset: the FP64 forward.
+  // FP32 trajectory alone; "kin32" runs only the kinetic passes in FP32 (the
+  // nonlinear phases in FP64), "nl32" only the nonlinear phases.  Unset: the
+  // FP64 forward.
   int fwd_mode = 0;
   if constexpr (sizeof(R) == 8) {
     if (const char* e = getenv("GPE_ADJ_FORWARD"))
-      if (c->prec == GPE_FP32 && &f == &c->polish) fwd_mode = strcmp(e, "fp32") == 0 ? 1 : strcmp(e, "round32") == 0 ? 2 : 0;
+      if (c->prec == GPE_FP32 && &f == &c->polish)
+        fwd_mode = strcmp(e, "fp32") == 0      ? 1
+                   : strcmp(e, "round32") == 0 ? 2
+                   : strcmp(e, "kin32") == 0   ? 3
+                   : strcmp(e, "nl32") == 0    ? 4
+                                               : 0;
     if (fwd_mode != 0 && !alloc(&fwd32, (size_t)P * sizeof(cx<float>))) {
       cleanup();
       return fail(c, GPE_ERR_ALLOC, "adjoint: device allocation of the FP32 forward buffer failed");
@@ -1562,6 +1569,29 @@ gpe_status adjoint_impl(gpe_ctx* c, Field& f, const gpe_adjoint_params* prm, con
         CHECK(strang_step<float>(c, c->main, (cx<float>*)fwd32, prm->ddt));
         launch_convert_cx<float, double>((const cx<float>*)fwd32, xs, P, nullptr, c->stream);
         c->launches += 2;
+        return GPE_OK;
+      }
+      if (fwd_mode == 3 || fwd_mode == 4) {
+        const double h = 0.5 * prm->ddt;
+        auto nl = [&]() {
+          if (fwd_mode == 3) {
+            launch_nl_phase<double>(xs, (const double*)f.V, P, c->prm.g, h, c->stream);
+          } else {
+            launch_convert_cx<double, float>(xs, (cx<float>*)fwd32, P, nullptr, c->stream);
+            launch_nl_phase<float>((cx<float>*)fwd32, (const float*)c->main.V, P, c->prm.g, h, c->stream);
+            launch_convert_cx<float, double>((const cx<float>*)fwd32, xs, P, nullptr, c->stream);
+          }
+        };
+        nl();
+        if (fwd_mode == 3) {
+          launch_convert_cx<double, float>(xs, (cx<float>*)fwd32, P, nullptr, c->stream);
+          CHECK(kinetic_on<float>(c, c->main, fwd32, prm->ddt));
+          launch_convert_cx<float, double>((const cx<float>*)fwd32, xs, P, nullptr, c->stream);
+        } else {
+          CHECK(kinetic_on<R>(c, f, xs, prm->ddt));
+        }
+        nl();
+        CU(cudaGetLastError());
         return GPE_OK;
       }
       CHECK(strang_step<R>(c, f, xs, prm->ddt));
@@ -1578,7 +1608,7 @@ gpe_status adjoint_impl(gpe_ctx* c, Field& f, const gpe_adjoint_params* prm, con
   gpe_status st = GPE_OK;
   auto run = [&]() -> gpe_status {
     CHECK(set_kinop<R>(c, f, 0.0, prm->ddt));
-    if (fwd_mode == 1) CHECK(set_kinop<float>(c, c->main, 0.0, prm->ddt));
+    if (fwd_mode == 1 || fwd_mode == 3) CHECK(set_kinop<float>(c, c->main, 0.0, prm->ddt));
     // target in the field's precision
     if constexpr (sizeof(R) == 8) {
       CU(cudaMemcpyAsync(tgt, target, (size_t)P * 16, cudaMemcpyHostToDevice, c->stream));

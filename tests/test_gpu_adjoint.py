@@ -228,6 +228,8 @@ def test_adjoint2d_256_fp32_error_sources(gpe, monkeypatch):
     kw = dict(phi0=psi0, V=Va, checkpoint_every=W.checkpoint_every)
     errs = {}
     for name, env, prec in (("fp32_sweep", None, None), ("fp64_sweep_fp32_forward", "fp32", "double"),
+                            ("fp64_sweep_fp32_kinetic_forward", "kin32", "double"),
+                            ("fp64_sweep_fp32_nonlinear_forward", "nl32", "double"),
                             ("fp64_sweep_fp64_forward_states_rounded_to_fp32", "round32", "double"),
                             ("fp64_sweep_fp64_forward", None, "double")):
         if env:

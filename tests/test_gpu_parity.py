@@ -167,7 +167,7 @@ def test_autotuner_choices_and_results(gpe):
     axes = (6.0, 128, 6.0, 256, 4.0, 64)
     grid, task, og, ot = make_pair(gpe, axes, harmonic((1.0, 1.0, 1.5)), "single", g=0.5)
     chosen = task.autotune(1)
-    assert chosen[0] in (0, 1) and chosen[1] in (0, 1) and chosen[2] == -1
+    assert chosen[0] in (0, 1, 2, 3) and chosen[1] in (0, 1, 2, 3) and chosen[2] == -1
     assert task.autotune(1) == chosen  # cached per device and shape
     X, Y, Z = og.mesh["x"], og.mesh["y"], og.mesh["z"]
     psi0 = (np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 2) * np.exp(0.2j * Y)).astype(complex)
@@ -317,6 +317,30 @@ def test_tma_pass_variant_matches_direct(gpe, precision):
     assert rel_l2(out[1][0], out[0][0]) < tol
     assert rel_l2(out[1][1], out[0][1]) < tol
     np.testing.assert_allclose(out[1][2], out[0][2], rtol=tol)
+
+
+@pytest.mark.parametrize("precision", ["double", "single"])
+@pytest.mark.parametrize("tensor", ["1", "0"], ids=["tensor_boxes", "row_copies"])
+def test_tma_strided_tiles_512_match_direct(gpe, monkeypatch, precision, tensor):
+    """The TMA pass's strided tiles as tensor-map boxes (two boxes of 256
+    positions per pencil at N = 512) and as per-row bulk copies: x pass of
+    length 512 and z pass of length 256 on a 512 x 32 x 256 grid, against the
+    direct passes (rounding of the sums only)."""
+    monkeypatch.setenv("GPE_TMA_TENSOR", tensor)
+    out = []
+    for variant in (0, 1):
+        grid = gpe.grid3d(8, 512, 4, 32, 6, 256, precision=precision)
+        task = gpe.GPEtask(grid, harmonic((1.0, 1.5, 1.2)))
+        task.set_pass_variant(variant)
+        task.Ntotal, task.g, task.gamma = 30.0, 0.8, 0.01
+        X, Y, Z = grid.mesh["x"], grid.mesh["y"], grid.mesh["z"]
+        task.init_state = (np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 3) * np.exp(0.3j * X)).astype(complex)
+        task.solve_split(0.002, 10, 2)
+        out.append((task.current_state, np.array(task.history["mu"])))
+        task.close()
+    tol = 1e-12 if precision == "double" else 2e-6
+    assert rel_l2(out[1][0], out[0][0]) < tol
+    np.testing.assert_allclose(out[1][1], out[0][1], rtol=tol)
 
 
 @pytest.mark.parametrize("precision", ["double", "single"])
