@@ -203,7 +203,14 @@ def test_adjoint2d_256_fp32_error_sources(gpe, monkeypatch):
     FP32 sweep; the FP64 sweep fed an FP32-arithmetic forward trajectory
     (GPE_ADJ_FORWARD=fp32); the FP64 sweep of an FP64 forward whose states
     are rounded to FP32 after every step (GPE_ADJ_FORWARD=round32); the FP64
-    sweep of the FP64 forward.  Printed as an ADJOINT-ERRORS line."""
+    sweep of the FP64 forward; and the two halves of the FP32 forward apart
+    (GPE_ADJ_FORWARD=kin32: FP32 kinetic passes, FP64 nonlinear phases;
+    nl32: the converse).  Printed as an ADJOINT-ERRORS line.  Measured on a
+    GB300 (dL/da): 9.4e-4, 4.5e-4, 6.6e-7, 2.9e-9; kin32 4.4e-4, nl32 4.3e-5.
+    Storing the trajectory in FP32 costs nothing measurable; the floor is the
+    FP32 kinetic step, whose rounded twiddle and kinetic-factor tables are the
+    same at every step, so their errors add up coherently over the window.
+    The bounds below pin that attribution."""
     import json
 
     from gpe_gb300.imprint import imprint_vortex
@@ -240,6 +247,12 @@ def test_adjoint2d_256_fp32_error_sources(gpe, monkeypatch):
         errs[name] = {"dLdV_rel_l2": rel_l2(dV, dVo), "dLda_rel_l2": rel_l2(t32.project_gradient(dV, basis), gao)}
     monkeypatch.delenv("GPE_ADJ_FORWARD", raising=False)
     print("ADJOINT-ERRORS " + json.dumps(errs), flush=True)
-    assert errs["fp64_sweep_fp64_forward"]["dLda_rel_l2"] < 1e-4
+    e = {k: v["dLda_rel_l2"] for k, v in errs.items()}
+    assert e["fp64_sweep_fp64_forward"] < 1e-8
+    assert e["fp64_sweep_fp64_forward_states_rounded_to_fp32"] < 1e-5  # FP32 storage: harmless
+    assert e["fp64_sweep_fp32_nonlinear_forward"] < 1e-4
+    assert e["fp64_sweep_fp32_kinetic_forward"] > 2e-4  # the floor: FP32 kinetic arithmetic
+    assert 0.7 < e["fp64_sweep_fp32_kinetic_forward"] / e["fp64_sweep_fp32_forward"] < 1.3
+    assert e["fp32_sweep"] < 2e-3
     t32.close()
     t64.close()
