@@ -99,6 +99,10 @@ struct gpe_ctx {
   cudaEvent_t ev_V[2] = {nullptr, nullptr};
   cudaEvent_t ev_sc[2] = {nullptr, nullptr};
   cudaEvent_t t0 = nullptr, t1 = nullptr;
+  // Side streams of the block-end energy passes (the three axes' sums run
+  // concurrently), created on first use, and their fork/join events.
+  cudaStream_t aux[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
   std::string err;
 
   int sms = 152;          // SM count of the device

@@ -918,12 +918,45 @@ gpe_status energy_passes(gpe_ctx* c, Field& f, bool pot, int nblk_kin[3], int* n
   CHECK(ensure_rot_weights<R>(c, f));
   auto passes = energy_axes(c);
   nblk_kin[0] = nblk_kin[1] = nblk_kin[2] = 0;
-  for (auto& ap : passes) {
+  // The axes' sums are independent (each pass reads the state and writes
+  // its own partial slots): the second and third pass run on side streams,
+  // concurrently with the first (each is latency-bound on its own).  Not
+  // while per-kernel profiling (its events live on the context stream) or
+  // stream capture is on, or with GPE_ENERGY_CONCURRENT=0.
+  bool conc = !c->prof && passes.size() > 1 && passes.size() <= 3;
+  if (conc) {
+    const char* e = getenv("GPE_ENERGY_CONCURRENT");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    conc = !(e && atoi(e) == 0) && cudaStreamIsCapturing(c->stream, &cap) == cudaSuccess &&
+           cap == cudaStreamCaptureStatusNone;
+  }
+  if (conc) {
+    for (int k = 0; k < 2; ++k) {
+      if (!c->aux[k]) CU(cudaStreamCreateWithFlags(&c->aux[k], cudaStreamNonBlocking));
+      if (!c->ev_join[k]) CU(cudaEventCreateWithFlags(&c->ev_join[k], cudaEventDisableTiming));
+    }
+    if (!c->ev_fork) CU(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CU(cudaEventRecord(c->ev_fork, c->stream));
+    for (size_t k = 1; k < passes.size(); ++k) CU(cudaStreamWaitEvent(c->aux[k - 1], c->ev_fork, 0));
+  }
+  for (size_t i = 0; i < passes.size(); ++i) {
+    const AxisPass& ap = passes[i];
     int nb = 0;
     const bool ep = pot && ap.axis == 1;
-    CHECK(run_pass<R>(c, f, ap, KIND_ENERGY, pot ? PRO_SCALE : PRO_NONE, EPI_NONE, ep ? 1 : 0, 0.0, 0.0, &nb));
+    const cudaStream_t main_stream = c->stream;
+    if (conc && i > 0) c->stream = c->aux[i - 1];
+    const gpe_status st =
+        run_pass<R>(c, f, ap, KIND_ENERGY, pot ? PRO_SCALE : PRO_NONE, EPI_NONE, ep ? 1 : 0, 0.0, 0.0, &nb);
+    c->stream = main_stream;
+    CHECK(st);
     nblk_kin[ap.axis] = nb;
     if (ep && nblk_pot) *nblk_pot = nb;
+  }
+  if (conc) {
+    for (size_t k = 1; k < passes.size(); ++k) {
+      CU(cudaEventRecord(c->ev_join[k - 1], c->aux[k - 1]));
+      CU(cudaStreamWaitEvent(c->stream, c->ev_join[k - 1], 0));
+    }
   }
   if (c->omega_field || c->lz_scalar) {
     // the -omega Lz term of applyh0 (GPEtask.m:92-94; GPEtaskSpinor.m:72-74
@@ -2426,6 +2459,11 @@ void gpe_destroy(gpe_ctx* c) {
   for (auto e : c->ev_pool) cudaEventDestroy(e);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
+  for (int k = 0; k < 2; ++k) {
+    if (c->aux[k]) cudaStreamDestroy(c->aux[k]);
+    if (c->ev_join[k]) cudaEventDestroy(c->ev_join[k]);
+  }
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
