@@ -24,6 +24,7 @@
 
 #include "cluster2d.h"
 #include "ctx.h"
+#include "grid2d.h"
 #include "pass_x2.cuh"
 
 using namespace gpe;
@@ -2070,14 +2071,185 @@ gpe_status cluster_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, 
   return GPE_OK;
 }
 
-// Runs solve_split on cs through the cluster kernel when every context is
-// eligible (same precision, a cluster shape that fits); *used = false leaves
-// the call to the per-pass paths.
+// ---- grid-wide persistent path of small 2D grids (grid2d.cu, FP32) -------------
+// Tables: the y axis on the cluster kernel's plan (C2Plan), the x axis on the
+// default plan (the pass bodies the persistent kernel runs).
+gpe_status grid2d_plans(gpe_ctx* c) {
+  const int want[2] = {0, c2_plan_var(c->n[1], (int)sizeof(cx<float>))};
+  for (int ax = 0; ax < 2; ++ax)
+    if (c->main.plan_var[ax] != want[ax]) {
+      c->main.plan_var[ax] = want[ax];
+      CHECK(build_axis_tables<float>(c, c->main, ax));
+    }
+  return GPE_OK;
+}
+
+gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, int nctas) {
+  gpe_ctx* c = cs[0];
+  const size_t n = cs.size();
+  std::vector<SplitRun> runs(n);
+  for (size_t i = 0; i < n; ++i) {
+    int vk = 0;
+    gpe_ctx* ci = cs[i];
+    ci->err.clear();
+    gpe_status st = grid2d_plans(ci);
+    if (st == GPE_OK) st = split_setup<float>(ci, prm, runs[i], vk, 3);
+    if (st != GPE_OK) return n > 1 ? fail(c, st, "batch: context " + std::to_string(i) + ": " + ci->err) : st;
+    CU(cudaStreamSynchronize(ci->stream));
+  }
+  const SplitRun& r0 = runs[0];
+  for (size_t i = 1; i < n; ++i)
+    if (runs[i].n_rec != r0.n_rec || runs[i].start != r0.start)
+      return fail(c, GPE_ERR_INVALID, "batch: all contexts need the same n_recalc and current_iter");
+  std::vector<G2Grid> grids(n);
+  std::vector<int> yoff{0}, xoff{0};
+  double bytes = 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    gpe_ctx* ci = cs[i];
+    Field& f = ci->main;
+    G2Grid& G = grids[i];
+    G.psi = f.psi;
+    G.V = f.V;
+    for (int ax = 0; ax < 2; ++ax) {
+      G.tws[ax] = f.tws[ax];
+      G.php[ax] = f.php[ax];
+      G.k2p[ax] = f.k2p[ax];
+    }
+    G.sc = ci->sc;
+    G.partials = ci->partials;
+    G.cap = ci->cap;
+    G.hist = ci->d_hist + runs[i].hist_off;
+    G.nx = ci->n[0];
+    G.ny = ci->n[1];
+    const int py = grid2d_tile_pencils(G.ny, false), px = grid2d_tile_pencils(G.nx, true);
+    G.ytiles = (G.nx + py - 1) / py;
+    G.xtiles = (G.ny + px - 1) / px;
+    if (G.ytiles > G.cap || G.xtiles > G.cap) return fail(c, GPE_ERR_INVALID, "grid2d: partial-sum buffer too small");
+    G.feedback = runs[i].feedback ? 1 : 0;
+    G.start = runs[i].start;
+    G.weight = ci->weight;
+    G.g = ci->prm.g;
+    G.tau = ci->prm.decay_rate;
+    G.dre = runs[i].dre;
+    G.dim = runs[i].dim;
+    yoff.push_back(yoff.back() + G.ytiles);
+    xoff.push_back(xoff.back() + G.xtiles);
+    bytes += (double)ci->P * (4 * sizeof(float) + sizeof(float)) * r0.n_rec * r0.nb;  // state r/w per pass, V
+  }
+  const size_t gb = n * sizeof(G2Grid), ob = (n + 1) * sizeof(int);
+  char* dbuf = nullptr;
+  CU(cudaMalloc(&dbuf, gb + 2 * ob + 16));
+  struct Free {
+    char* p;
+    ~Free() { cudaFree(p); }
+  } free_dbuf{dbuf};
+  CU(cudaMemcpy(dbuf, grids.data(), gb, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(dbuf + gb, yoff.data(), ob, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(dbuf + gb + ob, xoff.data(), ob, cudaMemcpyHostToDevice));
+  unsigned* bar = reinterpret_cast<unsigned*>(dbuf + ((gb + 2 * ob + 7) & ~(size_t)7));
+  int* failf = reinterpret_cast<int*>(bar + 1);
+  CU(cudaMemset(bar, 0, 8));
+  G2Args a;
+  a.grids = reinterpret_cast<const G2Grid*>(dbuf);
+  a.ngrids = (int)n;
+  a.yoff = reinterpret_cast<const int*>(dbuf + gb);
+  a.xoff = reinterpret_cast<const int*>(dbuf + gb + ob);
+  a.n_rec = r0.n_rec;
+  a.nb = r0.nb;
+  a.nouter = 1;
+  a.ddt = r0.ddt;
+  a.dt_outer = r0.dt_outer;
+  a.bar = bar;
+  a.fail = failf;
+  cudaStream_t master = c->stream;
+  int last_j = r0.start;
+  bool stop_req = false;
+  const bool direct = c->prof || prm->on_step;
+  BatchGraph gr;
+  auto enqueue = [&]() -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(unsigned), master);  // the failure flag stays once set
+    if (e == cudaSuccess) e = launch_grid2d(a, nctas, master);
+    return e;
+  };
+  if (!direct && r0.nout > r0.start) {
+    CU(cudaStreamBeginCapture(master, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t e = enqueue();
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(master, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return fail(c, GPE_ERR_CUDA, std::string("grid2d graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    gr.g = g;
+    CU(cudaGraphInstantiate(&gr.x, g, 0));
+  }
+  for (int j = r0.start + 1; j <= r0.nout && !stop_req; ++j) {
+    if (direct) {
+      Launch L(c, PC_CLUSTER, bytes);
+      CU(enqueue());
+    } else {
+      c->launches++;
+      CU(cudaGraphLaunch(gr.x, master));
+    }
+    last_j = j;
+    if (prm->on_step) {  // ext_callback (solve_split.m:80); one context only
+      DevScalars h;
+      CHECK(read_scalars(c, &h));
+      if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
+      const double time2 = (j - 1) * r0.dt_outer + (r0.nb - 1) * r0.ddt * r0.n_rec;
+      c->cur.current_iter = j;
+      c->cur.current_time = time2;
+      c->cur.current_mu = h.muc;
+      c->cur.current_n = h.ncur;
+      if ((int)c->hist_mu.size() < j) {
+        c->hist_mu.resize(j, 0.0);
+        c->hist_n.resize(j, 0.0);
+        c->hist_e.resize(j, 0.0);
+      }
+      c->hist_mu[j - 1] = h.muc;
+      c->hist_n[j - 1] = h.ncur;
+      c->hist_e[j - 1] = h.energy;
+      if (prm->on_step(prm->step_user, j, time2, h.muc, h.ncur) != 0) stop_req = true;
+    }
+  }
+  CU(cudaStreamSynchronize(master));
+  int failed = 0;
+  CU(cudaMemcpy(&failed, failf, sizeof(int), cudaMemcpyDeviceToHost));
+  if (failed) {
+    for (auto* ci : cs) {
+      DevScalars h;
+      CHECK(read_scalars(ci, &h));
+      h.timeout = 1;
+      h.stop = 1;
+      CHECK(write_scalars(ci, h));
+    }
+  }
+  for (size_t i = 0; i < n; ++i) {
+    const double time2 = (last_j - 1) * runs[i].dt_outer + (runs[i].nb - 1) * runs[i].ddt * runs[i].n_rec;
+    const gpe_status st2 = split_finish<float>(cs[i], runs[i], last_j, time2);
+    if (st2 != GPE_OK) return n > 1 ? fail(c, st2, "batch: context " + std::to_string(i) + ": " + cs[i]->err) : st2;
+  }
+  return GPE_OK;
+}
+
+// Runs solve_split on cs through a persistent kernel of small 2D grids when
+// every context is eligible (same precision, a shape that fits): the
+// grid-wide kernel (FP32; GPE_SMALL2D=grid, or the default rule below) or
+// the cluster kernel.  *used = false leaves the call to the per-pass paths.
 gpe_status cluster_run(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, bool* used) {
   *used = false;
   if (c2_env("GPE_CLUSTER", 1) == 0) return GPE_OK;
   for (auto* ci : cs)
     if (!c2_eligible(ci) || ci->prec != cs[0]->prec) return GPE_OK;
+  const char* mode = getenv("GPE_SMALL2D");
+  const bool want_grid = cs[0]->prec == GPE_FP32 && mode && strcmp(mode, "grid") == 0;
+  if (want_grid) {
+    const int nctas = grid2d_max_ctas();
+    if (nctas > 0) {
+      *used = true;
+      return grid2d_impl(cs, prm, nctas);
+    }
+  }
   const C2Plan pl = cs[0]->prec == GPE_FP32 ? c2_plan<float>(cs) : c2_plan<double>(cs);
   if (pl.cs == 0) return GPE_OK;
   *used = true;

@@ -1,0 +1,324 @@
+// grid2d.cu - grid-wide persistent solve_split of small 2D grids (FP32).
+//
+// One cooperative launch advances every grid of a batch (or the single grid
+// of solve_split) through an outer step of solve_split (solve_split.m:49-80)
+// with all SMs on every pass: the y pass of step i is a list of work items
+// (grid, tile of y pencils) over all grids, dealt round-robin to the CTAs;
+// a grid barrier; the x pass likewise (with the block-end epilogue at the
+// last step of a block); a grid barrier; and at a block end the kinetic-
+// energy sums (forward FFTs) of the grids whose mu is needed, a barrier, the
+// block finalizer of every grid (solve_split.m:65-78, one CTA per grid), a
+// barrier.  Each item runs the axis-pass body of the per-pass kernels
+// (pass.cuh pass_body) on its tile, so the arithmetic is that of the
+// per-pass path; the states (a few hundred KB per grid) stay in L2 between
+// passes.  Against the cluster kernel (cluster2d.cuh, one cluster of at most
+// 16 SMs per grid) a single grid gets every SM; against the per-pass path a
+// pass costs a grid barrier instead of a kernel launch.
+//
+// The grid barrier is a monotone arrival counter in global memory (zeroed
+// before each launch): each CTA's thread 0 releases its writes
+// (__threadfence), arrives, and polls the counter with acquire loads; the
+// poll is bounded (about a second), after which the CTA raises the failure
+// flag and returns, and every other CTA stops at its next barrier.  The
+// cooperative launch guarantees all CTAs are resident, so the barrier
+// completes on any correct run.
+#include <algorithm>
+#include <type_traits>
+
+#include "cluster2d.h"
+#include "grid2d.h"
+#include "pass.cuh"
+
+namespace gpe {
+
+template <int N>
+using G2Y = ContigLayout<C2Plan<float, N>, float>;
+template <int N>
+using G2X = StridedLayout<Plan<N>, float>;
+
+#define X(v)                                                                                   \
+  static_assert(G2Y<v>::THREADS == G2_THREADS && G2X<v>::THREADS == G2_THREADS,                \
+                "grid2d kernel: every pass body of length " #v " runs on G2_THREADS threads");
+GPE_C2_SIZES(X)
+#undef X
+
+template <class P, class L>
+constexpr size_t g2_body_smem() {
+  const size_t a = pass_smem_bytes<float, P, L, KIND_STEP>(), b = pass_smem_bytes<float, P, L, KIND_ENERGY>();
+  return a > b ? a : b;
+}
+constexpr size_t g2_smem_max() {
+  size_t m = 0;
+#define X(v)                                                         \
+  m = m > g2_body_smem<C2Plan<float, v>, G2Y<v>>() ? m : g2_body_smem<C2Plan<float, v>, G2Y<v>>(); \
+  m = m > g2_body_smem<Plan<v>, G2X<v>>() ? m : g2_body_smem<Plan<v>, G2X<v>>();
+  GPE_C2_SIZES(X)
+#undef X
+  return m;
+}
+constexpr size_t G2_SMEM = g2_smem_max();
+
+// Bounded grid barrier (see the file comment).  False: the wait ran out
+// somewhere; the caller returns.
+__device__ __forceinline__ bool g2_sync(const G2Args& a, unsigned& target) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    target += gridDim.x;
+    __threadfence();
+    atomicAdd(a.bar, 1u);
+    int good = 1;
+    for (long long it = 0;; ++it) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a.bar) : "memory");
+      if ((int)(v - target) >= 0) break;
+      if (*(volatile int*)a.fail) {
+        good = 0;
+        break;
+      }
+      if (it > (1LL << 22)) {
+        good = 0;
+        atomicExch(a.fail, 1);
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Grid of item `item`: the last g with off[g] <= item.
+__device__ __forceinline__ int g2_find(const int* off, int ng, int item) {
+  int lo = 0, hi = ng - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= item) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Pass arguments of grid G's y pass (axis 1) or x pass (axis 0).
+__device__ __forceinline__ PassArgs<float> g2_args(const G2Grid& G, int axis) {
+  PassArgs<float> p{};
+  p.psi = static_cast<cx<float>*>(G.psi);
+  p.V = static_cast<const float*>(G.V);
+  p.php = static_cast<const cx<float>*>(G.php[axis]);
+  p.tws = static_cast<const cx<float>*>(G.tws[axis]);
+  p.k2p = static_cast<const float*>(G.k2p[axis]);
+  p.partials = G.partials;
+  p.sc = G.sc;
+  p.cap = G.cap;
+  if (axis == 1) {
+    p.n_batch = G.nx;
+    p.stride = 1;
+    p.inner = 1;
+    p.outer = 0;
+    p.kin_slot = S_KY;
+  } else {
+    p.n_batch = G.ny;
+    p.stride = G.ny;
+    p.inner = G.ny;
+    p.outer = (long long)G.nx * G.ny;
+    p.kin_slot = S_KX;
+  }
+  p.g = G.g;
+  p.dre = G.dre;
+  p.dim = G.dim;
+  p.gr = (float)G.g;
+  p.drer = (float)G.dre;
+  p.dimr = (float)G.dim;
+  return p;
+}
+
+// The pass bodies by axis length: one dispatcher per (axis, kind), each
+// called from one place, so that every body is inlined once.
+template <int AXIS, int KIND>
+__device__ __forceinline__ void g2_body(int n, const PassArgs<float>& p, long long tile, unsigned char* smem,
+                                        float s, float mu) {
+  switch (n) {
+#define X(v)                                                                        \
+  case v:                                                                           \
+    if constexpr (AXIS == 1)                                                        \
+      pass_body<float, C2Plan<float, v>, G2Y<v>, KIND>(p, tile, smem, s, mu);        \
+    else                                                                            \
+      pass_body<float, Plan<v>, G2X<v>, KIND>(p, tile, smem, s, mu);                 \
+    break;
+    GPE_C2_SIZES(X)
+#undef X
+  }
+}
+
+// Sum of partials[0 .. n) over the CTA in FP64 (fixed order: thread t sums
+// t, t + G2_THREADS, ..., then a fixed tree), broadcast to every thread.
+__device__ __forceinline__ double g2_cta_sum(const double* p, int n, double* red) {
+  double x = 0.0;
+  for (int i = threadIdx.x; i < n; i += G2_THREADS) x += p[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < G2_THREADS / 32; ++w) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+// The block finalizer of grid g (the arithmetic of aux_kernels.cu
+// k_finalize_block): sums of the block-end epilogue (x tiles) and, when mu
+// is needed, the kinetic sums (y and x tiles); mu, the renormalisation
+// factor, the history record of the outer step's last block.
+__device__ void g2_finalize(const G2Args& a, int g, int jj, bool last, double* red) {
+  const G2Grid& G = a.grids[g];
+  DevScalars* sc = G.sc;
+  if (__syncthreads_or(sc->stop != 0)) return;
+  const bool need = G.feedback || last;
+  const int cap = G.cap;
+  const double n = g2_cta_sum(G.partials + S_N * cap, G.xtiles, red);
+  const double vn = g2_cta_sum(G.partials + S_VN * cap, G.xtiles, red);
+  const double n2 = g2_cta_sum(G.partials + S_N2 * cap, G.xtiles, red);
+  double kin = 0.0;
+  if (need) kin = g2_cta_sum(G.partials + S_KY * cap, G.ytiles, red) + g2_cta_sum(G.partials + S_KX * cap, G.xtiles, red);
+  if (threadIdx.x != 0) return;
+  const int outer = sc->outer;
+  const int j = G.start + 1 + outer;                                  // solve_split.m:49
+  const double time2 = (j - 1) * a.dt_outer + (jj - 1) * a.ddt * a.n_rec;  // solve_split.m:53
+  const double w = G.weight;
+  const double ncur = n * w;  // solve_split.m:67
+  double muc, scale = 1.0, energy = 0.0;
+  if (G.feedback) {  // solve_split.m:68-75
+    double NNN = sc->NNN;
+    if (G.tau > 0) NNN = sc->NN0 * exp(-time2 / G.tau);
+    sc->NNN = NNN;
+    scale = sqrt(NNN / ncur);
+    const double s2 = scale * scale;
+    muc = (s2 * (kin + vn) * w + s2 * s2 * G.g * n2 * w) / NNN;
+    energy = s2 * (kin + vn) * w + 0.5 * s2 * s2 * G.g * n2 * w;
+    sc->mu = muc;
+  } else {  // solve_split.m:76-77
+    muc = (kin + vn + G.g * n2) * w / ncur;
+    energy = (kin + vn + 0.5 * G.g * n2) * w;
+  }
+  sc->energy = energy;
+  sc->scale = scale;
+  sc->ncur = ncur;
+  sc->muc = muc;
+  sc->sums[S_N] = n * w;
+  sc->sums[S_VN] = vn * w;
+  sc->sums[S_N2] = n2 * w;
+  const bool bad = !isfinite(ncur) || !isfinite(muc) || !isfinite(scale);
+  if (bad) {
+    sc->nonfinite = 1;
+    sc->status = NONFINITE;
+    sc->stop = 1;
+  }
+  if (last && !bad) {
+    double* h = G.hist + 3 * (size_t)outer;
+    h[0] = muc;
+    h[1] = ncur;
+    h[2] = energy;
+    sc->outer = outer + 1;
+  }
+}
+
+__global__ void __launch_bounds__(G2_THREADS, 2) k_grid2d(const G2Args a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float s_sc[2];
+  __shared__ double red[G2_THREADS / 32];
+  unsigned target = 0;
+  const int ng = a.ngrids;
+  const int ny_items = a.yoff[ng], nx_items = a.xoff[ng];
+  // one item of a pass: the grid's pending scale and mu, the stop vote
+  auto item_run = [&](auto axis_c, auto kind_c, const int* off, int pro, int epi, int item, bool skip_unneeded,
+                      bool last) {
+    constexpr int AXIS = decltype(axis_c)::value, KIND = decltype(kind_c)::value;
+    const int g = g2_find(off, ng, item);
+    const G2Grid& G = a.grids[g];
+    if (threadIdx.x == 0) {
+      s_sc[0] = (float)G.sc->scale;
+      s_sc[1] = (float)G.sc->mu;
+    }
+    const bool skip = __syncthreads_or(G.sc->stop != 0) || (skip_unneeded && !(G.feedback || last));
+    if (!skip) {
+      PassArgs<float> p = g2_args(G, AXIS);
+      p.kind = KIND;
+      p.pro = pro;
+      p.epi = epi;
+      g2_body<AXIS, KIND>(AXIS == 1 ? G.ny : G.nx, p, item - off[g], smem, s_sc[0], s_sc[1]);
+    }
+    __syncthreads();  // shared memory and s_sc are reused by the next item
+  };
+  using Y = std::integral_constant<int, 1>;
+  using Xa = std::integral_constant<int, 0>;
+  using Step = std::integral_constant<int, KIND_STEP>;
+  using Energy = std::integral_constant<int, KIND_ENERGY>;
+  for (int o = 0; o < a.nouter; ++o) {
+    for (int jj = 1; jj <= a.nb; ++jj) {
+      const bool last = jj == a.nb;
+      for (int i = 1; i <= a.n_rec; ++i) {
+        const int pro = i == 1 ? PRO_RT_HALF : PRO_RT_FULL;  // solve_split.m:55-56 / 60-61
+        for (int item = blockIdx.x; item < ny_items; item += gridDim.x)
+          item_run(Y{}, Step{}, a.yoff, pro, EPI_NONE, item, false, last);
+        if (!g2_sync(a, target)) return;
+        const int epi = i == a.n_rec ? EPI_RT_END : EPI_NONE;  // solve_split.m:60-67
+        for (int item = blockIdx.x; item < nx_items; item += gridDim.x)
+          item_run(Xa{}, Step{}, a.xoff, PRO_NONE, epi, item, false, last);
+        if (!g2_sync(a, target)) return;
+      }
+      // kinetic sums of the block-end state of the grids whose mu is needed
+      for (int item = blockIdx.x; item < ny_items + nx_items; item += gridDim.x) {
+        if (item < ny_items) item_run(Y{}, Energy{}, a.yoff, PRO_NONE, EPI_NONE, item, true, last);
+        else item_run(Xa{}, Energy{}, a.xoff, PRO_NONE, EPI_NONE, item - ny_items, true, last);
+      }
+      if (!g2_sync(a, target)) return;
+      for (int g = blockIdx.x; g < ng; g += gridDim.x) g2_finalize(a, g, jj, last, red);
+      if (!g2_sync(a, target)) return;
+    }
+  }
+}
+
+int grid2d_tile_pencils(int n, bool strided) {
+  switch (n) {
+#define X(v) \
+  case v:    \
+    return strided ? G2X<v>::FFTS : G2Y<v>::FFTS;
+    GPE_C2_SIZES(X)
+#undef X
+  }
+  return 0;
+}
+
+size_t grid2d_smem() { return G2_SMEM; }
+
+int grid2d_max_ctas() {
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  if (cudaFuncSetAttribute(k_grid2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G2_SMEM) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_grid2d, G2_THREADS, G2_SMEM) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return per * sms;
+}
+
+cudaError_t launch_grid2d(const G2Args& a, int nctas, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)nctas);
+  cfg.blockDim = dim3(G2_THREADS);
+  cfg.dynamicSmemBytes = G2_SMEM;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_grid2d, a);
+}
+
+}  // namespace gpe

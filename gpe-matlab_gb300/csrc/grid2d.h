@@ -1,0 +1,56 @@
+// grid2d.h - host-visible part of the grid-wide persistent kernel of small
+// 2D grids (grid2d.cuh): the launch arguments and the launchers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace gpe {
+
+constexpr int G2_THREADS = 256;
+
+// One realisation (context) of the batch.  The y pass runs on the plan the
+// cluster kernel uses (C2Plan: the alternative plan where the length has
+// one), the x pass on the default plan Plan<nx>; the context's tables are
+// built for those plans.
+struct G2Grid {
+  void* psi;                 // cx<R> state, ny x nx, y fastest
+  const void* V;             // R potential
+  const void* tws[2];        // stage twiddle rows: [0] x axis, [1] y axis
+  const void* php[2];        // kinetic factors exp(-k^2/2 dt)/n in slot order
+  const void* k2p[2];        // k^2/2/n in slot order (energy sums)
+  DevScalars* sc;
+  double* partials;          // [NSLOTS + 1][cap] per-tile partial sums of this context
+  double* hist;              // record (muc, ncur, energy) of outer step k at hist + 3*k
+  int cap;
+  int nx, ny;
+  int ytiles, xtiles;        // tiles of the y pass (x columns) and of the x pass (y rows)
+  int feedback;              // gamma > 0 and mu_init == 0: mu and the norm feed back every block
+  int start;                 // current_iter at the start of the run
+  double weight, g, tau;     // cell volume, coupling, decay time (0: none)
+  double dre, dim;           // complex time step dt = i ddt/(1 + i gamma)
+};
+
+struct G2Args {
+  const G2Grid* grids;
+  int ngrids;
+  const int* yoff;  // [ngrids + 1] first y item of each grid (prefix sums of ytiles)
+  const int* xoff;  // [ngrids + 1] first x item of each grid
+  int n_rec, nb;    // steps per block, blocks per outer step
+  int nouter;       // outer steps per launch
+  double ddt, dt_outer;
+  unsigned* bar;    // grid-barrier arrival counter, zero at launch
+  int* fail;        // set when a grid barrier's bounded wait ran out
+};
+
+// Pencils per tile of the y pass (contiguous) and the x pass (strided) for
+// an axis length of the persistent kernel (0: length not handled).
+int grid2d_tile_pencils(int n, bool strided);
+// Dynamic shared memory of the kernel (the largest pass body).
+size_t grid2d_smem();
+// CTAs of a cooperative launch that fit the device at once.
+int grid2d_max_ctas();
+// Cooperative launch of nctas CTAs.
+cudaError_t launch_grid2d(const G2Args& a, int nctas, cudaStream_t s);
+
+}  // namespace gpe

@@ -159,10 +159,11 @@ __device__ __forceinline__ void pair_add(float& h, float& l, float h2, float l2)
 }
 
 // Sum `nred` per-thread values over the CTA in FP64 and store the CTA's
-// partial of each to partials[slot*cap + blockIdx.x].
+// partial of each to partials[slot*cap + idx] (idx: the tile, by default the
+// CTA index).
 template <int THREADS>
 __device__ __forceinline__ void cta_reduce_store(double* vals, const int* slots, int nred,
-                                                 double* partials, int cap);
+                                                 double* partials, int cap, long long idx = -1);
 
 // The same for per-thread compensated sums.  FP32: each thread's Kahan sum
 // s - c is kept as the float pair (s, -c) and the warp combines pairs with
@@ -170,12 +171,13 @@ __device__ __forceinline__ void cta_reduce_store(double* vals, const int* slots,
 // of its FP32 rate), converting to FP64 once per warp.
 template <int THREADS, typename R>
 __device__ __forceinline__ void cta_reduce_store(const Kahan<R>* acc, const int* slots, int nred,
-                                                 double* partials, int cap) {
+                                                 double* partials, int cap, long long idx = -1) {
+  if (idx < 0) idx = blockIdx.x;
   if constexpr (sizeof(R) == 8) {
     double vals[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) vals[i] = i < nred ? acc[i].value() : 0.0;
-    cta_reduce_store<THREADS>(vals, slots, nred, partials, cap);
+    cta_reduce_store<THREADS>(vals, slots, nred, partials, cap, idx);
   } else {
     __shared__ double red[THREADS / 32 > 0 ? THREADS / 32 : 1][4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -196,7 +198,7 @@ __device__ __forceinline__ void cta_reduce_store(const Kahan<R>* acc, const int*
       for (int i = 0; i < nred; ++i) {
         double s = 0.0;
         for (int w = 0; w < (THREADS + 31) / 32; ++w) s += red[w][i];
-        partials[(size_t)slots[i] * cap + blockIdx.x] = s;
+        partials[(size_t)slots[i] * cap + idx] = s;
       }
     }
   }
@@ -204,7 +206,8 @@ __device__ __forceinline__ void cta_reduce_store(const Kahan<R>* acc, const int*
 
 template <int THREADS>
 __device__ __forceinline__ void cta_reduce_store(double* vals, const int* slots, int nred,
-                                                 double* partials, int cap) {
+                                                 double* partials, int cap, long long idx) {
+  if (idx < 0) idx = blockIdx.x;
   __shared__ double red[THREADS / 32 > 0 ? THREADS / 32 : 1][4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -220,7 +223,7 @@ __device__ __forceinline__ void cta_reduce_store(double* vals, const int* slots,
     for (int i = 0; i < nred; ++i) {
       double s = 0.0;
       for (int w = 0; w < (THREADS + 31) / 32; ++w) s += red[w][i];
-      partials[(size_t)slots[i] * cap + blockIdx.x] = s;
+      partials[(size_t)slots[i] * cap + idx] = s;
     }
   }
 }
@@ -359,40 +362,20 @@ __device__ __forceinline__ void epilogue(cx<R>* v, const R* sv, const PassArgs<R
   }
 }
 
-// KIND is a template parameter so the step and energy variants are separate
-// kernels, each with only its own live ranges and code.
+// One tile (FFTS pencils) of an axis pass: tile `tile` of the pass, with
+// the pending scale s and mu of the run (read once per CTA by the caller).
+// The pass kernel runs tile blockIdx.x; the grid-wide persistent kernel of
+// small 2D grids (grid2d.cuh) runs many tiles per CTA.
 template <typename R, class P, class L, int KIND>
-__global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_kernel(const PassArgs<R> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void pass_body(const PassArgs<R>& a, long long tile, unsigned char* smem_raw, R s_scale,
+                                          R s_mu) {
   cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);
-  // Programmatic dependent launch: the next kernel in the stream may be
-  // scheduled as soon as every CTA of this one has started.  A CTA of the
-  // first wave, started early that way, hints its own tile into L2 while the
-  // previous kernel drains (L2 is the point of coherence, so the hint cannot
-  // hold stale data), then waits for that kernel's completion and memory
-  // before it reads anything.  Without the launch attribute both are no-ops.
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  if (a.pdl && a.pf_ahead > 0 && (long long)blockIdx.x < a.pf_ahead) {
-    const long long b0 = (long long)blockIdx.x * L::FFTS;
-    if (b0 < a.n_batch) L::prefetch(a, b0, a.n_batch - b0 < L::FFTS ? a.n_batch - b0 : (long long)L::FFTS);
-  }
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  // The pending scale and mu, converted to R once per CTA (the FP64 pipe of
-  // this GPU is narrow: per-thread conversions showed up in the pass time).
-  __shared__ R scal[2];
-  if (threadIdx.x == 0) {
-    scal[0] = (R)a.sc->scale;
-    scal[1] = (R)a.sc->mu;
-  }
-  // An earlier finalizer (or a timed-out pass) ended the run; the block-wide
-  // vote keeps the decision uniform within the CTA (and publishes scal).
-  if (__syncthreads_or(a.sc->stop != 0)) return;
-
+  const R scal[2] = {s_scale, s_mu};
   constexpr int T = P::T, E = P::E;
   using St = typename P::template St<R>;
   int f, t;
   L::map(threadIdx.x, f, t);
-  const long long b = (long long)blockIdx.x * L::FFTS + f;
+  const long long b = tile * L::FFTS + f;
   const bool valid = b < a.n_batch;
   const long long st = L::step(a);
   // element m of this thread sits at offset m*dm from its first element
@@ -409,7 +392,7 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
   // With the own loads in flight, hint the tile of the CTA one wave of
   // resident CTAs later into L2, so that CTA's loads hit L2.
   if (a.pf_ahead > 0) {
-    const long long b0 = ((long long)blockIdx.x + a.pf_ahead) * L::FFTS;
+    const long long b0 = (tile + a.pf_ahead) * L::FFTS;
     if (b0 < a.n_batch) L::prefetch(a, b0, a.n_batch - b0 < L::FFTS ? a.n_batch - b0 : (long long)L::FFTS);
   }
   // Step-pass tables in shared memory (SmemTables): copied while the pencil
@@ -476,7 +459,7 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
       slots[0] = a.kin_slot;
       nred = 1;
     }
-    cta_reduce_store<L::THREADS>(sums, slots, nred, a.partials, a.cap);
+    cta_reduce_store<L::THREADS>(sums, slots, nred, a.partials, a.cap, tile);
   } else {
     // The side array (V for the phase factors, or the ITP factors) is read
     // right before the phase that uses it: a pass has a prologue or an
@@ -532,9 +515,39 @@ __global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_ke
     const int nred = a.epi == EPI_RT_END ? 3 : a.epi == EPI_ITP ? 1 : 0;
     if (nred > 0) {
       const int slots[4] = {S_N, S_VN, S_N2, 0};
-      cta_reduce_store<L::THREADS>(acc, slots, nred, a.partials, a.cap);
+      cta_reduce_store<L::THREADS>(acc, slots, nred, a.partials, a.cap, tile);
     }
   }
+}
+
+// KIND is a template parameter so the step and energy variants are separate
+// kernels, each with only its own live ranges and code.
+template <typename R, class P, class L, int KIND>
+__global__ void __launch_bounds__(L::THREADS, MinBlocks<R, P, L>::value) pass_kernel(const PassArgs<R> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // Programmatic dependent launch: the next kernel in the stream may be
+  // scheduled as soon as every CTA of this one has started.  A CTA of the
+  // first wave, started early that way, hints its own tile into L2 while the
+  // previous kernel drains (L2 is the point of coherence, so the hint cannot
+  // hold stale data), then waits for that kernel's completion and memory
+  // before it reads anything.  Without the launch attribute both are no-ops.
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if (a.pdl && a.pf_ahead > 0 && (long long)blockIdx.x < a.pf_ahead) {
+    const long long b0 = (long long)blockIdx.x * L::FFTS;
+    if (b0 < a.n_batch) L::prefetch(a, b0, a.n_batch - b0 < L::FFTS ? a.n_batch - b0 : (long long)L::FFTS);
+  }
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  // The pending scale and mu, converted to R once per CTA (the FP64 pipe of
+  // this GPU is narrow: per-thread conversions showed up in the pass time).
+  __shared__ R scal[2];
+  if (threadIdx.x == 0) {
+    scal[0] = (R)a.sc->scale;
+    scal[1] = (R)a.sc->mu;
+  }
+  // An earlier finalizer (or a timed-out pass) ended the run; the block-wide
+  // vote keeps the decision uniform within the CTA (and publishes scal).
+  if (__syncthreads_or(a.sc->stop != 0)) return;
+  pass_body<R, P, L, KIND>(a, (long long)blockIdx.x, smem_raw, scal[0], scal[1]);
 }
 
 // Host-side launch description of a pass for one axis length.

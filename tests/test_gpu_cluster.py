@@ -1,7 +1,10 @@
-"""The persistent cluster kernel of small 2D grids (solve_split of one
-context, or solve_split_batch of many, one launch per outer step for all of
-them) against the per-pass path (pass variant 2: two axis-pass launches per
-step and grid) and against the FP64 oracle, through the C ABI.
+"""The persistent kernels of small 2D grids (solve_split of one context, or
+solve_split_batch of many, one launch per outer step for all of them): the
+cluster kernel (state in distributed shared memory, one cluster per grid)
+and the grid-wide kernel (FP32, GPE_SMALL2D=grid: every pass spread over all
+SMs, grid barriers between passes), against the per-pass path (pass variant
+2: two axis-pass launches per step and grid) and against the FP64 oracle,
+through the C ABI.
 
 The per-point arithmetic of both paths is the same code (the axis passes'
 FFT, kinetic factor, prologue and epilogue), so the states agree to the
@@ -42,14 +45,19 @@ def make(gpe, spec, precision, variant):
     return t
 
 
-@pytest.mark.parametrize("precision", ["double", "single"])
-def test_cluster_batch_matches_per_pass_path(gpe, precision):
-    # the per-pass path on the FFT plans the cluster kernel runs (FP32: the
-    # alternative plan where a length has one), so that both paths do the
-    # same arithmetic and differ only in the order of the block-end sums
+PATHS = [("cluster", "double"), ("cluster", "single"), ("grid", "single")]
+
+
+@pytest.mark.parametrize("path,precision", PATHS)
+def test_cluster_batch_matches_per_pass_path(gpe, monkeypatch, path, precision):
+    monkeypatch.setenv("GPE_SMALL2D", path)
+    # the per-pass path on the FFT plans the persistent kernel runs (FP32:
+    # the cluster kernel takes the alternative plan where a length has one,
+    # the grid kernel on y only), so that both paths do the same arithmetic
+    # and differ only in the order of the block-end sums
     ref = [make(gpe, s, precision, 2) for s in SPECS]
     for t in ref:
-        t.autotune(3)
+        t.autotune(3 if path == "cluster" else 18)
         t.solve_split(0.003, 20, 3)
     batch = [make(gpe, s, precision, 0) for s in SPECS]
     k0 = sum(t.kernel_launches() for t in batch)
@@ -69,8 +77,9 @@ def test_cluster_batch_matches_per_pass_path(gpe, precision):
         t.close()
 
 
-@pytest.mark.parametrize("precision", ["double", "single"])
-def test_cluster_single_context_with_feedback_decay_and_callbacks(gpe, precision):
+@pytest.mark.parametrize("path,precision", PATHS)
+def test_cluster_single_context_with_feedback_decay_and_callbacks(gpe, monkeypatch, path, precision):
+    monkeypatch.setenv("GPE_SMALL2D", path)
     """gamma > 0 with the mu feedback, a decaying target norm and an outer-step
     callback, on one 128 x 96 context, against the FP64 oracle."""
     V = harmonic((1.0, 1.4))
@@ -95,9 +104,11 @@ def test_cluster_single_context_with_feedback_decay_and_callbacks(gpe, precision
     task.close()
 
 
-def test_cluster_kernel_is_the_launched_kernel(gpe):
-    """With per-launch profiling the cluster path launches directly: one
+@pytest.mark.parametrize("path", ["cluster", "grid"])
+def test_cluster_kernel_is_the_launched_kernel(gpe, monkeypatch, path):
+    """With per-launch profiling the persistent path launches directly: one
     cluster_step launch per outer step and no axis-pass launch."""
+    monkeypatch.setenv("GPE_SMALL2D", path)
     grid = gpe.grid2d(6.0, 256, 6.0, 256, precision="single")
     task = gpe.GPEtask(grid, harmonic((1.0, 1.0)))
     task.g, task.Ntotal = 0.5, 10.0
