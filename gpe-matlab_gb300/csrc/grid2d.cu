@@ -247,6 +247,8 @@ __global__ void __launch_bounds__(G2_THREADS, 2) k_grid2d(const G2Args a) {
       p.kind = KIND;
       p.pro = pro;
       p.epi = epi;
+      // the pass body reads V for a phase prologue only when side says so
+      p.side = (pro == PRO_RT_HALF || pro == PRO_RT_FULL || epi == EPI_RT_END) ? 1 : 0;
       g2_body<AXIS, KIND>(AXIS == 1 ? G.ny : G.nx, p, item - off[g], smem, s_sc[0], s_sc[1]);
     }
     __syncthreads();  // shared memory and s_sc are reused by the next item
