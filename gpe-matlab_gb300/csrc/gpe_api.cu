@@ -2138,7 +2138,7 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
   }
   const size_t gb = n * sizeof(G2Grid), ob = (n + 1) * sizeof(int);
   char* dbuf = nullptr;
-  CU(cudaMalloc(&dbuf, gb + 2 * ob + 16));
+  CU(cudaMalloc(&dbuf, gb + 2 * ob + 32));
   struct Free {
     char* p;
     ~Free() { cudaFree(p); }
@@ -2146,9 +2146,9 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
   CU(cudaMemcpy(dbuf, grids.data(), gb, cudaMemcpyHostToDevice));
   CU(cudaMemcpy(dbuf + gb, yoff.data(), ob, cudaMemcpyHostToDevice));
   CU(cudaMemcpy(dbuf + gb + ob, xoff.data(), ob, cudaMemcpyHostToDevice));
-  unsigned* bar = reinterpret_cast<unsigned*>(dbuf + ((gb + 2 * ob + 7) & ~(size_t)7));
-  int* failf = reinterpret_cast<int*>(bar + 1);
-  CU(cudaMemset(bar, 0, 8));
+  unsigned* bar = reinterpret_cast<unsigned*>(dbuf + ((gb + 2 * ob + 15) & ~(size_t)15));
+  int* failf = reinterpret_cast<int*>(bar + 2);
+  CU(cudaMemset(bar, 0, 12));
   G2Args a;
   a.grids = reinterpret_cast<const G2Grid*>(dbuf);
   a.ngrids = (int)n;
@@ -2167,7 +2167,7 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
   const bool direct = c->prof || prm->on_step;
   BatchGraph gr;
   auto enqueue = [&]() -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(unsigned), master);  // the failure flag stays once set
+    cudaError_t e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), master);  // the failure flag stays once set
     if (e == cudaSuccess) e = launch_grid2d(a, nctas, master);
     return e;
   };
@@ -2241,8 +2241,14 @@ gpe_status cluster_run(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, b
   if (c2_env("GPE_CLUSTER", 1) == 0) return GPE_OK;
   for (auto* ci : cs)
     if (!c2_eligible(ci) || ci->prec != cs[0]->prec) return GPE_OK;
+  // Default: the grid-wide kernel for batches (every SM busy on the tiles of
+  // many grids: 64 uneven grids 3.9e10 -> 4.9e10 grid-pt-steps/s), the
+  // cluster kernel for a single grid (a few tiles per pass: the grid
+  // barriers cost more than the cluster's own latency, 256^2 5.7e9 against
+  // 4.2e9).  GPE_SMALL2D=grid|cluster forces one.
   const char* mode = getenv("GPE_SMALL2D");
-  const bool want_grid = cs[0]->prec == GPE_FP32 && mode && strcmp(mode, "grid") == 0;
+  const bool want_grid = cs[0]->prec == GPE_FP32 &&
+                         (mode ? strcmp(mode, "grid") == 0 : cs.size() > 1);
   if (want_grid) {
     const int nctas = grid2d_max_ctas();
     if (nctas > 0) {

@@ -17,7 +17,7 @@
 //
 // The grid barrier is a monotone arrival counter in global memory (zeroed
 // before each launch): each CTA's thread 0 releases its writes
-// (__threadfence), arrives, and polls the counter with acquire loads; the
+// (__threadfence and a release reduction), and polls the counter with acquire loads; the
 // poll is bounded (about a second), after which the CTA raises the failure
 // flag and returns, and every other CTA stops at its next barrier.  The
 // cooperative launch guarantees all CTAs are resident, so the barrier
@@ -57,6 +57,11 @@ constexpr size_t g2_smem_max() {
   return m;
 }
 constexpr size_t G2_SMEM = g2_smem_max();
+// Resident CTAs per SM the kernel is compiled for (registers per thread =
+// 65536 / (G2_THREADS * G2_MIN_BLOCKS), capped at 255).
+#ifndef G2_MIN_BLOCKS
+#define G2_MIN_BLOCKS 2
+#endif
 
 // Bounded grid barrier (see the file comment).  False: the wait ran out
 // somewhere; the caller returns.
@@ -66,7 +71,7 @@ __device__ __forceinline__ bool g2_sync(const G2Args& a, unsigned& target) {
   if (threadIdx.x == 0) {
     target += gridDim.x;
     __threadfence();
-    atomicAdd(a.bar, 1u);
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.bar) : "memory");
     int good = 1;
     for (long long it = 0;; ++it) {
       unsigned v;
@@ -224,11 +229,28 @@ __device__ void g2_finalize(const G2Args& a, int g, int jj, bool last, double* r
   }
 }
 
-__global__ void __launch_bounds__(G2_THREADS, 2) k_grid2d(const G2Args a) {
+__global__ void __launch_bounds__(G2_THREADS, G2_MIN_BLOCKS) k_grid2d(const G2Args a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float s_sc[2];
   __shared__ double red[G2_THREADS / 32];
+  __shared__ int s_item;
   unsigned target = 0;
+  // Items are taken from a monotone counter (a.bar[1], zero at launch): the
+  // phase with n items owns the values base .. base + n - 1; every CTA ends a
+  // phase with one grab past its end, so the next phase's base is
+  // base + n + gridDim.x on every CTA.  Items of uneven cost (grids of
+  // different sizes) spread evenly over the CTAs.
+  unsigned base = 0;
+  auto grab = [&](unsigned n) -> int {
+    if (threadIdx.x == 0) {
+      const unsigned v = atomicAdd(a.bar + 1, 1u) - base;
+      s_item = v < n ? (int)v : -1;
+    }
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();
+    return it;
+  };
   const int ng = a.ngrids;
   const int ny_items = a.yoff[ng], nx_items = a.xoff[ng];
   // one item of a pass: the grid's pending scale and mu, the stop vote
@@ -262,19 +284,22 @@ __global__ void __launch_bounds__(G2_THREADS, 2) k_grid2d(const G2Args a) {
       const bool last = jj == a.nb;
       for (int i = 1; i <= a.n_rec; ++i) {
         const int pro = i == 1 ? PRO_RT_HALF : PRO_RT_FULL;  // solve_split.m:55-56 / 60-61
-        for (int item = blockIdx.x; item < ny_items; item += gridDim.x)
+        for (int item = grab(ny_items); item >= 0; item = grab(ny_items))
           item_run(Y{}, Step{}, a.yoff, pro, EPI_NONE, item, false, last);
+        base += ny_items + gridDim.x;
         if (!g2_sync(a, target)) return;
         const int epi = i == a.n_rec ? EPI_RT_END : EPI_NONE;  // solve_split.m:60-67
-        for (int item = blockIdx.x; item < nx_items; item += gridDim.x)
+        for (int item = grab(nx_items); item >= 0; item = grab(nx_items))
           item_run(Xa{}, Step{}, a.xoff, PRO_NONE, epi, item, false, last);
+        base += nx_items + gridDim.x;
         if (!g2_sync(a, target)) return;
       }
       // kinetic sums of the block-end state of the grids whose mu is needed
-      for (int item = blockIdx.x; item < ny_items + nx_items; item += gridDim.x) {
+      for (int item = grab(ny_items + nx_items); item >= 0; item = grab(ny_items + nx_items)) {
         if (item < ny_items) item_run(Y{}, Energy{}, a.yoff, PRO_NONE, EPI_NONE, item, true, last);
         else item_run(Xa{}, Energy{}, a.xoff, PRO_NONE, EPI_NONE, item - ny_items, true, last);
       }
+      base += ny_items + nx_items + gridDim.x;
       if (!g2_sync(a, target)) return;
       for (int g = blockIdx.x; g < ng; g += gridDim.x) g2_finalize(a, g, jj, last, red);
       if (!g2_sync(a, target)) return;

@@ -39,7 +39,7 @@ struct G2Args {
   int n_rec, nb;    // steps per block, blocks per outer step
   int nouter;       // outer steps per launch
   double ddt, dt_outer;
-  unsigned* bar;    // grid-barrier arrival counter, zero at launch
+  unsigned* bar;    // [0] grid-barrier arrival counter, [1] work-item counter; zero at launch
   int* fail;        // set when a grid barrier's bounded wait ran out
 };
 
