@@ -2250,7 +2250,11 @@ gpe_status cluster_run(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, b
   const bool want_grid = cs[0]->prec == GPE_FP32 &&
                          (mode ? strcmp(mode, "grid") == 0 : cs.size() > 1);
   if (want_grid) {
-    const int nctas = grid2d_max_ctas();
+    // GPE_G2_CTAS caps the CTAs of the grid-wide kernel (measurement: fewer
+    // CTAs make each grid barrier cheaper)
+    int nctas = grid2d_max_ctas();
+    const int cap_ctas = c2_env("GPE_G2_CTAS", 0);
+    if (cap_ctas > 0 && cap_ctas < nctas) nctas = cap_ctas;
     if (nctas > 0) {
       *used = true;
       return grid2d_impl(cs, prm, nctas);
