@@ -2072,10 +2072,10 @@ gpe_status cluster_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, 
 }
 
 // ---- grid-wide persistent path of small 2D grids (grid2d.cu, FP32) -------------
-// Tables: the y axis on the cluster kernel's plan (C2Plan), the x axis on the
-// default plan (the pass bodies the persistent kernel runs).
+// Tables: both axes on the default plans (the pass bodies the persistent
+// kernel runs).
 gpe_status grid2d_plans(gpe_ctx* c) {
-  const int want[2] = {0, c2_plan_var(c->n[1], (int)sizeof(cx<float>))};
+  const int want[2] = {0, 0};
   for (int ax = 0; ax < 2; ++ax)
     if (c->main.plan_var[ax] != want[ax]) {
       c->main.plan_var[ax] = want[ax];

@@ -31,8 +31,13 @@
 
 namespace gpe {
 
+// Both passes on the default plans (fewer instructions and exchanges than
+// the alternative plans; the contiguous exchange of PlanAlt<256> also has
+// 2-way bank conflicts).
 template <int N>
-using G2Y = ContigLayout<C2Plan<float, N>, float>;
+using G2P = Plan<N>;
+template <int N>
+using G2Y = ContigLayout<G2P<N>, float>;
 template <int N>
 using G2X = StridedLayout<Plan<N>, float>;
 
@@ -50,7 +55,7 @@ constexpr size_t g2_body_smem() {
 constexpr size_t g2_smem_max() {
   size_t m = 0;
 #define X(v)                                                         \
-  m = m > g2_body_smem<C2Plan<float, v>, G2Y<v>>() ? m : g2_body_smem<C2Plan<float, v>, G2Y<v>>(); \
+  m = m > g2_body_smem<G2P<v>, G2Y<v>>() ? m : g2_body_smem<G2P<v>, G2Y<v>>(); \
   m = m > g2_body_smem<Plan<v>, G2X<v>>() ? m : g2_body_smem<Plan<v>, G2X<v>>();
   GPE_C2_SIZES(X)
 #undef X
@@ -148,7 +153,7 @@ __device__ __forceinline__ void g2_body(int n, const PassArgs<float>& p, long lo
 #define X(v)                                                                        \
   case v:                                                                           \
     if constexpr (AXIS == 1)                                                        \
-      pass_body<float, C2Plan<float, v>, G2Y<v>, KIND>(p, tile, smem, s, mu);        \
+      pass_body<float, G2P<v>, G2Y<v>, KIND>(p, tile, smem, s, mu);        \
     else                                                                            \
       pass_body<float, Plan<v>, G2X<v>, KIND>(p, tile, smem, s, mu);                 \
     break;

@@ -9,10 +9,8 @@ namespace gpe {
 
 constexpr int G2_THREADS = 256;
 
-// One realisation (context) of the batch.  The y pass runs on the plan the
-// cluster kernel uses (C2Plan: the alternative plan where the length has
-// one), the x pass on the default plan Plan<nx>; the context's tables are
-// built for those plans.
+// One realisation (context) of the batch.  Both passes run on the default
+// plans Plan<n>; the context's tables are built for them.
 struct G2Grid {
   void* psi;                 // cx<R> state, ny x nx, y fastest
   const void* V;             // R potential
