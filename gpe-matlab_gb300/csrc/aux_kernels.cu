@@ -314,6 +314,8 @@ __global__ void k_reset_scalars(DevScalars* sc) {
   sc->status = RUNNING;
   sc->nonfinite = 0;
   sc->timeout = 0;
+  sc->bounds_site = 0;
+  sc->bounds_index = 0;
   sc->stall = 0;
   sc->best_delta = INFINITY;
 }

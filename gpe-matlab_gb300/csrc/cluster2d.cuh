@@ -105,6 +105,7 @@ struct C2XPol {
   int f;
   __device__ __forceinline__ int idx(int p) const { return p * GX + f; }
   __device__ __forceinline__ void sync() const { __syncthreads(); }
+  GPE_POL_CHECK_MEMBERS
 };
 
 // ---- the passes ----------------------------------------------------------------
@@ -126,10 +127,11 @@ __device__ __forceinline__ void c2_y_step(cx<R>* home, const C2Geom& g, const C2
     // the ones in [cols, cols_pad) run on scratch space.
     if (p0 + (int)(threadIdx.x / 32) * (32 / T) >= g.cols_pad) continue;
     const bool valid = pc < g.cols;
-    const typename ContigLayout<P, R>::Pol pol{pc * g.regy};
+    typename ContigLayout<P, R>::Pol pol{pc * g.regy};
+    GPE_POL_BOUNDS(pol, G.sc, g.home);
     cx<R> v[E];
 #pragma unroll
-    for (int m = 0; m < E; ++m) v[m] = valid ? home[pol.idx(t + T * m)] : mk<R>(R(0), R(0));
+    for (int m = 0; m < E; ++m) v[m] = valid ? home[GPE_SMI(pol, pol.idx(t + T * m))] : mk<R>(R(0), R(0));
     if (pa.pro != PRO_NONE) {
       R sv[E];
       const R* vs = V + (long long)(col0 + pc) * N + t;
@@ -142,7 +144,7 @@ __device__ __forceinline__ void c2_y_step(cx<R>* home, const C2Geom& g, const C2
     apply_phase<T, E, false>(v, php, t);
     St::template inverse<false>(v, home, pol, t, tws);
 #pragma unroll
-    for (int m = 0; m < E; ++m) home[pol.idx(t + T * m)] = v[m];
+    for (int m = 0; m < E; ++m) home[GPE_SMI(pol, pol.idx(t + T * m))] = v[m];
   }
 }
 
@@ -160,10 +162,12 @@ __device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const C2Geom
   const cx<R>* php = static_cast<const cx<R>*>(G.php[0]);
   const R* V = static_cast<const R*>(G.V);
   const uint32_t hb = smem_u32(home);
-  const C2XPol<GX> pol{f};
+  C2XPol<GX> pol{f};
+  GPE_POL_BOUNDS(pol, G.sc, g.xbuf);
   const int c0 = t / g.cols, lc0 = t - c0 * g.cols;  // x = t lives in CTA c0, column lc0
   for (int r0 = 0; r0 < g.rows; r0 += GX) {
-    const bool valid = r0 + f < g.rows;
+    // bounds-checked build: the thread's last x column lies inside the grid
+    const bool valid = r0 + f < g.rows && bounds_ok(G.sc, BS_CLUSTER, t + (long long)T * (E - 1), G.nx);
     const int y = rank * g.rows + (valid ? r0 + f : 0);
     const uint32_t yoff = (uint32_t)padpos<4>(y) * (uint32_t)sizeof(cx<R>);
     cx<R> v[E];
@@ -216,15 +220,18 @@ __device__ __forceinline__ void c2_y_energy(const cx<R>* home, cx<R>* xbuf, cons
   const int f = threadIdx.x / T, t = threadIdx.x % T;
   const cx<R>* tws = static_cast<const cx<R>*>(G.tws[1]);
   const R* k2p = static_cast<const R*>(G.k2p[1]);
-  const typename ContigLayout<P, R>::Pol pol{f * g.regy};
+  typename ContigLayout<P, R>::Pol pol{f * g.regy};
+  GPE_POL_BOUNDS(pol, G.sc, g.xbuf);
   for (int p0 = 0; p0 < g.cols; p0 += FPI) {
     const int pc = p0 + f;
     if (p0 + (int)(threadIdx.x / 32) * (32 / T) >= g.cols_pad) continue;  // as in c2_y_step
     const bool valid = pc < g.cols;
     cx<R> v[E];
 #pragma unroll
-    for (int m = 0; m < E; ++m)
-      v[m] = valid ? home[pc * g.regy + padpos<4>(t + T * m)] : mk<R>(R(0), R(0));
+    for (int m = 0; m < E; ++m) {
+      const int hi = pc * g.regy + padpos<4>(t + T * m);
+      v[m] = valid && bounds_ok(G.sc, BS_SMEM, hi, g.home) ? home[hi] : mk<R>(R(0), R(0));
+    }
     St::template forward<false>(v, xbuf, pol, t, tws);
     if (valid) {
 #pragma unroll
@@ -244,10 +251,11 @@ __device__ __forceinline__ void c2_x_energy(const cx<R>* home, cx<R>* xbuf, cons
   const cx<R>* tws = static_cast<const cx<R>*>(G.tws[0]);
   const R* k2p = static_cast<const R*>(G.k2p[0]);
   const uint32_t hb = smem_u32(home);
-  const C2XPol<GX> pol{f};
+  C2XPol<GX> pol{f};
+  GPE_POL_BOUNDS(pol, G.sc, g.xbuf);
   const int c0 = t / g.cols, lc0 = t - c0 * g.cols;
   for (int r0 = 0; r0 < g.rows; r0 += GX) {
-    const bool valid = r0 + f < g.rows;
+    const bool valid = r0 + f < g.rows && bounds_ok(G.sc, BS_CLUSTER, t + (long long)T * (E - 1), G.nx);
     const int y = rank * g.rows + (valid ? r0 + f : 0);
     const uint32_t yoff = (uint32_t)padpos<4>(y) * (uint32_t)sizeof(cx<R>);
     cx<R> v[E];

@@ -348,9 +348,56 @@ struct DevScalars {
   int timeout;        // a bounded device-side wait gave up
   int fin_count;      // CTAs of a multi-CTA finalizer that are done (0 between launches)
   int outer;         // outer steps the cluster kernel has completed in this run (history slot)
+  int bounds_site;   // bounds-checked build: the first site that met an index out of range (0: none)
+  long long bounds_index;  // ... and that index
 };
 
 enum StopReason { RUNNING = 0, CONVERGED = 1, SWITCH_FP64 = 2, HALVE_DT = 3, NONFINITE = 4 };
+
+// Bounds-checked build (-DGPE_CHECK=1, a separate library): every global
+// index of the axis-pass kernels is checked against its array's length and
+// every shared-memory index against its buffer; the first violation is
+// recorded in the context's device scalars (bounds_site, bounds_index), the
+// access is skipped (a load reads 0, a store is dropped), and the run
+// returns GPE_ERR_BOUNDS.  Nothing out of range is ever accessed.  Sites:
+enum BoundsSite {
+  BS_NONE = 0,
+  BS_LOAD = 1,       // state load of a pass
+  BS_STORE = 2,      // state store of a pass
+  BS_SIDE = 3,       // V / ITP-factor load
+  BS_AUX_STORE = 4,  // ITP-factor store
+  BS_SMEM = 5,       // shared-memory exchange index
+  BS_PARTIAL = 6,    // per-tile partial sum slot
+  BS_CLUSTER = 7,    // cluster kernel: distributed shared memory rank or offset
+};
+#ifndef GPE_CHECK
+#define GPE_CHECK 0
+#endif
+// The shared-memory exchange policies (fft.cuh) carry their buffer's
+// length in checked builds: GPE_SMI(pol, i) is i, or 0 after recording i.
+#if GPE_CHECK
+#define GPE_SMI(pol, i) (pol).checked(i)
+#define GPE_POL_CHECK_MEMBERS                                                                     \
+  DevScalars* chk_sc = nullptr;                                                                   \
+  int chk_lim = 0;                                                                                \
+  __device__ __forceinline__ int checked(int i) const { return bounds_ok(chk_sc, BS_SMEM, i, chk_lim) ? i : 0; }
+#define GPE_POL_BOUNDS(pol, scp, n) ((pol).chk_sc = (scp), (pol).chk_lim = (int)(n))
+#else
+#define GPE_SMI(pol, i) (i)
+#define GPE_POL_CHECK_MEMBERS
+#define GPE_POL_BOUNDS(pol, scp, n) ((void)0)
+#endif
+// True when 0 <= i < n; otherwise records (site, i) once in *sc.
+__device__ __forceinline__ bool bounds_ok(DevScalars* sc, int site, long long i, long long n) {
+#if GPE_CHECK
+  if (i >= 0 && i < n) return true;
+  if (atomicCAS(&sc->bounds_site, 0, site) == 0) sc->bounds_index = i;
+  return false;
+#else
+  (void)sc, (void)site, (void)i, (void)n;
+  return true;
+#endif
+}
 
 // Reduction slots of the per-CTA partial-sum buffer.
 enum Slot {
@@ -435,6 +482,8 @@ struct PassArgs {
   // TMA pass, test of the timeout path only (0 = off): arm the barriers for
   // copies that are never issued and give up after this many polls.
   int tma_stall = 0;
+  // Elements of the arrays the pass reads and writes (bounds-checked build).
+  long long npts = 0;
   // TMA pass, strided axes: the state (and side array) as 4D tensors
   // (y, x, z, component) of extents tdim, copied one box per tile through
   // the kernel's tensor-map parameters (tma_tensor = 1); otherwise one bulk

@@ -293,10 +293,10 @@ __device__ __forceinline__ void xchg_scatter_to_own(cx<R>* v, cx<R>* sm, const S
 #pragma unroll
   for (int b = 0; b < NB; ++b)
 #pragma unroll
-    for (int r = 0; r < RAD; ++r) sm[pol.idx(scatter_pos<Ns, RAD>(t + T * b, r))] = v[b + r * NB];
+    for (int r = 0; r < RAD; ++r) sm[GPE_SMI(pol, pol.idx(scatter_pos<Ns, RAD>(t + T * b, r)))] = v[b + r * NB];
   pol.sync();
 #pragma unroll
-  for (int m = 0; m < E; ++m) v[m] = sm[pol.idx(t + T * m)];
+  for (int m = 0; m < E; ++m) v[m] = sm[GPE_SMI(pol, pol.idx(t + T * m))];
   pol.sync();
 }
 
@@ -306,12 +306,12 @@ __device__ __forceinline__ void xchg_own_to_scatter(cx<R>* v, cx<R>* sm, const S
   constexpr int E = N / T;
   constexpr int NB = E / RAD;
 #pragma unroll
-  for (int m = 0; m < E; ++m) sm[pol.idx(t + T * m)] = v[m];
+  for (int m = 0; m < E; ++m) sm[GPE_SMI(pol, pol.idx(t + T * m))] = v[m];
   pol.sync();
 #pragma unroll
   for (int b = 0; b < NB; ++b)
 #pragma unroll
-    for (int r = 0; r < RAD; ++r) v[b + r * NB] = sm[pol.idx(scatter_pos<Ns, RAD>(t + T * b, r))];
+    for (int r = 0; r < RAD; ++r) v[b + r * NB] = sm[GPE_SMI(pol, pol.idx(scatter_pos<Ns, RAD>(t + T * b, r)))];
   pol.sync();
 }
 

@@ -52,6 +52,15 @@ gpe_status fail(gpe_ctx* c, gpe_status st, const std::string& msg) {
     if (s_ != GPE_OK) return s_;   \
   } while (0)
 
+// The bounds-checked build's report (common.cuh BoundsSite).
+std::string bounds_message(const char* where, const DevScalars& h) {
+  static const char* names[] = {"none", "state load", "state store", "side-array load", "ITP-factor store",
+                                "shared-memory exchange", "partial-sum slot", "cluster shared memory"};
+  const int s = h.bounds_site;
+  return std::string(where) + ": index out of range at " + (s >= 0 && s < 8 ? names[s] : "an unknown site") +
+         " (index " + std::to_string(h.bounds_index) + ")";
+}
+
 bool supported_n(int n) {
   switch (n) {
 #define X(v) case v:
@@ -771,6 +780,7 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.stride = ap.stride;
   a.inner = ap.inner;
   a.outer = ap.outer;
+  a.npts = ap.n_batch * (long long)ap.N;  // the pencils of a pass tile the array it covers
   a.cap = c->cap;
   // rotating-frame terms and the cut-off chain run in the extended step kernel
   a.kind = (kind == KIND_STEP && (ap.rot != 0 || ap.split != SPLIT_FULL)) ? KIND_STEP_EXT : kind;
@@ -1120,6 +1130,7 @@ gpe_status itp_phase(gpe_ctx* c, Field& f, const gpe_itp_params* prm, ItpState& 
   st.i = h.iter;
   *reason = h.stop ? h.status : RUNNING;
   if (h.timeout) return fail(c, GPE_ERR_TIMEOUT, "groundstate_itp: a device-side wait for staged data expired");
+  if (h.bounds_site) return fail(c, GPE_ERR_BOUNDS, bounds_message("groundstate_itp", h));
   if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "groundstate_itp: non-finite norm or residual");
   return GPE_OK;
 }
@@ -1144,6 +1155,8 @@ gpe_status itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* M
   s0.status = RUNNING;
   s0.nonfinite = 0;
   s0.timeout = 0;  // a timed-out earlier call does not fail this one
+  s0.bounds_site = 0;
+  s0.bounds_index = 0;
   s0.iter = 0;
   s0.stall = 0;
   s0.best_delta = INFINITY;
@@ -1304,6 +1317,8 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
   s0.status = RUNNING;
   s0.nonfinite = 0;
   s0.timeout = 0;  // a timed-out earlier call does not fail this one
+  s0.bounds_site = 0;
+  s0.bounds_index = 0;
   s0.outer = 0;
   s0.NN0 = NN0;
   s0.NNN = NN0;
@@ -1417,6 +1432,7 @@ gpe_status split_finish(gpe_ctx* c, const SplitRun& run, int last_j, double last
   DevScalars h;
   CHECK(read_scalars(c, &h));
   if (h.timeout) return fail(c, GPE_ERR_TIMEOUT, "solve_split: a device-side wait for staged data expired");
+  if (h.bounds_site) return fail(c, GPE_ERR_BOUNDS, bounds_message("solve_split", h));
   if (h.nonfinite) return fail(c, GPE_ERR_NONFINITE, "solve_split: non-finite norm or chemical potential");
   const int start = run.start;
   if (last_j > start) {

@@ -122,6 +122,7 @@ __device__ __forceinline__ PassArgs<float> g2_args(const G2Grid& G, int axis) {
   p.partials = G.partials;
   p.sc = G.sc;
   p.cap = G.cap;
+  p.npts = (long long)G.nx * G.ny;
   if (axis == 1) {
     p.n_batch = G.nx;
     p.stride = 1;

@@ -59,6 +59,7 @@ __host__ __device__ constexpr int padpos(int p) {
 
 template <class P, typename R>
 struct ContigLayout {
+  static constexpr bool CONTIG = true;
   static constexpr int T = P::T;
   static constexpr int FFTS = (T >= GPE_DIRECT_CTA_THREADS) ? 1 : GPE_DIRECT_CTA_THREADS / T;
   static constexpr int THREADS = FFTS * T;
@@ -72,6 +73,7 @@ struct ContigLayout {
       if constexpr (T <= 32) __syncwarp();
       else __syncthreads();
     }
+    GPE_POL_CHECK_MEMBERS
   };
   static __device__ __forceinline__ void map(int tid, int& f, int& t) {
     f = tid / T;
@@ -102,6 +104,7 @@ struct ContigLayout {
 
 template <class P, typename R>
 struct StridedLayout {
+  static constexpr bool CONTIG = false;
   static constexpr int T = P::T;
   // Adjacent pencils per CTA: one 128-byte row.  (64-byte rows, which halve
   // the CTA of T > 16 plans, measured 5% faster on the 512^3 x pass and 28%
@@ -115,6 +118,7 @@ struct StridedLayout {
     int f;
     __device__ __forceinline__ int idx(int p) const { return p * FFTS + f; }
     __device__ __forceinline__ void sync() const { __syncthreads(); }
+    GPE_POL_CHECK_MEMBERS
   };
   static __device__ __forceinline__ void map(int tid, int& f, int& t) {
     f = tid % FFTS;
@@ -382,12 +386,15 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, long long tile, 
   int f, t;
   L::map(threadIdx.x, f, t);
   const long long b = tile * L::FFTS + f;
-  const bool valid = b < a.n_batch;
+  const bool valid0 = b < a.n_batch;
   const long long st = L::step(a);
   // element m of this thread sits at offset m*dm from its first element
-  const long long first = (valid ? L::base(a, b) : 0) + (long long)t * st;
+  const long long first = (valid0 ? L::base(a, b) : 0) + (long long)t * st;
   const long long dm = (long long)T * st;
-  const auto pol = L::pol(f);
+  auto pol = L::pol(f);
+  GPE_POL_BOUNDS(pol, a.sc, L::smem_bytes() / sizeof(cx<R>));
+  // bounds-checked build: the thread's last element inside the pass's extent
+  const bool valid = valid0 && bounds_ok(a.sc, BS_LOAD, first + (E - 1) * dm, a.npts);
 
   cx<R> v[E];
   {
@@ -395,11 +402,13 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, long long tile, 
 #pragma unroll
     for (int m = 0; m < E; ++m) v[m] = valid ? ld_stream(src + m * dm) : mk<R>(R(0), R(0));
   }
-  // The side array of a phase prologue (V or the ITP factors) goes out with
-  // the state loads (GPE_EARLY_SIDE), so the two latencies overlap instead of
-  // the side loads waiting behind the table copy's barrier.
+  // The side array of a phase prologue (V or the ITP factors) of the
+  // contiguous pass goes out with the state loads (GPE_EARLY_SIDE), so the
+  // two latencies overlap instead of the side loads waiting behind the table
+  // copy's barrier.  (The strided passes carry no prologue on the hot path;
+  // the extra live registers would cost them spills.)
   R sv[E];
-  const bool early_side = GPE_EARLY_SIDE && KIND != KIND_ENERGY && a.pro != PRO_NONE && a.side != 0;
+  const bool early_side = GPE_EARLY_SIDE && L::CONTIG && KIND != KIND_ENERGY && a.pro != PRO_NONE && a.side != 0;
   if (early_side) {
     const R* __restrict__ ss = (a.side == 2 ? a.aux : a.V) + first;
 #pragma unroll
@@ -475,7 +484,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, long long tile, 
       slots[0] = a.kin_slot;
       nred = 1;
     }
-    cta_reduce_store<L::THREADS>(sums, slots, nred, a.partials, a.cap, tile);
+    if (bounds_ok(a.sc, BS_PARTIAL, tile, a.cap)) cta_reduce_store<L::THREADS>(sums, slots, nred, a.partials, a.cap, tile);
   } else {
     // The side array (V for the phase factors, or the ITP factors) is read
     // right before the phase that uses it: a pass has a prologue or an
@@ -530,7 +539,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, long long tile, 
     const int nred = a.epi == EPI_RT_END ? 3 : a.epi == EPI_ITP ? 1 : 0;
     if (nred > 0) {
       const int slots[4] = {S_N, S_VN, S_N2, 0};
-      cta_reduce_store<L::THREADS>(acc, slots, nred, a.partials, a.cap, tile);
+      if (bounds_ok(a.sc, BS_PARTIAL, tile, a.cap)) cta_reduce_store<L::THREADS>(acc, slots, nred, a.partials, a.cap, tile);
     }
   }
 }

@@ -41,6 +41,7 @@ struct TContig {
       if constexpr (T <= 32) __syncwarp();
       else __syncthreads();
     }
+    GPE_POL_CHECK_MEMBERS
   };
   static __device__ __forceinline__ Pol pol(int f) { return Pol{f * REG}; }
 };
@@ -62,6 +63,7 @@ struct TStrided {
     int f;
     __device__ __forceinline__ int idx(int p) const { return p * FFTS + f; }
     __device__ __forceinline__ void sync() const { __syncthreads(); }
+    GPE_POL_CHECK_MEMBERS
   };
   static __device__ __forceinline__ Pol pol(int f) { return Pol{f}; }
 };
@@ -222,7 +224,8 @@ __global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value)
     };
     __syncthreads();  // staging reads done before the exchanges reuse the buffer
 
-    const auto pol = L::pol(f);
+    auto pol = L::pol(f);
+    GPE_POL_BOUNDS(pol, a.sc, L::PSI_ELEMS);
     cx<R>* xb = psib[slot];
     if constexpr (KIND == KIND_ENERGY) {
       const R s = a.pro == PRO_SCALE ? (R)a.sc->scale : R(1);
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(L::THREADS, TmaMinBlocks<R, L>::value)
         load_side();
         epilogue<R, E>(v, sv, a, acc, valid, (R)a.sc->mu);
       }
-      if (valid) {
+      if (valid && bounds_ok(a.sc, BS_STORE, first + (E - 1) * dm, a.npts)) {
         cx<R>* __restrict__ dst = a.psi + first;
 #pragma unroll
         for (int m = 0; m < E; ++m) dst[m * dm] = v[m];

@@ -49,6 +49,7 @@ struct ContigX2 {
       if constexpr (T <= 32) __syncwarp();
       else __syncthreads();
     }
+    GPE_POL_CHECK_MEMBERS
   };
   static __device__ __forceinline__ void map(int tid, int& f, int& t) {
     f = tid / T;
@@ -103,6 +104,7 @@ struct StridedX2 {
     int f;
     __device__ __forceinline__ int idx(int p) const { return p * FP + f; }
     __device__ __forceinline__ void sync() const { __syncthreads(); }
+    GPE_POL_CHECK_MEMBERS
   };
   static __device__ __forceinline__ void map(int tid, int& f, int& t) {
     f = tid % FP;
@@ -319,12 +321,15 @@ __global__ void __launch_bounds__(L::THREADS, X2MinBlocks<P, L>::value) pass_x2_
   int f, t;
   L::map(threadIdx.x, f, t);
   const long long b = (long long)blockIdx.x * L::PENCILS + 2 * f;  // pencil A; B is its neighbour
-  const bool valid = b < a.n_batch;  // n_batch is even: A and B are valid together
+  const bool valid0 = b < a.n_batch;  // n_batch is even: A and B are valid together
   const long long st = L::step(a);
-  const long long first = (valid ? L::base(a, b) : 0) + (long long)t * st;
+  const long long first = (valid0 ? L::base(a, b) : 0) + (long long)t * st;
   const long long dm = (long long)T * st;
   const long long pb = L::pair_off(a);
-  const auto pol = L::pol(f);
+  auto pol = L::pol(f);
+  GPE_POL_BOUNDS(pol, a.sc, L::smem_bytes() / sizeof(cx<fx2>));
+  // bounds-checked build: the pair's last element inside the pass's extent
+  const bool valid = valid0 && bounds_ok(a.sc, BS_LOAD, first + (E - 1) * dm + pb, a.npts);
 
   cx<fx2> v[E];
   L::load(a.psi + first, dm, pb, valid, v);
@@ -360,7 +365,7 @@ __global__ void __launch_bounds__(L::THREADS, X2MinBlocks<P, L>::value) pass_x2_
 #pragma unroll
     for (int i = 0; i < 3; ++i) k[i] = acc[i].merged();
     const int slots[4] = {S_N, S_VN, S_N2, 0};
-    cta_reduce_store<L::THREADS>(k, slots, nred, a.partials, a.cap);
+    if (bounds_ok(a.sc, BS_PARTIAL, blockIdx.x, a.cap)) cta_reduce_store<L::THREADS>(k, slots, nred, a.partials, a.cap);
   }
 }
 
