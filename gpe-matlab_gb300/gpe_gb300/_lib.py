@@ -15,11 +15,12 @@ LIB_PATH = Path(os.environ.get("GPE_LIB", _HERE.parent / "libgpe.so"))
 
 GPE_OK, GPE_ERR_INVALID, GPE_ERR_UNSUPPORTED, GPE_ERR_CUDA, GPE_ERR_ALLOC = 0, 1, 2, 3, 4
 GPE_ERR_STATE, GPE_ERR_TIMEOUT, GPE_ERR_NONFINITE, GPE_ERR_NO_DEVICE, GPE_ERR_CALLBACK = 5, 6, 7, 8, 9
+GPE_ERR_BOUNDS = 10
 GPE_FP32, GPE_FP64 = 1, 2
 
 STATUS_NAMES = {0: "GPE_OK", 1: "GPE_ERR_INVALID", 2: "GPE_ERR_UNSUPPORTED", 3: "GPE_ERR_CUDA",
                 4: "GPE_ERR_ALLOC", 5: "GPE_ERR_STATE", 6: "GPE_ERR_TIMEOUT", 7: "GPE_ERR_NONFINITE",
-                8: "GPE_ERR_NO_DEVICE", 9: "GPE_ERR_CALLBACK"}
+                8: "GPE_ERR_NO_DEVICE", 9: "GPE_ERR_CALLBACK", 10: "GPE_ERR_BOUNDS"}
 
 
 class gpe_grid_desc(C.Structure):

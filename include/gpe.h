@@ -48,7 +48,9 @@ typedef enum {
     GPE_ERR_TIMEOUT = 6,     /* a bounded device-side wait expired            */
     GPE_ERR_NONFINITE = 7,   /* NaN/Inf met in a reduction (norm, mu, delta)  */
     GPE_ERR_NO_DEVICE = 8,   /* no CUDA device, or not an sm_103 device       */
-    GPE_ERR_CALLBACK = 9     /* a host callback returned nonzero              */
+    GPE_ERR_CALLBACK = 9,    /* a host callback returned nonzero              */
+    GPE_ERR_BOUNDS = 10      /* bounds-checked build only: a kernel index was
+                              * out of range (the access was skipped)        */
 } gpe_status;
 
 enum { GPE_FP32 = 1, GPE_FP64 = 2 };
