@@ -46,12 +46,6 @@ __host__ __device__ constexpr int padpos(int p) {
   else return p + (p >> PADSH);
 }
 
-// Side-array loads of a prologue issued with the state loads (1) or right
-// before the prologue (0).
-#ifndef GPE_EARLY_SIDE
-#define GPE_EARLY_SIDE 1
-#endif
-
 // Threads per CTA of the direct passes (pencils per CTA follow from it).
 #ifndef GPE_DIRECT_CTA_THREADS
 #define GPE_DIRECT_CTA_THREADS 256
@@ -402,18 +396,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, long long tile, 
 #pragma unroll
     for (int m = 0; m < E; ++m) v[m] = valid ? ld_stream(src + m * dm) : mk<R>(R(0), R(0));
   }
-  // The side array of a phase prologue (V or the ITP factors) of the
-  // contiguous pass goes out with the state loads (GPE_EARLY_SIDE), so the
-  // two latencies overlap instead of the side loads waiting behind the table
-  // copy's barrier.  (The strided passes carry no prologue on the hot path;
-  // the extra live registers would cost them spills.)
   R sv[E];
-  const bool early_side = GPE_EARLY_SIDE && L::CONTIG && KIND != KIND_ENERGY && a.pro != PRO_NONE && a.side != 0;
-  if (early_side) {
-    const R* __restrict__ ss = (a.side == 2 ? a.aux : a.V) + first;
-#pragma unroll
-    for (int m = 0; m < E; ++m) sv[m] = valid ? ld_stream(ss + m * dm) : R(0);
-  }
   // With the own loads in flight, hint the tile of the CTA one wave of
   // resident CTAs later into L2, so that CTA's loads hit L2.
   if (a.pf_ahead > 0) {
@@ -495,7 +478,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, long long tile, 
       for (int m = 0; m < E; ++m) sv[m] = valid ? ld_stream(ss + m * dm) : R(0);
     };
     if (a.pro != PRO_NONE) {
-      if (a.side != 0 && !early_side) load_side();
+      if (a.side != 0) load_side();
       prologue<R, E>(v, sv, a, valid, first, dm, scal[0], scal[1]);
     }
     constexpr bool SMT = SmemTables<R, P, KIND>::value;
