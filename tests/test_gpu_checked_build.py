@@ -100,7 +100,7 @@ def run_cases():
     X, Y = og.mesh["x"], og.mesh["y"]
     psi0 = np.exp(-(X ** 2 + Y ** 2) / 4).astype(complex)
     phi, MU = task.groundstate_itp(0.01, 1e-6, psi0, nargout=2)
-    ophi, oMU = ot.groundstate_itp(0.01, 1e-6, psi0, nargout=2)
+    ophi, oMU = ot.groundstate_itp(0.01, 1e-6, psi0, nargout=2)[:2]
     assert abs(MU[-1] - oMU[-1]) / abs(oMU[-1]) < 1e-6
     o = task.observables(phi)
     assert o["energy"] == o["energy"]
