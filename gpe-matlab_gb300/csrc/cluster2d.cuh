@@ -111,7 +111,7 @@ struct C2XPol {
 // ---- the passes ----------------------------------------------------------------
 // y pass over this CTA's pencils, in place in `home` (pencil pc at pc*regy).
 template <typename R, class P>
-__device__ __forceinline__ void c2_y_step(cx<R>* home, const C2Geom& g, const C2Grid& G, int col0,
+__device__ __forceinline__ void c2_y_step(cx<R>* home, const R* vloc, const C2Geom& g, const C2Grid& G, int col0,
                                           const PassArgs<R>& pa, R s, R mu) {
   constexpr int T = P::T, E = P::E, N = P::N;
   constexpr int FPI = C2Threads<R>::value / T;
@@ -134,9 +134,15 @@ __device__ __forceinline__ void c2_y_step(cx<R>* home, const C2Geom& g, const C2
     for (int m = 0; m < E; ++m) v[m] = valid ? home[GPE_SMI(pol, pol.idx(t + T * m))] : mk<R>(R(0), R(0));
     if (pa.pro != PRO_NONE) {
       R sv[E];
-      const R* vs = V + (long long)(col0 + pc) * N + t;
+      if (vloc) {  // this CTA's V columns in shared memory
+        const R* vs = vloc + pc * N + t;
 #pragma unroll
-      for (int m = 0; m < E; ++m) sv[m] = valid ? __ldg(vs + T * m) : R(0);
+        for (int m = 0; m < E; ++m) sv[m] = valid ? vs[T * m] : R(0);
+      } else {
+        const R* vs = V + (long long)(col0 + pc) * N + t;
+#pragma unroll
+        for (int m = 0; m < E; ++m) sv[m] = valid ? __ldg(vs + T * m) : R(0);
+      }
       prologue<R, E>(v, sv, pa, valid, 0, 0, s, mu);
     }
     pol.sync();  // every lane has read its values before the exchanges reuse the pencil
@@ -280,12 +286,12 @@ __device__ __forceinline__ void c2_x_energy(const cx<R>* home, cx<R>* xbuf, cons
 
 // Runtime dispatch over the axis length.
 template <typename R>
-__device__ void c2_y_step_n(int n, cx<R>* home, const C2Geom& g, const C2Grid& G, int col0, const PassArgs<R>& pa,
-                            R s, R mu) {
+__device__ void c2_y_step_n(int n, cx<R>* home, const R* vloc, const C2Geom& g, const C2Grid& G, int col0,
+                            const PassArgs<R>& pa, R s, R mu) {
   switch (n) {
-#define X(v)                                                  \
-  case v:                                                     \
-    c2_y_step<R, C2Plan<R, v>>(home, g, G, col0, pa, s, mu);       \
+#define X(v)                                                          \
+  case v:                                                             \
+    c2_y_step<R, C2Plan<R, v>>(home, vloc, g, G, col0, pa, s, mu);    \
     break;
     GPE_C2_SIZES(X)
 #undef X
@@ -368,7 +374,8 @@ __global__ void __launch_bounds__(C2Threads<R>::value, C2Threads<R>::min_blocks)
   // warp partials of the CTA reduction.
   for (int k = a.offs[cid]; k < a.offs[cid + 1]; ++k) {
     const C2Grid& G = a.grids[a.order[k]];
-    const C2Geom g = c2_geom(G.nx, G.ny, cs, (int)sizeof(cx<R>));
+    const C2Geom g = c2_geom(G.nx, G.ny, cs, (int)sizeof(cx<R>), a.vsm);
+    R* vloc = a.vsm ? reinterpret_cast<R*>(smem + g.vofs) : nullptr;
     cx<R>* home = reinterpret_cast<cx<R>*>(smem);
     cx<R>* xbuf = home + g.home;
     double* red = reinterpret_cast<double*>(smem + (size_t)(g.home + g.xbuf) * sizeof(cx<R>));
@@ -391,6 +398,10 @@ __global__ void __launch_bounds__(C2Threads<R>::value, C2Threads<R>::min_blocks)
         const int pc = i / G.ny, y = i - pc * G.ny;
         home[pc * g.regy + padpos<4>(y)] = src[i];
       }
+      if (vloc) {  // this CTA's columns of V, dense [column][y]
+        const R* vsrc = static_cast<const R*>(G.V) + (long long)col0 * G.ny;
+        for (int i = threadIdx.x; i < total; i += C2Threads<R>::value) vloc[i] = vsrc[i];
+      }
     }
     c2_sync();
     PassArgs<R> pa{};
@@ -407,7 +418,7 @@ __global__ void __launch_bounds__(C2Threads<R>::value, C2Threads<R>::min_blocks)
         Kahan<R> acc[3];
         for (int i = 1; i <= a.n_rec; ++i) {
           pa.pro = i == 1 ? PRO_RT_HALF : PRO_RT_FULL;  // solve_split.m:55-56 / 60-61
-          c2_y_step_n<R>(G.ny, home, g, G, col0, pa, s, mu);
+          c2_y_step_n<R>(G.ny, home, vloc, g, G, col0, pa, s, mu);
           c2_sync();
           pa.epi = i == a.n_rec ? EPI_RT_END : EPI_NONE;  // solve_split.m:60-67
           c2_x_step_n<R>(G.nx, home, xbuf, g, G, rank, pa, mu, acc);

@@ -55,11 +55,15 @@ __host__ __device__ constexpr int c2_reg(int n) {
 }
 
 // Shared-memory plan of one CTA for an nx x ny grid on clusters of cs CTAs.
+// vsm: the CTA also keeps its columns of V (cols x ny reals, constant over
+// the launch) after the reduction scratch, so the y pass's nonlinear phase
+// reads V from shared memory instead of L2 at every step.
 struct C2Geom {
   int cols, cols_pad, rows, regy, home, xbuf;  // home/xbuf in complex elements
+  size_t vofs;                                 // byte offset of the V columns (vsm)
   size_t bytes;
 };
-__host__ __device__ inline C2Geom c2_geom(int nx, int ny, int cs, int esz) {
+__host__ __device__ inline C2Geom c2_geom(int nx, int ny, int cs, int esz, int vsm = 0) {
   C2Geom g;
   g.cols = nx / cs;
   g.rows = ny / cs;
@@ -71,6 +75,8 @@ __host__ __device__ inline C2Geom c2_geom(int nx, int ny, int cs, int esz) {
   const int gx = c2_threads(esz) / c2_T(nx, esz);
   g.xbuf = gx * nx > fpi * g.regy ? gx * nx : fpi * g.regy;
   g.bytes = (size_t)(g.home + g.xbuf) * (size_t)esz + C2_RED_BYTES;
+  g.vofs = g.bytes;
+  if (vsm) g.bytes += (size_t)g.cols * ny * (size_t)(esz / 2);
   return g;
 }
 
@@ -96,6 +102,7 @@ struct C2Args {
   const int* offs;   // cluster c runs order[offs[c] .. offs[c+1])
   int n_rec, nb;     // steps per block, blocks per outer step
   int nouter;        // outer steps per launch
+  int vsm;           // V columns in shared memory (C2Geom)
   double ddt, dt_outer;
 };
 

@@ -1892,6 +1892,7 @@ bool c2_eligible(const gpe_ctx* c) {
 
 struct C2Plan {
   int cs = 0, nclusters = 0;
+  int vsm = 0;  // V columns in shared memory
   size_t smem = 0;
 };
 
@@ -1914,15 +1915,24 @@ C2Plan c2_plan(const std::vector<gpe_ctx*>& cs) {
   long long best_score = -1;
   for (int cand : {16, 8}) {
     if (forced && cand != forced) continue;
-    size_t smem = 0;
+    size_t smem = 0, smem_v = 0;
     bool ok = true;
     for (auto* c : cs) {
       if (c->n[0] % cand || c->n[1] % cand) ok = false;
       smem = std::max(smem, c2_geom(c->n[0], c->n[1], cand, (int)sizeof(cx<R>)).bytes);
+      smem_v = std::max(smem_v, c2_geom(c->n[0], c->n[1], cand, (int)sizeof(cx<R>), 1).bytes);
     }
     if (!ok || smem > (size_t)optin) continue;
     const int maxc = cluster2d_max_clusters<R>(cand, smem);
     if (maxc <= 0) continue;
+    // V columns in shared memory where they fit without losing clusters
+    // (GPE_C2_VSM=0 turns this off)
+    int vsm = 0;
+    if (c2_env("GPE_C2_VSM", 1) != 0 && smem_v <= (size_t)optin &&
+        cluster2d_max_clusters<R>(cand, smem_v) >= std::min<int>((int)cs.size(), maxc)) {
+      vsm = 1;
+      smem = smem_v;
+    }
     const int ncl = std::min<int>((int)cs.size(), maxc);
     const long long score = (long long)ncl * cand;
     if (score > best_score) {
@@ -1930,6 +1940,7 @@ C2Plan c2_plan(const std::vector<gpe_ctx*>& cs) {
       best.cs = cand;
       best.nclusters = ncl;
       best.smem = smem;
+      best.vsm = vsm;
     }
   }
   return best;
@@ -2030,6 +2041,7 @@ gpe_status cluster_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, 
   a.n_rec = r0.n_rec;
   a.nb = r0.nb;
   a.nouter = 1;
+  a.vsm = pl.vsm;
   a.ddt = r0.ddt;
   a.dt_outer = r0.dt_outer;
   cudaStream_t master = c->stream;
