@@ -172,10 +172,20 @@ extern "C" GPE_API gpe_status gpe_norm_noalloc(const void* d_psi, long long npoi
   if (pa.type == cudaMemoryTypeDevice && pa.device != dev)
     return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: d_psi lives on device " + std::to_string(pa.device) +
                                         ", not on the current device " + std::to_string(dev));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // The call waits on the host for its result (a copy to pageable memory
+  // and a stream synchronisation), which a stream under capture cannot do:
+  // refuse it before touching the stream, so the caller's capture survives.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(s, &cap);
+  if (e != cudaSuccess) return na_fail(GPE_ERR_CUDA, std::string("gpe_norm_noalloc: cudaStreamIsCapturing: ") +
+                                                         cudaGetErrorString(e));
+  if (cap != cudaStreamCaptureStatusNone)
+    return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: the stream is capturing; this call waits on the host for its "
+                                    "result");
   double* scratch = nullptr;
   gpe_status st = na_scratch(dev, &scratch);
   if (st != GPE_OK) return st;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nparts = (int)((npoints + NA_CHUNK - 1) / NA_CHUNK);
   if (precision == GPE_FP32)
     k_na_partials<float><<<nparts, NA_THREADS, 0, s>>>(static_cast<const cx<float>*>(d_psi), npoints, scratch);

@@ -387,7 +387,8 @@ GPE_API gpe_status gpe_set_pass_variant(gpe_ctx *ctx, int variant);
  * GPE_ERR_INVALID.  The first call on each device looks up that array's
  * address and should come before any stream capture; the address lives as
  * long as the device's CUDA context, so no call may follow a cudaDeviceReset.
- * Each call waits on the host for its result.  All calls share the array:
+ * Each call waits on the host for its result; a call on a stream that is
+ * being captured is refused with GPE_ERR_INVALID.  All calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller.
  * Errors: gpe_last_error(NULL). */
 GPE_API gpe_status gpe_norm_noalloc(const void *d_psi, long long npoints, int precision, double weight,
