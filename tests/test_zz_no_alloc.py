@@ -119,3 +119,28 @@ def test_norm_noalloc_refuses_host_and_misaligned_pointers(gpe):
     assert out.value == -1.0
     # the library is still usable afterwards
     assert _noalloc_norm(dev, 4096, L.GPE_FP64, 1.0) == 0.0
+
+
+def test_norm_noalloc_refuses_a_capturing_stream(gpe):
+    """The call waits on the host for its result, which a stream under
+    capture cannot do: it is refused before the stream is touched, and the
+    caller's capture goes on."""
+    torch = pytest.importorskip("torch")
+    from gpe_gb300 import _lib as L
+
+    buf = torch.ones(64, dtype=torch.float32, device="cuda")
+    _noalloc_norm(buf, 32, L.GPE_FP32, 1.0)  # first call on the device: the scratch lookup
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    out = C.c_double(-1.0)
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            y = buf * 2.0
+            st = L.lib.gpe_norm_noalloc(C.c_void_p(buf.data_ptr()), 32, L.GPE_FP32, 1.0,
+                                        C.c_void_p(s.cuda_stream), C.byref(out))
+    assert st == L.GPE_ERR_INVALID
+    assert b"capturing" in L.lib.gpe_last_error(None)
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(y.sum()) == pytest.approx(128.0)
+    assert _noalloc_norm(buf, 32, L.GPE_FP32, 1.0) == pytest.approx(32.0)
