@@ -154,8 +154,18 @@ extern "C" GPE_API gpe_status gpe_norm_noalloc(const void* d_psi, long long npoi
   if (reinterpret_cast<uintptr_t>(d_psi) % align != 0)
     return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: d_psi is not aligned to one complex element (" +
                                         std::to_string(align) + " bytes)");
+  // The call waits on the host for its result (a copy to pageable memory
+  // and a stream synchronisation), which a stream under capture cannot do:
+  // refuse it with the first CUDA call, so the caller's capture survives.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap);
+  if (e != cudaSuccess) return na_fail(GPE_ERR_CUDA, std::string("gpe_norm_noalloc: cudaStreamIsCapturing: ") +
+                                                         cudaGetErrorString(e));
+  if (cap != cudaStreamCaptureStatusNone)
+    return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: the stream is capturing; this call waits on the host for its "
+                                    "result");
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return na_fail(GPE_ERR_CUDA, std::string("gpe_norm_noalloc: cudaGetDevice: ") +
                                                          cudaGetErrorString(e));
   // Only memory of the current device (or managed memory) goes to the kernel.
@@ -173,16 +183,6 @@ extern "C" GPE_API gpe_status gpe_norm_noalloc(const void* d_psi, long long npoi
     return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: d_psi lives on device " + std::to_string(pa.device) +
                                         ", not on the current device " + std::to_string(dev));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // The call waits on the host for its result (a copy to pageable memory
-  // and a stream synchronisation), which a stream under capture cannot do:
-  // refuse it before touching the stream, so the caller's capture survives.
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  e = cudaStreamIsCapturing(s, &cap);
-  if (e != cudaSuccess) return na_fail(GPE_ERR_CUDA, std::string("gpe_norm_noalloc: cudaStreamIsCapturing: ") +
-                                                         cudaGetErrorString(e));
-  if (cap != cudaStreamCaptureStatusNone)
-    return na_fail(GPE_ERR_INVALID, "gpe_norm_noalloc: the stream is capturing; this call waits on the host for its "
-                                    "result");
   double* scratch = nullptr;
   gpe_status st = na_scratch(dev, &scratch);
   if (st != GPE_OK) return st;
