@@ -143,4 +143,4 @@ def test_norm_noalloc_refuses_a_capturing_stream(gpe):
     g.replay()
     torch.cuda.synchronize()
     assert float(y.sum()) == pytest.approx(128.0)
-    assert _noalloc_norm(buf, 32, L.GPE_FP32, 1.0) == pytest.approx(32.0)
+    assert _noalloc_norm(buf, 32, L.GPE_FP32, 1.0) == pytest.approx(64.0)  # 32 points of 1 + 1i
