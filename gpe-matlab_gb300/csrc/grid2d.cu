@@ -257,20 +257,6 @@ __global__ void __launch_bounds__(G2_THREADS, G2_MIN_BLOCKS) k_grid2d(const G2Ar
     __syncthreads();
     return it;
   };
-  // All items of a phase: the next item's index is taken (thread 0's
-  // atomic) before the current item runs, so its latency overlaps the work.
-  auto for_items = [&](unsigned n, auto&& run) {
-    int cur = grab(n);
-    while (cur >= 0) {
-      unsigned nxt = 0;
-      if (threadIdx.x == 0) nxt = atomicAdd(a.bar + 1, 1u) - base;
-      run(cur);  // ends with a __syncthreads
-      if (threadIdx.x == 0) s_item = nxt < n ? (int)nxt : -1;
-      __syncthreads();
-      cur = s_item;
-      __syncthreads();
-    }
-  };
   const int ng = a.ngrids;
   const int ny_items = a.yoff[ng], nx_items = a.xoff[ng];
   // one item of a pass: the grid's pending scale and mu, the stop vote
@@ -304,19 +290,21 @@ __global__ void __launch_bounds__(G2_THREADS, G2_MIN_BLOCKS) k_grid2d(const G2Ar
       const bool last = jj == a.nb;
       for (int i = 1; i <= a.n_rec; ++i) {
         const int pro = i == 1 ? PRO_RT_HALF : PRO_RT_FULL;  // solve_split.m:55-56 / 60-61
-        for_items(ny_items, [&](int item) { item_run(Y{}, Step{}, a.yoff, pro, EPI_NONE, item, false, last); });
+        for (int item = grab(ny_items); item >= 0; item = grab(ny_items))
+          item_run(Y{}, Step{}, a.yoff, pro, EPI_NONE, item, false, last);
         base += ny_items + gridDim.x;
         if (!g2_sync(a, target)) return;
         const int epi = i == a.n_rec ? EPI_RT_END : EPI_NONE;  // solve_split.m:60-67
-        for_items(nx_items, [&](int item) { item_run(Xa{}, Step{}, a.xoff, PRO_NONE, epi, item, false, last); });
+        for (int item = grab(nx_items); item >= 0; item = grab(nx_items))
+          item_run(Xa{}, Step{}, a.xoff, PRO_NONE, epi, item, false, last);
         base += nx_items + gridDim.x;
         if (!g2_sync(a, target)) return;
       }
       // kinetic sums of the block-end state of the grids whose mu is needed
-      for_items(ny_items + nx_items, [&](int item) {
+      for (int item = grab(ny_items + nx_items); item >= 0; item = grab(ny_items + nx_items)) {
         if (item < ny_items) item_run(Y{}, Energy{}, a.yoff, PRO_NONE, EPI_NONE, item, true, last);
         else item_run(Xa{}, Energy{}, a.xoff, PRO_NONE, EPI_NONE, item - ny_items, true, last);
-      });
+      }
       base += ny_items + nx_items + gridDim.x;
       if (!g2_sync(a, target)) return;
       for (int g = blockIdx.x; g < ng; g += gridDim.x) g2_finalize(a, g, jj, last, red);
