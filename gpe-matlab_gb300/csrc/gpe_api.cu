@@ -2112,6 +2112,9 @@ gpe_status grid2d_plans(gpe_ctx* c) {
   return GPE_OK;
 }
 
+// nctas > 0: the grid-wide cooperative kernel on nctas CTAs; nctas == 0:
+// the multi-grid pass kernels, one group of grids per shape, each group on
+// its own stream.
 gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, int nctas) {
   gpe_ctx* c = cs[0];
   const size_t n = cs.size();
@@ -2190,13 +2193,96 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
   a.bar = bar;
   a.fail = failf;
   cudaStream_t master = c->stream;
+  // multi-grid pass kernels: the grids grouped by shape, a group's grid
+  // table and item offsets in a buffer of its own, a stream per group
+  struct Group {
+    G2Args a;
+    int ny, nx, ny_items, nx_items;
+    bool feedback;
+    cudaStream_t s;
+    cudaEvent_t done;
+  };
+  std::vector<Group> groups;
+  struct GroupRes {
+    std::vector<void*> bufs;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;
+    ~GroupRes() {
+      for (auto* p : bufs) cudaFree(p);
+      for (auto st : streams) cudaStreamDestroy(st);
+      for (auto ev : events) cudaEventDestroy(ev);
+    }
+  } gres;
+  cudaEvent_t fork_ev = nullptr;
+  if (nctas == 0) {
+    std::vector<std::pair<int, int>> shapes;
+    for (const auto& G : grids)
+      if (std::find(shapes.begin(), shapes.end(), std::make_pair(G.ny, G.nx)) == shapes.end())
+        shapes.push_back({G.ny, G.nx});
+    CU(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    gres.events.push_back(fork_ev);
+    for (const auto& sh : shapes) {
+      std::vector<G2Grid> gg;
+      std::vector<int> yo{0}, xo{0};
+      bool fb = false;
+      for (const auto& G : grids)
+        if (G.ny == sh.first && G.nx == sh.second) {
+          gg.push_back(G);
+          yo.push_back(yo.back() + G.ytiles);
+          xo.push_back(xo.back() + G.xtiles);
+          fb = fb || G.feedback;
+        }
+      const size_t ggb = gg.size() * sizeof(G2Grid), gob = (gg.size() + 1) * sizeof(int);
+      char* buf = nullptr;
+      CU(cudaMalloc(&buf, ggb + 2 * gob));
+      gres.bufs.push_back(buf);
+      CU(cudaMemcpy(buf, gg.data(), ggb, cudaMemcpyHostToDevice));
+      CU(cudaMemcpy(buf + ggb, yo.data(), gob, cudaMemcpyHostToDevice));
+      CU(cudaMemcpy(buf + ggb + gob, xo.data(), gob, cudaMemcpyHostToDevice));
+      Group grp;
+      grp.a = a;
+      grp.a.grids = reinterpret_cast<const G2Grid*>(buf);
+      grp.a.ngrids = (int)gg.size();
+      grp.a.yoff = reinterpret_cast<const int*>(buf + ggb);
+      grp.a.xoff = reinterpret_cast<const int*>(buf + ggb + gob);
+      grp.ny = sh.first;
+      grp.nx = sh.second;
+      grp.ny_items = yo.back();
+      grp.nx_items = xo.back();
+      grp.feedback = fb;
+      if (groups.empty()) {
+        grp.s = master;
+      } else {
+        CU(cudaStreamCreateWithFlags(&grp.s, cudaStreamNonBlocking));
+        gres.streams.push_back(grp.s);
+      }
+      CU(cudaEventCreateWithFlags(&grp.done, cudaEventDisableTiming));
+      gres.events.push_back(grp.done);
+      groups.push_back(grp);
+    }
+  }
   int last_j = r0.start;
   bool stop_req = false;
   const bool direct = c->prof || prm->on_step;
   BatchGraph gr;
   auto enqueue = [&]() -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), master);  // the failure flag stays once set
-    if (e == cudaSuccess) e = launch_grid2d(a, nctas, master);
+    if (nctas > 0) {
+      cudaError_t e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), master);  // the failure flag stays once set
+      if (e == cudaSuccess) e = launch_grid2d(a, nctas, master);
+      return e;
+    }
+    cudaError_t e = cudaEventRecord(fork_ev, master);
+    for (size_t k = 1; k < groups.size() && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(groups[k].s, fork_ev, 0);
+    for (const Group& grp : groups)
+      for (int jj = 1; jj <= r0.nb && e == cudaSuccess; ++jj) {
+        const bool last = jj == r0.nb;
+        e = launch_multi2d_block(grp.a, grp.ny, grp.nx, grp.ny_items, grp.nx_items, jj, last, grp.feedback || last,
+                                 grp.s);
+      }
+    for (size_t k = 1; k < groups.size() && e == cudaSuccess; ++k) {
+      e = cudaEventRecord(groups[k].done, groups[k].s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(master, groups[k].done, 0);
+    }
     return e;
   };
   if (!direct && r0.nout > r0.start) {
@@ -2262,22 +2348,26 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
 
 // Runs solve_split on cs through a persistent kernel of small 2D grids when
 // every context is eligible (same precision, a shape that fits): the
-// grid-wide kernel (FP32; GPE_SMALL2D=grid, or the default rule below) or
-// the cluster kernel.  *used = false leaves the call to the per-pass paths.
+// multi-grid pass kernels (FP32 batches), the grid-wide kernel (FP32,
+// GPE_SMALL2D=grid) or the cluster kernel (the default rule below).  *used = false leaves the call to the per-pass paths.
 gpe_status cluster_run(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, bool* used) {
   *used = false;
   if (c2_env("GPE_CLUSTER", 1) == 0) return GPE_OK;
   for (auto* ci : cs)
     if (!c2_eligible(ci) || ci->prec != cs[0]->prec) return GPE_OK;
-  // Default: the grid-wide kernel for batches (every SM busy on the tiles of
-  // many grids: 64 uneven grids 3.9e10 -> 4.9e10 grid-pt-steps/s), the
-  // cluster kernel for a single grid (a few tiles per pass: the grid
-  // barriers cost more than the cluster's own latency, 256^2 5.7e9 against
-  // 4.2e9).  GPE_SMALL2D=grid|cluster forces one.
+  // Default: the multi-grid pass kernels for FP32 batches (every SM busy on
+  // the tiles of many grids, each pass kernel at the per-pass kernels'
+  // occupancy: 64 uneven grids 5.7e10 grid-pt-steps/s against 4.9e10 for the
+  // grid-wide kernel and 3.9e10 for the cluster kernel), the cluster kernel
+  // for a single grid (a few tiles per pass: 256^2 5.7e9 against 4.2e9 for
+  // either of the others).  GPE_SMALL2D=multi|grid|cluster forces one.
   const char* mode = getenv("GPE_SMALL2D");
-  const bool want_grid = cs[0]->prec == GPE_FP32 &&
-                         (mode ? strcmp(mode, "grid") == 0 : cs.size() > 1);
-  if (want_grid) {
+  const bool fp32 = cs[0]->prec == GPE_FP32;
+  if (fp32 && (mode ? strcmp(mode, "multi") == 0 : cs.size() > 1)) {
+    *used = true;
+    return grid2d_impl(cs, prm, 0);
+  }
+  if (fp32 && mode && strcmp(mode, "grid") == 0) {
     // GPE_G2_CTAS caps the CTAs of the grid-wide kernel (measurement: fewer
     // CTAs make each grid barrier cheaper)
     int nctas = grid2d_max_ctas();

@@ -1,4 +1,5 @@
-// grid2d.cu - grid-wide persistent solve_split of small 2D grids (FP32).
+// grid2d.cu - grid-wide persistent solve_split of small 2D grids (FP32), and
+// the multi-grid pass kernels of batches (end of the file).
 //
 // One cooperative launch advances every grid of a batch (or the single grid
 // of solve_split) through an outer step of solve_split (solve_split.m:49-80)
@@ -352,6 +353,145 @@ cudaError_t launch_grid2d(const G2Args& a, int nctas, cudaStream_t s) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, k_grid2d, a);
+}
+
+// ---- multi-grid pass kernels ------------------------------------------------------
+// The work items of the grid-wide kernel, one launch per pass over the tiles
+// of a group of grids of one shape (CTA = item): each (axis, kind, length)
+// kernel has the register allocation of the per-pass kernels (768 threads
+// per SM), kernel boundaries replace the grid barriers, and the groups of a
+// batch run on their own streams.  The launches of an outer step are one
+// CUDA graph with programmatic dependent launch between them.
+
+template <int AXIS, int KIND, int N>
+__device__ __forceinline__ void g2m_item(const G2Args& a, int pro, int epi, int item, bool skip_unneeded, bool last,
+                                         unsigned char* smem) {
+  __shared__ float s_sc[2];
+  const int* off = AXIS == 1 ? a.yoff : a.xoff;
+  const int g = g2_find(off, a.ngrids, item);
+  const G2Grid& G = a.grids[g];
+  if (threadIdx.x == 0) {
+    s_sc[0] = (float)G.sc->scale;
+    s_sc[1] = (float)G.sc->mu;
+  }
+  if (__syncthreads_or(G.sc->stop != 0) || (skip_unneeded && !(G.feedback || last))) return;
+  PassArgs<float> p = g2_args(G, AXIS);
+  p.kind = KIND;
+  p.pro = pro;
+  p.epi = epi;
+  // the pass body reads V for a phase prologue only when side says so
+  p.side = (pro == PRO_RT_HALF || pro == PRO_RT_FULL || epi == EPI_RT_END) ? 1 : 0;
+  if constexpr (AXIS == 1)
+    pass_body<float, G2P<N>, G2Y<N>, KIND>(p, item - off[g], smem, s_sc[0], s_sc[1]);
+  else
+    pass_body<float, Plan<N>, G2X<N>, KIND>(p, item - off[g], smem, s_sc[0], s_sc[1]);
+}
+
+template <int AXIS, int N>
+struct G2MBounds {
+  using P = std::conditional_t<AXIS == 1, G2P<N>, Plan<N>>;
+  using L = std::conditional_t<AXIS == 1, G2Y<N>, G2X<N>>;
+  static constexpr int value = MinBlocks<float, P, L>::value;
+};
+
+// One pass (AXIS 1: y, 0: x) over the tiles of every grid of the group:
+// KIND_STEP with the given prologue and epilogue, or KIND_ENERGY (the
+// kinetic sums of the grids whose mu is needed at this block end).
+template <int AXIS, int KIND, int N>
+__global__ void __launch_bounds__(G2_THREADS, G2MBounds<AXIS, N>::value)
+    k_multi2d(const G2Args a, int pro, int epi, int last) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  g2m_item<AXIS, KIND, N>(a, pro, epi, (int)blockIdx.x, KIND == KIND_ENERGY, last != 0, smem);
+}
+
+// The block finalizer of every grid of the group: CTA g = grid g.
+__global__ void __launch_bounds__(G2_THREADS) k_multi2d_final(const G2Args a, int jj, int last) {
+  __shared__ double red[G2_THREADS / 32];
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  g2_finalize(a, (int)blockIdx.x, jj, last != 0, red);
+}
+
+static cudaError_t g2m_launch(const void* kern, void** args, int nblocks, size_t smem, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)nblocks);
+  cfg.blockDim = dim3(G2_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, kern, args);
+}
+
+struct G2MKernels {
+  const void* k[2][2];  // [axis][kind: 0 step, 1 energy]
+  size_t smem[2][2];
+};
+
+template <int N>
+static G2MKernels g2m_kernels() {
+  G2MKernels K;
+  K.k[1][0] = (const void*)k_multi2d<1, KIND_STEP, N>;
+  K.k[1][1] = (const void*)k_multi2d<1, KIND_ENERGY, N>;
+  K.k[0][0] = (const void*)k_multi2d<0, KIND_STEP, N>;
+  K.k[0][1] = (const void*)k_multi2d<0, KIND_ENERGY, N>;
+  K.smem[1][0] = pass_smem_bytes<float, G2P<N>, G2Y<N>, KIND_STEP>();
+  K.smem[1][1] = pass_smem_bytes<float, G2P<N>, G2Y<N>, KIND_ENERGY>();
+  K.smem[0][0] = pass_smem_bytes<float, Plan<N>, G2X<N>, KIND_STEP>();
+  K.smem[0][1] = pass_smem_bytes<float, Plan<N>, G2X<N>, KIND_ENERGY>();
+  return K;
+}
+
+static bool g2m_lookup(int n, G2MKernels* K) {
+  switch (n) {
+#define X(v)               \
+  case v:                  \
+    *K = g2m_kernels<v>(); \
+    return true;
+    GPE_C2_SIZES(X)
+#undef X
+  }
+  return false;
+}
+
+cudaError_t launch_multi2d_block(const G2Args& a, int ny, int nx, int ny_items, int nx_items, int jj, bool last,
+                                 bool energy, cudaStream_t s) {
+  G2MKernels KY, KX;
+  if (!g2m_lookup(ny, &KY) || !g2m_lookup(nx, &KX)) return cudaErrorInvalidValue;
+  const void* ky[2] = {KY.k[1][0], KY.k[1][1]};
+  const void* kx[2] = {KX.k[0][0], KX.k[0][1]};
+  const size_t sy[2] = {KY.smem[1][0], KY.smem[1][1]}, sx[2] = {KX.smem[0][0], KX.smem[0][1]};
+  for (int k = 0; k < 2; ++k) {
+    cudaError_t e = cudaFuncSetAttribute(ky[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy[k]);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kx[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx[k]);
+    if (e != cudaSuccess) return e;
+  }
+  G2Args args = a;
+  int lst = last ? 1 : 0, j = jj, pnone = PRO_NONE, enone = EPI_NONE;
+  cudaError_t e = cudaSuccess;
+  for (int i = 1; i <= a.n_rec && e == cudaSuccess; ++i) {
+    int pro = i == 1 ? PRO_RT_HALF : PRO_RT_FULL;  // solve_split.m:55-56 / 60-61
+    void* ay[4] = {&args, &pro, &enone, &lst};
+    e = g2m_launch(ky[0], ay, ny_items, sy[0], s);
+    int epi = i == a.n_rec ? EPI_RT_END : EPI_NONE;  // solve_split.m:60-67
+    void* ax[4] = {&args, &pnone, &epi, &lst};
+    if (e == cudaSuccess) e = g2m_launch(kx[0], ax, nx_items, sx[0], s);
+  }
+  if (e == cudaSuccess && energy) {
+    void* ae[4] = {&args, &pnone, &enone, &lst};
+    e = g2m_launch(ky[1], ae, ny_items, sy[1], s);
+    if (e == cudaSuccess) e = g2m_launch(kx[1], ae, nx_items, sx[1], s);
+  }
+  if (e == cudaSuccess) {
+    void* af[3] = {&args, &j, &lst};
+    e = g2m_launch((const void*)k_multi2d_final, af, a.ngrids, 0, s);
+  }
+  return e;
 }
 
 }  // namespace gpe

@@ -50,5 +50,13 @@ size_t grid2d_smem();
 int grid2d_max_ctas();
 // Cooperative launch of nctas CTAs.
 cudaError_t launch_grid2d(const G2Args& a, int nctas, cudaStream_t s);
+// The launches of one block of n_rec steps on the multi-grid pass kernels,
+// for a group of grids of one shape (ny x nx): per step a y pass and an x
+// pass over the group's tiles, then (energy: some grid of the group needs mu
+// at this block end) the kinetic sums, and the block finalizer of every grid
+// (jj: the block's index in the outer step, last: the outer step's last
+// block).
+cudaError_t launch_multi2d_block(const G2Args& a, int ny, int nx, int ny_items, int nx_items, int jj, bool last,
+                                 bool energy, cudaStream_t s);
 
 }  // namespace gpe

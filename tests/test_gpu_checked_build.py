@@ -2,7 +2,7 @@
 parity cases.
 
 In that build every global index of the axis-pass kernels (scalar, paired,
-TMA-staged, cluster and grid-wide) is checked against the extent of its
+TMA-staged, cluster, grid-wide and multi-grid) is checked against the extent of its
 pass, and every shared-memory exchange index against its buffer; a
 violation is recorded, the access skipped, and the run returns
 GPE_ERR_BOUNDS.  The cases below run in a child process that loads the
@@ -106,8 +106,10 @@ def run_cases():
     assert o["energy"] == o["energy"]
     task.close()
     n += 1
-    # the persistent kernels of small 2D grids: cluster (FP64) and grid-wide (FP32) batches
-    for precision in ("double", "single"):
+    # the kernels of small 2D grids: cluster (FP64), multi-grid pass kernels
+    # and grid-wide (FP32) batches
+    for precision, path in (("double", "cluster"), ("single", "multi"), ("single", "grid")):
+        os.environ["GPE_SMALL2D"] = path
         tasks, refs = [], []
         for axes in ((4.0, 64, 4.0, 64), (5.0, 96, 4.0, 128), (6.0, 256, 6.0, 256)):
             grid, task, og, ot = make_pair(gpe, axes, harmonic((1.0, 1.3)), precision, g=0.8, gamma=0.01, Ntotal=5.0)
@@ -123,6 +125,7 @@ def run_cases():
             assert rel_l2(t.current_state, ot.current_state) < tol
             t.close()
         n += 1
+    os.environ.pop("GPE_SMALL2D", None)
     print(f"CHECKED-BUILD ok {n}", flush=True)
 
 

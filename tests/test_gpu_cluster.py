@@ -1,8 +1,10 @@
 """The persistent kernels of small 2D grids (solve_split of one context, or
 solve_split_batch of many, one launch per outer step for all of them): the
 cluster kernel (state in distributed shared memory, one cluster per grid)
-and the grid-wide kernel (FP32, GPE_SMALL2D=grid: every pass spread over all
-SMs, grid barriers between passes), against the per-pass path (pass variant
+the grid-wide kernel (FP32, GPE_SMALL2D=grid: every pass spread over all
+SMs, grid barriers between passes) and the multi-grid pass kernels (FP32,
+GPE_SMALL2D=multi: one launch per pass over the tiles of all grids of one
+shape, a stream per shape, one graph per outer step), against the per-pass path (pass variant
 2: two axis-pass launches per step and grid) and against the FP64 oracle,
 through the C ABI.
 
@@ -45,7 +47,7 @@ def make(gpe, spec, precision, variant):
     return t
 
 
-PATHS = [("cluster", "double"), ("cluster", "single"), ("grid", "single")]
+PATHS = [("cluster", "double"), ("cluster", "single"), ("grid", "single"), ("multi", "single")]
 
 
 @pytest.mark.parametrize("path,precision", PATHS)
@@ -104,7 +106,7 @@ def test_cluster_single_context_with_feedback_decay_and_callbacks(gpe, monkeypat
     task.close()
 
 
-@pytest.mark.parametrize("path", ["cluster", "grid"])
+@pytest.mark.parametrize("path", ["cluster", "grid", "multi"])
 def test_cluster_kernel_is_the_launched_kernel(gpe, monkeypatch, path):
     """With per-launch profiling the persistent path launches directly: one
     cluster_step launch per outer step and no axis-pass launch."""
