@@ -2215,23 +2215,34 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
   } gres;
   cudaEvent_t fork_ev = nullptr;
   if (nctas == 0) {
-    std::vector<std::pair<int, int>> shapes;
-    for (const auto& G : grids)
-      if (std::find(shapes.begin(), shapes.end(), std::make_pair(G.ny, G.nx)) == shapes.end())
-        shapes.push_back({G.ny, G.nx});
+    // groups: the grids of one shape (splitting a shape that holds most of
+    // the points over several streams measured no faster)
+    std::vector<std::vector<int>> members;
+    {
+      std::vector<std::pair<int, int>> shapes;
+      for (size_t i = 0; i < grids.size(); ++i) {
+        const auto sh = std::make_pair(grids[i].ny, grids[i].nx);
+        const size_t k = std::find(shapes.begin(), shapes.end(), sh) - shapes.begin();
+        if (k == shapes.size()) {
+          shapes.push_back(sh);
+          members.emplace_back();
+        }
+        members[k].push_back((int)i);
+      }
+    }
     CU(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
     gres.events.push_back(fork_ev);
-    for (const auto& sh : shapes) {
+    for (const auto& mem : members) {
       std::vector<G2Grid> gg;
       std::vector<int> yo{0}, xo{0};
       bool fb = false;
-      for (const auto& G : grids)
-        if (G.ny == sh.first && G.nx == sh.second) {
-          gg.push_back(G);
-          yo.push_back(yo.back() + G.ytiles);
-          xo.push_back(xo.back() + G.xtiles);
-          fb = fb || G.feedback;
-        }
+      for (int i : mem) {
+        const G2Grid& G = grids[i];
+        gg.push_back(G);
+        yo.push_back(yo.back() + G.ytiles);
+        xo.push_back(xo.back() + G.xtiles);
+        fb = fb || G.feedback;
+      }
       const size_t ggb = gg.size() * sizeof(G2Grid), gob = (gg.size() + 1) * sizeof(int);
       char* buf = nullptr;
       CU(cudaMalloc(&buf, ggb + 2 * gob));
@@ -2245,8 +2256,8 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
       grp.a.ngrids = (int)gg.size();
       grp.a.yoff = reinterpret_cast<const int*>(buf + ggb);
       grp.a.xoff = reinterpret_cast<const int*>(buf + ggb + gob);
-      grp.ny = sh.first;
-      grp.nx = sh.second;
+      grp.ny = gg[0].ny;
+      grp.nx = gg[0].nx;
       grp.ny_items = yo.back();
       grp.nx_items = xo.back();
       grp.feedback = fb;
