@@ -490,6 +490,11 @@ struct PassArgs {
   // copy per 128-byte row.
   int tma_tensor = 0;
   long long tdim[4] = {1, 1, 1, 1};
+  // Step pass (scalar kernels): 1 = transform, the full nonlinear step
+  // (PRO_RT_FULL's phase, V read from L2), transform again: the passes of
+  // this axis that end one split step and begin the next, when consecutive
+  // steps take the axes in opposite orders.
+  int fold = 0;
 };
 
 }  // namespace gpe

@@ -380,11 +380,12 @@ size_t rsize() {
 // ---- profiling --------------------------------------------------------------
 enum ProfCls {
   PC_PASS_Y, PC_PASS_X, PC_PASS_Z, PC_ENERGY_Y, PC_ENERGY_X, PC_ENERGY_Z, PC_FINALIZE, PC_ITP_CHECK,
-  PC_NORM, PC_ELEMENTWISE, PC_NL_PHASE, PC_ADJ_NL, PC_COPY, PC_CLUSTER, PC_COUNT
+  PC_NORM, PC_ELEMENTWISE, PC_NL_PHASE, PC_ADJ_NL, PC_COPY, PC_CLUSTER, PC_FOLD_Y, PC_FOLD_X, PC_FOLD_Z, PC_COUNT
 };
 const char* kProfNames[PC_COUNT] = {"pass_y",   "pass_x",    "pass_z",      "energy_y",  "energy_x",
                                     "energy_z", "finalize",  "itp_check",   "norm",      "elementwise",
-                                    "nl_phase", "adjoint_nl", "state_copy", "cluster_step"};
+                                    "nl_phase", "adjoint_nl", "state_copy", "cluster_step", "pass_yy",
+                                    "pass_xx",  "pass_zz"};
 
 cudaEvent_t pool_event(gpe_ctx* c) {
   if (!c->ev_pool.empty()) {
@@ -763,9 +764,10 @@ gpe_status write_scalars(gpe_ctx* c, const DevScalars& v) {
 }
 
 // ---- passes ---------------------------------------------------------------------
+// fold = 1: a folded step pass (PassArgs::fold), scalar kernels only.
 template <typename R>
 gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro, int epi, int energy_pot,
-                    double dre, double dim, int* nblk, void* psi_buf = nullptr) {
+                    double dre, double dim, int* nblk, void* psi_buf = nullptr, int fold = 0) {
   PassArgs<R> a;
   a.psi = (cx<R>*)(psi_buf ? psi_buf : f.psi);  // psi_buf: another array of the grid's shape
   a.V = (const R*)f.V;
@@ -783,7 +785,8 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   a.npts = ap.n_batch * (long long)ap.N;  // the pencils of a pass tile the array it covers
   a.cap = c->cap;
   // rotating-frame terms and the cut-off chain run in the extended step kernel
-  a.kind = (kind == KIND_STEP && (ap.rot != 0 || ap.split != SPLIT_FULL)) ? KIND_STEP_EXT : kind;
+  // (and the folded passes)
+  a.kind = (kind == KIND_STEP && (ap.rot != 0 || ap.split != SPLIT_FULL || fold)) ? KIND_STEP_EXT : kind;
   a.pro = pro;
   a.epi = epi;
   a.kin_slot = S_KX + ap.axis;
@@ -822,16 +825,18 @@ gpe_status run_pass(gpe_ctx* c, Field& f, const AxisPass& ap, int kind, int pro,
   double bytes = (kind == KIND_ENERGY ? 1.0 : 2.0) * P * 2 * sizeof(R);
   const bool useV = pro == PRO_RT_HALF || pro == PRO_RT_FULL || pro == PRO_ITP || epi == EPI_RT_END ||
                     (kind == KIND_ENERGY && energy_pot);
-  if (useV) bytes += P * sizeof(R);
+  if (useV || fold) bytes += P * sizeof(R);
   if (pro == PRO_ITP || epi == EPI_ITP) bytes += P * sizeof(R);
-  int cls = (kind == KIND_ENERGY ? PC_ENERGY_Y : PC_PASS_Y);
+  int cls = (kind == KIND_ENERGY ? PC_ENERGY_Y : fold ? PC_FOLD_Y : PC_PASS_Y);
   cls += (ap.axis == 1 ? 0 : ap.axis == 0 ? 1 : 2);
+  a.fold = fold;
   // The array staged with each tile by the TMA pass.
   a.side = (pro == PRO_RT_HALF || pro == PRO_RT_FULL || pro == PRO_ITP || epi == EPI_RT_END ||
             (kind == KIND_ENERGY && energy_pot))
                ? 1
                : (epi == EPI_ITP ? 2 : 0);
-  if (use_tma<R>(c, f, ap)) {
+  if (fold) a.side = 1;
+  if (!fold && use_tma<R>(c, f, ap)) {
     // Test knob of the timeout path (off unless GPE_TEST_TMA_STALL is set):
     // the TMA pass arms its barriers for copies it never issues and polls
     // them GPE_TEST_TMA_STALL times, so its bounded wait runs out with no
@@ -1362,12 +1367,57 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
 
 // One block of n_rec steps, solve_split.m:51-79 (VV refresh is the caller's).
 // hist: where the block-end finalizer stores (muc, ncur), or nullptr.
+// Folded steps (3D, one component, plain axis passes; GPE_FOLD=0 turns
+// them off): the odd steps of a block take the axes in the order y x z, the
+// even steps z x y, so that the last pass of a step and the first of the
+// next are on one axis; those two run as one folded pass (transform, full
+// nonlinear step, transform), a block of n steps is 2n + 1 passes instead
+// of 3n.  The kinetic factors of the axes commute (solve_split.m:58-59
+// applies them together in Fourier space), so the reordering changes only
+// the rounding.
+bool fold_steps(const gpe_ctx* c, const SplitRun& run) {
+  if (c->ndims != 3 || c->ncomp != 1 || run.sgpe || run.sgpe_cn || c->omega_field || run.passes.size() != 3)
+    return false;
+  for (const auto& ap : run.passes)
+    if (ap.axis < 0 || ap.rot != 0 || ap.split != SPLIT_FULL || ap.half != 0 || ap.one_comp) return false;
+  const char* e = getenv("GPE_FOLD");
+  return !(e && atoi(e) == 0);
+}
+
 template <typename R>
 gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool last_block, double* hist,
                          unsigned long long step0 = 0) {
   Field& f = c->main;
   int nb_epi = 0;
-  for (int i = 1; i <= run.n_rec; ++i) {
+  if (fold_steps(c, run)) {
+    const int np = (int)run.passes.size();
+    // the axis order of step i (1-based): y x z for odd i, z x y for even i;
+    // GPE_FOLD=2: a block with an even step count keeps y x z for its last
+    // step (the block then ends on z, one pass more)
+    const char* fe = getenv("GPE_FOLD");
+    const bool end_z = fe && atoi(fe) == 2 && run.n_rec % 2 == 0;
+    auto order = [&](int i, int j) -> const AxisPass& {
+      const bool rev = i % 2 == 0 && !(end_z && i == run.n_rec);
+      return run.passes[rev ? np - 1 - j : j];
+    };
+    auto folds = [&](int i) {  // the last pass of step i folds with the first of step i+1
+      return i < run.n_rec && order(i, np - 1).axis == order(i + 1, 0).axis;
+    };
+    for (int i = 1; i <= run.n_rec; ++i) {
+      for (int j = 0; j < np; ++j) {
+        if (j == 0 && i > 1 && folds(i - 1)) continue;  // run by the previous step's last pass
+        const AxisPass& ap = order(i, j);
+        const bool lastp = j == np - 1;
+        // solve_split.m:55-56 (block start) / 60-61 (between unfolded steps)
+        const int pro = j == 0 ? (i == 1 ? PRO_RT_HALF : PRO_RT_FULL) : PRO_NONE;
+        const bool end = lastp && i == run.n_rec;
+        const int fold = (lastp && folds(i)) ? 1 : 0;  // solve_split.m:60-61 between the transforms
+        CHECK(run_pass<R>(c, f, ap, KIND_STEP, pro, end ? EPI_RT_END : EPI_NONE, 0, run.dre, run.dim,
+                          end ? &nb_epi : nullptr, nullptr, fold));
+      }
+    }
+  }
+  for (int i = 1; i <= run.n_rec && !fold_steps(c, run); ++i) {
     if (run.sgpe) {
       // SGPE (solve_split.m:57-66): the nonlinear factor (half at the block
       // start, else the full one of the previous step) and the noise of step

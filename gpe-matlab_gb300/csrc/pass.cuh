@@ -277,6 +277,25 @@ struct MinBlocks {
   static constexpr int value = (sizeof(R) == 4 && L::THREADS <= TPS) ? TPS / L::THREADS : 1;
 };
 
+// The full nonlinear step of real time, exp((-(V - mu) - g|psi|^2) dt) psi
+// (solve_split.m:60-61), on one pencil's E values (sv: V).
+template <typename R, int E>
+__device__ __forceinline__ void rt_full_phase(cx<R>* v, const R* sv, const PassArgs<R>& a, R mu) {
+  const R g = a.gr, dre = a.drer, dim = a.dimr;
+  if constexpr (sizeof(R) == 4) {
+    float ex[E];
+#pragma unroll
+    for (int m = 0; m < E; ++m) ex[m] = -(sv[m] - mu) - g * norm2(v[m]);
+    apply_rt_phase<E>(v, ex, dre, dim);
+  } else {
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const R ex = -(sv[m] - mu) - g * norm2(v[m]);
+      v[m] = cmul(cexp_real_times(ex, dre, dim), v[m]);
+    }
+  }
+}
+
 // Prologue of the first pass on one pencil's E values (sv: V for the phase
 // modes, unused otherwise).  The mode switch sits outside the unrolled loops
 // so only the selected variant executes (branches inside an unrolled loop
@@ -310,18 +329,7 @@ __device__ __forceinline__ void prologue(cx<R>* v, const R* sv, const PassArgs<R
       }
       break;
     case PRO_RT_FULL:  // solve_split.m:60-61
-      if constexpr (sizeof(R) == 4) {
-        float ex[E];
-#pragma unroll
-        for (int m = 0; m < E; ++m) ex[m] = -(sv[m] - mu) - g * norm2(v[m]);
-        apply_rt_phase<E>(v, ex, dre, dim);
-      } else {
-#pragma unroll
-        for (int m = 0; m < E; ++m) {
-          const R ex = -(sv[m] - mu) - g * norm2(v[m]);
-          v[m] = cmul(cexp_real_times(ex, dre, dim), v[m]);
-        }
-      }
+      rt_full_phase<R, E>(v, sv, a, mu);
       break;
     case PRO_ITP:  // groundstate_itp.m:36/76, :40
 #pragma unroll
@@ -343,19 +351,44 @@ __device__ __forceinline__ void epilogue(cx<R>* v, const R* sv, const PassArgs<R
                                          bool valid, R mu) {
   if (a.epi == EPI_RT_END) {
     const R g = a.gr, dre = a.drer, dim = a.dimr;
+    if constexpr (sizeof(R) == 4) {
+      // FP32: both phases through the packed sin/cos/exp of apply_rt_phase,
+      // in halves of the thread's values (fewer live registers)
+      constexpr int H = E % 4 == 0 ? E / 2 : E;
 #pragma unroll
-    for (int m = 0; m < E; ++m) {
-      cx<R> p = v[m];
-      const R VV = sv[m] - mu;
-      p = cmul(cexp_real_times(-VV - g * norm2(p), dre, dim), p);            // solve_split.m:60-61
-      p = cmul(cexp_real_times((VV + g * norm2(p)) * R(0.5), dre, dim), p);  // solve_split.m:63-64
-      const R n = norm2(p);                                                  // solve_split.m:65
-      if (valid) {
-        acc[0].add(n);
-        acc[1].add(sv[m] * n);
-        acc[2].add(n * n);
+      for (int h = 0; h < E; h += H) {
+        float ex[H];
+#pragma unroll
+        for (int m = 0; m < H; ++m) ex[m] = -(sv[h + m] - mu) - g * norm2(v[h + m]);  // solve_split.m:60-61
+        apply_rt_phase<H>(v + h, ex, dre, dim);
+#pragma unroll
+        for (int m = 0; m < H; ++m) ex[m] = ((sv[h + m] - mu) + g * norm2(v[h + m])) * 0.5f;  // :63-64
+        apply_rt_phase<H>(v + h, ex, dre, dim);
+#pragma unroll
+        for (int m = 0; m < H; ++m) {
+          const R n = norm2(v[h + m]);  // solve_split.m:65
+          if (valid) {
+            acc[0].add(n);
+            acc[1].add(sv[h + m] * n);
+            acc[2].add(n * n);
+          }
+        }
       }
-      v[m] = p;
+    } else {
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        cx<R> p = v[m];
+        const R VV = sv[m] - mu;
+        p = cmul(cexp_real_times(-VV - g * norm2(p), dre, dim), p);            // solve_split.m:60-61
+        p = cmul(cexp_real_times((VV + g * norm2(p)) * R(0.5), dre, dim), p);  // solve_split.m:63-64
+        const R n = norm2(p);                                                  // solve_split.m:65
+        if (valid) {
+          acc[0].add(n);
+          acc[1].add(sv[m] * n);
+          acc[2].add(n * n);
+        }
+        v[m] = p;
+      }
     }
   } else if (a.epi == EPI_ITP) {
 #pragma unroll
@@ -483,27 +516,35 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, long long tile, 
     }
     constexpr bool SMT = SmemTables<R, P, KIND>::value;
     if constexpr (KIND == KIND_STEP_EXT) {
-      if (!a.skip_fwd) {
-        St::template forward<SMT>(v, sm, pol, t, tws);
-        apply_phase<T, E, SMT>(v, php, t);
-        if (a.rot) {
-          // rotating frame: the cross term of this pencil's transverse coordinate
-          const unsigned ci = valid ? (unsigned)b % (unsigned)a.rot_period : 0u;
-          apply_phase<T, E, false>(v, a.rot + (size_t)ci * P::N, t);
-        }
-        if (a.mask_c) {
-          // energy cut-off, ekk .* (kk < ecut) (SGPEtask/solve_split.m:40-42)
-          R kab = R(0);
-          if (valid) {
-            kab = __ldg(a.mask_a + b % a.mask_pa);
-            if (a.mask_b) kab += __ldg(a.mask_b + b / a.mask_pa);
+      // a folded pass (a.fold = 1): the transform, the full nonlinear step,
+      // the transform again (the state stays in registers between the steps)
+#pragma unroll 1
+      for (int rep = 0;; ++rep) {
+        if (!a.skip_fwd) {
+          St::template forward<SMT>(v, sm, pol, t, tws);
+          apply_phase<T, E, SMT>(v, php, t);
+          if (a.rot) {
+            // rotating frame: the cross term of this pencil's transverse coordinate
+            const unsigned ci = valid ? (unsigned)b % (unsigned)a.rot_period : 0u;
+            apply_phase<T, E, false>(v, a.rot + (size_t)ci * P::N, t);
           }
+          if (a.mask_c) {
+            // energy cut-off, ekk .* (kk < ecut) (SGPEtask/solve_split.m:40-42)
+            R kab = R(0);
+            if (valid) {
+              kab = __ldg(a.mask_a + b % a.mask_pa);
+              if (a.mask_b) kab += __ldg(a.mask_b + b / a.mask_pa);
+            }
 #pragma unroll
-          for (int m = 0; m < E; ++m)
-            if (!(kab + __ldg(a.mask_c + m * T + t) < a.ecut)) v[m] = mk<R>(R(0), R(0));
+            for (int m = 0; m < E; ++m)
+              if (!(kab + __ldg(a.mask_c + m * T + t) < a.ecut)) v[m] = mk<R>(R(0), R(0));
+          }
         }
+        if (!a.skip_inv) St::template inverse<SMT>(v, sm, pol, t, tws);
+        if (rep >= a.fold) break;
+        load_side();
+        rt_full_phase<R, E>(v, sv, a, scal[1]);
       }
-      if (!a.skip_inv) St::template inverse<SMT>(v, sm, pol, t, tws);
     } else {
       St::template forward<SMT>(v, sm, pol, t, tws);
       apply_phase<T, E, SMT>(v, php, t);

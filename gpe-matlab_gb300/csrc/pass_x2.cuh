@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(L::THREADS, X2MinBlocks<P, L>::value) pass_x2_
 // adjacent, 16-byte aligned elements: an even pencil count, and even row
 // offsets and strides on the strided axes.
 inline bool x2_applies(const PassArgs<float>& a, bool strided) {
-  if (a.kind != KIND_STEP || a.rot || a.skip_fwd || a.skip_inv || a.mask_c) return false;
+  if (a.kind != KIND_STEP || a.rot || a.skip_fwd || a.skip_inv || a.mask_c || a.fold) return false;
   if (a.n_batch % 2 != 0) return false;
   if (strided) return a.inner % 2 == 0 && a.outer % 2 == 0 && a.stride % 2 == 0;
   return true;
