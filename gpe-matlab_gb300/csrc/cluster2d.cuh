@@ -110,9 +110,12 @@ struct C2XPol {
 
 // ---- the passes ----------------------------------------------------------------
 // y pass over this CTA's pencils, in place in `home` (pencil pc at pc*regy).
+// pa.fold = 1: a folded pass (the transform, the full nonlinear step, the
+// transform again: the last pass of one step and the first of the next);
+// pa.epi = EPI_RT_END: the block-end phases and the n, Vn, n^2 sums.
 template <typename R, class P>
 __device__ __forceinline__ void c2_y_step(cx<R>* home, const R* vloc, const C2Geom& g, const C2Grid& G, int col0,
-                                          const PassArgs<R>& pa, R s, R mu) {
+                                          const PassArgs<R>& pa, R s, R mu, Kahan<R>* acc) {
   constexpr int T = P::T, E = P::E, N = P::N;
   constexpr int FPI = C2Threads<R>::value / T;
   using St = typename P::template St<R>;
@@ -132,8 +135,8 @@ __device__ __forceinline__ void c2_y_step(cx<R>* home, const R* vloc, const C2Ge
     cx<R> v[E];
 #pragma unroll
     for (int m = 0; m < E; ++m) v[m] = valid ? home[GPE_SMI(pol, pol.idx(t + T * m))] : mk<R>(R(0), R(0));
-    if (pa.pro != PRO_NONE) {
-      R sv[E];
+    R sv[E];
+    auto load_v = [&]() {
       if (vloc) {  // this CTA's V columns in shared memory
         const R* vs = vloc + pc * N + t;
 #pragma unroll
@@ -143,20 +146,33 @@ __device__ __forceinline__ void c2_y_step(cx<R>* home, const R* vloc, const C2Ge
 #pragma unroll
         for (int m = 0; m < E; ++m) sv[m] = valid ? __ldg(vs + T * m) : R(0);
       }
+    };
+    if (pa.pro != PRO_NONE) {
+      load_v();
       prologue<R, E>(v, sv, pa, valid, 0, 0, s, mu);
     }
     pol.sync();  // every lane has read its values before the exchanges reuse the pencil
-    St::template forward<false>(v, home, pol, t, tws);
-    apply_phase<T, E, false>(v, php, t);
-    St::template inverse<false>(v, home, pol, t, tws);
+#pragma unroll 1
+    for (int rep = 0;; ++rep) {
+      St::template forward<false>(v, home, pol, t, tws);
+      apply_phase<T, E, false>(v, php, t);
+      St::template inverse<false>(v, home, pol, t, tws);
+      if (rep >= pa.fold) break;
+      load_v();
+      rt_full_phase<R, E>(v, sv, pa, mu);  // solve_split.m:60-61
+    }
+    if (pa.epi != EPI_NONE) {
+      load_v();
+      epilogue<R, E>(v, sv, pa, acc, valid, mu);
+    }
 #pragma unroll
     for (int m = 0; m < E; ++m) home[GPE_SMI(pol, pol.idx(t + T * m))] = v[m];
   }
 }
 
 // x pass over rows [rank*rows, (rank+1)*rows): elements read from and
-// written back to the owning CTAs' pencils.  epi = EPI_RT_END adds the
-// block-end phases and the n, Vn, n^2 sums.
+// written back to the owning CTAs' pencils.  pa.fold and epi = EPI_RT_END as
+// in the y pass.
 template <typename R, class P>
 __device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const C2Geom& g, const C2Grid& G, int rank,
                                           const PassArgs<R>& pa, R mu, Kahan<R>* acc) {
@@ -190,14 +206,23 @@ __device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const C2Geom
         }
       }
     }
-    St::template forward<false>(v, xbuf, pol, t, tws);
-    apply_phase<T, E, false>(v, php, t);
-    St::template inverse<false>(v, xbuf, pol, t, tws);
-    if (pa.epi != EPI_NONE) {
-      R sv[E];
+    R sv[E];
+    auto load_v = [&]() {
       const R* vs = V + (long long)t * G.ny + y;
 #pragma unroll
       for (int m = 0; m < E; ++m) sv[m] = valid ? __ldg(vs + (long long)T * m * G.ny) : R(0);
+    };
+#pragma unroll 1
+    for (int rep = 0;; ++rep) {
+      St::template forward<false>(v, xbuf, pol, t, tws);
+      apply_phase<T, E, false>(v, php, t);
+      St::template inverse<false>(v, xbuf, pol, t, tws);
+      if (rep >= pa.fold) break;
+      load_v();
+      rt_full_phase<R, E>(v, sv, pa, mu);  // solve_split.m:60-61
+    }
+    if (pa.epi != EPI_NONE) {
+      load_v();
       epilogue<R, E>(v, sv, pa, acc, valid, mu);
     }
     if (valid) {
@@ -287,11 +312,11 @@ __device__ __forceinline__ void c2_x_energy(const cx<R>* home, cx<R>* xbuf, cons
 // Runtime dispatch over the axis length.
 template <typename R>
 __device__ void c2_y_step_n(int n, cx<R>* home, const R* vloc, const C2Geom& g, const C2Grid& G, int col0,
-                            const PassArgs<R>& pa, R s, R mu) {
+                            const PassArgs<R>& pa, R s, R mu, Kahan<R>* acc) {
   switch (n) {
-#define X(v)                                                          \
-  case v:                                                             \
-    c2_y_step<R, C2Plan<R, v>>(home, vloc, g, G, col0, pa, s, mu);    \
+#define X(v)                                                             \
+  case v:                                                                \
+    c2_y_step<R, C2Plan<R, v>>(home, vloc, g, G, col0, pa, s, mu, acc);  \
     break;
     GPE_C2_SIZES(X)
 #undef X
@@ -416,12 +441,31 @@ __global__ void __launch_bounds__(C2Threads<R>::value, C2Threads<R>::min_blocks)
       for (int jj = 1; jj <= a.nb && !stopped; ++jj) {
         const double time2 = time + (jj - 1) * a.ddt * a.n_rec;  // solve_split.m:53
         Kahan<R> acc[3];
+        // Folded steps: step i takes the axes in the order y x (odd i) or
+        // x y (even i), so the last pass of a step and the first of the
+        // next are one folded pass with the full nonlinear step between its
+        // transforms (solve_split.m:60-61): 1 + n_rec passes and cluster
+        // barriers per block instead of 2 n_rec.  The kinetic factors of
+        // the axes commute; only the rounding differs.
+        // (a.fold = 0: y x every step, 2 n_rec passes)
+        pa.pro = PRO_RT_HALF;  // solve_split.m:55-56
+        pa.epi = EPI_NONE;
+        pa.fold = 0;
+        c2_y_step_n<R>(G.ny, home, vloc, g, G, col0, pa, s, mu, acc);
+        c2_sync();
+        pa.pro = PRO_NONE;
         for (int i = 1; i <= a.n_rec; ++i) {
-          pa.pro = i == 1 ? PRO_RT_HALF : PRO_RT_FULL;  // solve_split.m:55-56 / 60-61
-          c2_y_step_n<R>(G.ny, home, vloc, g, G, col0, pa, s, mu);
-          c2_sync();
+          const bool xa = !a.fold || i % 2 == 1;
+          if (!a.fold && i > 1) {
+            pa.pro = PRO_RT_FULL;  // solve_split.m:60-61
+            c2_y_step_n<R>(G.ny, home, vloc, g, G, col0, pa, s, mu, acc);
+            c2_sync();
+            pa.pro = PRO_NONE;
+          }
+          pa.fold = a.fold && i < a.n_rec ? 1 : 0;
           pa.epi = i == a.n_rec ? EPI_RT_END : EPI_NONE;  // solve_split.m:60-67
-          c2_x_step_n<R>(G.nx, home, xbuf, g, G, rank, pa, mu, acc);
+          if (xa) c2_x_step_n<R>(G.nx, home, xbuf, g, G, rank, pa, mu, acc);
+          else c2_y_step_n<R>(G.ny, home, vloc, g, G, col0, pa, s, mu, acc);
           c2_sync();
         }
         const bool last = jj == a.nb;

@@ -103,6 +103,7 @@ struct C2Args {
   int n_rec, nb;     // steps per block, blocks per outer step
   int nouter;        // outer steps per launch
   int vsm;           // V columns in shared memory (C2Geom)
+  int fold;          // folded steps (y x, x y, ...: 1 + n_rec passes per block)
   double ddt, dt_outer;
 };
 

@@ -1367,21 +1367,23 @@ gpe_status split_setup(gpe_ctx* c, const gpe_split_params* prm, SplitRun& run, i
 
 // One block of n_rec steps, solve_split.m:51-79 (VV refresh is the caller's).
 // hist: where the block-end finalizer stores (muc, ncur), or nullptr.
-// Folded steps (3D, one component, plain axis passes; GPE_FOLD=0 turns
-// them off): the odd steps of a block take the axes in the order y x z, the
-// even steps z x y, so that the last pass of a step and the first of the
-// next are on one axis; those two run as one folded pass (transform, full
-// nonlinear step, transform), a block of n steps is 2n + 1 passes instead
-// of 3n.  The kinetic factors of the axes commute (solve_split.m:58-59
-// applies them together in Fourier space), so the reordering changes only
-// the rounding.
-bool fold_steps(const gpe_ctx* c, const SplitRun& run) {
-  if (c->ndims != 3 || c->ncomp != 1 || run.sgpe || run.sgpe_cn || c->omega_field || run.passes.size() != 3)
-    return false;
-  for (const auto& ap : run.passes)
-    if (ap.axis < 0 || ap.rot != 0 || ap.split != SPLIT_FULL || ap.half != 0 || ap.one_comp) return false;
+// Folded steps (one component, plain axis passes; GPE_FOLD=0 turns them
+// off): the odd steps of a block take the axes in the order y x z (2D: y x),
+// the even steps z x y (x y), so that the last pass of a step and the first
+// of the next are on one axis; those two run as one folded pass (transform,
+// full nonlinear step, transform).  A block of n steps is 2n + 1 passes
+// instead of 3n (2D: n + 1 instead of 2n).  The kinetic factors of the axes
+// commute (ssft_kin_step.m:17 applies them together in Fourier space), so
+// the reordering changes only the rounding.
+bool fold_env() {
   const char* e = getenv("GPE_FOLD");
   return !(e && atoi(e) == 0);
+}
+bool fold_steps(const gpe_ctx* c, const SplitRun& run) {
+  if (c->ncomp != 1 || run.sgpe || run.sgpe_cn || c->omega_field || (int)run.passes.size() != c->ndims) return false;
+  for (const auto& ap : run.passes)
+    if (ap.axis < 0 || ap.rot != 0 || ap.split != SPLIT_FULL || ap.half != 0 || ap.one_comp) return false;
+  return fold_env();
 }
 
 template <typename R>
@@ -2092,6 +2094,7 @@ gpe_status cluster_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, 
   a.nb = r0.nb;
   a.nouter = 1;
   a.vsm = pl.vsm;
+  a.fold = fold_env() ? 1 : 0;
   a.ddt = r0.ddt;
   a.dt_outer = r0.dt_outer;
   cudaStream_t master = c->stream;
@@ -2338,7 +2341,7 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
       for (int jj = 1; jj <= r0.nb && e == cudaSuccess; ++jj) {
         const bool last = jj == r0.nb;
         e = launch_multi2d_block(grp.a, grp.ny, grp.nx, grp.ny_items, grp.nx_items, jj, last, grp.feedback || last,
-                                 grp.s);
+                                 fold_env(), grp.s);
       }
     for (size_t k = 1; k < groups.size() && e == cudaSuccess; ++k) {
       e = cudaEventRecord(groups[k].done, groups[k].s);

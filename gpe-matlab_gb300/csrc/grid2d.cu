@@ -180,7 +180,8 @@ __device__ __forceinline__ double g2_cta_sum(const double* p, int n, double* red
 }
 
 // The block finalizer of grid g (the arithmetic of aux_kernels.cu
-// k_finalize_block): sums of the block-end epilogue (x tiles) and, when mu
+// k_finalize_block): sums of the block-end epilogue (the tiles of the pass
+// that ran it: x, or y after folded steps with an even n_rec) and, when mu
 // is needed, the kinetic sums (y and x tiles); mu, the renormalisation
 // factor, the history record of the outer step's last block.
 __device__ void g2_finalize(const G2Args& a, int g, int jj, bool last, double* red) {
@@ -189,9 +190,10 @@ __device__ void g2_finalize(const G2Args& a, int g, int jj, bool last, double* r
   if (__syncthreads_or(sc->stop != 0)) return;
   const bool need = G.feedback || last;
   const int cap = G.cap;
-  const double n = g2_cta_sum(G.partials + S_N * cap, G.xtiles, red);
-  const double vn = g2_cta_sum(G.partials + S_VN * cap, G.xtiles, red);
-  const double n2 = g2_cta_sum(G.partials + S_N2 * cap, G.xtiles, red);
+  const int ne = a.epi_y ? G.ytiles : G.xtiles;  // tiles of the pass that ran the epilogue
+  const double n = g2_cta_sum(G.partials + S_N * cap, ne, red);
+  const double vn = g2_cta_sum(G.partials + S_VN * cap, ne, red);
+  const double n2 = g2_cta_sum(G.partials + S_N2 * cap, ne, red);
   double kin = 0.0;
   if (need) kin = g2_cta_sum(G.partials + S_KY * cap, G.ytiles, red) + g2_cta_sum(G.partials + S_KX * cap, G.xtiles, red);
   if (threadIdx.x != 0) return;
@@ -381,6 +383,7 @@ __device__ __forceinline__ void g2m_item(const G2Args& a, int pro, int epi, int 
   p.epi = epi;
   // the pass body reads V for a phase prologue only when side says so
   p.side = (pro == PRO_RT_HALF || pro == PRO_RT_FULL || epi == EPI_RT_END) ? 1 : 0;
+  p.fold = KIND == KIND_STEP_EXT ? 1 : 0;  // the extended kernel runs the folded passes
   if constexpr (AXIS == 1)
     pass_body<float, G2P<N>, G2Y<N>, KIND>(p, item - off[g], smem, s_sc[0], s_sc[1]);
   else
@@ -429,8 +432,8 @@ static cudaError_t g2m_launch(const void* kern, void** args, int nblocks, size_t
 }
 
 struct G2MKernels {
-  const void* k[2][2];  // [axis][kind: 0 step, 1 energy]
-  size_t smem[2][2];
+  const void* k[2][3];  // [axis][kind: 0 step, 1 energy, 2 folded step]
+  size_t smem[2][3];
 };
 
 template <int N>
@@ -440,6 +443,10 @@ static G2MKernels g2m_kernels() {
   K.k[1][1] = (const void*)k_multi2d<1, KIND_ENERGY, N>;
   K.k[0][0] = (const void*)k_multi2d<0, KIND_STEP, N>;
   K.k[0][1] = (const void*)k_multi2d<0, KIND_ENERGY, N>;
+  K.k[1][2] = (const void*)k_multi2d<1, KIND_STEP_EXT, N>;
+  K.k[0][2] = (const void*)k_multi2d<0, KIND_STEP_EXT, N>;
+  K.smem[1][2] = pass_smem_bytes<float, G2P<N>, G2Y<N>, KIND_STEP_EXT>();
+  K.smem[0][2] = pass_smem_bytes<float, Plan<N>, G2X<N>, KIND_STEP_EXT>();
   K.smem[1][0] = pass_smem_bytes<float, G2P<N>, G2Y<N>, KIND_STEP>();
   K.smem[1][1] = pass_smem_bytes<float, G2P<N>, G2Y<N>, KIND_ENERGY>();
   K.smem[0][0] = pass_smem_bytes<float, Plan<N>, G2X<N>, KIND_STEP>();
@@ -460,21 +467,38 @@ static bool g2m_lookup(int n, G2MKernels* K) {
 }
 
 cudaError_t launch_multi2d_block(const G2Args& a, int ny, int nx, int ny_items, int nx_items, int jj, bool last,
-                                 bool energy, cudaStream_t s) {
+                                 bool energy, bool fold, cudaStream_t s) {
   G2MKernels KY, KX;
   if (!g2m_lookup(ny, &KY) || !g2m_lookup(nx, &KX)) return cudaErrorInvalidValue;
-  const void* ky[2] = {KY.k[1][0], KY.k[1][1]};
-  const void* kx[2] = {KX.k[0][0], KX.k[0][1]};
-  const size_t sy[2] = {KY.smem[1][0], KY.smem[1][1]}, sx[2] = {KX.smem[0][0], KX.smem[0][1]};
-  for (int k = 0; k < 2; ++k) {
+  const void* ky[3] = {KY.k[1][0], KY.k[1][1], KY.k[1][2]};
+  const void* kx[3] = {KX.k[0][0], KX.k[0][1], KX.k[0][2]};
+  const size_t sy[3] = {KY.smem[1][0], KY.smem[1][1], KY.smem[1][2]};
+  const size_t sx[3] = {KX.smem[0][0], KX.smem[0][1], KX.smem[0][2]};
+  for (int k = 0; k < 3; ++k) {
     cudaError_t e = cudaFuncSetAttribute(ky[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy[k]);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(kx[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx[k]);
     if (e != cudaSuccess) return e;
   }
   G2Args args = a;
+  args.epi_y = fold && a.n_rec % 2 == 0 ? 1 : 0;  // the last step's order is x y
   int lst = last ? 1 : 0, j = jj, pnone = PRO_NONE, enone = EPI_NONE;
   cudaError_t e = cudaSuccess;
-  for (int i = 1; i <= a.n_rec && e == cudaSuccess; ++i) {
+  if (fold) {
+    // folded steps: y x for odd steps, x y for even ones; the shared axis of
+    // consecutive steps is one folded pass (the extended kernel): 1 + n_rec
+    // pass launches per block
+    int pro = PRO_RT_HALF;  // solve_split.m:55-56
+    void* ay[4] = {&args, &pro, &enone, &lst};
+    e = g2m_launch(ky[0], ay, ny_items, sy[0], s);
+    for (int i = 1; i <= a.n_rec && e == cudaSuccess; ++i) {
+      const bool xa = i % 2 == 1;
+      const int k = i < a.n_rec ? 2 : 0;
+      int epi = i == a.n_rec ? EPI_RT_END : EPI_NONE;  // solve_split.m:60-67
+      void* ar[4] = {&args, &pnone, &epi, &lst};
+      e = xa ? g2m_launch(kx[k], ar, nx_items, sx[k], s) : g2m_launch(ky[k], ar, ny_items, sy[k], s);
+    }
+  }
+  for (int i = 1; i <= a.n_rec && e == cudaSuccess && !fold; ++i) {
     int pro = i == 1 ? PRO_RT_HALF : PRO_RT_FULL;  // solve_split.m:55-56 / 60-61
     void* ay[4] = {&args, &pro, &enone, &lst};
     e = g2m_launch(ky[0], ay, ny_items, sy[0], s);

@@ -39,6 +39,7 @@ struct G2Args {
   double ddt, dt_outer;
   unsigned* bar;    // [0] grid-barrier arrival counter, [1] work-item counter; zero at launch
   int* fail;        // set when a grid barrier's bounded wait ran out
+  int epi_y = 0;    // the block-end epilogue ran on the y pass (folded steps, even n_rec)
 };
 
 // Pencils per tile of the y pass (contiguous) and the x pass (strided) for
@@ -56,7 +57,9 @@ cudaError_t launch_grid2d(const G2Args& a, int nctas, cudaStream_t s);
 // at this block end) the kinetic sums, and the block finalizer of every grid
 // (jj: the block's index in the outer step, last: the outer step's last
 // block).
+// fold: folded steps (y x, x y, ...; the shared axis of consecutive steps
+// as one pass).
 cudaError_t launch_multi2d_block(const G2Args& a, int ny, int nx, int ny_items, int nx_items, int jj, bool last,
-                                 bool energy, cudaStream_t s);
+                                 bool energy, bool fold, cudaStream_t s);
 
 }  // namespace gpe

@@ -167,6 +167,20 @@ __device__ __forceinline__ cx<fx2> cexp_real_times_x2(fx2 a, float dre, float di
   return mk<fx2>(m * c, m * s);
 }
 
+// The full nonlinear step of real time on both pencils (solve_split.m:60-61):
+// the PRO_RT_FULL prologue, and the middle of a folded pass.
+template <class L, int E>
+__device__ __forceinline__ void rt_full_x2(cx<fx2>* v, const PassArgs<float>& a, bool valid, long long first,
+                                           long long dm, long long pb, float mu) {
+  const fx2 g(a.gr);
+#pragma unroll
+  for (int m = 0; m < E; ++m) {
+    const fx2 V = L::load_side(a.V + first, dm, pb, m, valid);
+    const fx2 ex = fma2(-g, norm2(v[m]), fx2(mu) - V);
+    v[m] = cmul(cexp_real_times_x2(ex, a.drer, a.dimr), v[m]);
+  }
+}
+
 // Prologue of the first pass (pass.cuh prologue, on both pencils).
 template <class L, int E>
 __device__ __forceinline__ void prologue_x2(cx<fx2>* v, const PassArgs<float>& a, bool valid, long long first,
@@ -188,12 +202,7 @@ __device__ __forceinline__ void prologue_x2(cx<fx2>* v, const PassArgs<float>& a
       }
       break;
     case PRO_RT_FULL:  // solve_split.m:60-61
-#pragma unroll
-      for (int m = 0; m < E; ++m) {
-        const fx2 V = L::load_side(a.V + first, dm, pb, m, valid);
-        const fx2 ex = fma2(-g, norm2(v[m]), fx2(mu) - V);
-        v[m] = cmul(cexp_real_times_x2(ex, dre, dim), v[m]);
-      }
+      rt_full_x2<L, E>(v, a, valid, first, dm, pb, mu);
       break;
     case PRO_ITP:  // groundstate_itp.m:36/76, :40
 #pragma unroll
@@ -297,8 +306,8 @@ constexpr size_t x2_smem_bytes() {
   return L::smem_bytes() + (X2SmemTables<P>::value ? sizeof(cx<float>) * (size_t)(P::TW_LEN + P::N) : 0);
 }
 
-// The paired step pass (KIND_STEP only).
-template <class P, class L>
+// The paired step pass (KIND_STEP; FOLD: the folded passes, a.fold = 1).
+template <class P, class L, bool FOLD>
 __global__ void __launch_bounds__(L::THREADS, X2MinBlocks<P, L>::value) pass_x2_kernel(const PassArgs<float> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<fx2>* sm = reinterpret_cast<cx<fx2>*>(smem_raw);
@@ -353,9 +362,22 @@ __global__ void __launch_bounds__(L::THREADS, X2MinBlocks<P, L>::value) pass_x2_
     php = tab + P::TW_LEN;
   }
   if (a.pro != PRO_NONE) prologue_x2<L, E>(v, a, valid, first, dm, pb, scal[0], scal[1]);
-  St::template forward<SMT>(v, sm, pol, t, tws);
-  apply_phase_x2<T, E, SMT>(v, php, t);
-  St::template inverse<SMT>(v, sm, pol, t, tws);
+  if constexpr (FOLD) {
+    // a folded pass: the transform, the full nonlinear step, the transform
+    // again
+#pragma unroll 1
+    for (int rep = 0;; ++rep) {
+      St::template forward<SMT>(v, sm, pol, t, tws);
+      apply_phase_x2<T, E, SMT>(v, php, t);
+      St::template inverse<SMT>(v, sm, pol, t, tws);
+      if (rep == 1) break;
+      rt_full_x2<L, E>(v, a, valid, first, dm, pb, scal[1]);
+    }
+  } else {
+    St::template forward<SMT>(v, sm, pol, t, tws);
+    apply_phase_x2<T, E, SMT>(v, php, t);
+    St::template inverse<SMT>(v, sm, pol, t, tws);
+  }
   Kahan2 acc[3];
   if (a.epi != EPI_NONE) epilogue_x2<L, E>(v, a, acc, valid, first, dm, pb, scal[1]);
   if (valid) L::store(a.psi + first, dm, pb, v);
@@ -373,7 +395,9 @@ __global__ void __launch_bounds__(L::THREADS, X2MinBlocks<P, L>::value) pass_x2_
 // adjacent, 16-byte aligned elements: an even pencil count, and even row
 // offsets and strides on the strided axes.
 inline bool x2_applies(const PassArgs<float>& a, bool strided) {
-  if (a.kind != KIND_STEP || a.rot || a.skip_fwd || a.skip_inv || a.mask_c || a.fold) return false;
+  if (!(a.kind == KIND_STEP || (a.kind == KIND_STEP_EXT && a.fold)) || a.rot || a.skip_fwd || a.skip_inv ||
+      a.mask_c)
+    return false;
   if (a.n_batch % 2 != 0) return false;
   if (strided) return a.inner % 2 == 0 && a.outer % 2 == 0 && a.stride % 2 == 0;
   return true;

@@ -11,7 +11,7 @@ namespace gpe {
 
 template <class P, class L>
 static cudaError_t launch_x2_layout(const PassArgs<float>& a, cudaStream_t s) {
-  auto kern = pass_x2_kernel<P, L>;
+  auto kern = a.fold ? pass_x2_kernel<P, L, true> : pass_x2_kernel<P, L, false>;
   const size_t smem = x2_smem_bytes<P, L>();
   if (smem > 32 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -9,7 +9,9 @@ shape, a stream per shape, one graph per outer step), against the per-pass path 
 through the C ABI.
 
 The per-point arithmetic of both paths is the same code (the axis passes'
-FFT, kinetic factor, prologue and epilogue), so the states agree to the
+FFT, kinetic factor, prologue and epilogue; both fold consecutive steps,
+except the grid-wide kernel, which is compared with folding off), so the
+states agree to the
 rounding of the norm / energy sums, which are summed in a different order:
 FP64 <= 1e-12 relative, FP32 <= 1e-6 (2e-6 with mu feedback, where those sums
 steer the next block).
@@ -53,6 +55,8 @@ PATHS = [("cluster", "double"), ("cluster", "single"), ("grid", "single"), ("mul
 @pytest.mark.parametrize("path,precision", PATHS)
 def test_cluster_batch_matches_per_pass_path(gpe, monkeypatch, path, precision):
     monkeypatch.setenv("GPE_SMALL2D", path)
+    if path == "grid":  # the grid-wide kernel runs unfolded steps: so does the reference path
+        monkeypatch.setenv("GPE_FOLD", "0")
     # the per-pass path on the FFT plans the persistent kernel runs (FP32:
     # the cluster kernel takes the alternative plan where a length has one,
     # the grid kernel the default plans), so that both paths do the same
@@ -82,6 +86,8 @@ def test_cluster_batch_matches_per_pass_path(gpe, monkeypatch, path, precision):
 @pytest.mark.parametrize("path,precision", PATHS)
 def test_cluster_single_context_with_feedback_decay_and_callbacks(gpe, monkeypatch, path, precision):
     monkeypatch.setenv("GPE_SMALL2D", path)
+    if path == "grid":
+        monkeypatch.setenv("GPE_FOLD", "0")
     """gamma > 0 with the mu feedback, a decaying target norm and an outer-step
     callback, on one 128 x 96 context, against the FP64 oracle."""
     V = harmonic((1.0, 1.4))
