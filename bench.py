@@ -494,7 +494,9 @@ def run_batch(args, dist):
                    "sharding": "realisations dealt round-robin over ranks, no data-path collective",
                    "sizes_rank0": {f"{k}^2": v for k, v in sorted(sizes.items())},
                    "points_total": P, "dt": B.dt, "step": f"{inner} split steps of every realisation",
-                   "execution": "one CUDA graph per block of 10 steps, realisations concurrent",
+                   "execution": "one CUDA graph per outer step: per shape of grid a stream of pass kernels over "
+                                "the tiles of all its grids (folded steps: 11 pass launches, 2 kinetic-sum "
+                                "launches and 1 finalizer per block of 10 steps)",
                    "l2": f"all states ({P * 12 / 1e6:.0f} MB with V) fit in L2: L2-resident workload"},
         "gpu_launches": int(launches), "clocks": clk.summary(),
     }

@@ -2325,6 +2325,15 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
       groups.push_back(grp);
     }
   }
+  // kernels of one outer step (the launch count the context reports)
+  long long kernels = 1;
+  if (nctas == 0) {
+    kernels = 0;
+    const bool fold = fold_env();
+    for (const Group& grp : groups)
+      for (int jj = 1; jj <= r0.nb; ++jj)
+        kernels += (fold ? 1 + r0.n_rec : 2 * r0.n_rec) + ((grp.feedback || jj == r0.nb) ? 2 : 0) + 1;
+  }
   int last_j = r0.start;
   bool stop_req = false;
   const bool direct = c->prof || prm->on_step;
@@ -2364,9 +2373,10 @@ gpe_status grid2d_impl(std::vector<gpe_ctx*>& cs, const gpe_split_params* prm, i
   for (int j = r0.start + 1; j <= r0.nout && !stop_req; ++j) {
     if (direct) {
       Launch L(c, PC_CLUSTER, bytes);
+      c->launches += kernels - 1;
       CU(enqueue());
     } else {
-      c->launches++;
+      c->launches += kernels;
       CU(cudaGraphLaunch(gr.x, master));
     }
     last_j = j;

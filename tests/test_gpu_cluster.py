@@ -62,9 +62,12 @@ def test_cluster_batch_matches_per_pass_path(gpe, monkeypatch, path, precision):
     # the grid kernel the default plans), so that both paths do the same
     # arithmetic and differ only in the order of the block-end sums
     ref = [make(gpe, s, precision, 2) for s in SPECS]
+    ref_launched = 0
     for t in ref:
         t.autotune(3 if path == "cluster" else 0)
+        k = t.kernel_launches()
         t.solve_split(0.003, 20, 3)
+        ref_launched += t.kernel_launches() - k
     batch = [make(gpe, s, precision, 0) for s in SPECS]
     k0 = sum(t.kernel_launches() for t in batch)
     gpe.solve_split_batch(batch, 0.003, 20, 3)
@@ -74,11 +77,16 @@ def test_cluster_batch_matches_per_pass_path(gpe, monkeypatch, path, precision):
         assert rel_l2(b.current_state, a.current_state) < tol
         np.testing.assert_allclose(b.history["mu"], a.history["mu"], rtol=tol)
         np.testing.assert_allclose(b.history["n"], a.history["n"], rtol=tol)
-    # one launch per outer step for the whole batch, plus each context's
-    # setup (state upload and initial mu: a few kernels); the per-pass path
-    # launches 2 passes per step and grid (360 here) plus the block ends
+    # persistent kernels: one launch per outer step for the whole batch, plus
+    # each context's setup (state upload and initial mu: a few kernels); the
+    # per-pass path launches the passes of every step and grid plus the block
+    # ends.  The multi-grid pass kernels launch one pass per shape of grid
+    # (here every grid has its own shape): no more than the per-pass path.
     launched = sum(t.kernel_launches() for t in batch) - k0
-    assert launched <= 3 + 8 * len(SPECS), launched
+    if path == "multi":
+        assert launched <= ref_launched, (launched, ref_launched)
+    else:
+        assert launched <= 3 + 8 * len(SPECS), launched
     for t in ref + batch:
         t.close()
 

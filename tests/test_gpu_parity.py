@@ -368,6 +368,38 @@ def test_l2_prefetch_variant_is_bit_identical(gpe, precision):
     np.testing.assert_array_equal(out[1][2], out[0][2])
 
 
+@pytest.mark.parametrize("axes,n_rec", [((4.0, 64, 5.0, 48), 10), ((4.0, 64, 5.0, 48), 5),
+                                         ((5.0, 24, 6.0, 32, 4.0, 16), 10), ((5.0, 24, 6.0, 32, 4.0, 16), 3)])
+def test_folded_steps_match_unfolded_and_oracle(gpe, monkeypatch, axes, n_rec):
+    """Folded steps (consecutive steps take the axes in opposite orders and
+    share one pass, the default) against the same run with GPE_FOLD=0 (y x z
+    every step) and against the FP64 oracle: the kinetic factors commute, so
+    the two orders agree to rounding.  FP64 with gamma > 0 (mu feeds back
+    every block) and an even and an odd n_recalc (the block ends on the y or
+    on the last axis)."""
+    V = harmonic((1.0, 1.3, 1.6)[: len(axes) // 2])
+    out = []
+    for fold in ("1", "0"):
+        monkeypatch.setenv("GPE_FOLD", fold)
+        monkeypatch.setenv("GPE_CLUSTER", "0")  # the per-pass path (2D grids this small take the cluster kernel)
+        grid, task, og, ot = make_pair(gpe, axes, V, "double", g=0.7, gamma=0.02, Ntotal=20.0)
+        task.n_recalc = n_rec
+        ot.n_recalc = n_rec
+        X = og.mesh["x"]
+        psi0 = np.exp(-sum(og.mesh[k] ** 2 for k in og.mesh) / 3) * np.exp(0.4j * X)
+        task.init_state = psi0
+        task.solve_split(0.003, 2 * n_rec, 2)
+        out.append((task.current_state, np.array(task.history["mu"])))
+        if fold == "1":
+            ot.init_state = psi0
+            ot.solve_split(0.003, 2 * n_rec, 2)
+            assert rel_l2(task.current_state, ot.current_state) < 1e-11
+            np.testing.assert_allclose(task.history["mu"], ot.history["mu"], rtol=1e-11)
+        task.close()
+    assert rel_l2(out[0][0], out[1][0]) < 1e-12
+    np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-12)
+
+
 def test_device_sincos_error_bound(gpe):
     """The FP32 phase factors' sin/cos: absolute error <= 2 ulp(1) = 2.4e-7
     against FP64 over the bounded range and beyond it (library fallback)."""
