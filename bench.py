@@ -144,6 +144,27 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def flop_roofline(grid_points, steps, seconds, sm_max_mhz, sms_used=None):
+    """Arithmetic roofline of an L2-resident workload: 10 log2(P) + 30 flops
+    per grid-point-step for a grid of P points (FFTs of both directions on
+    every axis, the kinetic factor, the phases), against the nominal FP32
+    CUDA-core peak (SMs x 128 lanes x 2 flops x the maximum SM clock)."""
+    import torch
+
+    flops = sum(p * (10.0 * math.log2(p) + 30.0) for p in grid_points) * steps
+    achieved = flops / seconds / 1e12
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = sm_max_mhz or 2070.0
+    peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+    out = {"bound": "fp32 (CUDA cores)", "flops_per_point_step": "10 log2(P) + 30",
+           "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+           "peak_kind": f"nominal: {sms} SMs x 128 lanes x 2 x {mhz:.0f} MHz"}
+    if sms_used:
+        out["sms_used"] = sms_used
+        out["frac_of_sms_used"] = achieved / (peak * sms_used / sms)
+    return out
+
+
 def ground_state(gpe, W, precision="single", device=0):
     """Untimed setup: FP32 ITP with FP64 polish from the seeded Gaussian."""
     grid, task = W.make_task(precision, device=device)
@@ -438,6 +459,7 @@ def run_gpu(args, dist):
         "error": {"fp32_vs_fp64_rel_l2_after_outer_step": err_l2,
                   "mu_rel_after_outer_step": abs(mu32 - mu64) / abs(mu64),
                   "itp_iters": itp.iters, "itp_fp32_iters": itp.fp32_iters, "itp_converged": bool(itp.converged),
+                  "itp_ms_fp32": itp.ms_main, "itp_ms_fp64_polish": itp.ms_fp64,
                   "vs_oracle": vs_oracle},
         "roofline": {"bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
@@ -453,6 +475,10 @@ def run_gpu(args, dist):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if W.npoints * 12 / 1e6 <= 129:  # L2-resident: the arithmetic roofline
+        cl = line["clocks"] if isinstance(line["clocks"], dict) else {}
+        line["flop_roofline"] = flop_roofline([P], INNER * args.steps, t_s, cl.get("sm_max_mhz"),
+                                              sms_used=16 if top["name"] == "cluster_step" else None)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     task.close()
@@ -500,6 +526,9 @@ def run_batch(args, dist):
                    "l2": f"all states ({P * 12 / 1e6:.0f} MB with V) fit in L2: L2-resident workload"},
         "gpu_launches": int(launches), "clocks": clk.summary(),
     }
+    cl = line["clocks"] if isinstance(line["clocks"], dict) else {}
+    line["flop_roofline"] = flop_roofline([t.grid.npoints for t in tasks], inner * args.steps, t_s,
+                                          cl.get("sm_max_mhz"))
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     for t in tasks:

@@ -1178,7 +1178,20 @@ gpe_status itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* M
   int reason = RUNNING;
   int fp32_iters = 0;
   const bool polish = (c->prec == GPE_FP32) && prm->fp64_polish;
+  // device time of the two phases (events on the context stream)
+  cudaEvent_t tev[3] = {nullptr, nullptr, nullptr};
+  struct EvFree {
+    cudaEvent_t* e;
+    ~EvFree() {
+      for (int k = 0; k < 3; ++k)
+        if (e[k]) cudaEventDestroy(e[k]);
+    }
+  } tev_free{tev};
+  for (int k = 0; k < 3; ++k) CU(cudaEventCreate(&tev[k]));
+  CU(cudaEventRecord(tev[0], c->stream));
   CHECK(itp_phase<R>(c, f, prm, st, polish, &reason));
+  CU(cudaEventRecord(tev[1], c->stream));
+  CU(cudaEventRecord(tev[2], c->stream));
   if (polish && reason == SWITCH_FP64 && st.i < maxit) {
     fp32_iters = st.i;
     CHECK(ensure_polish(c));
@@ -1198,6 +1211,7 @@ gpe_status itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* M
       launch_set_scale_one(c->sc, c->stream);
       CU(cudaGetLastError());
     }
+    CU(cudaEventRecord(tev[2], c->stream));
   } else if (polish) {
     fp32_iters = st.i;
   }
@@ -1233,6 +1247,12 @@ gpe_status itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, double* M
     res->fp32_iters = fp32_iters;
     res->final_dt = st.dt;
     res->last_delta = h.delta;
+    float m0 = 0.f, m1 = 0.f;
+    CU(cudaEventSynchronize(tev[2]));
+    CU(cudaEventElapsedTime(&m0, tev[0], tev[1]));
+    CU(cudaEventElapsedTime(&m1, tev[1], tev[2]));
+    res->ms_main = m0;
+    res->ms_fp64 = m1;
   }
   if (reason == RUNNING && iters >= maxit)
     c->err = "groundstate_itp: Convergence not reached";  // groundstate_itp.m:79 (a warning)

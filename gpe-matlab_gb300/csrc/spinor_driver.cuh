@@ -378,6 +378,8 @@ gpe_status spinor_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double* MU, do
     res->fp32_iters = 0;
     res->final_dt = dt;
     res->last_delta = last_delta;  // the last convergence test's delta (NaN: none ran)
+    res->ms_main = 0.0;  // not timed on this path
+    res->ms_fp64 = 0.0;
   }
   if (!converged) c->err = "groundstate_itp: Convergence not reached";
   return GPE_OK;
@@ -567,6 +569,8 @@ gpe_status mix_itp_impl(gpe_ctx* c, const gpe_itp_params* prm, double N1, double
     res->fp32_iters = 0;
     res->final_dt = dt;
     res->last_delta = last_delta;
+    res->ms_main = 0.0;  // not timed on this path
+    res->ms_fp64 = 0.0;
   }
   if (!converged) c->err = "groundstate_itp: Convergence not reached";
   return GPE_OK;

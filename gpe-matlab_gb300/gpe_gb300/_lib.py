@@ -41,7 +41,7 @@ class gpe_itp_params(C.Structure):
 
 class gpe_itp_result(C.Structure):
     _fields_ = [("iters", C.c_int), ("converged", C.c_int), ("fp32_iters", C.c_int), ("final_dt", C.c_double),
-                ("last_delta", C.c_double)]
+                ("last_delta", C.c_double), ("ms_main", C.c_double), ("ms_fp64", C.c_double)]
 
 
 VTD_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, C.POINTER(C.c_double))

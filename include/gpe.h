@@ -104,6 +104,10 @@ typedef struct {
     int fp32_iters;         /* iterations run in FP32 before the FP64 polish     */
     double final_dt;        /* dt at exit (differs if itp_adjust_stepsize)       */
     double last_delta;      /* last residual delta                               */
+    double ms_main;         /* device time of the iterations in the context's
+                               precision (CUDA events on the context stream)     */
+    double ms_fp64;         /* device time of the FP64 polish, conversions
+                               included (0 without one)                          */
 } gpe_itp_result;
 
 /* Host callbacks of solve_split.  Both run on the calling thread. */

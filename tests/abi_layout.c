@@ -15,7 +15,7 @@ int main(void) {
     F(gpe_grid_desc, precision); F(gpe_grid_desc, device);
     S(gpe_params); F(gpe_params, n_recalc); F(gpe_params, itp_adjust_stepsize); F(gpe_params, omega);
     S(gpe_itp_params); F(gpe_itp_params, fp64_polish); F(gpe_itp_params, switch_delta);
-    S(gpe_itp_result); F(gpe_itp_result, final_dt); F(gpe_itp_result, last_delta);
+    S(gpe_itp_result); F(gpe_itp_result, final_dt); F(gpe_itp_result, last_delta); F(gpe_itp_result, ms_fp64);
     S(gpe_split_params); F(gpe_split_params, vtd); F(gpe_split_params, on_step); F(gpe_split_params, step_user);
     S(gpe_adjoint_params); F(gpe_adjoint_params, checkpoint_every); F(gpe_adjoint_params, mem_budget);
     F(gpe_adjoint_params, precision);
