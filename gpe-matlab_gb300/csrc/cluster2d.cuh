@@ -1,8 +1,8 @@
 // cluster2d.cuh - persistent solve_split of many small 2D grids in one launch.
 //
-// The graph path runs a 2D split step as two axis-pass launches per step
-// and per grid: for grids of a few hundred KB (all of them L2-resident)
-// that is launch- and latency-bound.  Here one launch advances every grid of
+// The graph path runs a 2D split step as axis-pass launches per step and
+// per grid: for grids of a few hundred KB (all of them L2-resident) that is
+// launch- and latency-bound.  Here one launch advances every grid of
 // a batch through a whole outer step of solve_split (solve_split.m:49-80):
 //
 //  * each grid is owned by one thread-block cluster of CS CTAs (CS = 8, or 16
@@ -20,6 +20,11 @@
 //    shared memory (ld.shared::cluster), transform them with a local exchange
 //    buffer, apply the block-end epilogue and write them back
 //    (st.shared::cluster), exactly the arithmetic of the x axis pass;
+//  * folded steps (C2Args::fold): odd steps take y then x, even steps x then
+//    y, and the shared axis of consecutive steps is one pass with the full
+//    nonlinear step between its two transforms, so a block of n_rec steps is
+//    1 + n_rec passes (the first y pass with the half-step prologue, the
+//    last with the block-end epilogue);
 //  * hardware cluster barriers separate the passes; at the end of a block
 //    whose mu is needed (gamma > 0 feedback, or the last block of the outer
 //    step) the kinetic-energy sums of both axes (Parseval, forward FFTs) and

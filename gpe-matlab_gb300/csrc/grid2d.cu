@@ -1,5 +1,6 @@
-// grid2d.cu - grid-wide persistent solve_split of small 2D grids (FP32), and
-// the multi-grid pass kernels of batches (end of the file).
+// grid2d.cu - grid-wide persistent solve_split of small 2D grids (FP32,
+// unfolded steps), and the multi-grid pass kernels of batches (end of the
+// file; folded steps).
 //
 // One cooperative launch advances every grid of a batch (or the single grid
 // of solve_split) through an outer step of solve_split (solve_split.m:49-80)
