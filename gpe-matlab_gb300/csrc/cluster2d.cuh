@@ -179,8 +179,8 @@ __device__ __forceinline__ void c2_y_step(cx<R>* home, const R* vloc, const C2Ge
 // written back to the owning CTAs' pencils.  pa.fold and epi = EPI_RT_END as
 // in the y pass.
 template <typename R, class P>
-__device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const C2Geom& g, const C2Grid& G, int rank,
-                                          const PassArgs<R>& pa, R mu, Kahan<R>* acc) {
+__device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const R* vrow, const C2Geom& g, const C2Grid& G,
+                                          int rank, const PassArgs<R>& pa, R mu, Kahan<R>* acc) {
   constexpr int T = P::T, E = P::E, N = P::N;
   constexpr int GX = C2Threads<R>::value / T;
   using St = typename P::template St<R>;
@@ -213,9 +213,15 @@ __device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const C2Geom
     }
     R sv[E];
     auto load_v = [&]() {
-      const R* vs = V + (long long)t * G.ny + y;
+      if (vrow) {  // this CTA's V rows in shared memory
+        const R* vs = vrow + (r0 + f) * g.vrstride + t;
 #pragma unroll
-      for (int m = 0; m < E; ++m) sv[m] = valid ? __ldg(vs + (long long)T * m * G.ny) : R(0);
+        for (int m = 0; m < E; ++m) sv[m] = valid ? vs[T * m] : R(0);
+      } else {
+        const R* vs = V + (long long)t * G.ny + y;
+#pragma unroll
+        for (int m = 0; m < E; ++m) sv[m] = valid ? __ldg(vs + (long long)T * m * G.ny) : R(0);
+      }
     };
 #pragma unroll 1
     for (int rep = 0;; ++rep) {
@@ -328,12 +334,12 @@ __device__ void c2_y_step_n(int n, cx<R>* home, const R* vloc, const C2Geom& g, 
   }
 }
 template <typename R>
-__device__ void c2_x_step_n(int n, cx<R>* home, cx<R>* xbuf, const C2Geom& g, const C2Grid& G, int rank,
-                            const PassArgs<R>& pa, R mu, Kahan<R>* acc) {
+__device__ void c2_x_step_n(int n, cx<R>* home, cx<R>* xbuf, const R* vrow, const C2Geom& g, const C2Grid& G,
+                            int rank, const PassArgs<R>& pa, R mu, Kahan<R>* acc) {
   switch (n) {
-#define X(v)                                                      \
-  case v:                                                         \
-    c2_x_step<R, C2Plan<R, v>>(home, xbuf, g, G, rank, pa, mu, acc);   \
+#define X(v)                                                                 \
+  case v:                                                                    \
+    c2_x_step<R, C2Plan<R, v>>(home, xbuf, vrow, g, G, rank, pa, mu, acc);   \
     break;
     GPE_C2_SIZES(X)
 #undef X
@@ -406,6 +412,7 @@ __global__ void __launch_bounds__(C2Threads<R>::value, C2Threads<R>::min_blocks)
     const C2Grid& G = a.grids[a.order[k]];
     const C2Geom g = c2_geom(G.nx, G.ny, cs, (int)sizeof(cx<R>), a.vsm);
     R* vloc = a.vsm ? reinterpret_cast<R*>(smem + g.vofs) : nullptr;
+    R* vrow = a.vsm ? reinterpret_cast<R*>(smem + g.vrofs) : nullptr;
     cx<R>* home = reinterpret_cast<cx<R>*>(smem);
     cx<R>* xbuf = home + g.home;
     double* red = reinterpret_cast<double*>(smem + (size_t)(g.home + g.xbuf) * sizeof(cx<R>));
@@ -431,6 +438,13 @@ __global__ void __launch_bounds__(C2Threads<R>::value, C2Threads<R>::min_blocks)
       if (vloc) {  // this CTA's columns of V, dense [column][y]
         const R* vsrc = static_cast<const R*>(G.V) + (long long)col0 * G.ny;
         for (int i = threadIdx.x; i < total; i += C2Threads<R>::value) vloc[i] = vsrc[i];
+        // and its x-pass rows y in [rank*rows, (rank+1)*rows), [row][x]
+        const R* vg = static_cast<const R*>(G.V) + (long long)rank * g.rows;
+        const int rtotal = g.rows * G.nx;
+        for (int i = threadIdx.x; i < rtotal; i += C2Threads<R>::value) {
+          const int x = i / g.rows, r = i - x * g.rows;
+          vrow[r * g.vrstride + x] = vg[(long long)x * G.ny + r];
+        }
       }
     }
     c2_sync();
@@ -469,7 +483,7 @@ __global__ void __launch_bounds__(C2Threads<R>::value, C2Threads<R>::min_blocks)
           }
           pa.fold = a.fold && i < a.n_rec ? 1 : 0;
           pa.epi = i == a.n_rec ? EPI_RT_END : EPI_NONE;  // solve_split.m:60-67
-          if (xa) c2_x_step_n<R>(G.nx, home, xbuf, g, G, rank, pa, mu, acc);
+          if (xa) c2_x_step_n<R>(G.nx, home, xbuf, vrow, g, G, rank, pa, mu, acc);
           else c2_y_step_n<R>(G.ny, home, vloc, g, G, col0, pa, s, mu, acc);
           c2_sync();
         }

@@ -61,6 +61,8 @@ __host__ __device__ constexpr int c2_reg(int n) {
 struct C2Geom {
   int cols, cols_pad, rows, regy, home, xbuf;  // home/xbuf in complex elements
   size_t vofs;                                 // byte offset of the V columns (vsm)
+  size_t vrofs;                                // byte offset of the V rows (vsm)
+  int vrstride;                                // row stride of the V rows: nx + 2 (conflict-free)
   size_t bytes;
 };
 __host__ __device__ inline C2Geom c2_geom(int nx, int ny, int cs, int esz, int vsm = 0) {
@@ -77,6 +79,11 @@ __host__ __device__ inline C2Geom c2_geom(int nx, int ny, int cs, int esz, int v
   g.bytes = (size_t)(g.home + g.xbuf) * (size_t)esz + C2_RED_BYTES;
   g.vofs = g.bytes;
   if (vsm) g.bytes += (size_t)g.cols * ny * (size_t)(esz / 2);
+  // V of the CTA's x-pass rows, [row][x] with stride nx + 2 (the x pass's
+  // lanes read 16 rows x 2 columns: banks 2 row + column, all distinct)
+  g.vrstride = nx + 2;
+  g.vrofs = (g.bytes + 15) & ~(size_t)15;
+  if (vsm) g.bytes = g.vrofs + (size_t)g.rows * g.vrstride * (size_t)(esz / 2);
   return g;
 }
 
