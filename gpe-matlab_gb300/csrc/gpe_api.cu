@@ -1411,16 +1411,12 @@ gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool las
                          unsigned long long step0 = 0) {
   Field& f = c->main;
   int nb_epi = 0;
-  if (fold_steps(c, run)) {
+  const bool folded = fold_steps(c, run);
+  if (folded) {
     const int np = (int)run.passes.size();
-    // the axis order of step i (1-based): y x z for odd i, z x y for even i;
-    // GPE_FOLD=2: a block with an even step count keeps y x z for its last
-    // step (the block then ends on z, one pass more)
-    const char* fe = getenv("GPE_FOLD");
-    const bool end_z = fe && atoi(fe) == 2 && run.n_rec % 2 == 0;
+    // the axis order of step i (1-based): y x z for odd i, z x y for even i
     auto order = [&](int i, int j) -> const AxisPass& {
-      const bool rev = i % 2 == 0 && !(end_z && i == run.n_rec);
-      return run.passes[rev ? np - 1 - j : j];
+      return run.passes[i % 2 == 0 ? np - 1 - j : j];
     };
     auto folds = [&](int i) {  // the last pass of step i folds with the first of step i+1
       return i < run.n_rec && order(i, np - 1).axis == order(i + 1, 0).axis;
@@ -1439,7 +1435,7 @@ gpe_status enqueue_block(gpe_ctx* c, const SplitRun& run, double time2, bool las
       }
     }
   }
-  for (int i = 1; i <= run.n_rec && !fold_steps(c, run); ++i) {
+  for (int i = 1; i <= run.n_rec && !folded; ++i) {
     if (run.sgpe) {
       // SGPE (solve_split.m:57-66): the nonlinear factor (half at the block
       // start, else the full one of the previous step) and the noise of step
