@@ -214,9 +214,11 @@ __device__ __forceinline__ void c2_x_step(cx<R>* home, cx<R>* xbuf, const R* vro
     R sv[E];
     auto load_v = [&]() {
       if (vrow) {  // this CTA's V rows in shared memory
-        const R* vs = vrow + (r0 + f) * g.vrstride + t;
+        const int v0 = (r0 + f) * g.vrstride + t;
 #pragma unroll
-        for (int m = 0; m < E; ++m) sv[m] = valid ? vs[T * m] : R(0);
+        for (int m = 0; m < E; ++m)
+          sv[m] = valid && bounds_ok(G.sc, BS_SMEM, v0 + T * m, (long long)g.rows * g.vrstride) ? vrow[v0 + T * m]
+                                                                                                : R(0);
       } else {
         const R* vs = V + (long long)t * G.ny + y;
 #pragma unroll
