@@ -211,7 +211,10 @@ class GPEtask:
         return detect_core(self, refine=refine, z_index=z_index, component=component, cap=cap)
 
     def groundstate_itp(self, dt, eps, phi0="rand", nargout=1, rng=None):
-        """groundstate_itp.m:1-112.  Returns phi, or (phi, MU, MU2, EE)[:nargout]."""
+        """groundstate_itp.m:1-112.  Returns phi, or (phi, MU, MU2, EE)[:nargout].
+        ``last_itp`` then holds the run's gpe_itp_result: iterations, the FP32
+        iterations before an FP64 polish, and the device time of each phase
+        (ms_main, ms_fp64)."""
         self._push_params()
         self._upload_V(np.ascontiguousarray(self.getVtotal(0)))
         phi = self.process_init_state(phi0, rng=rng)
