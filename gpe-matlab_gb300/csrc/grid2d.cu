@@ -361,9 +361,9 @@ cudaError_t launch_grid2d(const G2Args& a, int nctas, cudaStream_t s) {
 // ---- multi-grid pass kernels ------------------------------------------------------
 // The work items of the grid-wide kernel, one launch per pass over the tiles
 // of a group of grids of one shape (CTA = item): each (axis, kind, length)
-// kernel has the register allocation of the per-pass kernels (768 threads
-// per SM), kernel boundaries replace the grid barriers, and the groups of a
-// batch run on their own streams.  The launches of an outer step are one
+// kernel has the register allocation and occupancy of the per-pass kernels,
+// kernel boundaries replace the grid barriers, and the groups of a batch run
+// on their own streams.  The launches of an outer step are one
 // CUDA graph with programmatic dependent launch between them.
 
 template <int AXIS, int KIND, int N>
@@ -399,8 +399,10 @@ struct G2MBounds {
 };
 
 // One pass (AXIS 1: y, 0: x) over the tiles of every grid of the group:
-// KIND_STEP with the given prologue and epilogue, or KIND_ENERGY (the
-// kinetic sums of the grids whose mu is needed at this block end).
+// KIND_STEP with the given prologue and epilogue, KIND_STEP_EXT (a folded
+// pass: two steps' transforms with the full nonlinear step between them),
+// or KIND_ENERGY (the kinetic sums of the grids whose mu is needed at this
+// block end).
 template <int AXIS, int KIND, int N>
 __global__ void __launch_bounds__(G2_THREADS, G2MBounds<AXIS, N>::value)
     k_multi2d(const G2Args a, int pro, int epi, int last) {
